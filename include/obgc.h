@@ -1,0 +1,404 @@
+/*
+ * obgc.h — C ABI of the GB300-native OceanBioME tracer-tendency engine (libobgc.so).
+ *
+ * Every entry point is extern "C", takes plain pointers, sizes and POD structs, and returns an
+ * int status (OBGC_OK == 0).  No exception crosses the ABI.  Device pointers are CUDA device
+ * addresses on the current device; `stream` is a cudaStream_t passed as void* (NULL = default
+ * stream).  Every asynchronous call is stream-ordered.  A context is single-stream and not
+ * thread-safe: serialise calls on one context externally.
+ *
+ * Each declaration names the OceanBioME.jl (v0.17.6) interface it replaces, as file:line within
+ * that project.  The Julia `ccall` bindings a maintainer would add are written out in
+ * INTEGRATION.md.
+ */
+#ifndef OBGC_H
+#define OBGC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OBGC_ABI_VERSION 1
+
+/* ---------------------------------------------------------------------------------------
+ * Status codes.  Host-side errors in the reference are Julia exceptions (ArgumentError at
+ * src/Light/multi_band.jl:106, src/BoxModel/boxmodel.jl:138) or `@warn` (src/Utils/solvers.jl:118);
+ * here they are return codes, with a message available from obgc_last_error_message().
+ * ------------------------------------------------------------------------------------- */
+enum obgc_status {
+    OBGC_OK = 0,
+    OBGC_ERR_INVALID_ARGUMENT = 1, /* bad descriptor, size, pointer or parameter           */
+    OBGC_ERR_CUDA = 2,             /* a CUDA runtime call failed                            */
+    OBGC_ERR_NOT_CONVERGED = 3,    /* a root solve hit its iteration limit                  */
+    OBGC_ERR_NAN = 4,              /* a NaN/Inf was detected in a result                    */
+    OBGC_ERR_UNSUPPORTED = 5,      /* the model variant/grid has no fused kernel            */
+    OBGC_ERR_OUT_OF_MEMORY = 6,    /* device allocation failed or budget exceeded           */
+    OBGC_ERR_NO_DEVICE = 7,        /* no CUDA device is visible                             */
+    OBGC_ERR_BUSY = 8,             /* service has no free slot / budget for the request     */
+    OBGC_ERR_TIMEOUT = 9           /* a bounded wait expired                                */
+};
+
+/* Storage / compute precision of a field or a run. */
+enum obgc_dtype { OBGC_F32 = 0, OBGC_F64 = 1 };
+enum obgc_precision {
+    OBGC_PREC_F32 = 0,   /* FP32 state, FP32 compute                                       */
+    OBGC_PREC_F64 = 1,   /* FP64 state, FP64 compute (plain FP64 path)                     */
+    OBGC_PREC_MIXED = 2  /* FP64 state (RK3 accumulation), FP32 stencil/BGC compute       */
+};
+
+/* ---------------------------------------------------------------------------------------
+ * Named tracer slots.  Every tendency entry point addresses tracers by these names, so the
+ * caller's field order never matters.  Names follow required_biogeochemical_tracers of the
+ * NutrientsPlanktonDetritus components (src/Models/AdvectedPopulations/NutrientsPlanktonDetritus/
+ * nutrients.jl:20,45,83; plankton.jl:80; detritus.jl:39,83,293; carbonate_system.jl:47;
+ * oxygen.jl:19).  T and S are carried (advected) and read by the carbonate chemistry.
+ * ------------------------------------------------------------------------------------- */
+enum obgc_tracer {
+    OBGC_NO3 = 0, OBGC_NH4, OBGC_FE, OBGC_N,
+    OBGC_P, OBGC_Z, OBGC_T,
+    OBGC_SPOM, OBGC_BPOM, OBGC_DOM,
+    OBGC_SPON, OBGC_BPON, OBGC_DON, OBGC_SPOC, OBGC_BPOC, OBGC_DOC,
+    OBGC_D,
+    OBGC_DIC, OBGC_ALK, OBGC_O2,
+    OBGC_S,
+    OBGC_NUM_NAMED
+};
+#define OBGC_MAX_PASSIVE 8
+
+/* Component kinds of NutrientsPlanktonDetritus (NutrientsPlanktonDetritus.jl:27-33). */
+enum obgc_nutrients { OBGC_NUT_NITRATE_AMMONIA = 0, OBGC_NUT_NITRATE_AMMONIA_IRON = 1, OBGC_NUT_NUTRIENT = 2 };
+enum obgc_detritus  { OBGC_DET_TWO_PARTICLE = 0, OBGC_DET_VARIABLE_REDFIELD = 1, OBGC_DET_SINGLE = 2, OBGC_DET_NONE = 3 };
+enum obgc_light_limitation { OBGC_LIGHT_MONDO = 0, OBGC_LIGHT_ANALYTICAL = 1 };   /* plankton.jl:216-220 */
+enum obgc_formulation { OBGC_LINEAR = 0, OBGC_QUADRATIC = 1 };                      /* plankton.jl:83-90   */
+enum obgc_preset { OBGC_PRESET_LOBSTER = 0, OBGC_PRESET_NPZD = 1 };                 /* constructors.jl     */
+
+/*
+ * Parameters of a NutrientsPlanktonDetritus model, field for field the @kwdef structs
+ * NitrateAmmonia (nutrients.jl:16-18), PhytoZoo (plankton.jl:19-58), TwoParticleAndDissolved
+ * (detritus.jl:25-37), VariableRedfieldDetritus (detritus.jl:71-81), Detritus (detritus.jl:264-270)
+ * and Oxygen (oxygen.jl:14-17).  Sinking speeds are the scalar speeds that setup_velocity_fields
+ * (src/Utils/sinking_velocity_fields.jl:10-35) turns into ZFaceFields, positive downwards, in m/s.
+ */
+typedef struct obgc_npd_params {
+    int32_t nutrients;            /* enum obgc_nutrients                                     */
+    int32_t detritus;             /* enum obgc_detritus                                      */
+    int32_t carbonate_system;     /* 0/1: CarbonateSystem() present                          */
+    int32_t oxygen;               /* 0/1: Oxygen() present                                   */
+    int32_t light_limitation;     /* enum obgc_light_limitation                              */
+    int32_t has_temperature_coefficient; /* 0 = `nothing` (no Q10), 1 = Q10 used             */
+    int32_t phytoplankton_mortality_formulation; /* enum obgc_formulation                    */
+    int32_t grazing_concentration_formulation;   /* enum obgc_formulation                    */
+    int32_t open_bottom;          /* sinking fields leave through the bottom (1) or taper (0) */
+    int32_t reserved0;
+    /* NitrateAmmonia / NitrateAmmoniaIron */
+    double nitrification_rate;
+    /* PhytoZoo */
+    double nitrate_half_saturation;
+    double ammonia_half_saturation;
+    double iron_half_saturation;
+    double nitrate_ammonia_inhibition;
+    double light_half_saturation;
+    double phytoplankton_maximum_growth_rate;
+    double iron_ratio;
+    double phytoplankton_exudation_fraction;
+    double ammonia_fraction_of_exudate;
+    double temperature_coefficient;
+    double phytoplankton_mortality_rate;
+    double zooplankton_mortality_rate;
+    double zooplankton_excretion_rate;
+    double phytoplankton_solid_waste_fraction;
+    double excretion_inorganic_fraction;
+    double preference_for_phytoplankton;
+    double maximum_grazing_rate;
+    double grazing_half_saturation;
+    double zooplankton_assimilation_fraction;
+    double zooplankton_calcite_dissolution;
+    double redfield_ratio;
+    double carbon_calcite_ratio;
+    double zooplankton_gut_calcite_dissolution;
+    double phytoplankton_chlorophyll_ratio;
+    double phytoplankton_sinking_speed;
+    double zooplankton_sinking_speed;
+    /* TwoParticleAndDissolved / VariableRedfieldDetritus */
+    double remineralisation_inorganic_fraction;
+    double small_remineralisation_rate;
+    double large_remineralisation_rate;
+    double dissolved_remineralisation_rate;
+    double small_solid_waste_fraction;
+    double detritus_redfield_ratio;
+    double small_particle_sinking_speed;
+    double large_particle_sinking_speed;
+    /* Detritus (single class) */
+    double detritus_remineralisation_rate;
+    double small_particle_fraction;
+    double detritus_sinking_speed;
+    /* Oxygen */
+    double respiration_oxygen_nitrogen_ratio;
+    double nitrification_oxygen_nitrogen_ratio;
+} obgc_npd_params;
+
+/* TwoBandPhotosyntheticallyActiveRadiation parameters (src/Light/2band.jl:106-117). */
+typedef struct obgc_twoband_params {
+    double water_red_attenuation;
+    double water_blue_attenuation;
+    double chlorophyll_red_attenuation;
+    double chlorophyll_blue_attenuation;
+    double chlorophyll_red_exponent;
+    double chlorophyll_blue_exponent;
+    double pigment_ratio;
+    double phytoplankton_chlorophyll_ratio;
+} obgc_twoband_params;
+
+/* Surface PAR forms accepted by the light models (src/Light/2band.jl:91-103; Light.jl:45-47). */
+enum obgc_surface_par {
+    OBGC_SURFACE_PAR_DEFAULT = 0,  /* default_surface_PAR(t) = 100*max(0, cos(t*pi/12h))      */
+    OBGC_SURFACE_PAR_CONSTANT = 1, /* `value`                                                   */
+    OBGC_SURFACE_PAR_FIELD = 2     /* per-column device array (Nx*Ny, i fastest), same dtype as the grid fields */
+};
+typedef struct obgc_surface {
+    int32_t kind;                  /* enum obgc_surface_par                                     */
+    int32_t reserved0;
+    double value;                  /* OBGC_SURFACE_PAR_CONSTANT                                 */
+    const void* field;             /* OBGC_SURFACE_PAR_FIELD (device)                           */
+} obgc_surface;
+
+/* Grid topologies (Oceananigans RectilinearGrid). z is always Bounded. */
+enum obgc_topology { OBGC_PERIODIC = 0, OBGC_BOUNDED = 1, OBGC_FLAT = 2 };
+
+/*
+ * A rectilinear grid with uniform spacing and the Oceananigans field layout: column-major,
+ * i fastest, k = 0 at the bottom, k = Nz-1 at the surface.  Strides are in elements; stride_i is
+ * 1.  An Oceananigans OffsetArray with halos is described by pointing at its first interior
+ * element and passing stride_j = Nx+2Hx, stride_k = (Nx+2Hx)(Ny+2Hy); the engine never reads or
+ * writes halo cells (periodic neighbours are wrapped in-kernel).
+ */
+typedef struct obgc_grid {
+    int32_t Nx, Ny, Nz;
+    int32_t topology_x, topology_y;   /* enum obgc_topology */
+    int32_t reserved0;
+    double Lx, Ly, Lz;                /* extents (m); z faces at -Lz + k*Lz/Nz                */
+    int64_t stride_j, stride_k;
+} obgc_grid;
+
+/* ---------------------------------------------------------------------------------------
+ * Library info
+ * ------------------------------------------------------------------------------------- */
+int obgc_abi_version(void);
+/* Human-readable text of the last error raised on the calling host thread. */
+const char* obgc_last_error_message(void);
+/* Number of kernels this library has launched in this process (all entry points). */
+int64_t obgc_kernel_launch_count(void);
+
+/* ---------------------------------------------------------------------------------------
+ * NutrientsPlanktonDetritus model description (host only, no device work)
+ * ------------------------------------------------------------------------------------- */
+
+/* Fill `out` with the LOBSTER (constructors.jl:65-96) or NPZD (constructors.jl:177-227)
+ * defaults.  LOBSTER: NitrateAmmonia, PhytoZoo, TwoParticleAndDissolved; NPZD: Nutrient, PhytoZoo
+ * with Q10 = 1.88, linear P mortality, analytical light limitation, single-class Detritus. */
+int obgc_npd_preset(int32_t preset, obgc_npd_params* out);
+
+/* required_biogeochemical_tracers (NutrientsPlanktonDetritus.jl:69-74): writes the names
+ * (enum obgc_tracer) in the reference's order into names[0..cap) and returns the count (<0 on
+ * error). */
+int obgc_npd_required_tracers(const obgc_npd_params* p, int32_t* names, int32_t cap);
+
+/* biogeochemical_drift_velocity (plankton.jl:60-63, detritus.jl:135-141,290-291): writes the
+ * w-component of tracer `name`'s drift velocity on the Nz+1 z-faces (m/s, bottom first) of a grid
+ * with Nz levels, exactly as setup_velocity_fields builds it.  Returns 1 if the tracer drifts, 0 if
+ * not (w_faces left untouched), <0 on error. */
+int obgc_npd_drift_velocity(const obgc_npd_params* p, int32_t name, int32_t Nz, double* w_faces);
+
+/* Continuous-form functor (bgc)(Val(:X), x, y, z, t, tracers..., PAR) for one point, host side
+ * (docs/src/model_implementation.md:75, src/BoxModel/timesteppers.jl:60-61).  `values` holds
+ * OBGC_NUM_NAMED entries indexed by enum obgc_tracer (absent tracers ignored).  Writes the
+ * tendency of `name` to *out. */
+int obgc_npd_eval_point(const obgc_npd_params* p, int32_t name, double x, double y, double z,
+                        double t, const double* values, double PAR, double* out);
+
+/* ---------------------------------------------------------------------------------------
+ * Stateless device kernels (functional entry points)
+ * ------------------------------------------------------------------------------------- */
+
+/* Discrete-form tendencies of every BGC tracer at every cell (mode (i) of the drop-in): replaces
+ * the per-tracer functor calls (bgc)(i, j, k, grid, Val(:X), clock, fields, auxiliary_fields)
+ * (NutrientsPlanktonDetritus.jl:88; src/OceanBioME.jl:158-159) that Oceananigans inlines into one
+ * tendency kernel per tracer.  fields[name] / G[name]: device pointers (NULL where absent), all of
+ * dtype `dtype` on `grid`'s layout; PAR: device field of the same layout. */
+int obgc_npd_tendencies(const obgc_npd_params* p, const obgc_grid* grid, int32_t dtype,
+                        const void* const* fields, const void* PAR, void* const* G,
+                        double t, void* stream);
+
+/* TwoBand PAR (update_TwoBandPhotosyntheticallyActiveRadiation!, src/Light/2band.jl:1-33 and
+ * its update, :148-155): PAR from phytoplankton P, one column scan per (i, j). */
+int obgc_twoband_par(const obgc_twoband_params* lp, const obgc_surface* surface,
+                     const obgc_grid* grid, int32_t dtype, const void* P, void* PAR,
+                     double t, void* stream);
+
+/* MultiBand PAR (update_MultiBandPhotosyntheticallyActiveRadiation!, src/Light/multi_band.jl:
+ * 147-185) for `nbands` bands: band_fields[n] written per band and PAR_total = sum of bands.
+ * kw, e, chi, division: nbands host doubles (the band-mean coefficients of multi_band.jl:93-104 and
+ * surface_PAR_division).  Chl: device chlorophyll field (mg Chl/m3). */
+int obgc_multiband_par(int32_t nbands, const double* kw, const double* e, const double* chi,
+                       const double* division, const obgc_surface* surface,
+                       const obgc_grid* grid, int32_t dtype, const void* Chl,
+                       void* const* band_fields, void* PAR_total, double t, void* stream);
+
+/* Band means of Morel (1988) coefficients (numerical_mean, multi_band.jl:93-104,136-140), host. */
+int obgc_multiband_coefficients(int32_t nbands, const double* band_edges /* 2*nbands nm */,
+                                int32_t nbase, const double* base_lambda, const double* base_kw,
+                                const double* base_e, const double* base_chi,
+                                double* kw, double* e, double* chi);
+
+/* Euphotic depth (_compute_euphotic_depth!, src/Light/compute_euphotic_depth.jl:3-29): first
+ * depth where PAR <= cutoff * surface PAR, log-interpolated; writes Nx*Ny values. */
+int obgc_euphotic_depth(const obgc_grid* grid, int32_t dtype, const void* PAR, void* zeu,
+                        double cutoff, void* stream);
+
+/* ---------------------------------------------------------------------------------------
+ * Carbon chemistry (src/Models/CarbonChemistry)
+ * ------------------------------------------------------------------------------------- */
+enum obgc_carbon_output {
+    OBGC_OUT_FCO2 = 0,   /* selected_output Val(:fCO₂) (carbon_chemistry.jl:167)  */
+    OBGC_OUT_PCO2 = 1,   /* Val(:pCO₂) (:170-193)                                  */
+    OBGC_OUT_PH_FREE = 2,/* Val(:pHᶠ) (:168)                                      */
+    OBGC_OUT_PH_TOTAL = 3,/* Val(:pHᵗ) (:195-200)                                 */
+    OBGC_OUT_PH_SWS = 4, /* Val(:pHˢ) (:202-210)                                   */
+    OBGC_OUT_H = 5,      /* the solved free [H+] (mol/kg)                          */
+    OBGC_OUT_CARBONATE = 6,/* carbonate_concentration (calcite_concentration.jl:1-53) */
+    OBGC_OUT_OMEGA_CALCITE = 7 /* calcite_saturation (calcite_concentration.jl:55-80)  */
+};
+enum obgc_density { OBGC_DENSITY_EOS80 = 0, OBGC_DENSITY_CONSTANT = 1 };
+
+/*
+ * Options of a batched carbonate solve, mirroring the keyword arguments of
+ * (p::CarbonChemistry)(; DIC, T, S, Alk, pH, P, output, boron, sulfate, fluoride, silicate,
+ * phosphate, initial_pH_guess) (carbon_chemistry.jl:111-121) and the DampedNewtonRaphsonSolver
+ * defaults (src/Utils/solvers.jl:81-88, carbon_chemistry.jl:81).
+ */
+typedef struct obgc_carbon_options {
+    int32_t output;              /* enum obgc_carbon_output                                   */
+    int32_t density;             /* enum obgc_density                                         */
+    int32_t has_pressure;        /* 0: P = nothing (no pressure correction); 1: use P          */
+    int32_t ph_given;            /* 1: `pH` array supplies free pH, no solve                  */
+    int32_t max_iters;           /* Newton iterations (reference default 100)                 */
+    int32_t warm_start;          /* 1: start from H_inout instead of 10^-initial_pH_guess     */
+    double density_value;        /* OBGC_DENSITY_CONSTANT                                     */
+    double initial_pH_guess;     /* 8                                                        */
+    double atol;                 /* 1e-20                                                     */
+    double damping;              /* 0.5                                                       */
+    double armijo_constant;      /* 0.5                                                       */
+    double min_damping;          /* 0.5^10                                                    */
+    double calcium_ion_per_salinity; /* 0.0103/35 (calcite_concentration.jl:78)             */
+} obgc_carbon_options;
+
+int obgc_carbon_default_options(obgc_carbon_options* out);
+
+/*
+ * Batched FP64 carbonate solve on the device: n cells.  Inputs DIC (mmol/m3), Alk (meq/m3),
+ * T (degC), S (psu) of dtype `dtype`; optional (NULL = zero / absent) silicate, phosphate
+ * (mmol/m3), P (bar), pH (free pH, when ph_given).  H_inout (FP64, optional) receives the solved
+ * [H+] and, with warm_start, supplies the start.  out: FP64 array of n.  iters (optional int32 n):
+ * Newton iterations used.  Returns OBGC_ERR_NOT_CONVERGED if any cell hit max_iters with
+ * |residual| > atol (all outputs still written).
+ */
+int obgc_carbon_chemistry(const obgc_carbon_options* opt, int64_t n, int32_t dtype,
+                          const void* DIC, const void* Alk, const void* T, const void* S,
+                          const void* silicate, const void* phosphate, const void* P,
+                          const void* pH, double* H_inout, double* out, int32_t* iters,
+                          void* stream);
+
+/* Host (CPU) evaluation of the same functor for one point, FP64 (used by the Julia shim for
+ * diagnostics and by the continuous-form path). */
+int obgc_carbon_chemistry_point(const obgc_carbon_options* opt, double DIC, double Alk,
+                                double T, double S, double silicate, double phosphate,
+                                double P, double pH, double* out);
+
+/* ---------------------------------------------------------------------------------------
+ * 3-D model context: fused advection + BGC + RK3 (mode (ii)) and the plugin hooks (mode (i))
+ * ------------------------------------------------------------------------------------- */
+typedef struct obgc_ctx obgc_ctx;
+
+enum obgc_advection { OBGC_ADVECTION_NONE = 0, OBGC_ADVECTION_WENO5 = 1 };
+
+typedef struct obgc_model_desc {
+    obgc_npd_params npd;          /* the biogeochemistry                                      */
+    obgc_twoband_params light;    /* TwoBand light attenuation                                */
+    obgc_surface surface;         /* surface PAR                                              */
+    obgc_grid grid;
+    int32_t precision;            /* enum obgc_precision                                      */
+    int32_t advection;            /* enum obgc_advection (tracer + drift advection scheme)    */
+    int32_t n_passive;            /* extra advected tracers with zero BGC tendency            */
+    int32_t carry_T;              /* T carried as an advected tracer even if BGC ignores it   */
+    int32_t carry_S;              /* S carried as an advected tracer                          */
+    int32_t reserved0;
+} obgc_model_desc;
+
+/* Fields a context works on.  Tracer arrays are device pointers of the context's state dtype
+ * (FP32 for OBGC_PREC_F32, FP64 otherwise); velocities u, v (Face, Center, Center / Center, Face,
+ * Center) and w (Center, Center, Face: w[k] on the face below cell k) are the same dtype and
+ * layout, or NULL for zero.  G (mode (i)) receives BGC tendencies; PAR is written by
+ * obgc_update_state.  All pointers may be re-bound at any time. */
+typedef struct obgc_fields {
+    void* tracers[OBGC_NUM_NAMED];
+    void* passive[OBGC_MAX_PASSIVE];
+    const void* u;
+    const void* v;
+    const void* w;
+    void* PAR;
+    void* G[OBGC_NUM_NAMED];
+} obgc_fields;
+
+/* Build a context (src/OceanBioME.jl:100-120 Biogeochemistry(...); Oceananigans
+ * NonhydrostaticModel(grid; biogeochemistry, advection)).  Allocates the RK3 tendency and
+ * ping-pong buffers on the current device. */
+int obgc_create(const obgc_model_desc* desc, obgc_ctx** out);
+int obgc_destroy(obgc_ctx* ctx);
+/* Bind (or re-bind) device fields. */
+int obgc_bind_fields(obgc_ctx* ctx, const obgc_fields* fields);
+/* update_biogeochemical_state! (src/OceanBioME.jl:161-167; 2band.jl:148-155): PAR at time t. */
+int obgc_update_state(obgc_ctx* ctx, double t, void* stream);
+/* Mode (i): BGC tendencies of all tracers into fields.G at time t (uses the bound PAR). */
+int obgc_compute_tendencies(obgc_ctx* ctx, double t, void* stream);
+/* Mode (ii): nsteps fused RK3 steps of size dt from time t (Oceananigans time_step! with
+ * RungeKutta3: per substep PAR scan + fused WENO5/drift/BGC/RK3 update).  The bound tracer arrays
+ * hold the state before and after. */
+int obgc_step(obgc_ctx* ctx, double t, double dt, int32_t nsteps, void* stream);
+/* Capture `nsteps` steps into a CUDA graph owned by the context and replay it (same semantics as
+ * obgc_step; re-captured when dt, nsteps or bindings change). */
+int obgc_step_graph(obgc_ctx* ctx, double t, double dt, int32_t nsteps, void* stream);
+/* Device kernel time of the last obgc_step / obgc_step_graph measured with CUDA events on the
+ * launching stream (ms), and the time share of the fused substep kernel. */
+int obgc_last_step_timing(const obgc_ctx* ctx, double* total_ms, double* substep_ms,
+                          int64_t* launches);
+
+/* Domain-integrated mass of a conserved group (conserved_tracers, NutrientsPlanktonDetritus/
+ * coupling_utils.jl:1-52): sum over cells of sum_n scale[n]*tracer_n, accumulated in FP64 with
+ * compensated summation.  group: 0 nitrogen, 1 carbon.  Result written to *total (host). */
+int obgc_tracer_budget(obgc_ctx* ctx, int32_t group, double* total, void* stream);
+
+/* ---------------------------------------------------------------------------------------
+ * Batched box models (src/BoxModel): many independent 0-D NutrientsPlanktonDetritus models
+ * ------------------------------------------------------------------------------------- */
+/*
+ * Advance n_models box models nsteps RK3 steps of dt from t0 (BoxModel time_step!,
+ * src/BoxModel/timesteppers.jl:30-93).  state: device FP64 array [n_models][OBGC_NUM_NAMED]
+ * (row per model, enum obgc_tracer columns) updated in place.  PAR: device FP64
+ * [n_models][3*nsteps] with the prescribed PAR at every RK3 stage time (t, t+8/15 dt, t+2/3 dt),
+ * or NULL with par_constant used.  params_per_model: optional device array of n_models
+ * obgc_npd_params (NULL = `p` for all).  record_every > 0 writes the state every record_every
+ * steps into record [n_records][n_models][OBGC_NUM_NAMED] (SpeedyOutput,
+ * src/BoxModel/output_writer.jl).  precision: OBGC_PREC_F64 or OBGC_PREC_F32 (state and math).
+ */
+int obgc_box_run(const obgc_npd_params* p, const obgc_npd_params* params_per_model,
+                 int64_t n_models, double* state, const double* PAR, double par_constant,
+                 double t0, double dt, int32_t nsteps, int32_t record_every, double* record,
+                 int32_t precision, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OBGC_H */

@@ -1,0 +1,205 @@
+"""ctypes mirror of include/obgc.h and the loader of libobgc.so.
+
+The structs below are field-for-field copies of the C declarations; tests check their sizes and
+offsets against the compiled library (obgc_struct_layout).  Loading fails loudly when the shared
+library has not been built: there is no CPU fallback for any entry point.
+"""
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libobgc.so")
+
+# ----------------------------------------------------------------------------- enums
+OBGC_OK = 0
+STATUS_NAMES = {
+    0: "OBGC_OK", 1: "OBGC_ERR_INVALID_ARGUMENT", 2: "OBGC_ERR_CUDA", 3: "OBGC_ERR_NOT_CONVERGED",
+    4: "OBGC_ERR_NAN", 5: "OBGC_ERR_UNSUPPORTED", 6: "OBGC_ERR_OUT_OF_MEMORY",
+    7: "OBGC_ERR_NO_DEVICE", 8: "OBGC_ERR_BUSY", 9: "OBGC_ERR_TIMEOUT",
+}
+F32, F64 = 0, 1
+PREC_F32, PREC_F64, PREC_MIXED = 0, 1, 2
+
+TRACER_NAMES = ["NO₃", "NH₄", "Fe", "N", "P", "Z", "T", "sPOM", "bPOM", "DOM", "sPON", "bPON",
+                "DON", "sPOC", "bPOC", "DOC", "D", "DIC", "Alk", "O₂", "S"]
+ASCII_NAMES = ["NO3", "NH4", "Fe", "N", "P", "Z", "T", "sPOM", "bPOM", "DOM", "sPON", "bPON",
+               "DON", "sPOC", "bPOC", "DOC", "D", "DIC", "Alk", "O2", "S"]
+NUM_NAMED = len(TRACER_NAMES)
+MAX_PASSIVE = 8
+NAME_INDEX = {n: i for i, n in enumerate(TRACER_NAMES)}
+NAME_INDEX.update({n: i for i, n in enumerate(ASCII_NAMES)})
+for _i, _n in enumerate(ASCII_NAMES):
+    globals()["OBGC_" + _n.upper()] = _i
+
+NUT_NITRATE_AMMONIA, NUT_NITRATE_AMMONIA_IRON, NUT_NUTRIENT = 0, 1, 2
+DET_TWO_PARTICLE, DET_VARIABLE_REDFIELD, DET_SINGLE, DET_NONE = 0, 1, 2, 3
+LIGHT_MONDO, LIGHT_ANALYTICAL = 0, 1
+LINEAR, QUADRATIC = 0, 1
+PRESET_LOBSTER, PRESET_NPZD = 0, 1
+SURFACE_DEFAULT, SURFACE_CONSTANT, SURFACE_FIELD = 0, 1, 2
+PERIODIC, BOUNDED, FLAT = 0, 1, 2
+ADVECTION_NONE, ADVECTION_WENO5 = 0, 1
+OUT_FCO2, OUT_PCO2, OUT_PH_FREE, OUT_PH_TOTAL, OUT_PH_SWS, OUT_H, OUT_CARBONATE, OUT_OMEGA = range(8)
+DENSITY_EOS80, DENSITY_CONSTANT = 0, 1
+
+
+# ----------------------------------------------------------------------------- structs
+_NPD_INT_FIELDS = ["nutrients", "detritus", "carbonate_system", "oxygen", "light_limitation",
+                   "has_temperature_coefficient", "phytoplankton_mortality_formulation",
+                   "grazing_concentration_formulation", "open_bottom", "reserved0"]
+_NPD_DBL_FIELDS = [
+    "nitrification_rate",
+    "nitrate_half_saturation", "ammonia_half_saturation", "iron_half_saturation",
+    "nitrate_ammonia_inhibition", "light_half_saturation", "phytoplankton_maximum_growth_rate",
+    "iron_ratio", "phytoplankton_exudation_fraction", "ammonia_fraction_of_exudate",
+    "temperature_coefficient", "phytoplankton_mortality_rate", "zooplankton_mortality_rate",
+    "zooplankton_excretion_rate", "phytoplankton_solid_waste_fraction",
+    "excretion_inorganic_fraction", "preference_for_phytoplankton", "maximum_grazing_rate",
+    "grazing_half_saturation", "zooplankton_assimilation_fraction",
+    "zooplankton_calcite_dissolution", "redfield_ratio", "carbon_calcite_ratio",
+    "zooplankton_gut_calcite_dissolution", "phytoplankton_chlorophyll_ratio",
+    "phytoplankton_sinking_speed", "zooplankton_sinking_speed",
+    "remineralisation_inorganic_fraction", "small_remineralisation_rate",
+    "large_remineralisation_rate", "dissolved_remineralisation_rate",
+    "small_solid_waste_fraction", "detritus_redfield_ratio", "small_particle_sinking_speed",
+    "large_particle_sinking_speed",
+    "detritus_remineralisation_rate", "small_particle_fraction", "detritus_sinking_speed",
+    "respiration_oxygen_nitrogen_ratio", "nitrification_oxygen_nitrogen_ratio",
+]
+
+
+class NPDParams(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in _NPD_INT_FIELDS] + [(n, C.c_double) for n in _NPD_DBL_FIELDS]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+    def copy(self):
+        out = NPDParams()
+        C.pointer(out)[0] = self
+        return out
+
+
+class TwoBandParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "water_red_attenuation", "water_blue_attenuation", "chlorophyll_red_attenuation",
+        "chlorophyll_blue_attenuation", "chlorophyll_red_exponent", "chlorophyll_blue_exponent",
+        "pigment_ratio", "phytoplankton_chlorophyll_ratio")]
+
+
+class Surface(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("reserved0", C.c_int32), ("value", C.c_double),
+                ("field", C.c_void_p)]
+
+
+class Grid(C.Structure):
+    _fields_ = [("Nx", C.c_int32), ("Ny", C.c_int32), ("Nz", C.c_int32),
+                ("topology_x", C.c_int32), ("topology_y", C.c_int32), ("reserved0", C.c_int32),
+                ("Lx", C.c_double), ("Ly", C.c_double), ("Lz", C.c_double),
+                ("stride_j", C.c_int64), ("stride_k", C.c_int64)]
+
+
+class CarbonOptions(C.Structure):
+    _fields_ = [("output", C.c_int32), ("density", C.c_int32), ("has_pressure", C.c_int32),
+                ("ph_given", C.c_int32), ("max_iters", C.c_int32), ("warm_start", C.c_int32),
+                ("density_value", C.c_double), ("initial_pH_guess", C.c_double),
+                ("atol", C.c_double), ("damping", C.c_double), ("armijo_constant", C.c_double),
+                ("min_damping", C.c_double), ("calcium_ion_per_salinity", C.c_double)]
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [("npd", NPDParams), ("light", TwoBandParams), ("surface", Surface),
+                ("grid", Grid), ("precision", C.c_int32), ("advection", C.c_int32),
+                ("n_passive", C.c_int32), ("carry_T", C.c_int32), ("carry_S", C.c_int32),
+                ("reserved0", C.c_int32)]
+
+
+class Fields(C.Structure):
+    _fields_ = [("tracers", C.c_void_p * NUM_NAMED), ("passive", C.c_void_p * MAX_PASSIVE),
+                ("u", C.c_void_p), ("v", C.c_void_p), ("w", C.c_void_p), ("PAR", C.c_void_p),
+                ("G", C.c_void_p * NUM_NAMED)]
+
+
+def default_twoband():
+    """TwoBandPhotosyntheticallyActiveRadiation defaults (src/Light/2band.jl:106-117)."""
+    return TwoBandParams(0.225, 0.0232, 0.037, 0.074, 0.629, 0.674, 0.7, 1.31)
+
+
+# ----------------------------------------------------------------------------- loader
+_lib = None
+
+
+class ObgcError(RuntimeError):
+    def __init__(self, status, where):
+        msg = ""
+        if _lib is not None:
+            raw = _lib.obgc_last_error_message()
+            msg = raw.decode() if raw else ""
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)} {msg}")
+        self.status = status
+
+
+def check(status, where):
+    if status != OBGC_OK:
+        raise ObgcError(status, where)
+    return status
+
+
+def _sig(lib, name, res, *args):
+    f = getattr(lib, name)
+    f.restype = res
+    f.argtypes = list(args)
+
+
+def load():
+    """Load libobgc.so (built by __graft_entry__.build()).  Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libobgc.so is not built ({LIB_PATH}); run __graft_entry__.build()")
+    lib = C.CDLL(LIB_PATH)
+    P, I32, I64, D, VP = C.POINTER, C.c_int32, C.c_int64, C.c_double, C.c_void_p
+    _sig(lib, "obgc_abi_version", C.c_int)
+    _sig(lib, "obgc_last_error_message", C.c_char_p)
+    _sig(lib, "obgc_kernel_launch_count", I64)
+    _sig(lib, "obgc_struct_layout", C.c_int, I32, P(I64), I32)
+    _sig(lib, "obgc_npd_preset", C.c_int, I32, P(NPDParams))
+    _sig(lib, "obgc_npd_required_tracers", C.c_int, P(NPDParams), P(I32), I32)
+    _sig(lib, "obgc_npd_drift_velocity", C.c_int, P(NPDParams), I32, I32, P(D))
+    _sig(lib, "obgc_npd_eval_point", C.c_int, P(NPDParams), I32, D, D, D, D, P(D), D, P(D))
+    _sig(lib, "obgc_npd_tendencies", C.c_int, P(NPDParams), P(Grid), I32, P(VP), VP, P(VP), D, VP)
+    _sig(lib, "obgc_twoband_par", C.c_int, P(TwoBandParams), P(Surface), P(Grid), I32, VP, VP, D, VP)
+    _sig(lib, "obgc_multiband_par", C.c_int, I32, P(D), P(D), P(D), P(D), P(Surface), P(Grid), I32,
+         VP, P(VP), VP, D, VP)
+    _sig(lib, "obgc_multiband_coefficients", C.c_int, I32, P(D), I32, P(D), P(D), P(D), P(D),
+         P(D), P(D), P(D))
+    _sig(lib, "obgc_euphotic_depth", C.c_int, P(Grid), I32, VP, VP, D, VP)
+    _sig(lib, "obgc_carbon_default_options", C.c_int, P(CarbonOptions))
+    _sig(lib, "obgc_carbon_chemistry", C.c_int, P(CarbonOptions), I64, I32, VP, VP, VP, VP, VP, VP,
+         VP, VP, VP, VP, VP, VP)
+    _sig(lib, "obgc_carbon_chemistry_point", C.c_int, P(CarbonOptions), D, D, D, D, D, D, D, D, P(D))
+    _sig(lib, "obgc_create", C.c_int, P(ModelDesc), P(VP))
+    _sig(lib, "obgc_destroy", C.c_int, VP)
+    _sig(lib, "obgc_bind_fields", C.c_int, VP, P(Fields))
+    _sig(lib, "obgc_update_state", C.c_int, VP, D, VP)
+    _sig(lib, "obgc_compute_tendencies", C.c_int, VP, D, VP)
+    _sig(lib, "obgc_step", C.c_int, VP, D, D, I32, VP)
+    _sig(lib, "obgc_step_graph", C.c_int, VP, D, D, I32, VP)
+    _sig(lib, "obgc_last_step_timing", C.c_int, VP, P(D), P(D), P(I64))
+    _sig(lib, "obgc_tracer_budget", C.c_int, VP, I32, P(D), VP)
+    _sig(lib, "obgc_box_run", C.c_int, P(NPDParams), VP, I64, VP, VP, D, D, D, I32, I32, VP, I32, VP)
+    _lib = lib
+    return lib
+
+
+# Every symbol include/obgc.h declares (checked by the CPU test suite).
+EXPORTED = [
+    "obgc_abi_version", "obgc_last_error_message", "obgc_kernel_launch_count",
+    "obgc_npd_preset", "obgc_npd_required_tracers", "obgc_npd_drift_velocity",
+    "obgc_npd_eval_point", "obgc_npd_tendencies", "obgc_twoband_par", "obgc_multiband_par",
+    "obgc_multiband_coefficients", "obgc_euphotic_depth", "obgc_carbon_default_options",
+    "obgc_carbon_chemistry", "obgc_carbon_chemistry_point", "obgc_create", "obgc_destroy",
+    "obgc_bind_fields", "obgc_update_state", "obgc_compute_tendencies", "obgc_step",
+    "obgc_step_graph", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run",
+]

@@ -1,0 +1,108 @@
+/*
+ * obgc_oracle.h — TEST INFRASTRUCTURE, NOT THE PRODUCT.
+ *
+ * A CPU, FP64 restatement of OceanBioME.jl's tracer-tendency path (NutrientsPlanktonDetritus
+ * functors, TwoBand/MultiBand light, CarbonChemistry + root solvers, BoxModel RK3) plus a
+ * restatement of the third-party Oceananigans pieces the path runs inside (WENO5 tracer
+ * advection, RK3 substeps, vertically implicit diffusion).  Only tests/, __graft_entry__.smoke()
+ * and bench.py's CPU-baseline leg may load it, and only as the checker.  It shares nothing with
+ * the CUDA product but the parameter structs of include/obgc.h (the interface).
+ *
+ * Parity pins: the reference's own known-answer tests (test/test_light.jl, test/test_solvers.jl,
+ * test/test_gasexchange_carbon_chem.jl, test/test_NutrientsPlanktonDetritus.jl) and the
+ * CarbonChemistry doctest digits (src/Models/CarbonChemistry/carbon_chemistry.jl:55-62).  WENO5
+ * and RK3 come from Oceananigans, which is absent here: those are restated from the published
+ * methods and are "parity unpinned" against the reference.
+ */
+#ifndef OBGC_ORACLE_H
+#define OBGC_ORACLE_H
+#include <stdint.h>
+#include "../include/obgc.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- NutrientsPlanktonDetritus ---- */
+int or_npd_preset(int preset, obgc_npd_params* out);
+int or_npd_required_tracers(const obgc_npd_params* p, int32_t* names, int cap);
+double or_npd_tendency(const obgc_npd_params* p, int name, const double* v, double PAR);
+void or_npd_drift_profile(const obgc_npd_params* p, int name, int Nz, double* w, int* drifts);
+
+/* ---- light ---- */
+void or_twoband_column(const obgc_twoband_params* lp, int Nz, const double* zc, const double* zf,
+                       const double* P, double PAR0, double* PAR);
+void or_multiband_column(int Nz, const double* zc, double kw, double e, double chi,
+                         const double* Chl, double surface, double* PAR);
+double or_euphotic_depth_column(int Nz, const double* zc, const double* PAR, double PAR_top_halo,
+                                double cutoff);
+void or_multiband_coefficients(int nbands, const double* band_edges, int nbase,
+                               const double* lambda, const double* kw, const double* e,
+                               const double* chi, double* okw, double* oe, double* ochi);
+double or_default_surface_PAR(double t);
+
+/* ---- carbon chemistry ---- */
+enum { OR_K0 = 0, OR_K1, OR_K2, OR_KB, OR_KW, OR_KS, OR_KF, OR_KP1, OR_KP2, OR_KP3, OR_KSI,
+       OR_KSP_CALCITE, OR_KSP_ARAGONITE, OR_NUM_K };
+double or_equilibrium_constant(int which, double Tk, double S, int has_P, double P);
+double or_pressure_correction(int which, double Tk, double P);
+double or_first_virial(double Tk);
+double or_cross_virial(double Tk);
+double or_density_eos80(double T, double S, double Pbar);
+int or_carbon_default_options(obgc_carbon_options* o);
+int or_carbon_chemistry(const obgc_carbon_options* o, double DIC, double Alk, double T, double S,
+                        double silicate, double phosphate, double P, double pH, double* out,
+                        int* iters);
+void or_carbon_chemistry_batch(const obgc_carbon_options* o, int64_t n, const double* DIC,
+                               const double* Alk, const double* T, const double* S,
+                               const double* Si, const double* PO4, const double* P,
+                               const double* pH, double* out, int nthreads);
+
+/* ---- root solvers (src/Utils/solvers.jl) on the test functions of test/test_solvers.jl ---- */
+enum { OR_SOLVER_NEWTON = 0, OR_SOLVER_NEWTON_SAFE, OR_SOLVER_BISECTION, OR_SOLVER_DAMPED };
+double or_solve_test_function(int solver, int fid, double x0, double x1, double damping,
+                              double pa, double pb);
+
+/* ---- BoxModel ---- */
+void or_box_run(const obgc_npd_params* p, double* v, const double* PAR_stages, double PAR_const,
+                double t0, double dt, int nsteps);
+
+/* ---- 3-D fused model: WENO5 + drift + BGC + TwoBand light + RK3 ---- */
+typedef struct or_model3d {
+    obgc_npd_params npd;
+    obgc_twoband_params light;
+    int32_t surface_kind;        /* enum obgc_surface_par (FIELD not supported here) */
+    int32_t advection;           /* enum obgc_advection */
+    double surface_value;
+    obgc_grid grid;              /* strides ignored: arrays are dense [Nz][Ny][Nx]   */
+    int32_t n_tracers;           /* number of advected tracers                         */
+    int32_t names[32];           /* enum obgc_tracer per tracer, or -1 for passive     */
+} or_model3d;
+/* state: [n_tracers][Nz*Ny*Nx]; u, v, w: [Nz*Ny*Nx] or NULL. */
+void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,
+               const double* w, double t, double dt, int nsteps, int nthreads);
+void or_par3d(const or_model3d* m, const double* state, double t, double* PAR, int nthreads);
+
+/* ---- batched uneven columns with vertically implicit diffusion ---- */
+typedef struct or_column {
+    int32_t Nz;
+    int32_t reserved;
+    double dz;
+    double surface_PAR;          /* constant surface PAR (W/m2)                          */
+    double mu0;                  /* phytoplankton_maximum_growth_rate override           */
+} or_column;
+/* state: per column [n_tracers][Nz] (offsets given); kappa: per column Nz+1 face values. */
+void or_columns_run(const obgc_npd_params* p, const obgc_twoband_params* lp, int n_cols,
+                    const or_column* cols, const int64_t* state_offsets,
+                    const int64_t* kappa_offsets, int n_tracers, const int32_t* names,
+                    double* state, const double* kappa, double t0, double dt, int nsteps,
+                    int nthreads);
+
+/* ---- ScaleNegativeTracers (src/Utils/negative_tracers.jl:250-276) ---- */
+void or_scale_negatives(int64_t n, int ntr, double* const* fields, const double* scalefactors,
+                        double invalid_fill_value);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,322 @@
+/*
+ * or_step.c — TEST INFRASTRUCTURE (the oracle).  FP64 time stepping around the BGC functors:
+ *  - BoxModel RK3 (src/BoxModel/timesteppers.jl:30-93): U += dt*(gamma*G + zeta*G-), with
+ *    Oceananigans' RungeKutta3 coefficients gamma = (8/15, 5/12, 3/4), zeta = (-, -17/60, -5/12)
+ *    and stage times t, t + 8/15 dt, t + 2/3 dt.
+ *  - 3-D tracer step: flux-form WENO5 advection by the model velocity and by each tracer's drift
+ *    velocity (Oceananigans div_Uc; restated from the published WENO-Z scheme of Borges et al.
+ *    2008 with p = 2 and eps = 1e-8, order reduced to WENO3 and first-order upwind next to Bounded
+ *    walls), the BGC functors, TwoBand PAR recomputed from the state at every stage
+ *    (update_biogeochemical_state! after every substep), RK3.  Parity with Oceananigans itself is
+ *    unpinned (it is not in this container).
+ *  - Columns with vertically implicit diffusion after every explicit substep (Oceananigans
+ *    VerticallyImplicitTimeDiscretization, stage dt = (gamma + zeta) dt), zero-flux walls.
+ *  - ScaleNegativeTracers (src/Utils/negative_tracers.jl:250-276).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include "obgc_oracle.h"
+
+static const double RK_G[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
+static const double RK_Z[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
+static const double RK_C[3] = {0.0, 8.0 / 15.0, 2.0 / 3.0};
+
+/* ------------------------------------------------------------------ WENO ---------- */
+static double weno5(double v1, double v2, double v3, double v4, double v5) {
+    const double eps = 1e-8;
+    double q0 = (2 * v1 - 7 * v2 + 11 * v3) / 6;
+    double q1 = (-v2 + 5 * v3 + 2 * v4) / 6;
+    double q2 = (2 * v3 + 5 * v4 - v5) / 6;
+    double a = v1 - 2 * v2 + v3, b = v1 - 4 * v2 + 3 * v3;
+    double b0 = 13.0 / 12.0 * a * a + 0.25 * b * b;
+    a = v2 - 2 * v3 + v4; b = v2 - v4;
+    double b1 = 13.0 / 12.0 * a * a + 0.25 * b * b;
+    a = v3 - 2 * v4 + v5; b = 3 * v3 - 4 * v4 + v5;
+    double b2 = 13.0 / 12.0 * a * a + 0.25 * b * b;
+    double tau = fabs(b0 - b2);
+    double r0 = tau / (b0 + eps), r1 = tau / (b1 + eps), r2 = tau / (b2 + eps);
+    double a0 = 0.1 * (1 + r0 * r0), a1 = 0.6 * (1 + r1 * r1), a2 = 0.3 * (1 + r2 * r2);
+    return (a0 * q0 + a1 * q1 + a2 * q2) / (a0 + a1 + a2);
+}
+static double weno3(double v1, double v2, double v3) {
+    const double eps = 1e-8;
+    double q0 = (-v1 + 3 * v2) / 2, q1 = (v2 + v3) / 2;
+    double b0 = (v2 - v1) * (v2 - v1), b1 = (v3 - v2) * (v3 - v2);
+    double tau = fabs(b0 - b1);
+    double r0 = tau / (b0 + eps), r1 = tau / (b1 + eps);
+    double a0 = (1.0 / 3.0) * (1 + r0 * r0), a1 = (2.0 / 3.0) * (1 + r1 * r1);
+    return (a0 * q0 + a1 * q1) / (a0 + a1);
+}
+
+/* Upwind-biased value at face f (between cells f-1 and f) of a line of N cells with stride s. */
+static double face_value(const double* c, long s, int N, int periodic, int f, double U) {
+#define C(m) c[(long)(periodic ? (((m) % N) + N) % N : (m)) * s]
+    if (periodic) {
+        if (U > 0) return weno5(C(f - 3), C(f - 2), C(f - 1), C(f), C(f + 1));
+        return weno5(C(f + 2), C(f + 1), C(f), C(f - 1), C(f - 2));
+    }
+    int b = f < N - f ? f : N - f;
+    if (b == 0) return f == 0 ? C(0) : C(N - 1);
+    if (b >= 3) {
+        if (U > 0) return weno5(C(f - 3), C(f - 2), C(f - 1), C(f), C(f + 1));
+        return weno5(C(f + 2), C(f + 1), C(f), C(f - 1), C(f - 2));
+    }
+    if (b == 2) {
+        if (U > 0) return weno3(C(f - 2), C(f - 1), C(f));
+        return weno3(C(f + 1), C(f), C(f - 1));
+    }
+    return U > 0 ? C(f - 1) : C(f);
+#undef C
+}
+
+/* ------------------------------------------------------------------ box ---------- */
+void or_box_run(const obgc_npd_params* p, double* v, const double* PAR_stages, double PAR_const,
+                double t0, double dt, int nsteps) {
+    int32_t names[32];
+    int n = or_npd_required_tracers(p, names, 32);
+    double G[OBGC_NUM_NAMED] = {0}, Gm[OBGC_NUM_NAMED] = {0};
+    (void)t0;
+    for (int s = 0; s < nsteps; s++) {
+        for (int st = 0; st < 3; st++) {
+            double PAR = PAR_stages ? PAR_stages[3 * s + st] : PAR_const;
+            for (int q = 0; q < n; q++) G[names[q]] = or_npd_tendency(p, names[q], v, PAR);
+            for (int q = 0; q < n; q++) {
+                int nm = names[q];
+                if (st == 0) v[nm] += dt * RK_G[0] * G[nm];
+                else v[nm] += dt * (RK_G[st] * G[nm] + RK_Z[st] * Gm[nm]);
+            }
+            memcpy(Gm, G, sizeof(G));
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ 3-D ---------- */
+static double surface_par(const or_model3d* m, double t) {
+    return m->surface_kind == OBGC_SURFACE_PAR_CONSTANT ? m->surface_value : or_default_surface_PAR(t);
+}
+
+static int slot_of(const or_model3d* m, int name) {
+    for (int q = 0; q < m->n_tracers; q++) if (m->names[q] == name) return q;
+    return -1;
+}
+
+void or_par3d(const or_model3d* m, const double* state, double t, double* PAR, int nthreads) {
+    const obgc_grid* g = &m->grid;
+    int Nx = g->Nx, Ny = g->Ny, Nz = g->Nz;
+    long NN = (long)Nx * Ny;
+    double dz = g->Lz / Nz;
+    double* zc = malloc(sizeof(double) * Nz);
+    double* zf = malloc(sizeof(double) * (Nz + 1));
+    for (int k = 0; k <= Nz; k++) zf[k] = -g->Lz + k * dz;
+    for (int k = 0; k < Nz; k++) zc[k] = -g->Lz + (k + 0.5) * dz;
+    int sP = slot_of(m, OBGC_P);
+    double PAR0 = surface_par(m, t);
+#pragma omp parallel num_threads(nthreads)
+    {
+        double* col = malloc(sizeof(double) * Nz);
+        double* out = malloc(sizeof(double) * Nz);
+#pragma omp for schedule(static)
+        for (long c = 0; c < NN; c++) {
+            for (int k = 0; k < Nz; k++) col[k] = state[(long)sP * NN * Nz + k * NN + c];
+            or_twoband_column(&m->light, Nz, zc, zf, col, PAR0, out);
+            for (int k = 0; k < Nz; k++) PAR[k * NN + c] = out[k];
+        }
+        free(col); free(out);
+    }
+    free(zc); free(zf);
+}
+
+void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,
+               const double* w, double t, double dt, int nsteps, int nthreads) {
+    const obgc_grid* g = &m->grid;
+    int Nx = g->Nx, Ny = g->Ny, Nz = g->Nz, nt = m->n_tracers;
+    long NN = (long)Nx * Ny, N = NN * Nz;
+    double dx = g->Lx / Nx, dy = g->Ly / Ny, dz = g->Lz / Nz;
+    int px = g->topology_x == OBGC_PERIODIC, py = g->topology_y == OBGC_PERIODIC;
+    int flat_y = g->topology_y == OBGC_FLAT || Ny == 1;
+    int flat_x = g->topology_x == OBGC_FLAT;
+    double* G = calloc((size_t)nt * N, sizeof(double));
+    double* Gm = calloc((size_t)nt * N, sizeof(double));
+    double* PAR = malloc(sizeof(double) * N);
+    double* drift = calloc((size_t)nt * (Nz + 1), sizeof(double));
+    int* has_drift = calloc(nt, sizeof(int));
+    int32_t req[32];
+    int nreq = or_npd_required_tracers(&m->npd, req, 32);
+    int is_bgc[32] = {0};
+    for (int q = 0; q < nt; q++) {
+        for (int r = 0; r < nreq; r++) if (m->names[q] == req[r]) is_bgc[q] = 1;
+        if (m->names[q] >= 0 && m->advection) {
+            or_npd_drift_profile(&m->npd, m->names[q], Nz, drift + (long)q * (Nz + 1), &has_drift[q]);
+            if (has_drift[q]) {
+                int nz = 0;
+                for (int f = 0; f <= Nz; f++) nz |= drift[(long)q * (Nz + 1) + f] != 0.0;
+                has_drift[q] = nz;
+            }
+        }
+    }
+    for (int s = 0; s < nsteps; s++) {
+        for (int st = 0; st < 3; st++) {
+            double ts = t + RK_C[st] * dt;
+            or_par3d(m, state, ts, PAR, nthreads);
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+            for (long c = 0; c < N; c++) {
+                int i = (int)(c % Nx), j = (int)((c / Nx) % Ny), k = (int)(c / NN);
+                double vals[OBGC_NUM_NAMED] = {0};
+                for (int q = 0; q < nt; q++) if (m->names[q] >= 0) vals[m->names[q]] = state[(long)q * N + c];
+                for (int q = 0; q < nt; q++) {
+                    double tend = is_bgc[q] ? or_npd_tendency(&m->npd, m->names[q], vals, PAR[c]) : 0.0;
+                    if (m->advection) {
+                        const double* cq = state + (long)q * N;
+                        double adv = 0.0;
+                        if (!flat_x && u) {
+                            const double* line = cq + (long)k * NN + (long)j * Nx;
+                            int f0 = i, f1 = i + 1;
+                            double U0 = (px || (f0 > 0 && f0 < Nx)) ? u[(long)k * NN + (long)j * Nx + (f0 % Nx)] : 0.0;
+                            double U1 = (px || (f1 > 0 && f1 < Nx)) ? u[(long)k * NN + (long)j * Nx + (f1 % Nx)] : 0.0;
+                            double F0 = U0 != 0.0 ? U0 * face_value(line, 1, Nx, px, f0, U0) : 0.0;
+                            double F1 = U1 != 0.0 ? U1 * face_value(line, 1, Nx, px, f1, U1) : 0.0;
+                            adv += (F1 - F0) / dx;
+                        }
+                        if (!flat_y && v) {
+                            const double* line = cq + (long)k * NN + i;
+                            int f0 = j, f1 = j + 1;
+                            double V0 = (py || (f0 > 0 && f0 < Ny)) ? v[(long)k * NN + (long)(f0 % Ny) * Nx + i] : 0.0;
+                            double V1 = (py || (f1 > 0 && f1 < Ny)) ? v[(long)k * NN + (long)(f1 % Ny) * Nx + i] : 0.0;
+                            double F0 = V0 != 0.0 ? V0 * face_value(line, Nx, Ny, py, f0, V0) : 0.0;
+                            double F1 = V1 != 0.0 ? V1 * face_value(line, Nx, Ny, py, f1, V1) : 0.0;
+                            adv += (F1 - F0) / dy;
+                        }
+                        const double* zline = cq + (long)j * Nx + i;
+                        if (w) {
+                            double W0 = (k > 0) ? w[(long)k * NN + (long)j * Nx + i] : 0.0;
+                            double W1 = (k + 1 < Nz) ? w[(long)(k + 1) * NN + (long)j * Nx + i] : 0.0;
+                            double F0 = W0 != 0.0 ? W0 * face_value(zline, NN, Nz, 0, k, W0) : 0.0;
+                            double F1 = W1 != 0.0 ? W1 * face_value(zline, NN, Nz, 0, k + 1, W1) : 0.0;
+                            adv += (F1 - F0) / dz;
+                        }
+                        if (has_drift[q]) {
+                            const double* wd = drift + (long)q * (Nz + 1);
+                            double W0 = wd[k], W1 = wd[k + 1];
+                            double F0 = W0 != 0.0 ? W0 * face_value(zline, NN, Nz, 0, k, W0) : 0.0;
+                            double F1 = W1 != 0.0 ? W1 * face_value(zline, NN, Nz, 0, k + 1, W1) : 0.0;
+                            adv += (F1 - F0) / dz;
+                        }
+                        tend -= adv;
+                    }
+                    G[(long)q * N + c] = tend;
+                }
+            }
+            double g = RK_G[st], z = RK_Z[st];
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+            for (long x = 0; x < (long)nt * N; x++) {
+                if (st == 0) state[x] += dt * g * G[x];
+                else state[x] += dt * (g * G[x] + z * Gm[x]);
+            }
+            double* tmp = G; G = Gm; Gm = tmp;
+        }
+        t += dt;
+    }
+    free(G); free(Gm); free(PAR); free(drift); free(has_drift);
+}
+
+/* ------------------------------------------------------------------ columns ---------- */
+/* Thomas solve of (I - dts * d/dz kappa d/dz) x = rhs on a column with zero-flux walls. */
+static void implicit_diffusion(int Nz, double dz, const double* kf, double dts, double* x, double* cp, double* dp) {
+    double r = dts / (dz * dz);
+    for (int k = 0; k < Nz; k++) {
+        double lo = k > 0 ? -r * kf[k] : 0.0;
+        double up = k < Nz - 1 ? -r * kf[k + 1] : 0.0;
+        double di = 1 - lo - up;
+        if (k == 0) { cp[0] = up / di; dp[0] = x[0] / di; }
+        else {
+            double den = di - lo * cp[k - 1];
+            cp[k] = up / den;
+            dp[k] = (x[k] - lo * dp[k - 1]) / den;
+        }
+    }
+    x[Nz - 1] = dp[Nz - 1];
+    for (int k = Nz - 2; k >= 0; k--) x[k] = dp[k] - cp[k] * x[k + 1];
+}
+
+void or_columns_run(const obgc_npd_params* p0, const obgc_twoband_params* lp, int n_cols,
+                    const or_column* cols, const int64_t* so, const int64_t* ko,
+                    int nt, const int32_t* names, double* state, const double* kappa,
+                    double t0, double dt, int nsteps, int nthreads) {
+    (void)t0;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4)
+    for (int c = 0; c < n_cols; c++) {
+        obgc_npd_params p = *p0;
+        p.phytoplankton_maximum_growth_rate = cols[c].mu0;
+        int Nz = cols[c].Nz;
+        double dz = cols[c].dz;
+        double* U = state + so[c];
+        const double* kf = kappa + ko[c];
+        double* G = calloc((size_t)nt * Nz, sizeof(double));
+        double* Gm = calloc((size_t)nt * Nz, sizeof(double));
+        double* PAR = malloc(sizeof(double) * Nz);
+        double* Pcol = malloc(sizeof(double) * Nz);
+        double* zc = malloc(sizeof(double) * (Nz + 1));
+        double* zf = malloc(sizeof(double) * (Nz + 1));
+        double* wd = malloc(sizeof(double) * (size_t)nt * (Nz + 1));
+        int* hd = calloc(nt, sizeof(int));
+        double* cp = malloc(sizeof(double) * Nz);
+        double* dp = malloc(sizeof(double) * Nz);
+        for (int k = 0; k <= Nz; k++) zf[k] = -Nz * dz + k * dz;
+        for (int k = 0; k < Nz; k++) zc[k] = -Nz * dz + (k + 0.5) * dz;
+        int sP = -1;
+        for (int q = 0; q < nt; q++) {
+            if (names[q] == OBGC_P) sP = q;
+            or_npd_drift_profile(&p, names[q], Nz, wd + (long)q * (Nz + 1), &hd[q]);
+        }
+        int32_t req[32];
+        int nreq = or_npd_required_tracers(&p, req, 32);
+        for (int s = 0; s < nsteps; s++) {
+            for (int st = 0; st < 3; st++) {
+                for (int k = 0; k < Nz; k++) Pcol[k] = U[(long)sP * Nz + k];
+                or_twoband_column(lp, Nz, zc, zf, Pcol, cols[c].surface_PAR, PAR);
+                for (int k = 0; k < Nz; k++) {
+                    double vals[OBGC_NUM_NAMED] = {0};
+                    for (int q = 0; q < nt; q++) vals[names[q]] = U[(long)q * Nz + k];
+                    for (int q = 0; q < nt; q++) {
+                        int bgc = 0;
+                        for (int r = 0; r < nreq; r++) bgc |= req[r] == names[q];
+                        double tend = bgc ? or_npd_tendency(&p, names[q], vals, PAR[k]) : 0.0;
+                        if (hd[q]) {
+                            const double* w = wd + (long)q * (Nz + 1);
+                            const double* line = U + (long)q * Nz;
+                            double W0 = w[k], W1 = w[k + 1];
+                            double F0 = W0 != 0.0 ? W0 * face_value(line, 1, Nz, 0, k, W0) : 0.0;
+                            double F1 = W1 != 0.0 ? W1 * face_value(line, 1, Nz, 0, k + 1, W1) : 0.0;
+                            tend -= (F1 - F0) / dz;
+                        }
+                        G[(long)q * Nz + k] = tend;
+                    }
+                }
+                double g = RK_G[st], z = RK_Z[st];
+                for (long x = 0; x < (long)nt * Nz; x++)
+                    U[x] += st == 0 ? dt * g * G[x] : dt * (g * G[x] + z * Gm[x]);
+                for (int q = 0; q < nt; q++) implicit_diffusion(Nz, dz, kf, (g + z) * dt, U + (long)q * Nz, cp, dp);
+                double* tmp = G; G = Gm; Gm = tmp;
+            }
+        }
+        free(G); free(Gm); free(PAR); free(Pcol); free(zc); free(zf); free(wd); free(hd); free(cp); free(dp);
+    }
+}
+
+/* ------------------------------------------------------------------ negatives ---------- */
+void or_scale_negatives(int64_t n, int ntr, double* const* fields, const double* sf, double fill) {
+    for (int64_t c = 0; c < n; c++) {
+        double t = 0.0, p = 0.0;
+        for (int q = 0; q < ntr; q++) {
+            double v = fields[q][c];
+            t += v * sf[q];
+            if (v > 0) p += v * sf[q];
+        }
+        t = t < 0 ? fill : t;
+        for (int q = 0; q < ntr; q++) {
+            double v = fields[q][c];
+            fields[q][c] = (!isfinite(v) || v > 0) ? v * t / p : 0.0;
+        }
+    }
+}

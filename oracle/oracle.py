@@ -1,0 +1,277 @@
+"""ctypes wrapper of liboracle.so — TEST INFRASTRUCTURE, NOT THE PRODUCT.
+
+The oracle is a CPU FP64 restatement of OceanBioME.jl's tracer-tendency path (see
+obgc_oracle.h).  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as
+the checker.  It reuses only the parameter-struct mirrors of include/obgc.h.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from obgc import _abi as A
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(_HERE, "liboracle.so")
+_lib = None
+
+NUM_K = 13
+K0, K1, K2, KB, KW, KS, KF, KP1, KP2, KP3, KSI, KSP_CALCITE, KSP_ARAGONITE = range(NUM_K)
+NEWTON, NEWTON_SAFE, BISECTION, DAMPED = range(4)
+
+
+class Model3D(C.Structure):
+    _fields_ = [("npd", A.NPDParams), ("light", A.TwoBandParams), ("surface_kind", C.c_int32),
+                ("advection", C.c_int32), ("surface_value", C.c_double), ("grid", A.Grid),
+                ("n_tracers", C.c_int32), ("names", C.c_int32 * 32)]
+
+
+class Column(C.Structure):
+    _fields_ = [("Nz", C.c_int32), ("reserved", C.c_int32), ("dz", C.c_double),
+                ("surface_PAR", C.c_double), ("mu0", C.c_double)]
+
+
+def build():
+    """Compile liboracle.so with the Makefile beside this file (gcc, a few seconds)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        P, D, I32, I64, VP = C.POINTER, C.c_double, C.c_int32, C.c_int64, C.c_void_p
+        L.or_npd_preset.argtypes = [C.c_int, P(A.NPDParams)]
+        L.or_npd_required_tracers.argtypes = [P(A.NPDParams), P(I32), C.c_int]
+        L.or_npd_tendency.argtypes = [P(A.NPDParams), C.c_int, P(D), D]
+        L.or_npd_tendency.restype = D
+        L.or_npd_drift_profile.argtypes = [P(A.NPDParams), C.c_int, C.c_int, P(D), P(C.c_int)]
+        L.or_twoband_column.argtypes = [P(A.TwoBandParams), C.c_int, P(D), P(D), P(D), D, P(D)]
+        L.or_multiband_column.argtypes = [C.c_int, P(D), D, D, D, P(D), D, P(D)]
+        L.or_euphotic_depth_column.argtypes = [C.c_int, P(D), P(D), D, D]
+        L.or_euphotic_depth_column.restype = D
+        L.or_multiband_coefficients.argtypes = [C.c_int, P(D), C.c_int, P(D), P(D), P(D), P(D), P(D), P(D), P(D)]
+        L.or_default_surface_PAR.argtypes = [D]
+        L.or_default_surface_PAR.restype = D
+        L.or_equilibrium_constant.argtypes = [C.c_int, D, D, C.c_int, D]
+        L.or_equilibrium_constant.restype = D
+        L.or_pressure_correction.argtypes = [C.c_int, D, D]
+        L.or_pressure_correction.restype = D
+        L.or_first_virial.argtypes = [D]
+        L.or_first_virial.restype = D
+        L.or_cross_virial.argtypes = [D]
+        L.or_cross_virial.restype = D
+        L.or_density_eos80.argtypes = [D, D, D]
+        L.or_density_eos80.restype = D
+        L.or_carbon_default_options.argtypes = [P(A.CarbonOptions)]
+        L.or_carbon_chemistry.argtypes = [P(A.CarbonOptions), D, D, D, D, D, D, D, D, P(D), P(C.c_int)]
+        L.or_carbon_chemistry_batch.argtypes = [P(A.CarbonOptions), I64, P(D), P(D), P(D), P(D),
+                                                VP, VP, VP, VP, P(D), C.c_int]
+        L.or_solve_test_function.argtypes = [C.c_int, C.c_int, D, D, D, D, D]
+        L.or_solve_test_function.restype = D
+        L.or_box_run.argtypes = [P(A.NPDParams), P(D), VP, D, D, D, C.c_int]
+        L.or_step3d.argtypes = [P(Model3D), P(D), VP, VP, VP, D, D, C.c_int, C.c_int]
+        L.or_par3d.argtypes = [P(Model3D), P(D), D, P(D), C.c_int]
+        L.or_columns_run.argtypes = [P(A.NPDParams), P(A.TwoBandParams), C.c_int, P(Column), P(I64),
+                                     P(I64), C.c_int, P(I32), P(D), P(D), D, D, C.c_int, C.c_int]
+        L.or_scale_negatives.argtypes = [I64, C.c_int, P(P(D)), P(D), D]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _opt(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def nthreads():
+    return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------- NPD
+def preset(name):
+    p = A.NPDParams()
+    lib().or_npd_preset({"LOBSTER": A.PRESET_LOBSTER, "NPZD": A.PRESET_NPZD}[name], C.byref(p))
+    return p
+
+
+def required_tracers(p):
+    buf = (C.c_int32 * 32)()
+    n = lib().or_npd_required_tracers(C.byref(p), buf, 32)
+    return [buf[i] for i in range(n)]
+
+
+def tendency(p, name, values, PAR):
+    v = np.zeros(A.NUM_NAMED)
+    for k, x in values.items():
+        v[A.NAME_INDEX[k] if isinstance(k, str) else k] = x
+    idx = A.NAME_INDEX[name] if isinstance(name, str) else name
+    return lib().or_npd_tendency(C.byref(p), idx, _dp(v), PAR)
+
+
+def tendencies_array(p, vals, PAR):
+    """vals: (n, NUM_NAMED) array, PAR (n,) -> (n, NUM_NAMED) tendencies (0 where not required)."""
+    out = np.zeros_like(vals)
+    names = required_tracers(p)
+    L = lib()
+    for c in range(vals.shape[0]):
+        row = np.ascontiguousarray(vals[c])
+        for nm in names:
+            out[c, nm] = L.or_npd_tendency(C.byref(p), nm, _dp(row), float(PAR[c]))
+    return out
+
+
+def drift_profile(p, name, Nz):
+    w = np.zeros(Nz + 1)
+    d = C.c_int(0)
+    lib().or_npd_drift_profile(C.byref(p), A.NAME_INDEX[name] if isinstance(name, str) else name, Nz, _dp(w), C.byref(d))
+    return w if d.value else None
+
+
+# ---------------------------------------------------------------------------- light
+def twoband_column(lp, zc, zf, P, PAR0):
+    zc, zf, P = (np.ascontiguousarray(x, dtype=np.float64) for x in (zc, zf, P))
+    out = np.zeros(len(zc))
+    lib().or_twoband_column(C.byref(lp), len(zc), _dp(zc), _dp(zf), _dp(P), PAR0, _dp(out))
+    return out
+
+
+def multiband_column(zc, kw, e, chi, Chl, surface):
+    zc, Chl = (np.ascontiguousarray(x, dtype=np.float64) for x in (zc, Chl))
+    out = np.zeros(len(zc))
+    lib().or_multiband_column(len(zc), _dp(zc), kw, e, chi, _dp(Chl), surface, _dp(out))
+    return out
+
+
+def multiband_coefficients(bands, lam, kw, e, chi):
+    edges = np.array([x for b in bands for x in b], dtype=np.float64)
+    lam, kw, e, chi = (np.ascontiguousarray(x, dtype=np.float64) for x in (lam, kw, e, chi))
+    n = len(bands)
+    okw, oe, ochi = np.zeros(n), np.zeros(n), np.zeros(n)
+    lib().or_multiband_coefficients(n, _dp(edges), len(lam), _dp(lam), _dp(kw), _dp(e), _dp(chi),
+                                    _dp(okw), _dp(oe), _dp(ochi))
+    return okw, oe, ochi
+
+
+def euphotic_depth_column(zc_with_halo, PAR, PAR_top_halo, cutoff=1e-3):
+    zc, PAR = (np.ascontiguousarray(x, dtype=np.float64) for x in (zc_with_halo, PAR))
+    return lib().or_euphotic_depth_column(len(PAR), _dp(zc), _dp(PAR), PAR_top_halo, cutoff)
+
+
+def default_surface_PAR(t):
+    return lib().or_default_surface_PAR(t)
+
+
+# ---------------------------------------------------------------------------- carbon
+def K(which, Tk, S, P=None):
+    return lib().or_equilibrium_constant(which, Tk, S, 0 if P is None else 1, 0.0 if P is None else P)
+
+
+def pressure_correction(which, Tk, P):
+    return lib().or_pressure_correction(which, Tk, P)
+
+
+def density_eos80(T, S, P):
+    return lib().or_density_eos80(T, S, P)
+
+
+def carbon_options(**kw):
+    o = A.CarbonOptions()
+    lib().or_carbon_default_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def carbon_chemistry(DIC, T, S, Alk=0.0, pH=None, P=None, silicate=0.0, phosphate=0.0,
+                     output=A.OUT_FCO2, density=None, return_iters=False, **kw):
+    o = carbon_options(output=output, **kw)
+    if density is not None:
+        o.density, o.density_value = A.DENSITY_CONSTANT, density
+    if pH is not None:
+        o.ph_given = 1
+    if P is not None:
+        o.has_pressure = 1
+    out = C.c_double(0)
+    it = C.c_int(0)
+    lib().or_carbon_chemistry(C.byref(o), DIC, Alk, T, S, silicate, phosphate,
+                              0.0 if P is None else P, 0.0 if pH is None else pH, C.byref(out), C.byref(it))
+    return (out.value, it.value) if return_iters else out.value
+
+
+def carbon_chemistry_batch(o, DIC, Alk, T, S, Si=None, PO4=None, P=None, pH=None, threads=None):
+    arrs = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else None
+            for x in (DIC, Alk, T, S, Si, PO4, P, pH)]
+    n = len(arrs[0])
+    out = np.zeros(n)
+    lib().or_carbon_chemistry_batch(C.byref(o), n, _dp(arrs[0]), _dp(arrs[1]), _dp(arrs[2]), _dp(arrs[3]),
+                                    _opt(arrs[4]), _opt(arrs[5]), _opt(arrs[6]), _opt(arrs[7]), _dp(out),
+                                    threads or nthreads())
+    return out
+
+
+def solve(solver, fid, x0, x1=0.0, damping=0.5, pa=1.0, pb=-2.0):
+    return lib().or_solve_test_function(solver, fid, float(x0), float(x1), damping, pa, pb)
+
+
+# ---------------------------------------------------------------------------- stepping
+def box_run(p, values, dt, nsteps, PAR_stages=None, PAR_const=0.0, t0=0.0):
+    v = np.zeros(A.NUM_NAMED)
+    for k, x in values.items():
+        v[A.NAME_INDEX[k] if isinstance(k, str) else k] = x
+    ps = None if PAR_stages is None else np.ascontiguousarray(PAR_stages, dtype=np.float64)
+    lib().or_box_run(C.byref(p), _dp(v), _opt(ps), PAR_const, t0, dt, nsteps)
+    return v
+
+
+def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_value=0.0, advection=1):
+    m = Model3D()
+    m.npd = p
+    m.light = light if light is not None else A.default_twoband()
+    m.surface_kind = surface_kind
+    m.surface_value = surface_value
+    m.advection = advection
+    m.grid = grid
+    m.n_tracers = len(names)
+    for q, nm in enumerate(names):
+        m.names[q] = -1 if nm is None else (A.NAME_INDEX[nm] if isinstance(nm, str) else nm)
+    return m
+
+
+def step3d(m, state, u=None, v=None, w=None, t=0.0, dt=1.0, nsteps=1, threads=None):
+    """state: float64 array (n_tracers, Nz, Ny, Nx), stepped in place."""
+    assert state.dtype == np.float64 and state.flags.c_contiguous
+    lib().or_step3d(C.byref(m), _dp(state), _opt(u), _opt(v), _opt(w), t, dt, nsteps, threads or nthreads())
+    return state
+
+
+def par3d(m, state, t, threads=None):
+    g = m.grid
+    out = np.zeros((g.Nz, g.Ny, g.Nx))
+    lib().or_par3d(C.byref(m), _dp(state), t, _dp(out), threads or nthreads())
+    return out
+
+
+def columns_run(p, lp, cols, names, state, kappa, state_offsets, kappa_offsets, dt, nsteps, threads=None):
+    n = len(cols)
+    carr = (Column * n)(*cols)
+    so = np.ascontiguousarray(state_offsets, dtype=np.int64)
+    ko = np.ascontiguousarray(kappa_offsets, dtype=np.int64)
+    nm = np.array([A.NAME_INDEX[x] if isinstance(x, str) else x for x in names], dtype=np.int32)
+    lib().or_columns_run(C.byref(p), C.byref(lp), n, carr, so.ctypes.data_as(C.POINTER(C.c_int64)),
+                         ko.ctypes.data_as(C.POINTER(C.c_int64)), len(names),
+                         nm.ctypes.data_as(C.POINTER(C.c_int32)), _dp(state), _dp(kappa), 0.0, dt,
+                         nsteps, threads or nthreads())
+    return state
+
+
+def scale_negatives(fields, scalefactors, fill=np.nan):
+    ptrs = (C.POINTER(C.c_double) * len(fields))(*[_dp(f) for f in fields])
+    sf = np.ascontiguousarray(scalefactors, dtype=np.float64)
+    lib().or_scale_negatives(len(fields[0]), len(fields), ptrs, _dp(sf), fill)
