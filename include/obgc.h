@@ -254,9 +254,12 @@ int obgc_multiband_coefficients(int32_t nbands, const double* band_edges /* 2*nb
                                 double* kw, double* e, double* chi);
 
 /* Euphotic depth (_compute_euphotic_depth!, src/Light/compute_euphotic_depth.jl:3-29): first
- * depth where PAR <= cutoff * surface PAR, log-interpolated; writes Nx*Ny values. */
-int obgc_euphotic_depth(const obgc_grid* grid, int32_t dtype, const void* PAR, void* zeu,
-                        double cutoff, void* stream);
+ * depth where PAR <= cutoff * surface PAR, log-interpolated; writes Nx*Ny values.  The surface
+ * value (PAR[Nz] + PAR[Nz+1])/2 of the reference is the surface PAR of a field whose top halo holds
+ * the value-boundary-condition mirror, so it is taken from `surface` at time t.  Columns that never
+ * cross the cutoff get the centre of the cell below the bottom. */
+int obgc_euphotic_depth(const obgc_surface* surface, const obgc_grid* grid, int32_t dtype,
+                        const void* PAR, void* zeu, double cutoff, double t, void* stream);
 
 /* ---------------------------------------------------------------------------------------
  * Carbon chemistry (src/Models/CarbonChemistry)
@@ -371,9 +374,18 @@ int obgc_step(obgc_ctx* ctx, double t, double dt, int32_t nsteps, void* stream);
  * obgc_step; re-captured when dt, nsteps or bindings change). */
 int obgc_step_graph(obgc_ctx* ctx, double t, double dt, int32_t nsteps, void* stream);
 /* Device kernel time of the last obgc_step / obgc_step_graph measured with CUDA events on the
- * launching stream (ms), and the time share of the fused substep kernel. */
+ * launching stream (ms); with profiling on, also the summed duration of the fused substep kernel
+ * launches (event pairs around each launch).  launches: kernels the call enqueued. */
 int obgc_last_step_timing(const obgc_ctx* ctx, double* total_ms, double* substep_ms,
                           int64_t* launches);
+/* Bracket every fused substep launch of obgc_step with CUDA events (off by default). */
+int obgc_set_profiling(obgc_ctx* ctx, int32_t on);
+/* Vertical segment length (levels) of the fused kernel's work items (default 16). */
+int obgc_set_tiling(obgc_ctx* ctx, int32_t levels_per_item);
+/* Size and selected field offsets of the ABI structs (which: 0 npd_params, 1 twoband,
+ * 2 surface, 3 grid, 4 carbon_options, 5 model_desc, 6 fields) for binding self-checks;
+ * no counterpart in the reference. */
+int obgc_struct_layout(int32_t which, int64_t* out, int32_t cap);
 
 /* Domain-integrated mass of a conserved group (conserved_tracers, NutrientsPlanktonDetritus/
  * coupling_utils.jl:1-52): sum over cells of sum_n scale[n]*tracer_n, accumulated in FP64 with
@@ -387,8 +399,8 @@ int obgc_tracer_budget(obgc_ctx* ctx, int32_t group, double* total, void* stream
  * Advance n_models box models nsteps RK3 steps of dt from t0 (BoxModel time_step!,
  * src/BoxModel/timesteppers.jl:30-93).  state: device FP64 array [n_models][OBGC_NUM_NAMED]
  * (row per model, enum obgc_tracer columns) updated in place.  PAR: device FP64
- * [n_models][3*nsteps] with the prescribed PAR at every RK3 stage time (t, t+8/15 dt, t+2/3 dt),
- * or NULL with par_constant used.  params_per_model: optional device array of n_models
+ * [3*nsteps][n_models] with the prescribed PAR at every RK3 stage time (t, t+8/15 dt, t+2/3 dt)
+ * of every step (stage-major, so a warp reads one coalesced row), or NULL with par_constant used.  params_per_model: optional device array of n_models
  * obgc_npd_params (NULL = `p` for all).  record_every > 0 writes the state every record_every
  * steps into record [n_records][n_models][OBGC_NUM_NAMED] (SpeedyOutput,
  * src/BoxModel/output_writer.jl).  precision: OBGC_PREC_F64 or OBGC_PREC_F32 (state and math).

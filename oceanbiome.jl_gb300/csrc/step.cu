@@ -1,0 +1,524 @@
+// step.cu — the 3-D model context: fused RK3 stepping (mode (ii)), the plugin hooks of mode (i)
+// (update_state / compute_tendencies), CUDA-graph replay, and the FP64 compensated tracer budget.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+#include "step_launch.cuh"
+
+namespace obgc {
+
+// ----------------------------------------------------------------------------- registry
+static std::vector<FusedEntry>& registry() {
+    static std::vector<FusedEntry> r;
+    return r;
+}
+static std::mutex& registry_mutex() {
+    static std::mutex m;
+    return m;
+}
+void register_fused(const FusedEntry& e) {
+    std::lock_guard<std::mutex> g(registry_mutex());
+    registry().push_back(e);
+}
+const FusedEntry* find_fused(int prec, int V, int NT) {
+    std::lock_guard<std::mutex> g(registry_mutex());
+    for (const auto& e : registry())
+        if (e.prec == prec && e.V == V && e.NT == NT) return &e;
+    return nullptr;
+}
+
+int required_tracers(const obgc_npd_params* p, int32_t* names);
+bool drift_speed(const obgc_npd_params* p, int name, double* w0);
+void drift_profile(double w0, int open_bottom, int Nz, double* w);
+
+// ----------------------------------------------------------------------------- small kernels
+__global__ void set_time_kernel(double* t, double v) { *t = v; }
+__global__ void advance_time_kernel(double* t, double dt) { *t += dt; }
+
+template <typename TS>
+__global__ void copy_interior_kernel(const TS* __restrict__ src, TS* __restrict__ dst, int Nx, int Ny, int Nz,
+                                     int64_t sj, int64_t sk) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t NN = (int64_t)Nx * Ny;
+    if (c >= NN * Nz) return;
+    const int64_t idx = (c % Nx) + ((c / Nx) % Ny) * sj + (c / NN) * sk;
+    dst[idx] = src[idx];
+}
+
+// Neumaier-compensated FP64 accumulation (sum, compensation).
+struct DD {
+    double s, c;
+};
+__device__ __forceinline__ void dd_add(DD& a, double x) {
+    const double t = a.s + x;
+    if (fabs(a.s) >= fabs(x)) a.c += (a.s - t) + x;
+    else a.c += (x - t) + a.s;
+    a.s = t;
+}
+__device__ __forceinline__ void dd_merge(DD& a, const DD& b) {
+    dd_add(a, b.s);
+    a.c += b.c;
+}
+
+constexpr int BUDGET_MAX_TRACERS = 8;
+template <typename TS>
+struct BudgetArgs {
+    const TS* f[BUDGET_MAX_TRACERS];
+    double scale[BUDGET_MAX_TRACERS];
+    int n;
+};
+
+constexpr int BUDGET_THREADS = 256;
+template <typename TS>
+__global__ void __launch_bounds__(BUDGET_THREADS) budget_partial_kernel(BudgetArgs<TS> b, int Nx, int Ny, int Nz,
+                                                                        int64_t sj, int64_t sk, DD* __restrict__ partial) {
+    const int64_t NN = (int64_t)Nx * Ny, N = NN * Nz;
+    DD acc = {0.0, 0.0};
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t idx = (c % Nx) + ((c / Nx) % Ny) * sj + (c / NN) * sk;
+        for (int q = 0; q < b.n; q++) dd_add(acc, b.scale[q] * (double)b.f[q][idx]);
+    }
+    __shared__ DD red[BUDGET_THREADS];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = BUDGET_THREADS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) dd_merge(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void __launch_bounds__(BUDGET_THREADS) budget_final_kernel(const DD* __restrict__ partial, int n, double* out) {
+    DD acc = {0.0, 0.0};
+    for (int q = threadIdx.x; q < n; q += blockDim.x) dd_merge(acc, partial[q]);
+    __shared__ DD red[BUDGET_THREADS];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = BUDGET_THREADS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) dd_merge(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0].s + red[0].c;
+}
+
+}  // namespace obgc
+
+using namespace obgc;
+
+// ----------------------------------------------------------------------------- context
+struct obgc_ctx {
+    obgc_model_desc desc;
+    int V = -1, NT = 0, NB = 0;
+    int names[MAX_NT];
+    int prec = 0;
+    size_t ts = 4, tc = 4;
+    int64_t extent = 0;                 // elements spanned by one field (strides * Nz)
+    obgc_fields fields;
+    void* user[MAX_NT] = {};
+    void* scratch[MAX_NT] = {};
+    void* G[MAX_NT] = {};
+    void* drift = nullptr;
+    uint32_t drift_mask = 0;
+    double* d_time = nullptr;
+    DD* partial = nullptr;
+    int n_partial = 0;
+    double* d_budget = nullptr;
+    int TZ = 16;
+    int blocks = 0;
+    bool bound = false;
+    // graph replay
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = 0;
+    int graph_nsteps = 0;
+    uint64_t bind_version = 0, graph_version = ~0ull;
+    cudaStream_t graph_stream = nullptr;
+    // timing
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    std::vector<cudaEvent_t> prof_events;
+    bool profile = false;
+    double last_total_ms = 0, last_substep_ms = 0;
+    int64_t last_launches = 0;
+};
+
+static int ctx_free(obgc_ctx* c) {
+    if (!c) return OBGC_OK;
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    for (int t = 0; t < MAX_NT; t++) {
+        if (c->scratch[t]) cudaFree(c->scratch[t]);
+        if (c->G[t]) cudaFree(c->G[t]);
+    }
+    if (c->drift) cudaFree(c->drift);
+    if (c->d_time) cudaFree(c->d_time);
+    if (c->partial) cudaFree(c->partial);
+    if (c->d_budget) cudaFree(c->d_budget);
+    if (c->ev_begin) cudaEventDestroy(c->ev_begin);
+    if (c->ev_end) cudaEventDestroy(c->ev_end);
+    for (auto e : c->prof_events) cudaEventDestroy(e);
+    delete c;
+    return OBGC_OK;
+}
+
+extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
+    if (!desc || !out) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: null argument");
+    *out = nullptr;
+    const obgc_grid& g = desc->grid;
+    if (!valid_grid(&g)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: invalid grid descriptor");
+    if (desc->precision < 0 || desc->precision > 2) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: bad precision");
+    if (desc->n_passive != 0) return fail(OBGC_ERR_UNSUPPORTED, "obgc_create: passive tracers are not supported");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(OBGC_ERR_NO_DEVICE, "obgc_create: no CUDA device");
+    obgc_ctx* c = new obgc_ctx();
+    c->desc = *desc;
+    std::memset(&c->fields, 0, sizeof(c->fields));
+    c->prec = desc->precision;
+    c->ts = c->prec == OBGC_PREC_F32 ? 4 : 8;
+    c->tc = c->prec == OBGC_PREC_F64 ? 8 : 4;
+    c->V = variant_of(desc->npd);
+    // slot order: required BGC tracers, then carried T / S
+    int32_t req[32];
+    const int nreq = required_tracers(&desc->npd, req);
+    c->NB = nreq;
+    int nt = 0;
+    for (int q = 0; q < nreq && nt < MAX_NT; q++) c->names[nt++] = req[q];
+    bool hasT = false;
+    for (int q = 0; q < nreq; q++) hasT |= req[q] == OBGC_T;
+    if (desc->carry_T && !hasT && nt < MAX_NT) c->names[nt++] = OBGC_T;
+    if (desc->carry_S && nt < MAX_NT) c->names[nt++] = OBGC_S;
+    c->NT = nt;
+    c->extent = g.stride_k * (int64_t)g.Nz;
+    int rc = OBGC_OK;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (rc != OBGC_OK) return;
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc");
+    };
+    for (int t = 0; t < c->NT; t++) {
+        alloc(&c->scratch[t], c->ts * c->extent);
+        alloc(&c->G[t], c->tc * c->extent);
+    }
+    // drift profiles of every slot (only non-zero ones are flagged)
+    std::vector<double> prof((size_t)MAX_NT * (g.Nz + 1), 0.0);
+    for (int t = 0; t < c->NT; t++) {
+        double w0;
+        if (desc->advection && drift_speed(&desc->npd, c->names[t], &w0) && w0 != 0.0) {
+            drift_profile(w0, desc->npd.open_bottom, g.Nz, &prof[(size_t)t * (g.Nz + 1)]);
+            c->drift_mask |= 1u << t;
+        }
+    }
+    alloc(&c->drift, c->tc * prof.size());
+    alloc((void**)&c->d_time, sizeof(double));
+    c->n_partial = 4 * 152;
+    alloc((void**)&c->partial, sizeof(DD) * c->n_partial);
+    alloc((void**)&c->d_budget, sizeof(double));
+    if (rc == OBGC_OK) {
+        cudaError_t e;
+        if (c->tc == 4) {
+            std::vector<float> pf(prof.begin(), prof.end());
+            e = cudaMemcpy(c->drift, pf.data(), 4 * pf.size(), cudaMemcpyHostToDevice);
+        } else {
+            e = cudaMemcpy(c->drift, prof.data(), 8 * prof.size(), cudaMemcpyHostToDevice);
+        }
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpy(drift)");
+    }
+    if (rc == OBGC_OK && (cudaEventCreate(&c->ev_begin) != cudaSuccess || cudaEventCreate(&c->ev_end) != cudaSuccess))
+        rc = fail(OBGC_ERR_CUDA, "cudaEventCreate");
+    // persistent grid size
+    if (rc == OBGC_OK) {
+        const FusedEntry* fe = c->V >= 0 ? find_fused(c->prec, c->V, c->NT) : nullptr;
+        int dev = 0, nsm = 152, bps = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (fe) {
+            int r2 = fe->occupancy(&bps);
+            if (r2 != OBGC_OK) rc = r2;
+        }
+        c->blocks = nsm * (bps > 0 ? bps : 1);
+    }
+    if (rc != OBGC_OK) {
+        ctx_free(c);
+        return rc;
+    }
+    *out = c;
+    return OBGC_OK;
+}
+
+extern "C" int obgc_destroy(obgc_ctx* ctx) { return ctx_free(ctx); }
+
+extern "C" int obgc_bind_fields(obgc_ctx* c, const obgc_fields* f) {
+    if (!c || !f) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_bind_fields: null argument");
+    for (int t = 0; t < c->NT; t++) {
+        void* p = f->tracers[c->names[t]];
+        if (!p) return fail(OBGC_ERR_INVALID_ARGUMENT, std::string("obgc_bind_fields: missing tracer slot ") + std::to_string(c->names[t]));
+        c->user[t] = p;
+    }
+    c->fields = *f;
+    c->bound = true;
+    c->bind_version++;
+    return OBGC_OK;
+}
+
+extern "C" int obgc_set_profiling(obgc_ctx* c, int32_t on) {
+    if (!c) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_profiling: null context");
+    c->profile = on != 0;
+    return OBGC_OK;
+}
+
+extern "C" int obgc_set_tiling(obgc_ctx* c, int32_t TZ) {
+    if (!c || TZ < 1) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_tiling: bad argument");
+    c->TZ = TZ;
+    c->graph_version = ~0ull;
+    return OBGC_OK;
+}
+
+extern "C" int obgc_update_state(obgc_ctx* c, double t, void* stream) {
+    if (!c || !c->bound) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_update_state: context not bound");
+    if (!c->fields.PAR) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_update_state: no PAR field bound");
+    const void* P = c->fields.tracers[OBGC_P];
+    return obgc_twoband_par(&c->desc.light, &c->desc.surface, &c->desc.grid, c->ts == 4 ? OBGC_F32 : OBGC_F64, P,
+                            c->fields.PAR, t, stream);
+}
+
+extern "C" int obgc_compute_tendencies(obgc_ctx* c, double t, void* stream) {
+    if (!c || !c->bound) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_compute_tendencies: context not bound");
+    if (!c->fields.PAR) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_compute_tendencies: no PAR field bound");
+    return obgc_npd_tendencies(&c->desc.npd, &c->desc.grid, c->ts == 4 ? OBGC_F32 : OBGC_F64,
+                               (const void* const*)c->fields.tracers, c->fields.PAR, c->fields.G, t, stream);
+}
+
+template <typename TS, typename TC>
+static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
+    const obgc_grid& g = c->desc.grid;
+    std::memset(&a, 0, sizeof(a));
+    a.Nx = g.Nx; a.Ny = g.Ny; a.Nz = g.Nz;
+    a.periodic_x = g.topology_x == OBGC_PERIODIC;
+    a.periodic_y = g.topology_y == OBGC_PERIODIC;
+    a.flat_x = g.topology_x == OBGC_FLAT || !c->desc.advection;
+    a.flat_y = g.topology_y == OBGC_FLAT || !c->desc.advection;
+    a.sj = g.stride_j; a.sk = g.stride_k;
+    a.dx = TC(g.Lx / g.Nx); a.dy = TC(g.Ly / g.Ny); a.dz = TC(g.Lz / g.Nz); a.Lz = TC(g.Lz);
+    a.TZ = c->TZ < g.Nz ? c->TZ : g.Nz;
+    a.nseg = (g.Nz + a.TZ - 1) / a.TZ;
+    a.ntx = (g.Nx + STEP_BX - 1) / STEP_BX;
+    a.nty = (g.Ny + STEP_BY - 1) / STEP_BY;
+    a.n_items = a.ntx * a.nty * a.nseg;
+    for (int t = 0; t < c->NT; t++) a.G[t] = (TC*)c->G[t];
+    a.u = c->desc.advection ? (const TS*)c->fields.u : nullptr;
+    a.v = c->desc.advection ? (const TS*)c->fields.v : nullptr;
+    a.w = c->desc.advection ? (const TS*)c->fields.w : nullptr;
+    a.drift = (const TC*)c->drift;
+    a.drift_mask = c->drift_mask;
+    a.bgc = make_params<TC>(c->desc.npd);
+    a.light = make_twoband<TC>(c->desc.light);
+    a.surf_kind = c->desc.surface.kind;
+    a.surf_value = TC(c->desc.surface.value);
+    a.surf_field = (const TS*)c->desc.surface.field;
+    a.d_time = c->d_time;
+}
+
+// Enqueue nsteps steps on stream st (no synchronisation).  The state ping-pongs between the bound
+// arrays and the context's scratch buffers; after an odd number of substeps the interior is copied
+// back so the bound arrays always hold the result.
+template <typename TS, typename TC>
+static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nsteps, cudaStream_t st, bool profile) {
+    SubstepArgs<TS, TC> a;
+    fill_args<TS, TC>(c, a);
+    a.dt_d = dt;
+    a.dt = TC(dt);
+    void* cur[MAX_NT];
+    void* nxt[MAX_NT];
+    for (int t = 0; t < c->NT; t++) { cur[t] = c->user[t]; nxt[t] = c->scratch[t]; }
+    const bool clock = c->desc.surface.kind == OBGC_SURFACE_PAR_DEFAULT;
+    int blocks = c->blocks < a.n_items ? c->blocks : a.n_items;
+    size_t ev = 0;
+    for (int s = 0; s < nsteps; s++) {
+        for (int stg = 0; stg < 3; stg++) {
+            for (int t = 0; t < c->NT; t++) { a.in[t] = (const TS*)cur[t]; a.out[t] = (TS*)nxt[t]; }
+            a.first_stage = stg == 0;
+            a.write_G = stg < 2;
+            a.gamma = TC(rk3_gamma(stg));
+            a.zeta = TC(rk3_zeta(stg));
+            a.c_stage = rk3_c(stg);
+            if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
+            int rc = fe->launch(&a, blocks, st);
+            if (rc != OBGC_OK) return rc;
+            if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
+            for (int t = 0; t < c->NT; t++) { void* tmp = cur[t]; cur[t] = nxt[t]; nxt[t] = tmp; }
+        }
+        if (clock) {
+            advance_time_kernel<<<1, 1, 0, st>>>(c->d_time, dt);
+            OBGC_LAUNCHED("advance_time_kernel");
+        }
+    }
+    if (nsteps % 2 == 1) {
+        const obgc_grid& g = c->desc.grid;
+        const int64_t N = (int64_t)g.Nx * g.Ny * g.Nz;
+        for (int t = 0; t < c->NT; t++) {
+            copy_interior_kernel<TS><<<(unsigned)((N + 255) / 256), 256, 0, st>>>((const TS*)cur[t], (TS*)c->user[t], g.Nx,
+                                                                                g.Ny, g.Nz, g.stride_j, g.stride_k);
+            OBGC_LAUNCHED("copy_interior_kernel");
+        }
+    }
+    return OBGC_OK;
+}
+
+static int dispatch_steps(obgc_ctx* c, double dt, int nsteps, cudaStream_t st, bool profile) {
+    const FusedEntry* fe = c->V >= 0 ? find_fused(c->prec, c->V, c->NT) : nullptr;
+    if (!fe) return fail(OBGC_ERR_UNSUPPORTED, "obgc_step: no fused kernel for this model variant / tracer set");
+    if (c->prec == OBGC_PREC_F32) return enqueue_steps<float, float>(c, fe, dt, nsteps, st, profile);
+    if (c->prec == OBGC_PREC_F64) return enqueue_steps<double, double>(c, fe, dt, nsteps, st, profile);
+    return enqueue_steps<double, float>(c, fe, dt, nsteps, st, profile);
+}
+
+static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
+    const bool clock = c->desc.surface.kind == OBGC_SURFACE_PAR_DEFAULT;
+    return (int64_t)nsteps * (3 + (clock ? 1 : 0)) + (nsteps % 2 ? c->NT : 0) + 1;
+}
+
+extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {
+    if (!c || !c->bound) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_step: context not bound");
+    if (nsteps < 0 || !(dt > 0)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_step: bad dt / nsteps");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (c->profile) {
+        const size_t need = (size_t)6 * nsteps;
+        while (c->prof_events.size() < need) {
+            cudaEvent_t e;
+            OBGC_CUDA(cudaEventCreate(&e));
+            c->prof_events.push_back(e);
+        }
+    }
+    OBGC_CUDA(cudaEventRecord(c->ev_begin, st));
+    set_time_kernel<<<1, 1, 0, st>>>(c->d_time, t);
+    OBGC_LAUNCHED("set_time_kernel");
+    int rc = dispatch_steps(c, dt, nsteps, st, c->profile);
+    if (rc != OBGC_OK) return rc;
+    OBGC_CUDA(cudaEventRecord(c->ev_end, st));
+    c->last_launches = launches_per_call(c, nsteps);
+    if (c->profile) {
+        OBGC_CUDA(cudaEventSynchronize(c->ev_end));
+        float ms = 0;
+        OBGC_CUDA(cudaEventElapsedTime(&ms, c->ev_begin, c->ev_end));
+        c->last_total_ms = ms;
+        double sub = 0;
+        for (size_t q = 0; q + 1 < (size_t)6 * nsteps; q += 2) {
+            float m = 0;
+            OBGC_CUDA(cudaEventElapsedTime(&m, c->prof_events[q], c->prof_events[q + 1]));
+            sub += m;
+        }
+        c->last_substep_ms = sub;
+    }
+    return OBGC_OK;
+}
+
+extern "C" int obgc_step_graph(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {
+    if (!c || !c->bound) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_step_graph: context not bound");
+    if (nsteps < 1 || !(dt > 0)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_step_graph: bad dt / nsteps");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!c->graph || c->graph_dt != dt || c->graph_nsteps != nsteps || c->graph_version != c->bind_version) {
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+        cudaStream_t cap;
+        OBGC_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t graph;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) { cudaStreamDestroy(cap); return cuda_fail(e, "cudaStreamBeginCapture"); }
+        int rc = dispatch_steps(c, dt, nsteps, cap, false);
+        e = cudaStreamEndCapture(cap, &graph);
+        cudaStreamDestroy(cap);
+        if (rc != OBGC_OK) { if (e == cudaSuccess) cudaGraphDestroy(graph); return rc; }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&c->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+        c->graph_dt = dt;
+        c->graph_nsteps = nsteps;
+        c->graph_version = c->bind_version;
+    }
+    OBGC_CUDA(cudaEventRecord(c->ev_begin, st));
+    set_time_kernel<<<1, 1, 0, st>>>(c->d_time, t);
+    OBGC_LAUNCHED("set_time_kernel");
+    OBGC_CUDA(cudaGraphLaunch(c->graph, st));
+    count_launches(launches_per_call(c, nsteps) - 1);
+    OBGC_CUDA(cudaEventRecord(c->ev_end, st));
+    c->last_launches = launches_per_call(c, nsteps);
+    return OBGC_OK;
+}
+
+extern "C" int obgc_last_step_timing(const obgc_ctx* c, double* total_ms, double* substep_ms, int64_t* launches) {
+    if (!c) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_last_step_timing: null context");
+    if (!c->profile) {
+        float ms = 0;
+        OBGC_CUDA(cudaEventSynchronize(c->ev_end));
+        OBGC_CUDA(cudaEventElapsedTime(&ms, c->ev_begin, c->ev_end));
+        if (total_ms) *total_ms = ms;
+        if (substep_ms) *substep_ms = 0;
+    } else {
+        if (total_ms) *total_ms = c->last_total_ms;
+        if (substep_ms) *substep_ms = c->last_substep_ms;
+    }
+    if (launches) *launches = c->last_launches;
+    return OBGC_OK;
+}
+
+// conserved_tracers (NutrientsPlanktonDetritus/coupling_utils.jl:1-52)
+static int conserved_group(const obgc_npd_params& p, int group, int* names, double* scale) {
+    int n = 0;
+    if (group == 0) {
+        names[n] = OBGC_P; scale[n++] = 1; names[n] = OBGC_Z; scale[n++] = 1;
+        if (p.nutrients == OBGC_NUT_NUTRIENT) { names[n] = OBGC_N; scale[n++] = 1; }
+        else { names[n] = OBGC_NO3; scale[n++] = 1; names[n] = OBGC_NH4; scale[n++] = 1; }
+        if (p.detritus == OBGC_DET_VARIABLE_REDFIELD) {
+            names[n] = OBGC_SPON; scale[n++] = 1; names[n] = OBGC_BPON; scale[n++] = 1; names[n] = OBGC_DON; scale[n++] = 1;
+        } else if (p.detritus == OBGC_DET_TWO_PARTICLE) {
+            names[n] = OBGC_SPOM; scale[n++] = 1; names[n] = OBGC_BPOM; scale[n++] = 1; names[n] = OBGC_DOM; scale[n++] = 1;
+        } else if (p.detritus == OBGC_DET_SINGLE) {
+            names[n] = OBGC_D; scale[n++] = 1;
+        }
+        return n;
+    }
+    if (!p.carbonate_system) return -1;
+    const double R = p.redfield_ratio, rho = p.carbon_calcite_ratio;
+    names[n] = OBGC_P; scale[n++] = (1 + rho) * R;
+    names[n] = OBGC_Z; scale[n++] = R;
+    names[n] = OBGC_DIC; scale[n++] = 1;
+    if (p.detritus == OBGC_DET_VARIABLE_REDFIELD) {
+        names[n] = OBGC_SPOC; scale[n++] = 1; names[n] = OBGC_BPOC; scale[n++] = 1; names[n] = OBGC_DOC; scale[n++] = 1;
+    } else if (p.detritus == OBGC_DET_TWO_PARTICLE) {
+        names[n] = OBGC_SPOM; scale[n++] = R; names[n] = OBGC_BPOM; scale[n++] = R; names[n] = OBGC_DOM; scale[n++] = R;
+    } else if (p.detritus == OBGC_DET_SINGLE) {
+        names[n] = OBGC_D; scale[n++] = R;
+    }
+    return n;
+}
+
+template <typename TS>
+static int launch_budget(obgc_ctx* c, const int* names, const double* scale, int n, double* total, cudaStream_t st) {
+    BudgetArgs<TS> b;
+    std::memset(&b, 0, sizeof(b));
+    b.n = n;
+    for (int q = 0; q < n; q++) {
+        b.f[q] = (const TS*)c->fields.tracers[names[q]];
+        if (!b.f[q]) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_tracer_budget: conserved tracer not bound");
+        b.scale[q] = scale[q];
+    }
+    const obgc_grid& g = c->desc.grid;
+    budget_partial_kernel<TS><<<c->n_partial, BUDGET_THREADS, 0, st>>>(b, g.Nx, g.Ny, g.Nz, g.stride_j, g.stride_k, c->partial);
+    OBGC_LAUNCHED("budget_partial_kernel");
+    budget_final_kernel<<<1, BUDGET_THREADS, 0, st>>>(c->partial, c->n_partial, c->d_budget);
+    OBGC_LAUNCHED("budget_final_kernel");
+    OBGC_CUDA(cudaMemcpyAsync(total, c->d_budget, sizeof(double), cudaMemcpyDeviceToHost, st));
+    OBGC_CUDA(cudaStreamSynchronize(st));
+    return OBGC_OK;
+}
+
+extern "C" int obgc_tracer_budget(obgc_ctx* c, int32_t group, double* total, void* stream) {
+    if (!c || !c->bound || !total || (group != 0 && group != 1))
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_tracer_budget: bad argument");
+    int names[16];
+    double scale[16];
+    const int n = conserved_group(c->desc.npd, group, names, scale);
+    if (n < 0) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_tracer_budget: model has no carbonate system");
+    if (n > BUDGET_MAX_TRACERS) return fail(OBGC_ERR_UNSUPPORTED, "obgc_tracer_budget: too many tracers");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (c->ts == 4) return launch_budget<float>(c, names, scale, n, total, st);
+    return launch_budget<double>(c, names, scale, n, total, st);
+}

@@ -1,0 +1,48 @@
+// step_inst.cu — one (precision, variant) slice of the fused substep kernels.  The build compiles
+// this file once per slice with -DOBGC_INST_PREC=<0 f32 | 1 f64 | 2 mixed> -DOBGC_INST_V=<variant>,
+// so the slices compile in parallel; each object registers its kernels with the dispatcher.
+#include "step_launch.cuh"
+
+#ifndef OBGC_INST_PREC
+#define OBGC_INST_PREC 0
+#endif
+#ifndef OBGC_INST_V
+#define OBGC_INST_V 1
+#endif
+
+namespace obgc {
+namespace {
+
+#if OBGC_INST_PREC == 0
+typedef float TS_;
+typedef float TC_;
+#elif OBGC_INST_PREC == 1
+typedef double TS_;
+typedef double TC_;
+#else
+typedef double TS_;
+typedef float TC_;
+#endif
+
+constexpr int V_ = OBGC_INST_V;
+// tracer counts with a kernel: the BGC tracers alone, and followed by the carried T/S
+constexpr int NT_A = n_bgc(V_);
+constexpr int NT_B = V_ == V_NPZD ? 6 : n_bgc(V_) + 2;
+
+template <int NT>
+int launch_fn(const void* a, int blocks, cudaStream_t st) {
+    return launch_one<V_, NT, TS_, TC_>(*static_cast<const SubstepArgs<TS_, TC_>*>(a), blocks, st);
+}
+template <int NT>
+int occupancy_fn(int* bps) { return occupancy_one<V_, NT, TS_, TC_>(bps); }
+
+struct Registrar {
+    Registrar() {
+        register_fused({OBGC_INST_PREC, V_, NT_A, &launch_fn<NT_A>, &occupancy_fn<NT_A>});
+        register_fused({OBGC_INST_PREC, V_, NT_B, &launch_fn<NT_B>, &occupancy_fn<NT_B>});
+    }
+};
+Registrar registrar;
+
+}  // namespace
+}  // namespace obgc

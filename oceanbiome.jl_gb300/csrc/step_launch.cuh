@@ -1,0 +1,62 @@
+// step_launch.cuh — instantiation helpers for the fused substep kernel.  Each precision lives in
+// its own translation unit (step_f32.cu, step_f64.cu, step_mixed.cu) so they compile in parallel.
+#pragma once
+#include "step_kernel.cuh"
+
+namespace obgc {
+
+// (variant, tracer count) pairs with a fused kernel: the BGC tracers alone, or followed by T and S.
+inline bool fused_supported(int V, int NT) {
+    switch (V) {
+        case V_LOBSTER: return NT == 7 || NT == 9;
+        case V_LOBSTER_C: return NT == 9 || NT == 11;
+        case V_LOBSTER_CO: return NT == 10 || NT == 12;
+        case V_LOBSTER_O: return NT == 8 || NT == 10;
+        case V_NPZD: return NT == 5 || NT == 6;
+    }
+    return false;
+}
+
+template <int V, int NT, typename TS, typename TC>
+int ensure_configured() {
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(substep_kernel<V, NT, TS, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)substep_smem_bytes<TC, NT>());
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(substep_kernel)");
+        configured = true;
+    }
+    return OBGC_OK;
+}
+
+template <int V, int NT, typename TS, typename TC>
+int launch_one(const SubstepArgs<TS, TC>& a, int blocks, cudaStream_t st) {
+    const int rc = ensure_configured<V, NT, TS, TC>();
+    if (rc != OBGC_OK) return rc;
+    substep_kernel<V, NT, TS, TC><<<blocks, dim3(STEP_BX, STEP_BY), substep_smem_bytes<TC, NT>(), st>>>(a);
+    OBGC_LAUNCHED("substep_kernel");
+    return OBGC_OK;
+}
+
+template <int V, int NT, typename TS, typename TC>
+int occupancy_one(int* blocks_per_sm) {
+    const int rc = ensure_configured<V, NT, TS, TC>();
+    if (rc != OBGC_OK) return rc;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, substep_kernel<V, NT, TS, TC>,
+                                                                  STEP_BX * STEP_BY, substep_smem_bytes<TC, NT>());
+    if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    return OBGC_OK;
+}
+
+// Registry of compiled fused kernels, filled by the step_inst.cu objects at load time.
+typedef int (*fused_launch_fn)(const void* args, int blocks, cudaStream_t st);
+typedef int (*fused_occupancy_fn)(int* blocks_per_sm);
+struct FusedEntry {
+    int prec, V, NT;
+    fused_launch_fn launch;
+    fused_occupancy_fn occupancy;
+};
+void register_fused(const FusedEntry& e);
+const FusedEntry* find_fused(int prec, int V, int NT);
+
+}  // namespace obgc

@@ -1,1 +1,23 @@
-"""obgc — GB300-native OceanBioME tracer-tendency engine (Python side of the C ABI)."""
+"""obgc — GB300-native OceanBioME tracer-tendency engine (Python side of the C ABI).
+
+The names mirror OceanBioME.jl's public API for the tracer-tendency path (the `!` of mutating
+functions dropped): LOBSTER / NPZD and their components, the biogeochemistry plugin functions,
+TwoBand / MultiBand / Prescribed light, CarbonChemistry, BoxModel, and an Oceananigans-style
+NonhydrostaticModel with set_, time_step and update_biogeochemical_state.  Every computation runs in
+libobgc.so (CUDA, sm_103a); importing works without it, calling does not.
+"""
+from . import _abi
+from .box import BoxModel
+from .carbon import CarbonChemistry
+from .grid import BoxModelGrid, RectilinearGrid
+from .light import (MultiBandPhotosyntheticallyActiveRadiation, PrescribedPhotosyntheticallyActiveRadiation,
+                    TwoBandPhotosyntheticallyActiveRadiation, default_surface_PAR, euphotic_depth)
+from .model3d import (Clock, NonhydrostaticModel, compute_tendencies, set_, time_step,
+                      update_biogeochemical_state)
+from .models import (LOBSTER, NPZD, CarbonateSystem, Detritus, NitrateAmmonia, NitrateAmmoniaIron, Nutrient,
+                     NutrientsPlanktonDetritus, Oxygen, PhytoZoo, TwoParticleAndDissolved, VariableRedfieldDetritus,
+                     biogeochemical_drift_velocity, conserved_tracers, eval_point, preset,
+                     required_biogeochemical_auxiliary_fields, required_biogeochemical_tracers)
+from .synthetic import lobster_initial_conditions, npzd_front_initial_conditions, random_streamfunction_velocity
+
+__all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,0 +1,140 @@
+"""NonhydrostaticModel mirror: tracers under a prescribed velocity, stepped by the fused kernels.
+
+NonhydrostaticModel(grid; biogeochemistry, advection, tracers, velocities) owns device tracer
+fields (torch tensors, shape (Nz, Ny, Nx)); time_step!(model, dt) advances one Oceananigans RK3
+step (three substeps, PAR recomputed from the state at every substep) through obgc_step.
+Dynamics (pressure solve, closures) are outside this engine: velocities are prescribed.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from .models import required_biogeochemical_tracers
+
+_PREC = {"f32": A.PREC_F32, "f64": A.PREC_F64, "mixed": A.PREC_MIXED}
+
+
+class Clock:
+    def __init__(self, time=0.0, iteration=0):
+        self.time = time
+        self.iteration = iteration
+
+
+class NonhydrostaticModel:
+    def __init__(self, grid, biogeochemistry, advection="WENO5", tracers=(), velocities=None,
+                 precision="f32", clock=None, device="cuda"):
+        import torch
+        self.grid = grid
+        self.biogeochemistry = bgc = biogeochemistry
+        self.precision = precision
+        self.clock = clock or Clock()
+        self.device = device
+        self.state_dtype = torch.float32 if precision == "f32" else torch.float64
+        bgc_names = list(required_biogeochemical_tracers(bgc))
+        extra = [t for t in tracers if t not in bgc_names]
+        for t in extra:
+            if t not in ("T", "S"):
+                raise ValueError(f"extra tracer {t!r}: only T and S can be carried alongside the BGC tracers")
+        self.tracer_names = bgc_names + [t for t in ("T", "S") if t in extra]
+        self.tracers = {n: torch.zeros(grid.shape, dtype=self.state_dtype, device=device) for n in self.tracer_names}
+        if velocities is None:
+            velocities = (None, None, None)
+        self.velocities = tuple(None if v is None else v.to(device=device, dtype=self.state_dtype).contiguous()
+                                for v in velocities)
+        self.PAR = torch.zeros(grid.shape, dtype=self.state_dtype, device=device)
+        self.G = {n: torch.zeros(grid.shape, dtype=self.state_dtype, device=device) for n in bgc_names}
+        light = bgc.light_attenuation
+        desc = A.ModelDesc()
+        desc.npd = bgc.params
+        desc.light = light.params
+        desc.surface = light.surface
+        desc.grid = grid.c_grid()
+        desc.precision = _PREC[precision]
+        desc.advection = A.ADVECTION_WENO5 if advection else A.ADVECTION_NONE
+        desc.carry_T = int("T" in extra)
+        desc.carry_S = int("S" in extra)
+        self._lib = lib = A.load()
+        ctx = C.c_void_p()
+        A.check(lib.obgc_create(C.byref(desc), C.byref(ctx)), "obgc_create")
+        self._ctx = ctx
+        self._bind()
+
+    def _bind(self):
+        f = A.Fields()
+        for n, t in self.tracers.items():
+            f.tracers[A.NAME_INDEX[n]] = t.data_ptr()
+        u, v, w = self.velocities
+        f.u = None if u is None else u.data_ptr()
+        f.v = None if v is None else v.data_ptr()
+        f.w = None if w is None else w.data_ptr()
+        f.PAR = self.PAR.data_ptr()
+        for n, t in self.G.items():
+            f.G[A.NAME_INDEX[n]] = t.data_ptr()
+        A.check(self._lib.obgc_bind_fields(self._ctx, C.byref(f)), "obgc_bind_fields")
+
+    def __del__(self):
+        ctx = getattr(self, "_ctx", None)
+        if ctx is not None and ctx.value:
+            self._lib.obgc_destroy(ctx)
+            self._ctx = None
+
+    @staticmethod
+    def _stream():
+        import torch
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def state_array(self):
+        import torch
+        return torch.stack([self.tracers[n] for n in self.tracer_names])
+
+    def set_profiling(self, on):
+        A.check(self._lib.obgc_set_profiling(self._ctx, int(on)), "obgc_set_profiling")
+
+    def set_tiling(self, levels):
+        A.check(self._lib.obgc_set_tiling(self._ctx, int(levels)), "obgc_set_tiling")
+
+    def last_timing(self):
+        tot, sub, n = C.c_double(0), C.c_double(0), C.c_int64(0)
+        A.check(self._lib.obgc_last_step_timing(self._ctx, C.byref(tot), C.byref(sub), C.byref(n)), "obgc_last_step_timing")
+        return tot.value, sub.value, n.value
+
+    def budget(self, group="nitrogen"):
+        out = C.c_double(0)
+        A.check(self._lib.obgc_tracer_budget(self._ctx, {"nitrogen": 0, "carbon": 1}[group], C.byref(out), self._stream()),
+                "obgc_tracer_budget")
+        return out.value
+
+
+def set_(model, **values):
+    """set!(model; kwargs...): numbers, numpy arrays or tensors of the grid shape."""
+    import torch
+    for k, v in values.items():
+        if k not in model.tracers:
+            raise ValueError(f"name {k} not found in model.tracers.")
+        t = model.tracers[k]
+        if isinstance(v, (int, float)):
+            t.fill_(float(v))
+        else:
+            t.copy_(torch.as_tensor(v).reshape(t.shape).to(device=t.device, dtype=t.dtype))
+
+
+def update_biogeochemical_state(model):
+    """update_biogeochemical_state! (src/OceanBioME.jl:161-167): PAR from the current state."""
+    A.check(model._lib.obgc_update_state(model._ctx, model.clock.time, model._stream()), "obgc_update_state")
+    return model.PAR
+
+
+def compute_tendencies(model):
+    """Mode (i): the BGC tendencies of every tracer into model.G (needs a current PAR)."""
+    A.check(model._lib.obgc_compute_tendencies(model._ctx, model.clock.time, model._stream()), "obgc_compute_tendencies")
+    return model.G
+
+
+def time_step(model, dt, nsteps=1, graph=False):
+    """time_step!(model, Δt): RK3 steps through the fused kernels (a CUDA graph with graph=True)."""
+    fn = model._lib.obgc_step_graph if graph else model._lib.obgc_step
+    A.check(fn(model._ctx, model.clock.time, float(dt), int(nsteps), model._stream()),
+            "obgc_step_graph" if graph else "obgc_step")
+    model.clock.time += dt * nsteps
+    model.clock.iteration += nsteps

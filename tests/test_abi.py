@@ -1,0 +1,74 @@
+"""The C-ABI library loads without a GPU, exports every symbol include/obgc.h declares, and the
+ctypes mirror matches the C struct layouts (no device work here)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from obgc import _abi as A
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "obgc.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(obgc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_loads_and_version():
+    lib = A.load()
+    assert lib.obgc_abi_version() == 1
+
+
+def test_every_declared_symbol_is_exported():
+    lib = A.load()
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(A.EXPORTED) <= set(names)
+
+
+@pytest.mark.parametrize("which,struct,fields", [
+    (0, A.NPDParams, ["nitrification_rate", "phytoplankton_sinking_speed", "nitrification_oxygen_nitrogen_ratio"]),
+    (1, A.TwoBandParams, ["chlorophyll_red_exponent", "pigment_ratio", "phytoplankton_chlorophyll_ratio"]),
+    (2, A.Surface, ["value", "field", None]),
+    (3, A.Grid, ["Lx", "stride_j", "stride_k"]),
+    (4, A.CarbonOptions, ["density_value", "atol", "calcium_ion_per_salinity"]),
+    (5, A.ModelDesc, ["surface", "grid", "precision"]),
+    (6, A.Fields, ["passive", "u", "G"]),
+])
+def test_struct_layouts(which, struct, fields):
+    lib = A.load()
+    out = (C.c_int64 * 4)()
+    assert lib.obgc_struct_layout(which, out, 4) == 0
+    assert out[0] == C.sizeof(struct)
+    for q, f in enumerate(fields):
+        if f is not None:
+            assert out[q + 1] == getattr(struct, f).offset, f
+
+
+def test_bad_arguments_return_status_not_crash():
+    lib = A.load()
+    assert lib.obgc_npd_preset(7, C.byref(A.NPDParams())) == 1
+    assert lib.obgc_npd_preset(0, None) == 1
+    assert lib.obgc_npd_required_tracers(None, None, 0) < 0
+    assert "preset" in lib.obgc_last_error_message().decode()
+
+
+def test_no_device_is_reported():
+    # In a container without a GPU, building a context fails with a status, not a crash.
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = A.load()
+    d = A.ModelDesc()
+    lib.obgc_npd_preset(0, C.byref(d.npd))
+    d.grid.Nx = d.grid.Ny = d.grid.Nz = 4
+    d.grid.Lx = d.grid.Ly = d.grid.Lz = 1.0
+    d.grid.stride_j, d.grid.stride_k = 4, 16
+    ctx = C.c_void_p()
+    rc = lib.obgc_create(C.byref(d), C.byref(ctx))
+    assert rc in (2, 7) and not ctx.value

@@ -1,0 +1,124 @@
+"""GPU parity of the fused 3-D RK3 step (WENO5 advection + drift + BGC + TwoBand PAR + RK3)
+against the oracle on seeded inputs, in FP64, FP32 and mixed precision, plus conservation,
+graph replay, halo'd layouts and the compensated budget."""
+import math
+
+import numpy as np
+import pytest
+
+import obgc
+import oracle as O
+from gpuhelp import cuda, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def lobster_model(shape=(40, 24, 12), extent=(4000.0, 2400.0, 120.0), precision="f64", topo=("Periodic", "Periodic", "Bounded"),
+                  seed=1, carbonates=True, TZ=None, open_bottom=True, w=False):
+    torch = cuda()
+    g = obgc.RectilinearGrid(shape, extent, topo, dtype="f32" if precision == "f32" else "f64")
+    bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem() if carbonates else None)
+    bgc.params.open_bottom = int(open_bottom)
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=seed)
+    wv = None
+    if w:
+        rng = np.random.default_rng(seed + 7)
+        wv = torch.as_tensor(rng.normal(0, 1e-4, g.shape), dtype=torch.float64, device="cuda")
+    model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S") if carbonates else (),
+                                     velocities=(u, v, wv), precision=precision)
+    if TZ:
+        model.set_tiling(TZ)
+    init = obgc.lobster_initial_conditions(g, seed=seed + 1)
+    obgc.set_(model, **{k: v for k, v in init.items() if k in model.tracers})
+    return g, bgc, model, (u, v, wv)
+
+
+def oracle_run(g, bgc, model, vel, state0, dt, nsteps, t0=0.0):
+    m = O.model3d(bgc.params, g.c_grid(), model.tracer_names)
+    ref = np.ascontiguousarray(state0.astype(np.float64))
+    u, v, w = (None if x is None else x.double().cpu().numpy().ravel().copy() for x in vel)
+    O.step3d(m, ref, u=u, v=v, w=w, t=t0, dt=dt, nsteps=nsteps)
+    return ref
+
+
+def per_tracer_err(model, got, ref):
+    return {n: rel_err(got[q], ref[q]) for q, n in enumerate(model.tracer_names)}
+
+
+@pytest.mark.parametrize("TZ", [None, 5])
+def test_fused_fp64_matches_oracle(TZ):
+    g, bgc, model, vel = lobster_model(TZ=TZ)
+    s0 = model.state_array().cpu().numpy()
+    obgc.time_step(model, 300.0, nsteps=4)
+    got = model.state_array().cpu().numpy()
+    ref = oracle_run(g, bgc, model, vel, s0, 300.0, 4)
+    errs = per_tracer_err(model, got, ref)
+    assert max(errs.values()) < 1e-11, errs
+    assert np.max(np.abs(got - s0)) > 0
+
+
+def test_fused_f32_and_mixed_within_tolerance():
+    for precision, tol in (("f32", 1e-5), ("mixed", 1e-5)):
+        g, bgc, model, vel = lobster_model(precision=precision, seed=4)
+        s0 = model.state_array().double().cpu().numpy()
+        obgc.time_step(model, 300.0, nsteps=6)
+        got = model.state_array().double().cpu().numpy()
+        ref = oracle_run(g, bgc, model, vel, s0, 300.0, 6)
+        errs = per_tracer_err(model, got, ref)
+        assert max(errs.values()) < tol, (precision, errs)
+
+
+def test_bounded_walls_vertical_velocity_and_sinking():
+    g, bgc, model, vel = lobster_model(shape=(21, 13, 17), extent=(2100.0, 1300.0, 170.0),
+                                       topo=("Bounded", "Bounded", "Bounded"), w=True, carbonates=False, seed=8)
+    s0 = model.state_array().cpu().numpy()
+    obgc.time_step(model, 200.0, nsteps=3)
+    got = model.state_array().cpu().numpy()
+    ref = oracle_run(g, bgc, model, vel, s0, 200.0, 3)
+    assert max(per_tracer_err(model, got, ref).values()) < 1e-11
+
+
+def test_npzd_front_2d_fp64():
+    torch = cuda()
+    g = obgc.RectilinearGrid((160, 32), (10000.0, 500.0), ("Bounded", "Flat", "Bounded"))
+    bgc = obgc.NPZD(g)
+    model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, precision="f64")
+    obgc.set_(model, **obgc.npzd_front_initial_conditions(g))
+    s0 = model.state_array().cpu().numpy()
+    obgc.time_step(model, 50.0, nsteps=20)
+    got = model.state_array().cpu().numpy()
+    ref = oracle_run(g, bgc, model, (None, None, None), s0, 50.0, 20)
+    assert max(per_tracer_err(model, got, ref).values()) < 1e-11
+
+
+def test_nitrogen_and_carbon_conserved_closed_bottom():
+    g, bgc, model, vel = lobster_model(open_bottom=False, seed=12)
+    N0, C0 = model.budget("nitrogen"), model.budget("carbon")
+    obgc.time_step(model, 300.0, nsteps=10)
+    N1, C1 = model.budget("nitrogen"), model.budget("carbon")
+    assert abs(N1 - N0) / N0 < 1e-12
+    assert abs(C1 - C0) / C0 < 1e-12
+
+
+def test_budget_is_compensated_sum():
+    torch = cuda()
+    g, bgc, model, vel = lobster_model(seed=13)
+    got = model.budget("nitrogen")
+    names = obgc.conserved_tracers(bgc)[0]
+    ref = math.fsum(float(x) for n in names for x in model.tracers[n].cpu().numpy().ravel())
+    assert abs(got - ref) <= 1e-15 * abs(ref)
+
+
+def test_graph_replay_and_odd_steps_are_bitwise_identical():
+    torch = cuda()
+    _, _, a, _ = lobster_model(precision="f32", seed=21)
+    _, _, b, _ = lobster_model(precision="f32", seed=21)
+    obgc.time_step(a, 300.0, nsteps=3)
+    obgc.time_step(b, 300.0, nsteps=3, graph=True)
+    torch.cuda.synchronize()
+    assert torch.equal(a.state_array(), b.state_array())
+    obgc.time_step(a, 300.0, nsteps=2)
+    obgc.time_step(b, 300.0, nsteps=1)
+    obgc.time_step(b, 300.0, nsteps=1)
+    torch.cuda.synchronize()
+    assert torch.equal(a.state_array(), b.state_array())
