@@ -24,12 +24,19 @@ inline TwoBandT<T> make_twoband(const obgc_twoband_params& p) {
     return o;
 }
 
-// Chlorophyll terms of one cell: (P Rchl/r)^e_r and ^e_b.
+// Chlorophyll terms of one cell: (P Rchl/r)^e_r and ^e_b, sharing one logarithm:
+// c^e = 2^(e log2 c).  c = 0 gives 0 and c < 0 gives NaN, as the power does.
 template <typename T>
 __host__ __device__ __forceinline__ void twoband_terms(const TwoBandT<T>& L, T P, T& fr, T& fb) {
     const T c = P * L.inv_r_times_Rc;
+#ifdef __CUDA_ARCH__
+    const T l2 = sizeof(T) == 4 ? T(log2f(float(c))) : T(log2(double(c)));
+    fr = sizeof(T) == 4 ? T(exp2f(float(L.er * l2))) : T(exp2(double(L.er * l2)));
+    fb = sizeof(T) == 4 ? T(exp2f(float(L.eb * l2))) : T(exp2(double(L.eb * l2)));
+#else
     fr = t_pow(c, L.er);
     fb = t_pow(c, L.eb);
+#endif
 }
 
 // PAR at a cell centre z given the sums over the cells above (Sr, Sb) and this cell's terms.

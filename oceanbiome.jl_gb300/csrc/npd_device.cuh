@@ -79,6 +79,16 @@ inline int variant_of(const obgc_npd_params& p) {
 
 // Fused evaluation of every tendency of the model at one point.  G receives the tendencies of
 // the model's tracers (others untouched).
+// Division by a denominator bounded away from zero (a half-saturation constant plus a
+// concentration): the fast FP32 division on the device (<= 2 ulp), IEEE division otherwise.
+template <typename T>
+__host__ __device__ __forceinline__ T qdiv(T a, T b) {
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(T) == 4) return __fdividef(a, b);
+#endif
+    return a / b;
+}
+
 template <int V, typename T>
 __host__ __device__ inline void npd_tendencies(const NPDParamsT<T>& p, const T* v, T PAR, T* G) {
     const int nut = V >= 0 ? vnut(V) : p.nutrients;
@@ -106,9 +116,10 @@ __host__ __device__ inline void npd_tendencies(const NPDParamsT<T>& p, const T* 
     // grazing (plankton.jl:118-135, 352-397)
     const T pp = p.p_pref * P / (p.p_pref * P + (one - p.p_pref) * sP + tiny<T>());
     const T food = pp * P + (one - pp) * sP;
-    const T L = p.graz == OBGC_LINEAR ? food / (food + p.kG) : (food * food) / (food * food + p.kG * p.kG);
+    const T L = p.graz == OBGC_LINEAR ? qdiv(food, food + p.kG) : qdiv(food * food, food * food + p.kG * p.kG);
     const T Gtot = p.g_max * L * Z;
     const T fden = food + jl_eps(food);
+    // the eps-guarded denominators need true division: their reciprocal overflows at zero
     const T GP = p.g_max * pp * L * P / fden * Z;
     const T Gs = p.g_max * (one - pp) * L * sP / fden * Z;
     const T nuP = p.pmort == OBGC_LINEAR ? p.mP * P : p.mP * (P * P);
@@ -117,14 +128,14 @@ __host__ __device__ inline void npd_tendencies(const NPDParamsT<T>& p, const T* 
     T nl = 0, al = 0, Ln;
     if (nut != OBGC_NUT_NUTRIENT) {
         const T NO3 = v[OBGC_NO3], NH4 = v[OBGC_NH4];
-        nl = NO3 * t_exp(-p.psi * NH4) / (NO3 + p.kNO3);
-        al = t_max0(NH4 / (p.kNH4 + NH4));
+        nl = qdiv(NO3 * t_exp(-p.psi * NH4), NO3 + p.kNO3);
+        al = t_max0(qdiv(NH4, p.kNH4 + NH4));
         Ln = (nl + al) / two;
         if (nut == OBGC_NUT_NITRATE_AMMONIA_IRON) Ln = Ln * (v[OBGC_FE] / (p.kFe + v[OBGC_FE]));
     } else {
-        Ln = v[OBGC_N] / (v[OBGC_N] + p.kNO3);
+        Ln = qdiv(v[OBGC_N], v[OBGC_N] + p.kNO3);
     }
-    const T Ll = p.light_limitation == OBGC_LIGHT_MONDO ? PAR / (p.kPAR + PAR)
+    const T Ll = p.light_limitation == OBGC_LIGHT_MONDO ? qdiv(PAR, p.kPAR + PAR)
                                                           : PAR / t_sqrt(PAR * PAR + p.kPAR * p.kPAR);
     const T Lt = q10 ? t_pow(p.Q10, v[OBGC_T] / T(10)) : one;
     const T muP = p.mu0 * Ll * Ln * Lt * P;

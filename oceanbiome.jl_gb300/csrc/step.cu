@@ -297,6 +297,7 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.flat_y = g.topology_y == OBGC_FLAT || !c->desc.advection;
     a.sj = g.stride_j; a.sk = g.stride_k;
     a.dx = TC(g.Lx / g.Nx); a.dy = TC(g.Ly / g.Ny); a.dz = TC(g.Lz / g.Nz); a.Lz = TC(g.Lz);
+    a.inv_dx = TC(g.Nx / g.Lx); a.inv_dy = TC(g.Ny / g.Ly); a.inv_dz = TC(g.Nz / g.Lz);
     a.TZ = c->TZ < g.Nz ? c->TZ : g.Nz;
     a.nseg = (g.Nz + a.TZ - 1) / a.TZ;
     a.ntx = (g.Nx + STEP_BX - 1) / STEP_BX;

@@ -18,6 +18,7 @@
 #include "light_device.cuh"
 #include "npd_device.cuh"
 #include "weno_device.cuh"
+#include "weno_x2.cuh"
 
 namespace obgc {
 
@@ -49,7 +50,7 @@ struct SubstepArgs {
     int Nx, Ny, Nz;
     int periodic_x, periodic_y, flat_x, flat_y;
     int64_t sj, sk;
-    TC dx, dy, dz, Lz;
+    TC dx, dy, dz, Lz, inv_dx, inv_dy, inv_dz;
     int TZ, nseg, ntx, nty, n_items;
     const TS* in[MAX_NT];
     TS* out[MAX_NT];
@@ -73,6 +74,13 @@ struct SubstepArgs {
 template <typename TS, typename TC>
 __device__ __forceinline__ TC ld(const TS* p, int64_t i) { return TC(__ldg(p + i)); }
 
+// WENO5 of the upwind stencil: the five values are selected by the velocity sign first, so lanes
+// of a warp with opposite signs still run one reconstruction.
+template <typename TC>
+__device__ __forceinline__ TC weno5_upwind(bool pos, TC c0, TC c1, TC c2, TC c3, TC c4, TC c5) {
+    return weno5(pos ? c0 : c5, pos ? c1 : c4, pos ? c2 : c3, pos ? c3 : c2, pos ? c4 : c1);
+}
+
 // Upwind-biased flux U * c_face at face f (between cells f-1 and f) of a line of N cells.
 template <typename TS, typename TC>
 __device__ __forceinline__ TC face_flux(const TS* __restrict__ line, int64_t s, int N, bool periodic, int f, TC U) {
@@ -88,8 +96,7 @@ __device__ __forceinline__ TC face_flux(const TS* __restrict__ line, int64_t s, 
         }
         const TC c0 = ld<TS, TC>(line, m[0] * s), c1 = ld<TS, TC>(line, m[1] * s), c2 = ld<TS, TC>(line, m[2] * s);
         const TC c3 = ld<TS, TC>(line, m[3] * s), c4 = ld<TS, TC>(line, m[4] * s), c5 = ld<TS, TC>(line, m[5] * s);
-        const TC r = pos ? weno5(c0, c1, c2, c3, c4) : weno5(c5, c4, c3, c2, c1);
-        return U * r;
+        return U * weno5_upwind(pos, c0, c1, c2, c3, c4, c5);
     }
     const int b = f < N - f ? f : N - f;
     TC r;
@@ -97,7 +104,7 @@ __device__ __forceinline__ TC face_flux(const TS* __restrict__ line, int64_t s, 
         const TC c0 = ld<TS, TC>(line, (int64_t)(f - 3) * s), c1 = ld<TS, TC>(line, (int64_t)(f - 2) * s);
         const TC c2 = ld<TS, TC>(line, (int64_t)(f - 1) * s), c3 = ld<TS, TC>(line, (int64_t)f * s);
         const TC c4 = ld<TS, TC>(line, (int64_t)(f + 1) * s), c5 = ld<TS, TC>(line, (int64_t)(f + 2) * s);
-        r = pos ? weno5(c0, c1, c2, c3, c4) : weno5(c5, c4, c3, c2, c1);
+        r = weno5_upwind(pos, c0, c1, c2, c3, c4, c5);
     } else if (b == 2) {
         const TC c1 = ld<TS, TC>(line, (int64_t)(f - 2) * s), c2 = ld<TS, TC>(line, (int64_t)(f - 1) * s);
         const TC c3 = ld<TS, TC>(line, (int64_t)f * s), c4 = ld<TS, TC>(line, (int64_t)(f + 1) * s);
@@ -121,23 +128,93 @@ __device__ __forceinline__ TC face_velocity(const TS* __restrict__ vel, int64_t 
 
 template <typename TC, int NT>
 constexpr size_t substep_smem_bytes() {
-    return sizeof(TC) * NT * (STEP_BY * (STEP_BX + 1) + (STEP_BY + 1) * STEP_BX);
+    // fx, fy face fluxes, the carried vertical flux and its divergence, and every tracer's tile
+    return sizeof(TC) * NT * (STEP_BY * (STEP_BX + 1) + (STEP_BY + 1) * STEP_BX + 2 * STEP_BX * STEP_BY +
+                              (STEP_BY + 6) * (STEP_BX + 6));
+}
+
+constexpr int HALO = 3;
+constexpr int TILE_W = STEP_BX + 2 * HALO;
+constexpr int TILE_H = STEP_BY + 2 * HALO;
+constexpr int TILE_LOADS = (TILE_W * TILE_H + STEP_BX * STEP_BY - 1) / (STEP_BX * STEP_BY);
+
+// Face flux from six tile values s[0], s[st], ..., s[5 st] = c[f-3 .. f+2] of a line of N cells,
+// with the Bounded-wall order reduction of face_flux.
+template <typename TC>
+__device__ __forceinline__ TC tile_face_flux(const TC* s, int st, bool periodic, int f, int N, TC U) {
+    if (U == TC(0)) return TC(0);
+    const bool pos = U > TC(0);
+    const int b = periodic ? 3 : min(f, N - f);
+    TC r;
+    if (b >= 3) r = weno5_upwind(pos, s[0], s[st], s[2 * st], s[3 * st], s[4 * st], s[5 * st]);
+    else if (b == 2) r = pos ? weno3(s[st], s[2 * st], s[3 * st]) : weno3(s[4 * st], s[3 * st], s[2 * st]);
+    else if (b == 1) r = pos ? s[2 * st] : s[3 * st];
+    else r = TC(0);
+    return U * r;
+}
+
+// Vertical face flux from a window w0..w5 = c[f-3 .. f+2] (same order reduction and wall rule as
+// face_flux: a wall face takes the adjacent interior value).
+template <typename TC>
+__device__ __forceinline__ TC window_face_flux(TC w0, TC w1, TC w2, TC w3, TC w4, TC w5, int f, int N, TC U) {
+    if (U == TC(0)) return TC(0);
+    const bool pos = U > TC(0);
+    const int b = min(f, N - f);
+    TC r;
+    if (b >= 3) r = weno5_upwind(pos, w0, w1, w2, w3, w4, w5);
+    else if (b == 2) r = pos ? weno3(w1, w2, w3) : weno3(w4, w3, w2);
+    else if (b == 1) r = pos ? w2 : w3;
+    else r = f == 0 ? w3 : w2;
+    return U * r;
+}
+
+__device__ __forceinline__ int wrap_or_clamp(int x, int N, bool periodic) {
+    if (periodic) {
+        while (x < 0) x += N;
+        while (x >= N) x -= N;
+        return x;
+    }
+    return min(max(x, 0), N - 1);
+}
+
+// Flux of tracer line `line` through vertical face f (model w and the tracer's drift velocity).
+template <typename TS, typename TC>
+__device__ __forceinline__ TC vertical_flux(const SubstepArgs<TS, TC>& a, const TS* __restrict__ line, int64_t col,
+                                            int t, int f) {
+    TC F = TC(0);
+    if (a.w) F += face_flux<TS, TC>(line, a.sk, a.Nz, false, f, face_velocity<TS, TC>(a.w, col, a.sk, a.Nz, false, f));
+    if ((a.drift_mask >> t) & 1u) F += face_flux<TS, TC>(line, a.sk, a.Nz, false, f, a.drift[t * (a.Nz + 1) + f]);
+    return F;
 }
 
 template <int V, int NT, typename TS, typename TC>
-__global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 2 : 1) substep_kernel(const SubstepArgs<TS, TC> a) {
+__global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 3 : 1)
+    substep_kernel(const __grid_constant__ SubstepArgs<TS, TC> a) {
     constexpr int NB = n_bgc(V);
     constexpr int SP = slot_of_P(V);
-    constexpr int NWARP = STEP_BX * STEP_BY / 32;
+    constexpr int NTH = STEP_BX * STEP_BY;
+    constexpr int NWARP = NTH / 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TC (*fx)[STEP_BY][STEP_BX + 1] = reinterpret_cast<TC (*)[STEP_BY][STEP_BX + 1]>(smem_raw);
     TC (*fy)[STEP_BY + 1][STEP_BX] =
         reinterpret_cast<TC (*)[STEP_BY + 1][STEP_BX]>(smem_raw + sizeof(TC) * NT * STEP_BY * (STEP_BX + 1));
+    TC* fzu = reinterpret_cast<TC*>(smem_raw + sizeof(TC) * NT * (STEP_BY * (STEP_BX + 1) + (STEP_BY + 1) * STEP_BX));
+    TC* vdv = fzu + NT * NTH;
+    TC* tiles = vdv + NT * NTH;     // NT tiles of TILE_H x TILE_W (tile + 3-cell halo)
+    constexpr int TILE_SZ = TILE_H * TILE_W;
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = tx + STEP_BX * ty;
     const int warp = tid >> 5, lane = tid & 31;
     const bool periodic_x = a.periodic_x, periodic_y = a.periodic_y;
+    // Sinking tracers advance their vertical stencil in a register window (one new load per
+    // level); two window slots per variant (LOBSTER: sPOM, bPOM; NPZD: P, D).  Any other
+    // vertically advected tracer, and every tracer when a model w is given, takes the generic path.
+    constexpr int WA = V == V_NPZD ? 1 : 4, WB = V == V_NPZD ? 4 : 5;
+    const bool winA = a.w == nullptr && ((a.drift_mask >> WA) & 1u);
+    const bool winB = a.w == nullptr && ((a.drift_mask >> WB) & 1u);
+    const uint32_t gen_mask = a.w != nullptr ? 0xffffffffu : (a.drift_mask & ~((1u << WA) | (1u << WB)));
+    const bool any_generic = (gen_mask & ((1u << NT) - 1u)) != 0u;
 
     TC PAR0;
     if (a.surf_kind == OBGC_SURFACE_PAR_DEFAULT) PAR0 = TC(default_surface_par(*a.d_time + a.c_stage * a.dt_d));
@@ -156,8 +233,20 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 2 : 1) su
         const int64_t col = ic + (int64_t)jc * a.sj;
         const TC P0 = a.surf_kind == OBGC_SURFACE_PAR_FIELD ? TC(a.surf_field[ic + (int64_t)jc * a.Nx]) : PAR0;
 
+        // horizontal offsets of the tile elements this thread stages (the same for every level
+        // and tracer of the work item)
+        int64_t toff[TILE_LOADS];
+#pragma unroll
+        for (int q = 0; q < TILE_LOADS; q++) {
+            const int e = min(tid + q * NTH, TILE_H * TILE_W - 1);
+            const int r = e / TILE_W, c = e - r * TILE_W;
+            toff[q] = wrap_or_clamp(i0 - HALO + c, a.Nx, periodic_x) +
+                      (int64_t)wrap_or_clamp(j0 - HALO + r, a.Ny, periodic_y) * a.sj;
+        }
+
         // chlorophyll integral of the cells above the segment
         TC Sr = TC(0), Sb = TC(0);
+#pragma unroll 1
         for (int k = a.Nz - 1; k > k_top; --k) {
             TC fr, fb;
             twoband_terms(a.light, ld<TS, TC>(a.in[SP], col + (int64_t)k * a.sk), fr, fb);
@@ -165,25 +254,143 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 2 : 1) su
             Sb += fb;
         }
 
-        // vertical flux through the face above the segment (k_top + 1)
-        TC Fz_up[NT];
-#pragma unroll
-        for (int t = 0; t < NT; t++) {
-            Fz_up[t] = TC(0);
-            const bool drifts = (a.drift_mask >> t) & 1u;
-            if (a.w || drifts) {
-                const TS* line = a.in[t] + col;
-                const int f = k_top + 1;
-                if (a.w) Fz_up[t] += face_flux<TS, TC>(line, a.sk, a.Nz, false, f, face_velocity<TS, TC>(a.w, col, a.sk, a.Nz, false, f));
-                if (drifts) Fz_up[t] += face_flux<TS, TC>(line, a.sk, a.Nz, false, f, a.drift[t * (a.Nz + 1) + f]);
+        // vertical flux through the face above the segment (k_top + 1), carried per thread in smem
+        if (any_generic) {
+#pragma unroll 1
+            for (int t = 0; t < NT; t++) {
+                const bool vert = (gen_mask >> t) & 1u;
+                fzu[t * NTH + tid] = vert ? vertical_flux(a, a.in[t] + col, col, t, k_top + 1) : TC(0);
+                vdv[t * NTH + tid] = TC(0);
             }
         }
+        // register windows wA/wB = c[k-3 .. k+3] of the two window tracers, and their carried
+        // flux through the face above the current level
+        TC wA[7], wB[7], FzA = TC(0), FzB = TC(0);
+#pragma unroll
+        for (int m = 0; m < 7; m++) {
+            const int kk = min(max(k_top - 3 + m, 0), a.Nz - 1);
+            wA[m] = winA ? ld<TS, TC>(a.in[WA], col + (int64_t)kk * a.sk) : TC(0);
+            wB[m] = winB ? ld<TS, TC>(a.in[WB], col + (int64_t)kk * a.sk) : TC(0);
+        }
+        if (winA) FzA = window_face_flux(wA[1], wA[2], wA[3], wA[4], wA[5], wA[6], k_top + 1, a.Nz, a.drift[WA * (a.Nz + 1) + k_top + 1]);
+        if (winB) FzB = window_face_flux(wB[1], wB[2], wB[3], wB[4], wB[5], wB[6], k_top + 1, a.Nz, a.drift[WB * (a.Nz + 1) + k_top + 1]);
 
+#pragma unroll 1
         for (int k = k_top; k >= k_bot; --k) {
             const int64_t idx = col + (int64_t)k * a.sk;
+            const int64_t kofs = (int64_t)k * a.sk;
+            // stage every tracer's tile and halo for this level: all loads in flight together
+#pragma unroll
+            for (int t = 0; t < NT; t++) {
+                const TS* __restrict__ base = a.in[t] + kofs;
+                TC* tl = tiles + t * TILE_SZ;
+#pragma unroll
+                for (int q = 0; q < TILE_LOADS; q++)
+                    if (q < TILE_LOADS - 1 || tid + q * NTH < TILE_SZ) tl[tid + q * NTH] = ld<TS, TC>(base, toff[q]);
+            }
+            const int64_t rowb = (int64_t)jc * a.sj + kofs;
+            const int64_t cb = ic + kofs;
+            const bool xok = !a.flat_x && i <= a.Nx && j < a.Ny;
+            const bool yok = !a.flat_y && i < a.Nx && j <= a.Ny;
+            const TC Ux = xok ? face_velocity<TS, TC>(a.u, rowb, 1, a.Nx, periodic_x, i) : TC(0);
+            const TC Uy = yok ? face_velocity<TS, TC>(a.v, cb, a.sj, a.Ny, periodic_y, j) : TC(0);
+            const bool full5 = (periodic_x || min(i, a.Nx - i) >= 3) && (periodic_y || min(j, a.Ny - j) >= 3);
+            __syncthreads();
+
             TC c[NT];
 #pragma unroll
-            for (int t = 0; t < NT; t++) c[t] = ld<TS, TC>(a.in[t], idx);
+            for (int t = 0; t < NT; t++) c[t] = tiles[t * TILE_SZ + (ty + HALO) * TILE_W + tx + HALO];
+
+            // west (x) and south (y) faces of this thread's cell for every tracer: one (not
+            // unrolled) loop keeps the code inside the instruction cache; in FP32 the two
+            // reconstructions run as one packed f32x2 WENO5
+#pragma unroll 1
+            for (int t = 0; t < NT; t++) {
+                const TC* tl = tiles + t * TILE_SZ;
+                const TC* xs = tl + (ty + HALO) * TILE_W + tx;   // c[i-3 .. i+2] along x
+                const TC* ys = tl + ty * TILE_W + tx + HALO;     // c[j-3 .. j+2] along y
+                TC Fx, Fy;
+#ifdef __CUDA_ARCH__
+                if constexpr (sizeof(TC) == 4) {
+                    if (full5) {
+                        const bool pxp = Ux > TC(0), pyp = Uy > TC(0);
+                        const f32x2 r = weno5_x2(
+                            pk2(pxp ? xs[0] : xs[5], pyp ? ys[0] : ys[5 * TILE_W]),
+                            pk2(pxp ? xs[1] : xs[4], pyp ? ys[TILE_W] : ys[4 * TILE_W]),
+                            pk2(pxp ? xs[2] : xs[3], pyp ? ys[2 * TILE_W] : ys[3 * TILE_W]),
+                            pk2(pxp ? xs[3] : xs[2], pyp ? ys[3 * TILE_W] : ys[2 * TILE_W]),
+                            pk2(pxp ? xs[4] : xs[1], pyp ? ys[4 * TILE_W] : ys[TILE_W]));
+                        float rx, ry;
+                        up2(r, rx, ry);
+                        Fx = Ux == TC(0) ? TC(0) : Ux * rx;
+                        Fy = Uy == TC(0) ? TC(0) : Uy * ry;
+                    } else {
+                        Fx = tile_face_flux<TC>(xs, 1, periodic_x, i, a.Nx, Ux);
+                        Fy = tile_face_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, Uy);
+                    }
+                } else
+#endif
+                {
+                    Fx = tile_face_flux<TC>(xs, 1, periodic_x, i, a.Nx, Ux);
+                    Fy = tile_face_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, Uy);
+                }
+                fx[t][ty][tx] = Fx;
+                fy[t][ty][tx] = Fy;
+                if ((gen_mask >> t) & 1u) {
+                    const TC Fz = vertical_flux(a, a.in[t] + col, col, t, k);   // face below this cell
+                    vdv[t * NTH + tid] = (fzu[t * NTH + tid] - Fz) * a.inv_dz;
+                    fzu[t * NTH + tid] = Fz;
+                }
+            }
+            // the tile's east (8 per tracer) and north (32 per tracer) edge faces, spread over
+            // every thread of the block
+            constexpr int NEDGE = STEP_BY + STEP_BX;
+#pragma unroll 1
+            for (int e = tid; e < NT * NEDGE; e += NTH) {
+                const int t = e / NEDGE, r = e - t * NEDGE;
+                const TC* tl = tiles + t * TILE_SZ;
+                if (r < STEP_BY) {
+                    const int jr = j0 + r, f = i0 + STEP_BX;
+                    TC Fe = TC(0);
+                    if (!a.flat_x && jr < a.Ny && f <= a.Nx) {
+                        const int64_t rb = (int64_t)jr * a.sj + kofs;
+                        Fe = tile_face_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx,
+                                                face_velocity<TS, TC>(a.u, rb, 1, a.Nx, periodic_x, f));
+                    }
+                    fx[t][r][STEP_BX] = Fe;
+                } else {
+                    const int cc = r - STEP_BY, ix = i0 + cc, f = j0 + STEP_BY;
+                    TC Fe = TC(0);
+                    if (!a.flat_y && ix < a.Nx && f <= a.Ny) {
+                        const int64_t cb2 = ix + kofs;
+                        Fe = tile_face_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny,
+                                                face_velocity<TS, TC>(a.v, cb2, a.sj, a.Ny, periodic_y, f));
+                    }
+                    fy[t][STEP_BY][cc] = Fe;
+                }
+            }
+            __syncthreads();
+
+            // window tracers: flux through the face below this cell, divergence, and slide the
+            // windows down one level (the next level needs c[k-4])
+            TC vdA = TC(0), vdB = TC(0);
+            if (winA) {
+                const TC F = window_face_flux(wA[0], wA[1], wA[2], wA[3], wA[4], wA[5], k, a.Nz, a.drift[WA * (a.Nz + 1) + k]);
+                vdA = (FzA - F) * a.inv_dz;
+                FzA = F;
+            }
+            if (winB) {
+                const TC F = window_face_flux(wB[0], wB[1], wB[2], wB[3], wB[4], wB[5], k, a.Nz, a.drift[WB * (a.Nz + 1) + k]);
+                vdB = (FzB - F) * a.inv_dz;
+                FzB = F;
+            }
+            if (k > k_bot) {
+                const int64_t nk = col + (int64_t)max(k - 4, 0) * a.sk;
+#pragma unroll
+                for (int m = 6; m > 0; m--) { wA[m] = wA[m - 1]; wB[m] = wB[m - 1]; }
+                if (winA) wA[0] = ld<TS, TC>(a.in[WA], nk);
+                if (winB) wB[0] = ld<TS, TC>(a.in[WB], nk);
+            }
 
             // PAR at this cell (2band.jl:26-31)
             TC fr, fb;
@@ -192,61 +399,6 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 2 : 1) su
             const TC PAR = twoband_par(a.light, P0, z, a.dz, Sr, Sb, fr, fb);
             Sr += fr;
             Sb += fb;
-
-            // horizontal face fluxes
-            __syncthreads();
-#pragma unroll
-            for (int t = 0; t < NT; t++) {
-                if (!a.flat_x) {
-                    const int64_t rowb = (int64_t)jc * a.sj + (int64_t)k * a.sk;
-                    const TS* line = a.in[t] + rowb;
-                    {
-                        const int f = i;   // left face of this cell
-                        TC F = TC(0);
-                        if (active || (i <= a.Nx && j < a.Ny)) {
-                            const TC U = face_velocity<TS, TC>(a.u, rowb, 1, a.Nx, periodic_x, f);
-                            F = face_flux<TS, TC>(line, 1, a.Nx, periodic_x, f, U);
-                        }
-                        fx[t][ty][tx] = F;
-                    }
-                    if (warp == (2 * t) % NWARP && lane < STEP_BY) {
-                        const int r = lane, jr = j0 + r;
-                        const int f = i0 + STEP_BX;
-                        TC F = TC(0);
-                        if (jr < a.Ny && f <= a.Nx) {
-                            const int64_t rb = (int64_t)jr * a.sj + (int64_t)k * a.sk;
-                            const TC U = face_velocity<TS, TC>(a.u, rb, 1, a.Nx, periodic_x, f);
-                            F = face_flux<TS, TC>(a.in[t] + rb, 1, a.Nx, periodic_x, f, U);
-                        }
-                        fx[t][r][STEP_BX] = F;
-                    }
-                }
-                if (!a.flat_y) {
-                    const int64_t cb = ic + (int64_t)k * a.sk;
-                    const TS* line = a.in[t] + cb;
-                    {
-                        const int f = j;   // south face of this cell
-                        TC F = TC(0);
-                        if (i < a.Nx && j <= a.Ny) {
-                            const TC U = face_velocity<TS, TC>(a.v, cb, a.sj, a.Ny, periodic_y, f);
-                            F = face_flux<TS, TC>(line, a.sj, a.Ny, periodic_y, f, U);
-                        }
-                        fy[t][ty][tx] = F;
-                    }
-                    if (warp == (2 * t + 1) % NWARP) {
-                        const int ix = i0 + lane;
-                        const int f = j0 + STEP_BY;
-                        TC F = TC(0);
-                        if (ix < a.Nx && f <= a.Ny) {
-                            const int64_t cb2 = ix + (int64_t)k * a.sk;
-                            const TC U = face_velocity<TS, TC>(a.v, cb2, a.sj, a.Ny, periodic_y, f);
-                            F = face_flux<TS, TC>(a.in[t] + cb2, a.sj, a.Ny, periodic_y, f, U);
-                        }
-                        fy[t][STEP_BY][lane] = F;
-                    }
-                }
-            }
-            __syncthreads();
 
             // named values for the BGC functors
             TC vals[OBGC_NUM_NAMED], g[OBGC_NUM_NAMED];
@@ -259,17 +411,11 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 2 : 1) su
 #pragma unroll
             for (int t = 0; t < NT; t++) {
                 TC adv = TC(0);
-                if (!a.flat_x) adv += (fx[t][ty][tx + 1] - fx[t][ty][tx]) / a.dx;
-                if (!a.flat_y) adv += (fy[t][ty + 1][tx] - fy[t][ty][tx]) / a.dy;
-                const bool drifts = (a.drift_mask >> t) & 1u;
-                if (a.w || drifts) {
-                    const TS* line = a.in[t] + col;
-                    TC Fz = TC(0);
-                    if (a.w) Fz += face_flux<TS, TC>(line, a.sk, a.Nz, false, k, face_velocity<TS, TC>(a.w, col, a.sk, a.Nz, false, k));
-                    if (drifts) Fz += face_flux<TS, TC>(line, a.sk, a.Nz, false, k, a.drift[t * (a.Nz + 1) + k]);
-                    adv += (Fz_up[t] - Fz) / a.dz;
-                    Fz_up[t] = Fz;
-                }
+                if (!a.flat_x) adv += (fx[t][ty][tx + 1] - fx[t][ty][tx]) * a.inv_dx;
+                if (!a.flat_y) adv += (fy[t][ty + 1][tx] - fy[t][ty][tx]) * a.inv_dy;
+                if (any_generic) adv += vdv[t * NTH + tid];
+                if (t == WA) adv += vdA;
+                if (t == WB) adv += vdB;
                 const TC Gt = (t < NB ? g[slot_name(V, t)] : TC(0)) - adv;
                 if (active) {
                     TC Un;
@@ -280,7 +426,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 2 : 1) su
                         Un = a.dt * (a.gamma * Gt + a.zeta * Gm);
                     }
                     // accumulate in the storage precision (FP64 for the mixed path)
-                    a.out[t][idx] = TS(__ldg(a.in[t] + idx)) + TS(Un);
+                    if constexpr (sizeof(TS) == sizeof(TC)) a.out[t][idx] = c[t] + Un;
+                    else a.out[t][idx] = TS(__ldg(a.in[t] + idx)) + TS(Un);
                     if (a.write_G) a.G[t][idx] = Gt;
                 }
             }

@@ -35,27 +35,40 @@ __host__ __device__ __forceinline__ T weno5(T v1, T v2, T v3, T v4, T v5) {
 }
 
 // FP32 specialisation with approximate reciprocals: four MUFU ops per face instead of four IEEE
-// divisions.  rcp.approx has <= 1 ulp error, well inside the FP32 path's stated tolerance.
+// divisions.  rcp.approx has <= 1 ulp error, well inside the FP32 path's stated tolerance; its
+// arguments here are >= 1e-8 (beta + eps) and >= 1 (sum of alphas), so flushing subnormals is moot.
 #ifdef __CUDA_ARCH__
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+// The operation sequence matches weno5_x2 (weno_x2.cuh) element for element, so a face rounds the
+// same whichever of the two computes it.
 template <>
 __device__ __forceinline__ float weno5<float>(float v1, float v2, float v3, float v4, float v5) {
     const float eps = 1e-8f;
-    const float c6 = 1.0f / 6.0f;
-    const float q0 = (2.f * v1 - 7.f * v2 + 11.f * v3) * c6;
-    const float q1 = (-v2 + 5.f * v3 + 2.f * v4) * c6;
-    const float q2 = (2.f * v3 + 5.f * v4 - v5) * c6;
-    float a = v1 - 2.f * v2 + v3, b = v1 - 4.f * v2 + 3.f * v3;
-    const float b0 = (13.f / 12.f) * a * a + 0.25f * b * b;
-    a = v2 - 2.f * v3 + v4; b = v2 - v4;
-    const float b1 = (13.f / 12.f) * a * a + 0.25f * b * b;
-    a = v3 - 2.f * v4 + v5; b = 3.f * v3 - 4.f * v4 + v5;
-    const float b2 = (13.f / 12.f) * a * a + 0.25f * b * b;
-    const float tau = fabsf(b0 - b2);
-    const float r0 = tau * __frcp_rn(b0 + eps), r1 = tau * __frcp_rn(b1 + eps), r2 = tau * __frcp_rn(b2 + eps);
-    const float a0 = 0.1f * fmaf(r0, r0, 1.f);
-    const float a1 = 0.6f * fmaf(r1, r1, 1.f);
-    const float a2 = 0.3f * fmaf(r2, r2, 1.f);
-    return (a0 * q0 + a1 * q1 + a2 * q2) * __frcp_rn(a0 + a1 + a2);
+    const float q0 = fmaf(2.f / 6.f, v1, fmaf(-7.f / 6.f, v2, __fmul_rn(11.f / 6.f, v3)));
+    const float q1 = fmaf(-1.f / 6.f, v2, fmaf(5.f / 6.f, v3, __fmul_rn(2.f / 6.f, v4)));
+    const float q2 = fmaf(2.f / 6.f, v3, fmaf(5.f / 6.f, v4, __fmul_rn(-1.f / 6.f, v5)));
+    float a = fmaf(-2.f, v2, __fadd_rn(v1, v3));
+    float b = fmaf(-4.f, v2, fmaf(3.f, v3, v1));
+    const float b0 = fmaf(__fmul_rn(13.f / 12.f, a), a, __fmul_rn(__fmul_rn(0.25f, b), b));
+    a = fmaf(-2.f, v3, __fadd_rn(v2, v4));
+    b = __fsub_rn(v2, v4);
+    const float b1 = fmaf(__fmul_rn(13.f / 12.f, a), a, __fmul_rn(__fmul_rn(0.25f, b), b));
+    a = fmaf(-2.f, v4, __fadd_rn(v3, v5));
+    b = fmaf(-4.f, v4, fmaf(3.f, v3, v5));
+    const float b2 = fmaf(__fmul_rn(13.f / 12.f, a), a, __fmul_rn(__fmul_rn(0.25f, b), b));
+    const float tau = fabsf(__fsub_rn(b0, b2));
+    const float r0 = __fmul_rn(tau, rcp_approx(__fadd_rn(b0, eps)));
+    const float r1 = __fmul_rn(tau, rcp_approx(__fadd_rn(b1, eps)));
+    const float r2 = __fmul_rn(tau, rcp_approx(__fadd_rn(b2, eps)));
+    const float a0 = __fmul_rn(0.1f, fmaf(r0, r0, 1.f));
+    const float a1 = __fmul_rn(0.6f, fmaf(r1, r1, 1.f));
+    const float a2 = __fmul_rn(0.3f, fmaf(r2, r2, 1.f));
+    const float num = fmaf(a0, q0, fmaf(a1, q1, __fmul_rn(a2, q2)));
+    return __fmul_rn(num, rcp_approx(__fadd_rn(__fadd_rn(a0, a1), a2)));
 }
 #endif
 

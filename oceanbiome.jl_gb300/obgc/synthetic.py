@@ -33,12 +33,51 @@ def random_streamfunction_velocity(grid, rms=0.1, seed=0, modes=6, device="cuda"
     return (torch.as_tensor(u, dtype=dt, device=device), torch.as_tensor(v, dtype=dt, device=device), None)
 
 
-def lobster_initial_conditions(grid, seed=0):
+def correlated_normal(shape, rng, length=(1.0, 2.0, 2.0)):
+    """Standard-normal field (zero mean, unit variance per cell) with Gaussian spatial correlation
+    of the given length in cells along (z, y, x), periodic in every direction."""
+    white = rng.standard_normal(shape)
+    spec = np.fft.rfftn(white)
+    kz = np.fft.fftfreq(shape[0])[:, None, None]
+    ky = np.fft.fftfreq(shape[1])[None, :, None]
+    kx = np.fft.rfftfreq(shape[2])[None, None, :]
+    filt = np.exp(-2 * np.pi ** 2 * ((kz * length[0]) ** 2 + (ky * length[1]) ** 2 + (kx * length[2]) ** 2))
+    f = np.fft.irfftn(spec * filt, s=shape)
+    f -= f.mean()
+    return f / f.std()
+
+
+def _uniform(g, lo, hi):
+    """Map a standard-normal field to U(lo, hi) through the normal CDF."""
+    return lo + (hi - lo) * 0.5 * (1 + _erf(g / np.sqrt(2)))
+
+
+def _erf(x):
+    # Abramowitz & Stegun 7.1.26 (|error| < 1.5e-7): only shapes a uniform marginal
+    s = np.sign(x)
+    a = np.abs(x)
+    t = 1 / (1 + 0.3275911 * a)
+    y = 1 - (((((1.061405429 * t - 1.453152027) * t) + 1.421413741) * t - 0.284496736) * t + 0.254829592) * t * np.exp(-a * a)
+    return s * y
+
+
+def lobster_initial_conditions(grid, seed=0, correlated=True):
     """NO3 ~ U(5,15); P, Z ~ LogNormal(log 0.1, 0.5); DIC ~ U(2100,2250); Alk ~ U(2300,2450);
-    T = 12 - 0.01 z; S = 35; NH4, sPOM, bPOM, DOM = 0."""
+    T = 12 - 0.01 z; S = 35; NH4, sPOM, bPOM, DOM = 0.  With `correlated`, each field keeps that
+    marginal distribution but is spatially correlated over ~2 cells (white noise at the grid scale
+    drives WENO undershoots, and a negative P makes the (P R/r)^e of the light model undefined)."""
     rng = np.random.default_rng(seed)
     shp = grid.shape
     z = grid.znodes()[:, None, None] * np.ones(shp)
+    if correlated:
+        n = lambda: correlated_normal(shp, rng)
+        return {
+            "NO3": _uniform(n(), 5, 15), "NH4": 0.0,
+            "P": np.exp(np.log(0.1) + 0.5 * n()), "Z": np.exp(np.log(0.1) + 0.5 * n()),
+            "sPOM": 0.0, "bPOM": 0.0, "DOM": 0.0,
+            "DIC": _uniform(n(), 2100, 2250), "Alk": _uniform(n(), 2300, 2450),
+            "T": 12 - 0.01 * z, "S": 35.0,
+        }
     return {
         "NO3": rng.uniform(5, 15, shp), "NH4": 0.0,
         "P": rng.lognormal(np.log(0.1), 0.5, shp), "Z": rng.lognormal(np.log(0.1), 0.5, shp),
