@@ -392,6 +392,31 @@ int obgc_struct_layout(int32_t which, int64_t* out, int32_t cap);
  * compensated summation.  group: 0 nitrogen, 1 carbon.  Result written to *total (host). */
 int obgc_tracer_budget(obgc_ctx* ctx, int32_t group, double* total, void* stream);
 
+/*
+ * The same compensated FP64 budget reduction as obgc_tracer_budget, for callers that cannot
+ * allocate device memory.  No counterpart in the reference.
+ *
+ * Who needs it: a host whose device memory is owned by another allocator (CUDA.jl's or PyTorch's
+ * caching pool, where a foreign cudaMalloc fragments the pool or exceeds its reservation), and
+ * callers that run under a fixed device-memory budget (the column service admits runs against
+ * one).  Such callers cannot create a context, whose set-up allocates its reduction buffer.
+ *
+ * This entry point allocates nothing: its partial sums live in a file-scope device array of
+ * OBGC_BUDGET_STATIC_SLOTS entries (16 bytes each, 16 KiB in total), which every GPU that loads the
+ * library holds until the process exits.  fields[0..n_fields) are device arrays of dtype `dtype`
+ * on `grid`'s layout, scale[0..n_fields) host doubles; the result sum over cells of
+ * sum_n scale[n]*fields[n] is written to *total (host) and the call returns after the stream has
+ * finished it.  n_fields above OBGC_BUDGET_STATIC_MAX_FIELDS is rejected (OBGC_ERR_INVALID_ARGUMENT).
+ *
+ * The first call on each device looks up the array's device address on that device; make that
+ * first call before any stream capture.  All calls share the one array: calls that overlap on
+ * the GPU (different streams or host threads without ordering) race and corrupt each other's sums.
+ */
+#define OBGC_BUDGET_STATIC_SLOTS 1024
+#define OBGC_BUDGET_STATIC_MAX_FIELDS 8
+int obgc_tracer_budget_static(const obgc_grid* grid, int32_t dtype, int32_t n_fields, const void* const* fields,
+                              const double* scale, double* total, void* stream);
+
 /* ---------------------------------------------------------------------------------------
  * Batched box models (src/BoxModel): many independent 0-D NutrientsPlanktonDetritus models
  * ------------------------------------------------------------------------------------- */

@@ -188,6 +188,7 @@ def load():
     _sig(lib, "obgc_step_graph", C.c_int, VP, D, D, I32, VP)
     _sig(lib, "obgc_last_step_timing", C.c_int, VP, P(D), P(D), P(I64))
     _sig(lib, "obgc_tracer_budget", C.c_int, VP, I32, P(D), VP)
+    _sig(lib, "obgc_tracer_budget_static", C.c_int, P(Grid), I32, I32, P(VP), P(D), P(D), VP)
     _sig(lib, "obgc_set_profiling", C.c_int, VP, I32)
     _sig(lib, "obgc_set_tiling", C.c_int, VP, I32)
     _sig(lib, "obgc_box_run", C.c_int, P(NPDParams), VP, I64, VP, VP, D, D, D, I32, I32, VP, I32, VP)
@@ -204,5 +205,5 @@ EXPORTED = [
     "obgc_carbon_chemistry", "obgc_carbon_chemistry_point", "obgc_create", "obgc_destroy",
     "obgc_bind_fields", "obgc_update_state", "obgc_compute_tendencies", "obgc_step",
     "obgc_step_graph", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run",
-    "obgc_set_profiling", "obgc_set_tiling", "obgc_struct_layout",
+    "obgc_set_profiling", "obgc_set_tiling", "obgc_struct_layout", "obgc_tracer_budget_static",
 ]
