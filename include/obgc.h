@@ -43,6 +43,14 @@ enum obgc_status {
 
 /* Storage / compute precision of a field or a run. */
 enum obgc_dtype { OBGC_F32 = 0, OBGC_F64 = 1 };
+/* Negative-tracer modifier applied to the initial state and after every RK3 stage, as
+ * Oceananigans' update_state! runs update_biogeochemical_state!(model, modifier)
+ * (src/OceanBioME.jl:161-169, src/Utils/negative_tracers.jl). */
+enum obgc_negatives {
+    OBGC_NEGATIVES_NONE = 0,
+    OBGC_NEGATIVES_SCALE = 1,  /* ScaleNegativeTracers over conserved_tracers (scale_negatives = true) */
+    OBGC_NEGATIVES_ZERO = 2    /* ZeroNegativeTracers(; exclude)                                      */
+};
 enum obgc_precision {
     OBGC_PREC_F32 = 0,   /* FP32 state, FP32 compute                                       */
     OBGC_PREC_F64 = 1,   /* FP64 state, FP64 compute (plain FP64 path)                     */
@@ -212,6 +220,21 @@ int obgc_npd_required_tracers(const obgc_npd_params* p, int32_t* names, int32_t 
  * not (w_faces left untouched), <0 on error. */
 int obgc_npd_drift_velocity(const obgc_npd_params* p, int32_t name, int32_t Nz, double* w_faces);
 
+/* conserved_tracers(bgc) (NutrientsPlanktonDetritus/coupling_utils.jl:1-52): group 0 is the
+ * nitrogen tracers (scale factors 1), group 1 the carbon tracers with their scale factors (only with
+ * the carbonate system).  Returns the member count, or <0 when the group does not exist. */
+int obgc_npd_conserved_tracers(const obgc_npd_params* p, int32_t group, int32_t* names, double* scalefactors,
+                               int32_t cap);
+
+/* ScaleNegativeTracers(tracers; scalefactors, invalid_fill_value) applied once to n_fields (<= 8)
+ * fields on the grid's interior (update_biogeochemical_state!(model, ::ScaleNegativeTracers),
+ * src/Utils/negative_tracers.jl:136-276).  scalefactors NULL = ones. */
+int obgc_scale_negatives(const obgc_grid* grid, int32_t dtype, int32_t n_fields, void* const* fields,
+                         const double* scalefactors, double invalid_fill_value, void* stream);
+/* ZeroNegativeTracers applied once: max(0, c) on each of n_fields (<= 16) fields
+ * (src/Utils/negative_tracers.jl:23-29). */
+int obgc_zero_negatives(const obgc_grid* grid, int32_t dtype, int32_t n_fields, void* const* fields, void* stream);
+
 /* Continuous-form functor (bgc)(Val(:X), x, y, z, t, tracers..., PAR) for one point, host side
  * (docs/src/model_implementation.md:75, src/BoxModel/timesteppers.jl:60-61).  `values` holds
  * OBGC_NUM_NAMED entries indexed by enum obgc_tracer (absent tracers ignored).  Writes the
@@ -337,7 +360,11 @@ typedef struct obgc_model_desc {
     int32_t n_passive;            /* extra advected tracers with zero BGC tendency            */
     int32_t carry_T;              /* T carried as an advected tracer even if BGC ignores it   */
     int32_t carry_S;              /* S carried as an advected tracer                          */
-    int32_t reserved0;
+    int32_t negatives;            /* enum obgc_negatives                                      */
+    uint32_t zero_exclude;        /* ZeroNegativeTracers exclude: bit n = enum obgc_tracer n,
+                                     bit 21 + p = passive tracer p                            */
+    int32_t reserved1;
+    double invalid_fill_value;    /* ScaleNegativeTracers(...; invalid_fill_value) (NaN)      */
 } obgc_model_desc;
 
 /* Fields a context works on.  Tracer arrays are device pointers of the context's state dtype
@@ -434,6 +461,82 @@ int obgc_box_run(const obgc_npd_params* p, const obgc_npd_params* params_per_mod
                  int64_t n_models, double* state, const double* PAR, double par_constant,
                  double t0, double dt, int32_t nsteps, int32_t record_every, double* record,
                  int32_t precision, void* stream);
+
+/* ---------------------------------------------------------------------------------------
+ * Batched uneven columns: many independent 1-D water columns (different depth, parameters,
+ * step and duration) advanced together.  Each column is the reference's column configuration
+ * (examples/column.jl: NonhydrostaticModel on a 1 x 1 x Nz grid with a LOBSTER or NPZD
+ * biogeochemistry, TwoBand light, sinking, and a vertical diffusivity treated implicitly as in
+ * Oceananigans' VerticallyImplicitTimeDiscretization), RK3 as src/BoxModel/timesteppers.jl:66-93.
+ * Columns are packed into thread blocks by cell count and stay in shared memory for a whole
+ * launch of up to max_steps steps.
+ * ------------------------------------------------------------------------------------- */
+/* ---------------------------------------------------------------------------------------------
+ * Batched single-column runs.  Each column is the reference's one-dimensional setup
+ * (examples/column.jl:41-66: RectilinearGrid(size = (1, 1, Nz)) + LOBSTER or NPZD +
+ * ScalarDiffusivity(kappa(z)) with kappa(z) = 1e-2 (1 + tanh((z - MLD) / 10)) / 2 + 1e-4 at :34),
+ * time-stepped with Oceananigans' RK3 and a vertically implicit diffusion solve; sinking follows
+ * setup_velocity_fields (src/Utils/sinking_velocity_fields.jl:10-35) and the light is TwoBand with
+ * a constant surface PAR (src/Light/2band.jl:1-33).  An alkalinity pulse stands in for the OAE
+ * release forcing (examples/oae_experiment.jl:56-73) as an instantaneous addition at one level.
+ * Replaces running one NonhydrostaticModel per column; the engine keeps every column resident on
+ * the device, packs whole columns into thread blocks and advances all of them per launch.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct obgc_columns obgc_columns;
+
+#define OBGC_COLUMN_MAX_LEVELS 512
+
+typedef struct obgc_column_spec {
+    int32_t Nz;              /* levels, 1..OBGC_COLUMN_MAX_LEVELS                              */
+    int32_t nsteps;          /* RK3 steps to run                                               */
+    double dz;               /* level thickness (m)                                            */
+    double dt;               /* step (s)                                                       */
+    double surface_PAR;      /* constant surface PAR (W/m2)                                    */
+    double mu0;              /* phytoplankton_maximum_growth_rate for this column (<= 0: model's) */
+    int32_t pulse_step;      /* step at whose start pulse_amount is added to Alk (-1: none)    */
+    int32_t pulse_k;         /* level of the pulse (0 = bottom)                                */
+    double pulse_amount;     /* alkalinity added (meq/m3)                                      */
+} obgc_column_spec;
+
+typedef struct obgc_columns_desc {
+    obgc_npd_params npd;         /* NPZD, or LOBSTER with the carbonate system                 */
+    obgc_twoband_params light;
+    int32_t precision;           /* OBGC_PREC_F32, OBGC_PREC_F64, or OBGC_PREC_MIXED (FP64 state
+                                    and diffusion solve, FP32 light / sinking / BGC)           */
+    int32_t pack_cells;          /* cells per thread-block pack (0: 1024)                      */
+    int32_t threads;             /* threads per block (0: 256)                                 */
+    int32_t max_columns;         /* column slots                                               */
+    int64_t arena_cells;         /* device cells reserved for column state (the HBM budget)    */
+    int32_t negatives;           /* enum obgc_negatives                                        */
+    uint32_t zero_exclude;       /* ZeroNegativeTracers exclude mask (bit n = enum obgc_tracer n) */
+    double invalid_fill_value;   /* ScaleNegativeTracers fill for a negative group total (NaN) */
+} obgc_columns_desc;
+
+int obgc_columns_create(const obgc_columns_desc* desc, obgc_columns** out);
+int obgc_columns_destroy(obgc_columns* eng);
+/* Tracer rows of a column's state, in required_biogeochemical_tracers order; returns the count. */
+int obgc_columns_tracers(const obgc_columns* eng, int32_t* names, int32_t cap);
+/* Add a column: init is host [n_tracers][Nz] (FP64), kappa host [Nz+1] face diffusivities (m2/s,
+ * bottom first; the two wall faces are ignored: no flux).  OBGC_ERR_BUSY when no slot or arena
+ * space is free. */
+int obgc_columns_add(obgc_columns* eng, const obgc_column_spec* spec, const double* init,
+                     const double* kappa, int64_t* slot);
+/* One launch: every live column advances min(max_steps, its remaining steps). */
+int obgc_columns_advance(obgc_columns* eng, int32_t max_steps, void* stream);
+/* Advance every live column by min(nsteps, its remaining steps) through ceil(nsteps /
+ * steps_per_launch) launches; with use_graph != 0 the launches are captured once into a CUDA graph
+ * (cached until columns are added or removed) and replayed. */
+int obgc_columns_run(obgc_columns* eng, int32_t nsteps, int32_t steps_per_launch, int32_t use_graph,
+                     void* stream);
+/* Remaining steps of a slot (0: finished). */
+int obgc_columns_remaining(const obgc_columns* eng, int64_t slot, int32_t* steps_left);
+/* Copy a slot's state to host [n_tracers][Nz] FP64 (synchronises the engine's last stream). */
+int obgc_columns_read(obgc_columns* eng, int64_t slot, double* state);
+int obgc_columns_remove(obgc_columns* eng, int64_t slot);
+/* Time a few candidate (threads, pack cells) shapes on the live columns (state restored
+ * afterwards) and keep the fastest; writes the choice to *threads / *pack_cells. */
+int obgc_columns_autotune(obgc_columns* eng, int32_t steps, int32_t* threads, int32_t* pack_cells,
+                          void* stream);
 
 #ifdef __cplusplus
 }

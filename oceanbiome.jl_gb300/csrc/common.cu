@@ -47,9 +47,13 @@ extern "C" int obgc_struct_layout(int32_t which, int64_t* out, int32_t cap) {
                 out[2] = offsetof(obgc_carbon_options, atol);
                 out[3] = offsetof(obgc_carbon_options, calcium_ion_per_salinity); return 0;
         case 5: out[0] = sizeof(obgc_model_desc); out[1] = offsetof(obgc_model_desc, surface);
-                out[2] = offsetof(obgc_model_desc, grid); out[3] = offsetof(obgc_model_desc, precision); return 0;
+                out[2] = offsetof(obgc_model_desc, grid); out[3] = offsetof(obgc_model_desc, invalid_fill_value); return 0;
         case 6: out[0] = sizeof(obgc_fields); out[1] = offsetof(obgc_fields, passive);
                 out[2] = offsetof(obgc_fields, u); out[3] = offsetof(obgc_fields, G); return 0;
+        case 7: out[0] = sizeof(obgc_column_spec); out[1] = offsetof(obgc_column_spec, dz);
+                out[2] = offsetof(obgc_column_spec, pulse_step); out[3] = offsetof(obgc_column_spec, pulse_amount); return 0;
+        case 8: out[0] = sizeof(obgc_columns_desc); out[1] = offsetof(obgc_columns_desc, light);
+                out[2] = offsetof(obgc_columns_desc, arena_cells); out[3] = offsetof(obgc_columns_desc, invalid_fill_value); return 0;
     }
     return OBGC_ERR_INVALID_ARGUMENT;
 }

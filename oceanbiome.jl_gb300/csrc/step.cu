@@ -4,6 +4,7 @@
 #include <cstring>
 #include <mutex>
 #include <vector>
+#include "negatives.cuh"
 #include "step_launch.cuh"
 
 namespace obgc {
@@ -120,6 +121,7 @@ struct obgc_ctx {
     void* G[MAX_NT] = {};
     void* drift = nullptr;
     uint32_t drift_mask = 0;
+    NegativesSpec neg;                  // negative-tracer modifier over the slots
     double* d_time = nullptr;
     DD* partial = nullptr;
     int n_partial = 0;
@@ -166,6 +168,8 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
     if (!valid_grid(&g)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: invalid grid descriptor");
     if (desc->precision < 0 || desc->precision > 2) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: bad precision");
     if (desc->n_passive != 0) return fail(OBGC_ERR_UNSUPPORTED, "obgc_create: passive tracers are not supported");
+    if (desc->negatives < OBGC_NEGATIVES_NONE || desc->negatives > OBGC_NEGATIVES_ZERO)
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: bad negatives mode");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(OBGC_ERR_NO_DEVICE, "obgc_create: no CUDA device");
     obgc_ctx* c = new obgc_ctx();
@@ -187,7 +191,8 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
     if (desc->carry_S && nt < MAX_NT) c->names[nt++] = OBGC_S;
     c->NT = nt;
     c->extent = g.stride_k * (int64_t)g.Nz;
-    int rc = OBGC_OK;
+    int rc = negatives_spec(desc->npd, desc->negatives, c->NT, c->names, desc->zero_exclude, desc->invalid_fill_value,
+                            &c->neg);
     auto alloc = [&](void** p, size_t bytes) {
         if (rc != OBGC_OK) return;
         cudaError_t e = cudaMalloc(p, bytes);
@@ -274,6 +279,13 @@ extern "C" int obgc_set_tiling(obgc_ctx* c, int32_t TZ) {
 extern "C" int obgc_update_state(obgc_ctx* c, double t, void* stream) {
     if (!c || !c->bound) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_update_state: context not bound");
     if (!c->fields.PAR) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_update_state: no PAR field bound");
+    if (c->neg.mode != OBGC_NEGATIVES_NONE) {
+        // update_biogeochemical_state! runs the modifiers before the light (src/OceanBioME.jl:161-167)
+        void* f[MAX_NT];
+        for (int t = 0; t < c->NT; t++) f[t] = c->user[t];
+        const int rc = launch_negatives(c->neg, c->ts, f, c->desc.grid, static_cast<cudaStream_t>(stream));
+        if (rc != OBGC_OK) return rc;
+    }
     const void* P = c->fields.tracers[OBGC_P];
     return obgc_twoband_par(&c->desc.light, &c->desc.surface, &c->desc.grid, c->ts == 4 ? OBGC_F32 : OBGC_F64, P,
                             c->fields.PAR, t, stream);
@@ -332,6 +344,13 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
     const bool clock = c->desc.surface.kind == OBGC_SURFACE_PAR_DEFAULT;
     int blocks = c->blocks < a.n_items ? c->blocks : a.n_items;
     size_t ev = 0;
+    const obgc_grid& grid = c->desc.grid;
+    if (c->neg.mode != OBGC_NEGATIVES_NONE) {
+        // the state entering the first stage has been through update_state! (iteration 0); applying
+        // the modifier again to a state it already produced changes nothing
+        const int rc = launch_negatives(c->neg, sizeof(TS), cur, grid, st);
+        if (rc != OBGC_OK) return rc;
+    }
     for (int s = 0; s < nsteps; s++) {
         for (int stg = 0; stg < 3; stg++) {
             for (int t = 0; t < c->NT; t++) { a.in[t] = (const TS*)cur[t]; a.out[t] = (TS*)nxt[t]; }
@@ -344,6 +363,10 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
             int rc = fe->launch(&a, blocks, st);
             if (rc != OBGC_OK) return rc;
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
+            if (c->neg.mode != OBGC_NEGATIVES_NONE) {
+                rc = launch_negatives(c->neg, sizeof(TS), nxt, grid, st);   // update_state! after the substep
+                if (rc != OBGC_OK) return rc;
+            }
             for (int t = 0; t < c->NT; t++) { void* tmp = cur[t]; cur[t] = nxt[t]; nxt[t] = tmp; }
         }
         if (clock) {
@@ -373,7 +396,8 @@ static int dispatch_steps(obgc_ctx* c, double dt, int nsteps, cudaStream_t st, b
 
 static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     const bool clock = c->desc.surface.kind == OBGC_SURFACE_PAR_DEFAULT;
-    return (int64_t)nsteps * (3 + (clock ? 1 : 0)) + (nsteps % 2 ? c->NT : 0) + 1;
+    const bool neg = c->neg.mode != OBGC_NEGATIVES_NONE;
+    return (int64_t)nsteps * (3 + (clock ? 1 : 0) + (neg ? 3 : 0)) + (nsteps % 2 ? c->NT : 0) + 1 + (neg ? 1 : 0);
 }
 
 extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {
@@ -458,37 +482,6 @@ extern "C" int obgc_last_step_timing(const obgc_ctx* c, double* total_ms, double
     }
     if (launches) *launches = c->last_launches;
     return OBGC_OK;
-}
-
-// conserved_tracers (NutrientsPlanktonDetritus/coupling_utils.jl:1-52)
-static int conserved_group(const obgc_npd_params& p, int group, int* names, double* scale) {
-    int n = 0;
-    if (group == 0) {
-        names[n] = OBGC_P; scale[n++] = 1; names[n] = OBGC_Z; scale[n++] = 1;
-        if (p.nutrients == OBGC_NUT_NUTRIENT) { names[n] = OBGC_N; scale[n++] = 1; }
-        else { names[n] = OBGC_NO3; scale[n++] = 1; names[n] = OBGC_NH4; scale[n++] = 1; }
-        if (p.detritus == OBGC_DET_VARIABLE_REDFIELD) {
-            names[n] = OBGC_SPON; scale[n++] = 1; names[n] = OBGC_BPON; scale[n++] = 1; names[n] = OBGC_DON; scale[n++] = 1;
-        } else if (p.detritus == OBGC_DET_TWO_PARTICLE) {
-            names[n] = OBGC_SPOM; scale[n++] = 1; names[n] = OBGC_BPOM; scale[n++] = 1; names[n] = OBGC_DOM; scale[n++] = 1;
-        } else if (p.detritus == OBGC_DET_SINGLE) {
-            names[n] = OBGC_D; scale[n++] = 1;
-        }
-        return n;
-    }
-    if (!p.carbonate_system) return -1;
-    const double R = p.redfield_ratio, rho = p.carbon_calcite_ratio;
-    names[n] = OBGC_P; scale[n++] = (1 + rho) * R;
-    names[n] = OBGC_Z; scale[n++] = R;
-    names[n] = OBGC_DIC; scale[n++] = 1;
-    if (p.detritus == OBGC_DET_VARIABLE_REDFIELD) {
-        names[n] = OBGC_SPOC; scale[n++] = 1; names[n] = OBGC_BPOC; scale[n++] = 1; names[n] = OBGC_DOC; scale[n++] = 1;
-    } else if (p.detritus == OBGC_DET_TWO_PARTICLE) {
-        names[n] = OBGC_SPOM; scale[n++] = R; names[n] = OBGC_BPOM; scale[n++] = R; names[n] = OBGC_DOM; scale[n++] = R;
-    } else if (p.detritus == OBGC_DET_SINGLE) {
-        names[n] = OBGC_D; scale[n++] = R;
-    }
-    return n;
 }
 
 template <typename TS>

@@ -193,7 +193,6 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 3 : 1)
     constexpr int NB = n_bgc(V);
     constexpr int SP = slot_of_P(V);
     constexpr int NTH = STEP_BX * STEP_BY;
-    constexpr int NWARP = NTH / 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TC (*fx)[STEP_BY][STEP_BX + 1] = reinterpret_cast<TC (*)[STEP_BY][STEP_BX + 1]>(smem_raw);
     TC (*fy)[STEP_BY + 1][STEP_BX] =
@@ -205,7 +204,6 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 3 : 1)
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = tx + STEP_BX * ty;
-    const int warp = tid >> 5, lane = tid & 31;
     const bool periodic_x = a.periodic_x, periodic_y = a.periodic_y;
     // Sinking tracers advance their vertical stencil in a register window (one new load per
     // level); two window slots per variant (LOBSTER: sPOM, bPOM; NPZD: P, D).  Any other

@@ -8,16 +8,19 @@ libobgc.so (CUDA, sm_103a); importing works without it, calling does not.
 """
 from . import _abi
 from .box import BoxModel
+from .columns import ColumnEngine
 from .carbon import CarbonChemistry
 from .grid import BoxModelGrid, RectilinearGrid
 from .light import (MultiBandPhotosyntheticallyActiveRadiation, PrescribedPhotosyntheticallyActiveRadiation,
                     TwoBandPhotosyntheticallyActiveRadiation, default_surface_PAR, euphotic_depth)
 from .model3d import (Clock, NonhydrostaticModel, compute_tendencies, set_, time_step,
                       update_biogeochemical_state)
+from .negatives import ScaleNegativeTracers, ZeroNegativeTracers
 from .models import (LOBSTER, NPZD, CarbonateSystem, Detritus, NitrateAmmonia, NitrateAmmoniaIron, Nutrient,
                      NutrientsPlanktonDetritus, Oxygen, PhytoZoo, TwoParticleAndDissolved, VariableRedfieldDetritus,
                      biogeochemical_drift_velocity, conserved_tracers, eval_point, preset,
                      required_biogeochemical_auxiliary_fields, required_biogeochemical_tracers)
-from .synthetic import lobster_initial_conditions, npzd_front_initial_conditions, random_streamfunction_velocity
+from .synthetic import (lobster_column_request, lobster_initial_conditions, mixed_layer_diffusivity,
+                        npzd_column_ensemble, npzd_front_initial_conditions, random_streamfunction_velocity)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -19,6 +19,7 @@ STATUS_NAMES = {
 }
 F32, F64 = 0, 1
 PREC_F32, PREC_F64, PREC_MIXED = 0, 1, 2
+NEGATIVES_NONE, NEGATIVES_SCALE, NEGATIVES_ZERO = 0, 1, 2
 
 TRACER_NAMES = ["NO₃", "NH₄", "Fe", "N", "P", "Z", "T", "sPOM", "bPOM", "DOM", "sPON", "bPON",
                 "DON", "sPOC", "bPOC", "DOC", "D", "DIC", "Alk", "O₂", "S"]
@@ -111,13 +112,27 @@ class ModelDesc(C.Structure):
     _fields_ = [("npd", NPDParams), ("light", TwoBandParams), ("surface", Surface),
                 ("grid", Grid), ("precision", C.c_int32), ("advection", C.c_int32),
                 ("n_passive", C.c_int32), ("carry_T", C.c_int32), ("carry_S", C.c_int32),
-                ("reserved0", C.c_int32)]
+                ("negatives", C.c_int32), ("zero_exclude", C.c_uint32), ("reserved1", C.c_int32),
+                ("invalid_fill_value", C.c_double)]
 
 
 class Fields(C.Structure):
     _fields_ = [("tracers", C.c_void_p * NUM_NAMED), ("passive", C.c_void_p * MAX_PASSIVE),
                 ("u", C.c_void_p), ("v", C.c_void_p), ("w", C.c_void_p), ("PAR", C.c_void_p),
                 ("G", C.c_void_p * NUM_NAMED)]
+
+
+class ColumnSpec(C.Structure):
+    _fields_ = [("Nz", C.c_int32), ("nsteps", C.c_int32), ("dz", C.c_double), ("dt", C.c_double),
+                ("surface_PAR", C.c_double), ("mu0", C.c_double), ("pulse_step", C.c_int32),
+                ("pulse_k", C.c_int32), ("pulse_amount", C.c_double)]
+
+
+class ColumnsDesc(C.Structure):
+    _fields_ = [("npd", NPDParams), ("light", TwoBandParams), ("precision", C.c_int32),
+                ("pack_cells", C.c_int32), ("threads", C.c_int32), ("max_columns", C.c_int32),
+                ("arena_cells", C.c_int64), ("negatives", C.c_int32), ("zero_exclude", C.c_uint32),
+                ("invalid_fill_value", C.c_double)]
 
 
 def default_twoband():
@@ -192,6 +207,19 @@ def load():
     _sig(lib, "obgc_set_profiling", C.c_int, VP, I32)
     _sig(lib, "obgc_set_tiling", C.c_int, VP, I32)
     _sig(lib, "obgc_box_run", C.c_int, P(NPDParams), VP, I64, VP, VP, D, D, D, I32, I32, VP, I32, VP)
+    _sig(lib, "obgc_npd_conserved_tracers", C.c_int, P(NPDParams), I32, P(I32), P(D), I32)
+    _sig(lib, "obgc_scale_negatives", C.c_int, P(Grid), I32, I32, P(VP), P(D), D, VP)
+    _sig(lib, "obgc_zero_negatives", C.c_int, P(Grid), I32, I32, P(VP), VP)
+    _sig(lib, "obgc_columns_create", C.c_int, P(ColumnsDesc), P(VP))
+    _sig(lib, "obgc_columns_destroy", C.c_int, VP)
+    _sig(lib, "obgc_columns_tracers", C.c_int, VP, P(I32), I32)
+    _sig(lib, "obgc_columns_add", C.c_int, VP, P(ColumnSpec), P(D), P(D), P(I64))
+    _sig(lib, "obgc_columns_advance", C.c_int, VP, I32, VP)
+    _sig(lib, "obgc_columns_run", C.c_int, VP, I32, I32, I32, VP)
+    _sig(lib, "obgc_columns_remaining", C.c_int, VP, I64, P(I32))
+    _sig(lib, "obgc_columns_read", C.c_int, VP, I64, P(D))
+    _sig(lib, "obgc_columns_remove", C.c_int, VP, I64)
+    _sig(lib, "obgc_columns_autotune", C.c_int, VP, I32, P(I32), P(I32), VP)
     _lib = lib
     return lib
 
@@ -206,4 +234,7 @@ EXPORTED = [
     "obgc_bind_fields", "obgc_update_state", "obgc_compute_tendencies", "obgc_step",
     "obgc_step_graph", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run",
     "obgc_set_profiling", "obgc_set_tiling", "obgc_struct_layout", "obgc_tracer_budget_static",
+    "obgc_columns_create", "obgc_columns_destroy", "obgc_columns_tracers", "obgc_columns_add",
+    "obgc_columns_advance", "obgc_columns_run", "obgc_columns_remaining", "obgc_columns_read", "obgc_columns_remove",
+    "obgc_columns_autotune", "obgc_npd_conserved_tracers", "obgc_scale_negatives", "obgc_zero_negatives",
 ]

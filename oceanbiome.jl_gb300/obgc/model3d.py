@@ -10,6 +10,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi as A
+from .negatives import negatives_config
 from .models import required_biogeochemical_tracers
 
 _PREC = {"f32": A.PREC_F32, "f64": A.PREC_F64, "mixed": A.PREC_MIXED}
@@ -54,6 +55,7 @@ class NonhydrostaticModel:
         desc.advection = A.ADVECTION_WENO5 if advection else A.ADVECTION_NONE
         desc.carry_T = int("T" in extra)
         desc.carry_S = int("S" in extra)
+        desc.negatives, desc.zero_exclude, desc.invalid_fill_value = negatives_config(bgc)
         self._lib = lib = A.load()
         ctx = C.c_void_p()
         A.check(lib.obgc_create(C.byref(desc), C.byref(ctx)), "obgc_create")

@@ -97,3 +97,58 @@ def npzd_front_initial_conditions(grid):
     front = np.tanh((X - 7000 + 4 * Zc) / 500)
     PZ = np.where(Zc > -50, 0.03, 0.01)
     return {"N": 2.5 - 2 * front, "T": 9 + 0.05 * front, "P": PZ, "Z": PZ.copy(), "D": 0.0}
+
+
+def mixed_layer_diffusivity(Nz, dz, mld, kappa_mixed=1e-2, kappa_deep=1e-4, width=10.0):
+    """Face diffusivities (bottom face first) of the reference's column example profile
+    kappa(z) = kappa_mixed (1 + tanh((z + mld) / width)) / 2 + kappa_deep (examples/column.jl:34)."""
+    zf = -Nz * dz + dz * np.arange(Nz + 1)
+    return kappa_mixed * (1 + np.tanh((zf + mld) / width)) / 2 + kappa_deep
+
+
+def npzd_column_ensemble(n, seed=0, levels=(16, 256), dz=2.0, dt=600.0, nsteps=1440):
+    """Seeded uneven NPZD columns: Nz ~ U{levels}, dz = 2 m, maximum phytoplankton growth
+    ~ lognormal(log 1.5e-5 s^-1, 0.3), mixed-layer depth ~ U(20, 200) m setting the diffusivity
+    1e-4 .. 1e-2 m^2/s (mixed_layer_diffusivity), surface PAR ~ U(50, 300) W/m^2.  Initial profiles
+    follow the NPZD front example's values: N rising from 2.5 at the surface to 10 at depth,
+    P = Z = 0.03 in the mixed layer and 0.01 below, D = 0, T = 12 + 0.01 z.  Each column is a dict
+    with init [N, P, Z, T, D] x Nz (bottom first), kappa, dz, dt, nsteps, surface_PAR, mu0."""
+    rng = np.random.default_rng(seed)
+    cols = []
+    for _ in range(n):
+        Nz = int(rng.integers(levels[0], levels[1] + 1))
+        mld = rng.uniform(20, 200)
+        z = -Nz * dz + dz * (np.arange(Nz) + 0.5)
+        inside = z > -mld
+        N = 2.5 + 7.5 * (1 - np.exp(z / 150.0))
+        P = np.where(inside, 0.03, 0.01)
+        init = np.stack([N, P, P.copy(), 12 + 0.01 * z, np.zeros(Nz)])
+        cols.append(dict(init=init, kappa=mixed_layer_diffusivity(Nz, dz, mld), dz=dz, dt=dt, nsteps=nsteps,
+                         surface_PAR=rng.uniform(50, 300), mu0=float(np.exp(rng.normal(np.log(1.5e-5), 0.3)))))
+    return cols
+
+
+def lobster_column_request(rng, levels=(8, 512), days=(1, 30), dts=(300.0, 1800.0), pulse=(0.0, 500.0),
+                           w_max=0.0023148148148148147):
+    """One column-run request of the alkalinity-addition scenario service: LOBSTER with carbonates,
+    Nz log-uniform in `levels`, duration U(days), dt U(dts), an alkalinity pulse U(pulse) added at a
+    random level and step.  The level thickness is U(2, 10) m but at least 1.5 w_max dt, so the
+    explicit sinking of large particles stays below CFL 0.7.  Values: NO3 ~ U(5, 15), NH4 0.05,
+    P, Z ~ lognormal(log 0.1, 0.5) in the mixed layer (a tenth below), sPOM = bPOM = DOM = 0.01,
+    DIC ~ U(2100, 2250), Alk ~ U(2300, 2450)."""
+    Nz = int(np.exp(rng.uniform(np.log(levels[0]), np.log(levels[1] + 1))))
+    Nz = max(levels[0], min(levels[1], Nz))
+    dt = float(rng.uniform(*dts))
+    dz = max(float(rng.uniform(2, 10)), 1.5 * w_max * dt)
+    nsteps = max(1, int(round(rng.uniform(*days) * 86400.0 / dt)))
+    mld = rng.uniform(20, 200)
+    z = -Nz * dz + dz * (np.arange(Nz) + 0.5)
+    inside = z > -mld
+    scale = np.where(inside, 1.0, 0.1)
+    P = np.exp(rng.normal(np.log(0.1), 0.5, Nz)) * scale
+    Zp = np.exp(rng.normal(np.log(0.1), 0.5, Nz)) * scale
+    init = np.stack([np.full(Nz, rng.uniform(5, 15)), np.full(Nz, 0.05), P, Zp, np.full(Nz, 0.01), np.full(Nz, 0.01),
+                     np.full(Nz, 0.01), np.full(Nz, rng.uniform(2100, 2250)), np.full(Nz, rng.uniform(2300, 2450))])
+    return dict(init=init, kappa=mixed_layer_diffusivity(Nz, dz, mld), dz=dz, dt=dt, nsteps=nsteps,
+                surface_PAR=float(rng.uniform(50, 300)), mu0=0.0, pulse_step=int(rng.integers(0, nsteps)),
+                pulse_k=int(rng.integers(0, Nz)), pulse_amount=float(rng.uniform(*pulse)))

@@ -77,6 +77,9 @@ typedef struct or_model3d {
     obgc_grid grid;              /* strides ignored: arrays are dense [Nz][Ny][Nx]   */
     int32_t n_tracers;           /* number of advected tracers                         */
     int32_t names[32];           /* enum obgc_tracer per tracer, or -1 for passive     */
+    int32_t negatives;           /* 0 none, 1 ScaleNegativeTracers, 2 ZeroNegativeTracers */
+    int32_t zero_exclude_mask;   /* ZeroNegativeTracers: bit q set = tracer slot q excluded */
+    double invalid_fill_value;   /* ScaleNegativeTracers(...; invalid_fill_value)      */
 } or_model3d;
 /* state: [n_tracers][Nz*Ny*Nx]; u, v, w: [Nz*Ny*Nx] or NULL. */
 void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,
@@ -86,17 +89,35 @@ void or_par3d(const or_model3d* m, const double* state, double t, double* PAR, i
 /* ---- batched uneven columns with vertically implicit diffusion ---- */
 typedef struct or_column {
     int32_t Nz;
-    int32_t reserved;
+    int32_t nsteps;              /* steps of this column (<= 0: the call's nsteps)        */
     double dz;
     double surface_PAR;          /* constant surface PAR (W/m2)                          */
     double mu0;                  /* phytoplankton_maximum_growth_rate override           */
+    double dt;                   /* step of this column (<= 0: the call's dt)            */
+    int32_t pulse_step;          /* step at whose start pulse_amount is added to Alk (-1) */
+    int32_t pulse_k;
+    double pulse_amount;
 } or_column;
-/* state: per column [n_tracers][Nz] (offsets given); kappa: per column Nz+1 face values. */
+/* state: per column [n_tracers][Nz] (offsets given); kappa: per column Nz+1 face values.
+ * negatives: 0 none, 1 ScaleNegativeTracers over conserved_tracers(bgc) (applied to the initial
+ * state and after every RK3 stage, as Oceananigans' update_state! does). */
 void or_columns_run(const obgc_npd_params* p, const obgc_twoband_params* lp, int n_cols,
                     const or_column* cols, const int64_t* state_offsets,
                     const int64_t* kappa_offsets, int n_tracers, const int32_t* names,
                     double* state, const double* kappa, double t0, double dt, int nsteps,
-                    int nthreads);
+                    int negatives, double invalid_fill_value, int nthreads);
+
+/* ---- negative tracers (src/Utils/negative_tracers.jl) ---- */
+#define OR_MAX_GROUPS 2
+#define OR_MAX_GROUP 8
+/* conserved_tracers(bgc) (NutrientsPlanktonDetritus/coupling_utils.jl:1-52) as slots of `names`
+ * and scale factors; returns the number of groups (nitrogen, then carbon with the carbonate
+ * system).  gn[g] members, gslot/gfac [OR_MAX_GROUPS][OR_MAX_GROUP]. */
+int or_conserved_groups(const obgc_npd_params* p, int n_tracers, const int32_t* names, int32_t* gn,
+                        int32_t* gslot, double* gfac);
+/* ScaleNegativeTracers on one cell whose tracer q is at v[q * stride] (negative_tracers.jl:250-276). */
+void or_scale_cell(double* v, long stride, int ng, const int32_t* gn, const int32_t* gslot,
+                   const double* gfac, double invalid_fill_value);
 
 /* ---- ScaleNegativeTracers (src/Utils/negative_tracers.jl:250-276) ---- */
 void or_scale_negatives(int64_t n, int ntr, double* const* fields, const double* scalefactors,

@@ -127,6 +127,23 @@ void or_par3d(const or_model3d* m, const double* state, double t, double* PAR, i
     free(zc); free(zf);
 }
 
+/* update_biogeochemical_state!(model, ::ScaleNegativeTracers / ::ZeroNegativeTracers)
+ * (negative_tracers.jl:23-29, :136-143) on every cell of a 3-D state. */
+static void or_negatives3d(const or_model3d* m, double* state, long N, int ng, const int32_t* gn,
+                           const int32_t* gslot, const double* gfac, int nthreads) {
+    if (m->negatives == 1) {
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+        for (long c = 0; c < N; c++) or_scale_cell(state + c, N, ng, gn, gslot, gfac, m->invalid_fill_value);
+    } else if (m->negatives == 2) {
+        for (int q = 0; q < m->n_tracers; q++) {
+            if ((m->zero_exclude_mask >> q) & 1) continue;
+            double* x = state + (long)q * N;
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+            for (long c = 0; c < N; c++) x[c] = x[c] > 0.0 ? x[c] : (isnan(x[c]) ? x[c] : 0.0);
+        }
+    }
+}
+
 void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,
                const double* w, double t, double dt, int nsteps, int nthreads) {
     const obgc_grid* g = &m->grid;
@@ -155,6 +172,10 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
             }
         }
     }
+    int32_t gn[OR_MAX_GROUPS], gslot[OR_MAX_GROUPS * OR_MAX_GROUP];
+    double gfac[OR_MAX_GROUPS * OR_MAX_GROUP];
+    const int ng = m->negatives == 1 ? or_conserved_groups(&m->npd, nt, m->names, gn, gslot, gfac) : 0;
+    if (m->negatives) or_negatives3d(m, state, N, ng, gn, gslot, gfac, nthreads);
     for (int s = 0; s < nsteps; s++) {
         for (int st = 0; st < 3; st++) {
             double ts = t + RK_C[st] * dt;
@@ -213,11 +234,78 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
                 if (st == 0) state[x] += dt * g * G[x];
                 else state[x] += dt * (g * G[x] + z * Gm[x]);
             }
+            if (m->negatives) or_negatives3d(m, state, N, ng, gn, gslot, gfac, nthreads);
             double* tmp = G; G = Gm; Gm = tmp;
         }
         t += dt;
     }
     free(G); free(Gm); free(PAR); free(drift); free(has_drift);
+}
+
+/* ------------------------------------------------------------------ negative tracers -- */
+static int slot_in(int nt, const int32_t* names, int name) {
+    for (int q = 0; q < nt; q++) if (names[q] == name) return q;
+    return -1;
+}
+
+static void group_add(int nt, const int32_t* names, int g, int name, double f, int32_t* gn, int32_t* gslot, double* gfac) {
+    int q = slot_in(nt, names, name);
+    if (q < 0 || gn[g] >= OR_MAX_GROUP) return;
+    gslot[g * OR_MAX_GROUP + gn[g]] = q;
+    gfac[g * OR_MAX_GROUP + gn[g]] = f;
+    gn[g]++;
+}
+
+int or_conserved_groups(const obgc_npd_params* p, int nt, const int32_t* names, int32_t* gn, int32_t* gslot,
+                        double* gfac) {
+    gn[0] = gn[1] = 0;
+    /* nitrogen: P, Z, nutrients, detritus (coupling_utils.jl:1-21) */
+    group_add(nt, names, 0, OBGC_P, 1.0, gn, gslot, gfac);
+    group_add(nt, names, 0, OBGC_Z, 1.0, gn, gslot, gfac);
+    if (p->nutrients == OBGC_NUT_NUTRIENT) group_add(nt, names, 0, OBGC_N, 1.0, gn, gslot, gfac);
+    else { group_add(nt, names, 0, OBGC_NO3, 1.0, gn, gslot, gfac); group_add(nt, names, 0, OBGC_NH4, 1.0, gn, gslot, gfac); }
+    if (p->detritus == OBGC_DET_VARIABLE_REDFIELD) {
+        group_add(nt, names, 0, OBGC_SPON, 1.0, gn, gslot, gfac); group_add(nt, names, 0, OBGC_BPON, 1.0, gn, gslot, gfac);
+        group_add(nt, names, 0, OBGC_DON, 1.0, gn, gslot, gfac);
+    } else if (p->detritus == OBGC_DET_TWO_PARTICLE) {
+        group_add(nt, names, 0, OBGC_SPOM, 1.0, gn, gslot, gfac); group_add(nt, names, 0, OBGC_BPOM, 1.0, gn, gslot, gfac);
+        group_add(nt, names, 0, OBGC_DOM, 1.0, gn, gslot, gfac);
+    } else if (p->detritus == OBGC_DET_SINGLE) {
+        group_add(nt, names, 0, OBGC_D, 1.0, gn, gslot, gfac);
+    }
+    if (!p->carbonate_system) return 1;
+    /* carbon: P, Z, DIC, detritus carbon with ((1 + rho) R, R, 1, ...) (coupling_utils.jl:23-52) */
+    const double R = p->redfield_ratio, rho = p->carbon_calcite_ratio;
+    group_add(nt, names, 1, OBGC_P, (1 + rho) * R, gn, gslot, gfac);
+    group_add(nt, names, 1, OBGC_Z, R, gn, gslot, gfac);
+    group_add(nt, names, 1, OBGC_DIC, 1.0, gn, gslot, gfac);
+    if (p->detritus == OBGC_DET_VARIABLE_REDFIELD) {
+        group_add(nt, names, 1, OBGC_SPOC, 1.0, gn, gslot, gfac); group_add(nt, names, 1, OBGC_BPOC, 1.0, gn, gslot, gfac);
+        group_add(nt, names, 1, OBGC_DOC, 1.0, gn, gslot, gfac);
+    } else if (p->detritus == OBGC_DET_TWO_PARTICLE) {
+        group_add(nt, names, 1, OBGC_SPOM, R, gn, gslot, gfac); group_add(nt, names, 1, OBGC_BPOM, R, gn, gslot, gfac);
+        group_add(nt, names, 1, OBGC_DOM, R, gn, gslot, gfac);
+    } else if (p->detritus == OBGC_DET_SINGLE) {
+        group_add(nt, names, 1, OBGC_D, R, gn, gslot, gfac);
+    }
+    return 2;
+}
+
+void or_scale_cell(double* v, long stride, int ng, const int32_t* gn, const int32_t* gslot, const double* gfac,
+                   double fill) {
+    for (int g = 0; g < ng; g++) {
+        double t = 0.0, p = 0.0;
+        for (int m = 0; m < gn[g]; m++) {
+            double x = v[(long)gslot[g * OR_MAX_GROUP + m] * stride] * gfac[g * OR_MAX_GROUP + m];
+            t += x;
+            if (v[(long)gslot[g * OR_MAX_GROUP + m] * stride] > 0) p += x;
+        }
+        t = t < 0 ? fill : t;
+        for (int m = 0; m < gn[g]; m++) {
+            double* x = v + (long)gslot[g * OR_MAX_GROUP + m] * stride;
+            *x = (!isfinite(*x) || *x > 0) ? *x * t / p : 0.0;
+        }
+    }
 }
 
 /* ------------------------------------------------------------------ columns ---------- */
@@ -242,14 +330,21 @@ static void implicit_diffusion(int Nz, double dz, const double* kf, double dts, 
 void or_columns_run(const obgc_npd_params* p0, const obgc_twoband_params* lp, int n_cols,
                     const or_column* cols, const int64_t* so, const int64_t* ko,
                     int nt, const int32_t* names, double* state, const double* kappa,
-                    double t0, double dt, int nsteps, int nthreads) {
+                    double t0, double dt_all, int nsteps_all, int negatives, double fill, int nthreads) {
     (void)t0;
+    int32_t gn[OR_MAX_GROUPS], gslot[OR_MAX_GROUPS * OR_MAX_GROUP];
+    double gfac[OR_MAX_GROUPS * OR_MAX_GROUP];
+    const int ng = negatives == 1 ? or_conserved_groups(p0, nt, names, gn, gslot, gfac) : 0;
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4)
     for (int c = 0; c < n_cols; c++) {
         obgc_npd_params p = *p0;
-        p.phytoplankton_maximum_growth_rate = cols[c].mu0;
+        if (cols[c].mu0 > 0) p.phytoplankton_maximum_growth_rate = cols[c].mu0;
         int Nz = cols[c].Nz;
         double dz = cols[c].dz;
+        double dt = cols[c].dt > 0 ? cols[c].dt : dt_all;
+        int nsteps = cols[c].nsteps > 0 ? cols[c].nsteps : nsteps_all;
+        int sAlk = -1;
+        for (int q = 0; q < nt; q++) if (names[q] == OBGC_ALK) sAlk = q;
         double* U = state + so[c];
         const double* kf = kappa + ko[c];
         double* G = calloc((size_t)nt * Nz, sizeof(double));
@@ -271,7 +366,10 @@ void or_columns_run(const obgc_npd_params* p0, const obgc_twoband_params* lp, in
         }
         int32_t req[32];
         int nreq = or_npd_required_tracers(&p, req, 32);
+        for (int k = 0; k < Nz && ng; k++) or_scale_cell(U + k, Nz, ng, gn, gslot, gfac, fill);
         for (int s = 0; s < nsteps; s++) {
+            if (s == cols[c].pulse_step && sAlk >= 0 && cols[c].pulse_k >= 0 && cols[c].pulse_k < Nz)
+                U[(long)sAlk * Nz + cols[c].pulse_k] += cols[c].pulse_amount;
             for (int st = 0; st < 3; st++) {
                 for (int k = 0; k < Nz; k++) Pcol[k] = U[(long)sP * Nz + k];
                 or_twoband_column(lp, Nz, zc, zf, Pcol, cols[c].surface_PAR, PAR);
@@ -297,6 +395,7 @@ void or_columns_run(const obgc_npd_params* p0, const obgc_twoband_params* lp, in
                 for (long x = 0; x < (long)nt * Nz; x++)
                     U[x] += st == 0 ? dt * g * G[x] : dt * (g * G[x] + z * Gm[x]);
                 for (int q = 0; q < nt; q++) implicit_diffusion(Nz, dz, kf, (g + z) * dt, U + (long)q * Nz, cp, dp);
+                for (int k = 0; k < Nz && ng; k++) or_scale_cell(U + k, Nz, ng, gn, gslot, gfac, fill);
                 double* tmp = G; G = Gm; Gm = tmp;
             }
         }

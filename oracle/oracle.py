@@ -24,12 +24,17 @@ NEWTON, NEWTON_SAFE, BISECTION, DAMPED = range(4)
 class Model3D(C.Structure):
     _fields_ = [("npd", A.NPDParams), ("light", A.TwoBandParams), ("surface_kind", C.c_int32),
                 ("advection", C.c_int32), ("surface_value", C.c_double), ("grid", A.Grid),
-                ("n_tracers", C.c_int32), ("names", C.c_int32 * 32)]
+                ("n_tracers", C.c_int32), ("names", C.c_int32 * 32), ("negatives", C.c_int32),
+                ("zero_exclude_mask", C.c_int32), ("invalid_fill_value", C.c_double)]
+
+
+NEG_NONE, NEG_SCALE, NEG_ZERO = 0, 1, 2
 
 
 class Column(C.Structure):
-    _fields_ = [("Nz", C.c_int32), ("reserved", C.c_int32), ("dz", C.c_double),
-                ("surface_PAR", C.c_double), ("mu0", C.c_double)]
+    _fields_ = [("Nz", C.c_int32), ("nsteps", C.c_int32), ("dz", C.c_double),
+                ("surface_PAR", C.c_double), ("mu0", C.c_double), ("dt", C.c_double),
+                ("pulse_step", C.c_int32), ("pulse_k", C.c_int32), ("pulse_amount", C.c_double)]
 
 
 def build():
@@ -76,8 +81,10 @@ def lib():
         L.or_step3d.argtypes = [P(Model3D), P(D), VP, VP, VP, D, D, C.c_int, C.c_int]
         L.or_par3d.argtypes = [P(Model3D), P(D), D, P(D), C.c_int]
         L.or_columns_run.argtypes = [P(A.NPDParams), P(A.TwoBandParams), C.c_int, P(Column), P(I64),
-                                     P(I64), C.c_int, P(I32), P(D), P(D), D, D, C.c_int, C.c_int]
+                                     P(I64), C.c_int, P(I32), P(D), P(D), D, D, C.c_int, C.c_int, D, C.c_int]
         L.or_scale_negatives.argtypes = [I64, C.c_int, P(P(D)), P(D), D]
+        L.or_conserved_groups.argtypes = [P(A.NPDParams), C.c_int, P(I32), P(I32), P(I32), P(D)]
+        L.or_scale_cell.argtypes = [P(D), C.c_long, C.c_int, P(I32), P(I32), P(D), D]
         _lib = L
     return _lib
 
@@ -230,8 +237,12 @@ def box_run(p, values, dt, nsteps, PAR_stages=None, PAR_const=0.0, t0=0.0):
     return v
 
 
-def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_value=0.0, advection=1):
+def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_value=0.0, advection=1,
+            negatives=NEG_NONE, zero_exclude=(), invalid_fill_value=float("nan")):
     m = Model3D()
+    m.negatives = negatives
+    m.invalid_fill_value = invalid_fill_value
+    m.zero_exclude_mask = sum(1 << q for q, nm in enumerate(names) if nm in zero_exclude)
     m.npd = p
     m.light = light if light is not None else A.default_twoband()
     m.surface_kind = surface_kind
@@ -258,7 +269,18 @@ def par3d(m, state, t, threads=None):
     return out
 
 
-def columns_run(p, lp, cols, names, state, kappa, state_offsets, kappa_offsets, dt, nsteps, threads=None):
+def conserved_groups(p, names):
+    """or_conserved_groups: [(slots, factors), ...] in the reference's group and member order."""
+    nm = np.array([A.NAME_INDEX[x] if isinstance(x, str) else x for x in names], dtype=np.int32)
+    gn = (C.c_int32 * 2)()
+    gs = (C.c_int32 * 16)()
+    gf = (C.c_double * 16)()
+    ng = lib().or_conserved_groups(C.byref(p), len(nm), nm.ctypes.data_as(C.POINTER(C.c_int32)), gn, gs, gf)
+    return [([gs[g * 8 + m] for m in range(gn[g])], [gf[g * 8 + m] for m in range(gn[g])]) for g in range(ng)]
+
+
+def columns_run(p, lp, cols, names, state, kappa, state_offsets, kappa_offsets, dt, nsteps, threads=None,
+                negatives=NEG_NONE, invalid_fill_value=float("nan")):
     n = len(cols)
     carr = (Column * n)(*cols)
     so = np.ascontiguousarray(state_offsets, dtype=np.int64)
@@ -267,7 +289,7 @@ def columns_run(p, lp, cols, names, state, kappa, state_offsets, kappa_offsets, 
     lib().or_columns_run(C.byref(p), C.byref(lp), n, carr, so.ctypes.data_as(C.POINTER(C.c_int64)),
                          ko.ctypes.data_as(C.POINTER(C.c_int64)), len(names),
                          nm.ctypes.data_as(C.POINTER(C.c_int32)), _dp(state), _dp(kappa), 0.0, dt,
-                         nsteps, threads or nthreads())
+                         nsteps, negatives, invalid_fill_value, threads or nthreads())
     return state
 
 

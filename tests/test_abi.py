@@ -37,8 +37,10 @@ def test_every_declared_symbol_is_exported():
     (2, A.Surface, ["value", "field", None]),
     (3, A.Grid, ["Lx", "stride_j", "stride_k"]),
     (4, A.CarbonOptions, ["density_value", "atol", "calcium_ion_per_salinity"]),
-    (5, A.ModelDesc, ["surface", "grid", "precision"]),
+    (5, A.ModelDesc, ["surface", "grid", "invalid_fill_value"]),
     (6, A.Fields, ["passive", "u", "G"]),
+    (7, A.ColumnSpec, ["dz", "pulse_step", "pulse_amount"]),
+    (8, A.ColumnsDesc, ["light", "arena_cells", "invalid_fill_value"]),
 ])
 def test_struct_layouts(which, struct, fields):
     lib = A.load()
