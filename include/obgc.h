@@ -538,6 +538,46 @@ int obgc_columns_remove(obgc_columns* eng, int64_t slot);
 int obgc_columns_autotune(obgc_columns* eng, int32_t steps, int32_t* threads, int32_t* pack_cells,
                           void* stream);
 
+/* ---------------------------------------------------------------------------------------------
+ * Continuous-batching column service.  Requests (one column run each) are submitted from any host
+ * thread; a worker thread admits them into the column engine while a slot and arena space (the
+ * HBM budget) are free, advances every resident run by chunk_steps per launch with two launches
+ * queued, copies finished runs back behind their last launch, and frees their space for the next
+ * requests.  A run's result does not depend on the runs it shares launches with.  This serving
+ * layer has no counterpart in the reference, which runs one model per process
+ * (examples/column.jl, examples/oae_experiment.jl).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct obgc_service obgc_service;
+
+typedef struct obgc_service_desc {
+    obgc_columns_desc columns;   /* engine: model, precision, slots, arena (HBM budget)       */
+    int32_t chunk_steps;         /* steps per launch (0: 32)                                  */
+    int32_t max_queue;           /* queued requests before submit returns OBGC_ERR_BUSY (0: no limit) */
+} obgc_service_desc;
+
+typedef struct obgc_service_stats {
+    int64_t submitted, admitted, completed, launches;
+    double p50_ms, p99_ms, mean_ms, max_ms;   /* submit -> result available, completed requests  */
+    double span_s;                            /* first submit -> last completion                 */
+} obgc_service_stats;
+
+/* Creates the engine and starts the worker on the calling thread's current device. */
+int obgc_service_create(const obgc_service_desc* desc, obgc_service** out);
+/* Stops the worker after the chunk in flight and frees everything (unfinished runs are dropped). */
+int obgc_service_destroy(obgc_service* svc);
+/* Queue a run: init host [n_tracers][Nz] FP64 and kappa [Nz+1] are copied; returns at once. */
+int obgc_service_submit(obgc_service* svc, const obgc_column_spec* spec, const double* init,
+                        const double* kappa, int64_t* request);
+/* Block until the run has finished (OBGC_ERR_TIMEOUT after timeout_s); copies its final state
+ * [n_tracers][Nz] and its latency, and forgets the request. */
+int obgc_service_wait(obgc_service* svc, int64_t request, double timeout_s, double* state, double* latency_ms);
+/* Block until every submitted run has finished. */
+int obgc_service_drain(obgc_service* svc, double timeout_s);
+int obgc_service_get_stats(obgc_service* svc, obgc_service_stats* out);
+int obgc_service_reset_stats(obgc_service* svc);
+/* The engine the worker drives (read-only use: its tracer list). */
+int obgc_service_engine(obgc_service* svc, obgc_columns** engine);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,23 +16,11 @@
 #include <cstring>
 #include <map>
 #include <vector>
+#include "columns_engine.h"
 #include "negatives.cuh"
 #include "step_kernel.cuh"
 
 namespace obgc {
-
-constexpr int COL_MAXC = 64;    // columns per pack
-
-template <typename T>
-struct ColSlot {
-    int64_t cell_off;           // first cell of the column's block (state at cell_off*NT, kappa at cell_off)
-    int32_t Nz, steps_left, steps_done, pulse_step, pulse_k, live;
-    T dz, dt, PAR0, mu0, pulse_amount, pad;
-};
-
-struct ColPack {
-    int32_t first, count, cells, pad;
-};
 
 // TS: state precision (shared-memory state, RK3 accumulation, diffusion solve); TC: compute
 // precision of the light, sinking fluxes and BGC tendencies.
@@ -299,34 +287,8 @@ bool drift_speed(const obgc_npd_params* p, int name, double* w0);
 
 using namespace obgc;
 
-struct obgc_columns {
-    obgc_columns_desc desc;
-    int V = -1, NT = 0;
-    size_t ts = 4;                           // state element size
-    int prec = OBGC_PREC_F32;
-    int threads = 256, cap = 1024;
-    int names[16];
-    NegativesSpec neg;
-    double w0A = 0, w0B = 0;
-    void* state = nullptr;
-    void* kappa = nullptr;
-    std::vector<ColSlot<double>> slots;
-    std::vector<int> free_slots;
-    std::map<int64_t, int64_t> free_cells;   // offset -> length
-    void* d_slots = nullptr;
-    int32_t* d_pack_slots = nullptr;
-    ColPack* d_packs = nullptr;
-    void* h_slots = nullptr;                 // pinned staging
-    int32_t* h_pack_slots = nullptr;
-    ColPack* h_packs = nullptr;
-    cudaStream_t last_stream = nullptr;      // stream of the last launch or copy
-    bool pending = false;                    // work may still be queued on last_stream
-    cudaStream_t capture_stream = nullptr;   // private stream the launch graphs are captured on
-    cudaGraphExec_t graph = nullptr;         // cached launches of obgc_columns_run
-    int64_t graph_key[5] = {0, 0, 0, 0, 0};  // packs, steps, steps per launch, threads, pack cells
-};
-
-namespace {
+namespace obgc {
+namespace cols {
 
 template <typename TS, typename TC>
 void* column_kernel_ptr(int V) {
@@ -383,8 +345,9 @@ size_t smem_for(const obgc_columns* e, int cap) {
     return npzd ? col_smem_bytes<double, float, 5>(cap) : col_smem_bytes<double, float, 9>(cap);
 }
 
-// First-fit decreasing packing of the live columns into packs of `cap` cells.
-int build_packs(obgc_columns* e, int cap) {
+// First-fit decreasing packing of the live columns into packs of `cap` cells, written to staging
+// buffer b.
+int build_packs(obgc_columns* e, int cap, int b) {
     std::vector<int> live;
     for (int s = 0; s < (int)e->slots.size(); s++)
         if (e->slots[s].live && e->slots[s].steps_left > 0) live.push_back(s);
@@ -402,16 +365,16 @@ int build_packs(obgc_columns* e, int cap) {
     }
     int n = 0;
     for (int q = 0; q < (int)packs.size(); q++) {
-        e->h_packs[q] = {n, (int)packs[q].size(), fill[q], 0};
-        for (int s : packs[q]) e->h_pack_slots[n++] = s;
+        e->h_packs[b][q] = {n, (int)packs[q].size(), fill[q], 0};
+        for (int s : packs[q]) e->h_pack_slots[b][n++] = s;
     }
     return (int)packs.size();
 }
 
 // Convert the host slot table to the kernel's precision; returns the slots in use (highest live + 1).
 template <typename T>
-int stage_slots(obgc_columns* e) {
-    ColSlot<T>* h = static_cast<ColSlot<T>*>(e->h_slots);
+int stage_slots(obgc_columns* e, int b) {
+    ColSlot<T>* h = static_cast<ColSlot<T>*>(e->h_slots[b]);
     int n = 0;
     for (size_t s = 0; s < e->slots.size(); s++)
         if (e->slots[s].live) n = (int)s + 1;
@@ -426,31 +389,39 @@ int stage_slots(obgc_columns* e) {
     return n;
 }
 
-// Wait for everything queued by the engine (launches and copies read its staging buffers).
 int drain(obgc_columns* e) {
     if (e->pending) OBGC_CUDA(cudaStreamSynchronize(e->last_stream));
     e->pending = false;
     return OBGC_OK;
 }
 
-// Pack the unfinished columns and copy the slot and pack tables to the device on `st`.
-// Returns the number of packs (0: nothing to do) or a negative status.
 int stage_tables(obgc_columns* e, int cap, cudaStream_t st) {
-    // the pinned staging buffers and the device slot table are rewritten below
-    int rc = drain(e);
-    if (rc != OBGC_OK) return -rc;
-    const int npacks = build_packs(e, cap);
+    // the device tables are read by the kernels already queued: another stream must wait for them
+    if (e->pending && st != e->last_stream) {
+        const int rc = drain(e);
+        if (rc != OBGC_OK) return -rc;
+    }
+    const int b = e->tb ^ 1;
+    if (e->tables_used[b]) {
+        const cudaError_t w = cudaEventSynchronize(e->tables_ev[b]);
+        if (w != cudaSuccess) return -cuda_fail(w, "cudaEventSynchronize(column tables)");
+    }
+    const int npacks = build_packs(e, cap, b);
     if (npacks == 0) return 0;
     const size_t sb = e->ts == 4 ? sizeof(ColSlot<float>) : sizeof(ColSlot<double>);
-    const int nslots = e->ts == 4 ? stage_slots<float>(e) : stage_slots<double>(e);
-    const int nlive = e->h_packs[npacks - 1].first + e->h_packs[npacks - 1].count;
+    const int nslots = e->ts == 4 ? stage_slots<float>(e, b) : stage_slots<double>(e, b);
+    const int nlive = e->h_packs[b][npacks - 1].first + e->h_packs[b][npacks - 1].count;
     e->last_stream = st;
     e->pending = true;
-    cudaError_t err = cudaMemcpyAsync(e->d_slots, e->h_slots, sb * nslots, cudaMemcpyHostToDevice, st);
+    cudaError_t err = cudaMemcpyAsync(e->d_slots, e->h_slots[b], sb * nslots, cudaMemcpyHostToDevice, st);
     if (err == cudaSuccess)
-        err = cudaMemcpyAsync(e->d_pack_slots, e->h_pack_slots, sizeof(int32_t) * nlive, cudaMemcpyHostToDevice, st);
-    if (err == cudaSuccess) err = cudaMemcpyAsync(e->d_packs, e->h_packs, sizeof(ColPack) * npacks, cudaMemcpyHostToDevice, st);
+        err = cudaMemcpyAsync(e->d_pack_slots, e->h_pack_slots[b], sizeof(int32_t) * nlive, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(e->d_packs, e->h_packs[b], sizeof(ColPack) * npacks, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaEventRecord(e->tables_ev[b], st);
     if (err != cudaSuccess) return -cuda_fail(err, "cudaMemcpyAsync(column tables)");
+    e->tables_used[b] = true;
+    e->tb = b;
     return npacks;
 }
 
@@ -478,7 +449,48 @@ int advance_with(obgc_columns* e, int max_steps, int threads, int cap, cudaStrea
     return OBGC_OK;
 }
 
-}  // namespace
+int reserve_column(obgc_columns* e, const obgc_column_spec* sp, int64_t* slot) {
+    if (e->free_slots.empty()) return fail(OBGC_ERR_BUSY, "no free column slot");
+    const int64_t need = sp->Nz + 1;   // Nz state cells and Nz+1 faces share the block
+    auto it = e->free_cells.begin();
+    for (; it != e->free_cells.end(); ++it)
+        if (it->second >= need) break;
+    if (it == e->free_cells.end()) return fail(OBGC_ERR_BUSY, "device budget exhausted");
+    const int64_t off = it->first;
+    const int64_t len = it->second;
+    e->free_cells.erase(it);
+    if (len > need) e->free_cells[off + need] = len - need;
+    const int s = e->free_slots.back();
+    e->free_slots.pop_back();
+    ColSlot<double>& c = e->slots[s];
+    std::memset(&c, 0, sizeof(c));
+    c.cell_off = off; c.Nz = sp->Nz; c.steps_left = sp->nsteps; c.steps_done = 0;
+    c.pulse_step = sp->pulse_step; c.pulse_k = sp->pulse_k; c.live = 1;
+    c.dz = sp->dz; c.dt = sp->dt; c.PAR0 = sp->surface_PAR; c.mu0 = sp->mu0; c.pulse_amount = sp->pulse_amount;
+    *slot = s;
+    return OBGC_OK;
+}
+
+void release_column(obgc_columns* e, int64_t slot) {
+    ColSlot<double>& c = e->slots[slot];
+    int64_t off = c.cell_off, len = c.Nz + 1;
+    c.live = 0;
+    // return the block to the free list, merging neighbours
+    auto next = e->free_cells.lower_bound(off);
+    if (next != e->free_cells.end() && next->first == off + len) { len += next->second; e->free_cells.erase(next); }
+    auto prev = e->free_cells.lower_bound(off);
+    if (prev != e->free_cells.begin()) {
+        --prev;
+        if (prev->first + prev->second == off) { off = prev->first; len += prev->second; e->free_cells.erase(prev); }
+    }
+    e->free_cells[off] = len;
+    e->free_slots.push_back((int)slot);
+}
+
+}  // namespace cols
+}  // namespace obgc
+
+using namespace obgc::cols;
 
 extern "C" int obgc_columns_create(const obgc_columns_desc* d, obgc_columns** out) {
     if (!d || !out || d->max_columns < 1 || d->arena_cells < 1 || d->precision < OBGC_PREC_F32 ||
@@ -529,9 +541,12 @@ extern "C" int obgc_columns_create(const obgc_columns_desc* d, obgc_columns** ou
     chk(cudaMalloc(&e->d_slots, sb * d->max_columns), "cudaMalloc(slots)");
     chk(cudaMalloc((void**)&e->d_pack_slots, sizeof(int32_t) * d->max_columns), "cudaMalloc(pack slots)");
     chk(cudaMalloc((void**)&e->d_packs, sizeof(ColPack) * d->max_columns), "cudaMalloc(packs)");
-    chk(cudaMallocHost(&e->h_slots, sb * d->max_columns), "cudaMallocHost(slots)");
-    chk(cudaMallocHost((void**)&e->h_pack_slots, sizeof(int32_t) * d->max_columns), "cudaMallocHost(pack slots)");
-    chk(cudaMallocHost((void**)&e->h_packs, sizeof(ColPack) * d->max_columns), "cudaMallocHost(packs)");
+    for (int b = 0; b < 2; b++) {
+        chk(cudaMallocHost(&e->h_slots[b], sb * d->max_columns), "cudaMallocHost(slots)");
+        chk(cudaMallocHost((void**)&e->h_pack_slots[b], sizeof(int32_t) * d->max_columns), "cudaMallocHost(pack slots)");
+        chk(cudaMallocHost((void**)&e->h_packs[b], sizeof(ColPack) * d->max_columns), "cudaMallocHost(packs)");
+        chk(cudaEventCreateWithFlags(&e->tables_ev[b], cudaEventDisableTiming), "cudaEventCreate(column tables)");
+    }
     if (rc != OBGC_OK) { obgc_columns_destroy(e); return rc; }
     e->slots.resize(d->max_columns);
     for (auto& s : e->slots) std::memset(&s, 0, sizeof(s));
@@ -547,7 +562,10 @@ extern "C" int obgc_columns_destroy(obgc_columns* e) {
     if (e->graph) cudaGraphExecDestroy(e->graph);
     if (e->capture_stream) cudaStreamDestroy(e->capture_stream);
     cudaFree(e->state); cudaFree(e->kappa); cudaFree(e->d_slots); cudaFree(e->d_pack_slots); cudaFree(e->d_packs);
-    cudaFreeHost(e->h_slots); cudaFreeHost(e->h_pack_slots); cudaFreeHost(e->h_packs);
+    for (int b = 0; b < 2; b++) {
+        cudaFreeHost(e->h_slots[b]); cudaFreeHost(e->h_pack_slots[b]); cudaFreeHost(e->h_packs[b]);
+        if (e->tables_ev[b]) cudaEventDestroy(e->tables_ev[b]);
+    }
     delete e;
     return OBGC_OK;
 }
@@ -563,22 +581,10 @@ extern "C" int obgc_columns_add(obgc_columns* e, const obgc_column_spec* sp, con
     if (!e || !sp || !init || !kappa || !slot || sp->Nz < 1 || sp->Nz > OBGC_COLUMN_MAX_LEVELS || sp->nsteps < 0 ||
         !(sp->dz > 0) || !(sp->dt > 0))
         return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_columns_add: bad column");
-    if (e->free_slots.empty()) return fail(OBGC_ERR_BUSY, "obgc_columns_add: no free column slot");
-    const int64_t need = sp->Nz + 1;   // Nz state cells and Nz+1 faces share the block
-    auto it = e->free_cells.begin();
-    for (; it != e->free_cells.end(); ++it) if (it->second >= need) break;
-    if (it == e->free_cells.end()) return fail(OBGC_ERR_BUSY, "obgc_columns_add: device budget exhausted");
-    const int64_t off = it->first;
-    const int64_t len = it->second;
-    e->free_cells.erase(it);
-    if (len > need) e->free_cells[off + need] = len - need;
-    const int s = e->free_slots.back();
-    e->free_slots.pop_back();
-    ColSlot<double>& c = e->slots[s];
-    std::memset(&c, 0, sizeof(c));
-    c.cell_off = off; c.Nz = sp->Nz; c.steps_left = sp->nsteps; c.steps_done = 0;
-    c.pulse_step = sp->pulse_step; c.pulse_k = sp->pulse_k; c.live = 1;
-    c.dz = sp->dz; c.dt = sp->dt; c.PAR0 = sp->surface_PAR; c.mu0 = sp->mu0; c.pulse_amount = sp->pulse_amount;
+    int64_t s = -1;
+    const int rs = reserve_column(e, sp, &s);
+    if (rs != OBGC_OK) return rs;
+    const int64_t off = e->slots[s].cell_off;
     // stage the column's state and diffusivities on the engine's stream, then wait for the copies
     const size_t n = (size_t)e->NT * sp->Nz;
     cudaStream_t st = e->last_stream;
@@ -675,19 +681,7 @@ extern "C" int obgc_columns_read(obgc_columns* e, int64_t slot, double* out) {
 extern "C" int obgc_columns_remove(obgc_columns* e, int64_t slot) {
     if (!e || slot < 0 || slot >= (int64_t)e->slots.size() || !e->slots[slot].live)
         return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_columns_remove: bad slot");
-    ColSlot<double>& c = e->slots[slot];
-    int64_t off = c.cell_off, len = c.Nz + 1;
-    c.live = 0;
-    // return the block to the free list, merging neighbours
-    auto next = e->free_cells.lower_bound(off);
-    if (next != e->free_cells.end() && next->first == off + len) { len += next->second; e->free_cells.erase(next); }
-    auto prev = e->free_cells.lower_bound(off);
-    if (prev != e->free_cells.begin()) {
-        --prev;
-        if (prev->first + prev->second == off) { off = prev->first; len += prev->second; e->free_cells.erase(prev); }
-    }
-    e->free_cells[off] = len;
-    e->free_slots.push_back((int)slot);
+    release_column(e, slot);
     return OBGC_OK;
 }
 

@@ -9,6 +9,7 @@ libobgc.so (CUDA, sm_103a); importing works without it, calling does not.
 from . import _abi
 from .box import BoxModel
 from .columns import ColumnEngine
+from .service import ColumnService
 from .carbon import CarbonChemistry
 from .grid import BoxModelGrid, RectilinearGrid
 from .light import (MultiBandPhotosyntheticallyActiveRadiation, PrescribedPhotosyntheticallyActiveRadiation,

@@ -135,6 +135,16 @@ class ColumnsDesc(C.Structure):
                 ("invalid_fill_value", C.c_double)]
 
 
+class ServiceDesc(C.Structure):
+    _fields_ = [("columns", ColumnsDesc), ("chunk_steps", C.c_int32), ("max_queue", C.c_int32)]
+
+
+class ServiceStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64),
+                ("launches", C.c_int64), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
+                ("max_ms", C.c_double), ("span_s", C.c_double)]
+
+
 def default_twoband():
     """TwoBandPhotosyntheticallyActiveRadiation defaults (src/Light/2band.jl:106-117)."""
     return TwoBandParams(0.225, 0.0232, 0.037, 0.074, 0.629, 0.674, 0.7, 1.31)
@@ -220,6 +230,14 @@ def load():
     _sig(lib, "obgc_columns_read", C.c_int, VP, I64, P(D))
     _sig(lib, "obgc_columns_remove", C.c_int, VP, I64)
     _sig(lib, "obgc_columns_autotune", C.c_int, VP, I32, P(I32), P(I32), VP)
+    _sig(lib, "obgc_service_create", C.c_int, P(ServiceDesc), P(VP))
+    _sig(lib, "obgc_service_destroy", C.c_int, VP)
+    _sig(lib, "obgc_service_submit", C.c_int, VP, P(ColumnSpec), P(D), P(D), P(I64))
+    _sig(lib, "obgc_service_wait", C.c_int, VP, I64, D, P(D), P(D))
+    _sig(lib, "obgc_service_drain", C.c_int, VP, D)
+    _sig(lib, "obgc_service_get_stats", C.c_int, VP, P(ServiceStats))
+    _sig(lib, "obgc_service_reset_stats", C.c_int, VP)
+    _sig(lib, "obgc_service_engine", C.c_int, VP, P(VP))
     _lib = lib
     return lib
 
@@ -237,4 +255,6 @@ EXPORTED = [
     "obgc_columns_create", "obgc_columns_destroy", "obgc_columns_tracers", "obgc_columns_add",
     "obgc_columns_advance", "obgc_columns_run", "obgc_columns_remaining", "obgc_columns_read", "obgc_columns_remove",
     "obgc_columns_autotune", "obgc_npd_conserved_tracers", "obgc_scale_negatives", "obgc_zero_negatives",
+    "obgc_service_create", "obgc_service_destroy", "obgc_service_submit", "obgc_service_wait", "obgc_service_drain",
+    "obgc_service_get_stats", "obgc_service_reset_stats", "obgc_service_engine",
 ]
