@@ -524,6 +524,77 @@ def run_service(args):
     return 0
 
 
+# ----------------------------------------------------------------------------- accuracy after 1000 steps
+def error_statement(got, ref, names):
+    """Per tracer max |x - x_ref| and max |x - x_ref| / max(|x_ref|, 1e-6 max|x_ref|)."""
+    import numpy as np
+    out = {}
+    for q, n in enumerate(names):
+        g, r = got[q].astype(np.float64), ref[q].astype(np.float64)
+        d = np.abs(g - r)
+        floor = 1e-6 * max(float(np.max(np.abs(r))), 1e-300)
+        out[n] = {"max_abs": float(d.max()), "max_rel": float(np.max(d / np.maximum(np.abs(r), floor)))}
+    return out
+
+
+def run_accuracy(args):
+    """FP32 and mixed (FP64 state, FP32 compute) LOBSTER+carbonates after `steps` steps against the
+    FP64 oracle (small grid, CPU) and against the FP64 GPU path (full grid), tracers and FP64 pH."""
+    import numpy as np
+    import torch
+    import obgc
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    torch.cuda.set_device(0)
+    steps = args.steps if args.steps_given else 1000
+    cc = obgc.CarbonChemistry()
+
+    def run(shape, prec, seed=3):
+        extent = (EXTENT[0] * shape[0] / SHAPE[0], EXTENT[1] * shape[1] / SHAPE[1], EXTENT[2])
+        g = obgc.RectilinearGrid(shape, extent, ("Periodic", "Periodic", "Bounded"),
+                                 dtype="f32" if prec == "f32" else "f64")
+        bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem())
+        u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=seed)
+        m = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None),
+                                     precision=prec)
+        obgc.set_(m, **obgc.lobster_initial_conditions(g, seed=seed + 1))
+        s0 = m.state_array().cpu().numpy().astype(np.float64)
+        obgc.time_step(m, DT, nsteps=steps, graph=True)
+        torch.cuda.synchronize()
+        return g, bgc, (u, v), m.tracer_names, s0, m.state_array().cpu().numpy().astype(np.float64)
+
+    def ph(state, names):
+        t = {n: torch.as_tensor(state[names.index(n)], device="cuda") for n in ("DIC", "Alk", "T", "S")}
+        return cc(t["DIC"], t["T"], t["S"], Alk=t["Alk"], output="pHt").cpu().numpy()
+
+    result = {}
+    # small grid against the oracle
+    small = (64, 64, 32)
+    g, bgc, (u, v), names, s0, f64 = run(small, "f64")
+    ref = np.ascontiguousarray(s0)
+    m = O.model3d(bgc.params, g.c_grid(), names)
+    t0 = time.perf_counter()
+    O.step3d(m, ref, u=u.double().cpu().numpy().ravel().copy(), v=v.double().cpu().numpy().ravel().copy(),
+             t=0.0, dt=DT, nsteps=steps, threads=os.cpu_count())
+    t_oracle = time.perf_counter() - t0
+    ph_ref = ph(ref, names)
+    for prec, state in (("f64", f64), ("mixed", run(small, "mixed")[5]), ("f32", run(small, "f32")[5])):
+        result[f"{prec}_vs_oracle_64x64x32"] = {"tracers": error_statement(state, ref, names),
+                                               "pH_max_abs": float(np.max(np.abs(ph(state, names) - ph_ref)))}
+    # full grid against the FP64 GPU path
+    _, _, _, names, _, f64 = run(SHAPE, "f64")
+    ph64 = ph(f64, names)
+    for prec in ("mixed", "f32"):
+        state = run(SHAPE, prec)[5]
+        result[f"{prec}_vs_gpu_f64_256x256x64"] = {"tracers": error_statement(state, f64, names),
+                                                  "pH_max_abs": float(np.max(np.abs(ph(state, names) - ph64)))}
+    worst = {k: max(v2["max_rel"] for v2 in v["tracers"].values()) for k, v in result.items()}
+    print(json.dumps({"workload": "accuracy", "steps": steps, "dt_s": DT, "oracle_seconds": t_oracle,
+                      "worst_max_rel": worst, "pH_max_abs": {k: v["pH_max_abs"] for k, v in result.items()},
+                      "detail": result}))
+    return 0
+
+
 # ----------------------------------------------------------------------------- carbonate chemistry
 def run_carbon(args):
     """pH (total scale) of every cell of the 256x256x64 LOBSTER state, FP64 Newton per cell."""
@@ -587,7 +658,7 @@ def run_carbon(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="lobster3d", choices=["lobster3d", "columns", "service", "carbon"])
+    ap.add_argument("--workload", default="lobster3d", choices=["lobster3d", "columns", "service", "carbon", "accuracy"])
     ap.add_argument("--rates", type=float, nargs="*", default=None, help="service: Poisson arrival rates (1/s)")
     ap.add_argument("--arrival-seconds", type=float, default=2.0, help="service: seconds of arrivals per rate")
     ap.add_argument("--chunk", type=int, default=32, help="service: steps per launch")
@@ -608,6 +679,8 @@ def main():
         return run_columns(args)
     if args.workload == "carbon":
         return run_carbon(args)
+    if args.workload == "accuracy":
+        return run_accuracy(args)
     if args.workload == "service":
         if "--precision" not in sys.argv:
             args.precision = "mixed"

@@ -47,25 +47,27 @@ __device__ __forceinline__ f32x2 rcp2(f32x2 a) {
     return pk2(rcp_approx(lo), rcp_approx(hi));
 }
 
-// WENO5-Z of two upwind stencils (v1..v5 from far upwind to downwind), packed lo/hi.
+// WENO5-Z of two upwind stencils (v1..v5 from far upwind to downwind), packed lo/hi, in the
+// difference form of weno5<float> (d_k = v_k - v3).
 __device__ __forceinline__ f32x2 weno5_x2(f32x2 v1, f32x2 v2, f32x2 v3, f32x2 v4, f32x2 v5) {
-    const f32x2 c13 = splat2(2.f / 6.f), c76 = splat2(-7.f / 6.f), c116 = splat2(11.f / 6.f);
+    const f32x2 c13 = splat2(2.f / 6.f), c76 = splat2(-7.f / 6.f);
     const f32x2 cm16 = splat2(-1.f / 6.f), c56 = splat2(5.f / 6.f);
-    const f32x2 m2 = splat2(-2.f), m4 = splat2(-4.f), p3 = splat2(3.f);
+    const f32x2 m2 = splat2(-2.f), m4 = splat2(-4.f);
     const f32x2 k1312 = splat2(13.f / 12.f), k14 = splat2(0.25f), one = splat2(1.f), eps = splat2(1e-8f);
-    // candidate stencils
-    const f32x2 q0 = fma2(c13, v1, fma2(c76, v2, mul2(c116, v3)));
-    const f32x2 q1 = fma2(cm16, v2, fma2(c56, v3, mul2(c13, v4)));
-    const f32x2 q2 = fma2(c13, v3, fma2(c56, v4, mul2(cm16, v5)));
+    const f32x2 d1 = sub2(v1, v3), d2 = sub2(v2, v3), d4 = sub2(v4, v3), d5 = sub2(v5, v3);
+    // candidate stencils relative to v3
+    const f32x2 p0 = fma2(c13, d1, mul2(c76, d2));
+    const f32x2 p1 = fma2(cm16, d2, mul2(c13, d4));
+    const f32x2 p2 = fma2(c56, d4, mul2(cm16, d5));
     // smoothness indicators
-    f32x2 a = fma2(m2, v2, add2(v1, v3));
-    f32x2 b = fma2(m4, v2, fma2(p3, v3, v1));
+    f32x2 a = fma2(m2, d2, d1);
+    f32x2 b = fma2(m4, d2, d1);
     const f32x2 b0 = fma2(mul2(k1312, a), a, mul2(mul2(k14, b), b));
-    a = fma2(m2, v3, add2(v2, v4));
-    b = sub2(v2, v4);
+    a = add2(d2, d4);
+    b = sub2(d2, d4);
     const f32x2 b1 = fma2(mul2(k1312, a), a, mul2(mul2(k14, b), b));
-    a = fma2(m2, v4, add2(v3, v5));
-    b = fma2(m4, v4, fma2(p3, v3, v5));
+    a = fma2(m2, d4, d5);
+    b = fma2(m4, d4, d5);
     const f32x2 b2 = fma2(mul2(k1312, a), a, mul2(mul2(k14, b), b));
     const f32x2 tau = abs2(sub2(b0, b2));
     const f32x2 r0 = mul2(tau, rcp2(add2(b0, eps)));
@@ -74,8 +76,8 @@ __device__ __forceinline__ f32x2 weno5_x2(f32x2 v1, f32x2 v2, f32x2 v3, f32x2 v4
     const f32x2 a0 = mul2(splat2(0.1f), fma2(r0, r0, one));
     const f32x2 a1 = mul2(splat2(0.6f), fma2(r1, r1, one));
     const f32x2 a2 = mul2(splat2(0.3f), fma2(r2, r2, one));
-    const f32x2 num = fma2(a0, q0, fma2(a1, q1, mul2(a2, q2)));
-    return mul2(num, rcp2(add2(add2(a0, a1), a2)));
+    const f32x2 num = fma2(a0, p0, fma2(a1, p1, mul2(a2, p2)));
+    return fma2(num, rcp2(add2(add2(a0, a1), a2)), v3);
 }
 #endif
 
