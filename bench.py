@@ -243,12 +243,9 @@ def run_gpu(args):
     bytes_per_launch = bytes_per_update * N_TRACERS * g.N / 3
     achieved = bytes_per_launch / (substep_avg_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "substep_traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            tj = json.load(f)
-        traffic = tj.get(prec)
+    # DRAM bytes per cell of one substep launch, FP32: dram__bytes_read.sum + dram__bytes_write.sum of
+    # the ncu capture at 256x256x32 (259.5 MB / 2,097,152 cells), scaled by the cells of this grid
+    traffic = 123.7 * g.N if prec == "f32" else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
