@@ -148,6 +148,94 @@ typedef struct obgc_npd_params {
     double nitrification_oxygen_nitrogen_ratio;
 } obgc_npd_params;
 
+/* ---------------------------------------------------------------------------------------------
+ * PISCES (src/Models/AdvectedPopulations/PISCES).  Tracer slots in required_biogeochemical_tracers
+ * order (PISCES.jl:86-98): P PChl PFe D DChl DFe DSi Z M DOC POC GOC SFe BFe PSi CaCO3 NO3 NH4 PO4 Fe
+ * Si DIC Alk O2, then T and S.
+ * ------------------------------------------------------------------------------------------- */
+enum obgc_pisces_tracer {
+    OBGC_PIS_P = 0, OBGC_PIS_PCHL, OBGC_PIS_PFE, OBGC_PIS_D, OBGC_PIS_DCHL, OBGC_PIS_DFE, OBGC_PIS_DSI,
+    OBGC_PIS_Z, OBGC_PIS_M, OBGC_PIS_DOC, OBGC_PIS_POC, OBGC_PIS_GOC, OBGC_PIS_SFE, OBGC_PIS_BFE,
+    OBGC_PIS_PSI, OBGC_PIS_CACO3, OBGC_PIS_NO3, OBGC_PIS_NH4, OBGC_PIS_PO4, OBGC_PIS_FE, OBGC_PIS_SI,
+    OBGC_PIS_DIC, OBGC_PIS_ALK, OBGC_PIS_O2, OBGC_PIS_T, OBGC_PIS_S,
+    OBGC_PIS_NUM_BGC = 24,       /* tracers with a tendency                                    */
+    OBGC_PIS_NUM = 26
+};
+/* Auxiliary inputs of a cell (required_biogeochemical_auxiliary_fields, PISCES.jl:100-101). */
+enum obgc_pisces_aux {
+    OBGC_PAUX_ZMXL = 0,   /* mixed-layer depth (m, negative)                                    */
+    OBGC_PAUX_ZEU,        /* euphotic depth (m, negative)                                       */
+    OBGC_PAUX_SICLIM,     /* silicate climatology Si'                                          */
+    OBGC_PAUX_OMEGA,      /* calcite saturation                                                 */
+    OBGC_PAUX_KAPPA,      /* mean mixed-layer vertical diffusivity                              */
+    OBGC_PAUX_MLPAR,      /* mean mixed-layer PAR                                               */
+    OBGC_PAUX_WPOC,       /* POC sinking velocity interpolated to the cell centre (m/s, <= 0)  */
+    OBGC_PAUX_WGOC,       /* GOC sinking velocity interpolated to the cell centre (m/s, <= 0)  */
+    OBGC_PAUX_PAR, OBGC_PAUX_PAR1, OBGC_PAUX_PAR2, OBGC_PAUX_PAR3,
+    OBGC_PAUX_NUM = 12
+};
+
+/* One MixedMondo phytoplankton class with its growth rate and nutrient limitation
+ * (phytoplankton/mixed_mondo.jl:23-99, growth_rate.jl:69-124, nutrient_limitation.jl:10-18). */
+typedef struct obgc_pisces_phyto {
+    int32_t growth_kind;         /* 0 NutrientLimitedProduction, 1 GrowthRespirationLimitedProduction */
+    int32_t silicate_limited;
+    double exudated_fraction, blue_light_absorption, green_light_absorption, red_light_absorption;
+    double mortality_half_saturation, linear_mortality_rate, base_quadratic_mortality, maximum_quadratic_mortality;
+    double minimum_chlorophyll_ratio, maximum_chlorophyll_ratio, maximum_iron_ratio;
+    double silicate_half_saturation, enhanced_silicate_half_saturation, optimal_silicate_ratio;
+    double half_saturation_for_iron_uptake, threshold_for_size_dependency, size_ratio;
+    double base_growth_rate, temperature_sensitivity, dark_tolerance, initial_slope_of_PI_curve,
+           low_light_adaptation, basal_respiration_rate, reference_growth_rate;
+    double minimum_ammonium_half_saturation, minimum_nitrate_half_saturation,
+           minimum_phosphate_half_saturation, optimal_iron_quota, minimum_silicate_half_saturation,
+           silicate_half_saturation_parameter;
+} obgc_pisces_phyto;
+
+/* One QualityDependantZooplankton class (zooplankton/food_quality_dependant.jl:11-108). */
+typedef struct obgc_pisces_zoo {
+    double temperature_sensitivity, maximum_grazing_rate;
+    double preference_P, preference_D, preference_POC, preference_Z;
+    double food_threshold_concentration, specific_food_threshold_concentration, grazing_half_saturation;
+    double maximum_flux_feeding_rate, iron_ratio, minimum_growth_efficiency, non_assimilated_fraction;
+    double mortality_half_saturation, quadratic_mortality, linear_mortality;
+    double dissolved_excretion_fraction, undissolved_calcite_fraction;
+} obgc_pisces_zoo;
+
+typedef struct obgc_pisces_params {
+    obgc_pisces_phyto nano, diatoms;
+    double base_rain_ratio;                       /* NanoAndDiatoms                         */
+    obgc_pisces_zoo micro, meso;
+    /* MicroAndMeso bacteria (zooplankton/micro_and_meso.jl:3-20) */
+    double micro_bacteria, meso_bacteria, maximum_bacteria, bacteria_depth_exponent;
+    double doc_half_saturation_bacteria, nitrate_half_saturation_bacteria, ammonia_half_saturation_bacteria,
+           phosphate_half_saturation_bacteria, iron_half_saturation_bacteria;
+    /* DissolvedOrganicCarbon (dissolved_organic_carbon.jl:9-37) */
+    double doc_remineralisation_rate, doc_bacteria_depth_exponent, doc_reference_bacteria,
+           doc_temperature_sensitivity, doc_aggregation[5];
+    /* TwoCompartmentCarbonIronParticles (two_size_class.jl:17-86) */
+    double pom_temperature_sensitivity, pom_base_breakdown_rate, pom_aggregation[4];
+    double minimum_iron_scavenging_rate, load_specific_iron_scavenging_rate, bacterial_iron_uptake_efficiency;
+    double small_fraction_bacterial_iron, large_fraction_bacterial_iron, base_liable_silicate_fraction;
+    double fast_dissolution_rate_of_silicate, slow_dissolution_rate_of_silicate;
+    double base_calcite_dissolution_rate, calcite_dissolution_exponent;
+    double maximum_iron_ratio_in_bacteria, iron_half_saturation_for_bacteria, maximum_bacterial_growth_rate;
+    /* NitrateAmmonia (nitrogen/nitrate_ammonia.jl:10-16) */
+    double maximum_nitrification_rate, maximum_fixation_rate, iron_half_saturation_for_fixation,
+           phosphate_half_saturation_for_fixation, light_saturation_for_fixation;
+    /* SimpleIron (iron/simple_iron.jl:9-13) */
+    double excess_scavenging_enhancement, maximum_ligand_concentration, dissolved_ligand_ratio;
+    /* Oxygen (oxygen.jl:21-24) */
+    double ratio_for_respiration, ratio_for_nitrification;
+    /* PISCES (PISCES.jl:288-340) */
+    double first_anoxia_threshold, second_anoxia_threshold, nitrogen_redfield_ratio, phosphate_redfield_ratio;
+    double mixed_layer_shear, background_shear, latitude, day_length_coefficient;
+    /* sinking: POC at a constant speed, GOC by DepthDependantSinkingSpeed (common.jl:39-56) */
+    double poc_sinking_speed, goc_minimum_speed, goc_maximum_speed, goc_maximum_depth;
+    double silicate_climatology;
+    int32_t open_bottom, reserved0;
+} obgc_pisces_params;
+
 /* TwoBandPhotosyntheticallyActiveRadiation parameters (src/Light/2band.jl:106-117). */
 typedef struct obgc_twoband_params {
     double water_red_attenuation;

@@ -122,6 +122,86 @@ class Fields(C.Structure):
                 ("G", C.c_void_p * NUM_NAMED)]
 
 
+def _fields(spec):
+    """[(name, ctype)] from 'int32 a, b; double c, d[5]; ...' in declaration order."""
+    out = []
+    for decl in spec.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        kind, names = decl.split(None, 1)
+        ct = {"int32": C.c_int32, "double": C.c_double}[kind]
+        for n in names.split(","):
+            n = n.strip()
+            if "[" in n:
+                base, cnt = n[:-1].split("[")
+                out.append((base, ct * int(cnt)))
+            else:
+                out.append((n, ct))
+    return out
+
+
+class PiscesPhyto(C.Structure):
+    _fields_ = _fields("""
+        int32 growth_kind, silicate_limited;
+        double exudated_fraction, blue_light_absorption, green_light_absorption, red_light_absorption;
+        double mortality_half_saturation, linear_mortality_rate, base_quadratic_mortality, maximum_quadratic_mortality;
+        double minimum_chlorophyll_ratio, maximum_chlorophyll_ratio, maximum_iron_ratio;
+        double silicate_half_saturation, enhanced_silicate_half_saturation, optimal_silicate_ratio;
+        double half_saturation_for_iron_uptake, threshold_for_size_dependency, size_ratio;
+        double base_growth_rate, temperature_sensitivity, dark_tolerance, initial_slope_of_PI_curve,
+               low_light_adaptation, basal_respiration_rate, reference_growth_rate;
+        double minimum_ammonium_half_saturation, minimum_nitrate_half_saturation,
+               minimum_phosphate_half_saturation, optimal_iron_quota, minimum_silicate_half_saturation,
+               silicate_half_saturation_parameter""")
+
+
+class PiscesZoo(C.Structure):
+    _fields_ = _fields("""
+        double temperature_sensitivity, maximum_grazing_rate;
+        double preference_P, preference_D, preference_POC, preference_Z;
+        double food_threshold_concentration, specific_food_threshold_concentration, grazing_half_saturation;
+        double maximum_flux_feeding_rate, iron_ratio, minimum_growth_efficiency, non_assimilated_fraction;
+        double mortality_half_saturation, quadratic_mortality, linear_mortality;
+        double dissolved_excretion_fraction, undissolved_calcite_fraction""")
+
+
+class PiscesParams(C.Structure):
+    _fields_ = ([("nano", PiscesPhyto), ("diatoms", PiscesPhyto), ("base_rain_ratio", C.c_double),
+                 ("micro", PiscesZoo), ("meso", PiscesZoo)] + _fields("""
+        double micro_bacteria, meso_bacteria, maximum_bacteria, bacteria_depth_exponent;
+        double doc_half_saturation_bacteria, nitrate_half_saturation_bacteria, ammonia_half_saturation_bacteria,
+               phosphate_half_saturation_bacteria, iron_half_saturation_bacteria;
+        double doc_remineralisation_rate, doc_bacteria_depth_exponent, doc_reference_bacteria,
+               doc_temperature_sensitivity, doc_aggregation[5];
+        double pom_temperature_sensitivity, pom_base_breakdown_rate, pom_aggregation[4];
+        double minimum_iron_scavenging_rate, load_specific_iron_scavenging_rate, bacterial_iron_uptake_efficiency;
+        double small_fraction_bacterial_iron, large_fraction_bacterial_iron, base_liable_silicate_fraction;
+        double fast_dissolution_rate_of_silicate, slow_dissolution_rate_of_silicate;
+        double base_calcite_dissolution_rate, calcite_dissolution_exponent;
+        double maximum_iron_ratio_in_bacteria, iron_half_saturation_for_bacteria, maximum_bacterial_growth_rate;
+        double maximum_nitrification_rate, maximum_fixation_rate, iron_half_saturation_for_fixation,
+               phosphate_half_saturation_for_fixation, light_saturation_for_fixation;
+        double excess_scavenging_enhancement, maximum_ligand_concentration, dissolved_ligand_ratio;
+        double ratio_for_respiration, ratio_for_nitrification;
+        double first_anoxia_threshold, second_anoxia_threshold, nitrogen_redfield_ratio, phosphate_redfield_ratio;
+        double mixed_layer_shear, background_shear, latitude, day_length_coefficient;
+        double poc_sinking_speed, goc_minimum_speed, goc_maximum_speed, goc_maximum_depth;
+        double silicate_climatology;
+        int32 open_bottom, reserved0"""))
+
+
+PISCES_TRACERS = ["P", "PChl", "PFe", "D", "DChl", "DFe", "DSi", "Z", "M", "DOC", "POC", "GOC", "SFe", "BFe", "PSi",
+                  "CaCO₃", "NO₃", "NH₄", "PO₄", "Fe", "Si", "DIC", "Alk", "O₂", "T", "S"]
+PISCES_ASCII = ["P", "PChl", "PFe", "D", "DChl", "DFe", "DSi", "Z", "M", "DOC", "POC", "GOC", "SFe", "BFe", "PSi",
+                "CaCO3", "NO3", "NH4", "PO4", "Fe", "Si", "DIC", "Alk", "O2", "T", "S"]
+PISCES_INDEX = {n: i for i, n in enumerate(PISCES_TRACERS)}
+PISCES_INDEX.update({n: i for i, n in enumerate(PISCES_ASCII)})
+PISCES_NUM_BGC = 24
+PISCES_AUX = ["zmxl", "zeu", "Si_clim", "Omega", "kappa", "mixed_layer_PAR", "wPOC", "wGOC", "PAR", "PAR1", "PAR2",
+              "PAR3"]
+
+
 class ColumnSpec(C.Structure):
     _fields_ = [("Nz", C.c_int32), ("nsteps", C.c_int32), ("dz", C.c_double), ("dt", C.c_double),
                 ("surface_PAR", C.c_double), ("mu0", C.c_double), ("pulse_step", C.c_int32),

@@ -108,8 +108,8 @@ void or_columns_run(const obgc_npd_params* p, const obgc_twoband_params* lp, int
                     int negatives, double invalid_fill_value, int nthreads);
 
 /* ---- negative tracers (src/Utils/negative_tracers.jl) ---- */
-#define OR_MAX_GROUPS 2
-#define OR_MAX_GROUP 8
+#define OR_MAX_GROUPS 5
+#define OR_MAX_GROUP 10
 /* conserved_tracers(bgc) (NutrientsPlanktonDetritus/coupling_utils.jl:1-52) as slots of `names`
  * and scale factors; returns the number of groups (nitrogen, then carbon with the carbonate
  * system).  gn[g] members, gslot/gfac [OR_MAX_GROUPS][OR_MAX_GROUP]. */
@@ -122,6 +122,17 @@ void or_scale_cell(double* v, long stride, int ng, const int32_t* gn, const int3
 /* ---- ScaleNegativeTracers (src/Utils/negative_tracers.jl:250-276) ---- */
 void or_scale_negatives(int64_t n, int ntr, double* const* fields, const double* scalefactors,
                         double invalid_fill_value);
+
+/* ---- PISCES (src/Models/AdvectedPopulations/PISCES) ---- */
+void or_pisces_defaults(obgc_pisces_params* p);
+double or_cbm_day_length(double coefficient, double t, double phi);
+/* values [OBGC_PIS_NUM] in the PISCES tracer order, aux [OBGC_PAUX_NUM]; z the cell centre (m),
+ * t the model time (s). */
+double or_pisces_tendency(const obgc_pisces_params* p, int n, const double* values, const double* aux, double z, double t);
+void or_pisces_tendencies(const obgc_pisces_params* p, const double* values, const double* aux, double z, double t, double* G);
+void or_pisces_goc_speed(const obgc_pisces_params* p, int Nz, const double* zc, double zmxl, double zeu, double* w_faces);
+double or_mixed_layer_mean(int Nz, const double* zf, const double* C, double zmxl);
+int or_pisces_conserved_groups(const obgc_pisces_params* p, int32_t* gn, int32_t* gslot, double* gfac);
 
 #ifdef __cplusplus
 }

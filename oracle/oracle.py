@@ -29,6 +29,7 @@ class Model3D(C.Structure):
 
 
 NEG_NONE, NEG_SCALE, NEG_ZERO = 0, 1, 2
+MAX_GROUPS, MAX_MEMBERS = 5, 10      # OR_MAX_GROUPS, OR_MAX_GROUP
 
 
 class Column(C.Structure):
@@ -83,6 +84,16 @@ def lib():
         L.or_columns_run.argtypes = [P(A.NPDParams), P(A.TwoBandParams), C.c_int, P(Column), P(I64),
                                      P(I64), C.c_int, P(I32), P(D), P(D), D, D, C.c_int, C.c_int, D, C.c_int]
         L.or_scale_negatives.argtypes = [I64, C.c_int, P(P(D)), P(D), D]
+        L.or_pisces_defaults.argtypes = [P(A.PiscesParams)]
+        L.or_cbm_day_length.argtypes = [D, D, D]
+        L.or_cbm_day_length.restype = D
+        L.or_pisces_tendency.argtypes = [P(A.PiscesParams), C.c_int, P(D), P(D), D, D]
+        L.or_pisces_tendency.restype = D
+        L.or_pisces_tendencies.argtypes = [P(A.PiscesParams), P(D), P(D), D, D, P(D)]
+        L.or_pisces_goc_speed.argtypes = [P(A.PiscesParams), C.c_int, P(D), D, D, P(D)]
+        L.or_mixed_layer_mean.argtypes = [C.c_int, P(D), P(D), D]
+        L.or_mixed_layer_mean.restype = D
+        L.or_pisces_conserved_groups.argtypes = [P(A.PiscesParams), P(I32), P(I32), P(D)]
         L.or_conserved_groups.argtypes = [P(A.NPDParams), C.c_int, P(I32), P(I32), P(I32), P(D)]
         L.or_scale_cell.argtypes = [P(D), C.c_long, C.c_int, P(I32), P(I32), P(D), D]
         _lib = L
@@ -272,11 +283,27 @@ def par3d(m, state, t, threads=None):
 def conserved_groups(p, names):
     """or_conserved_groups: [(slots, factors), ...] in the reference's group and member order."""
     nm = np.array([A.NAME_INDEX[x] if isinstance(x, str) else x for x in names], dtype=np.int32)
-    gn = (C.c_int32 * 2)()
-    gs = (C.c_int32 * 16)()
-    gf = (C.c_double * 16)()
+    gn = (C.c_int32 * MAX_GROUPS)()
+    gs = (C.c_int32 * (MAX_GROUPS * MAX_MEMBERS))()
+    gf = (C.c_double * (MAX_GROUPS * MAX_MEMBERS))()
     ng = lib().or_conserved_groups(C.byref(p), len(nm), nm.ctypes.data_as(C.POINTER(C.c_int32)), gn, gs, gf)
-    return [([gs[g * 8 + m] for m in range(gn[g])], [gf[g * 8 + m] for m in range(gn[g])]) for g in range(ng)]
+    return _groups(ng, gn, gs, gf)
+
+
+def _groups(ng, gn, gs, gf):
+    return [([gs[g * MAX_MEMBERS + m] for m in range(gn[g])], [gf[g * MAX_MEMBERS + m] for m in range(gn[g])])
+            for g in range(ng)]
+
+
+def group_arrays(groups):
+    """(gn, gslot, gfac) arrays in or_scale_cell's layout for a list of (slots, factors)."""
+    gn = np.array([len(g[0]) for g in groups], dtype=np.int32)
+    gs = np.zeros(MAX_GROUPS * MAX_MEMBERS, dtype=np.int32)
+    gf = np.zeros(MAX_GROUPS * MAX_MEMBERS)
+    for g, (sl, fa) in enumerate(groups):
+        gs[g * MAX_MEMBERS:g * MAX_MEMBERS + len(sl)] = sl
+        gf[g * MAX_MEMBERS:g * MAX_MEMBERS + len(fa)] = fa
+    return gn, gs, gf
 
 
 def columns_run(p, lp, cols, names, state, kappa, state_offsets, kappa_offsets, dt, nsteps, threads=None,
@@ -297,3 +324,45 @@ def scale_negatives(fields, scalefactors, fill=np.nan):
     ptrs = (C.POINTER(C.c_double) * len(fields))(*[_dp(f) for f in fields])
     sf = np.ascontiguousarray(scalefactors, dtype=np.float64)
     lib().or_scale_negatives(len(fields[0]), len(fields), ptrs, _dp(sf), fill)
+
+
+# ----------------------------------------------------------------------------- PISCES
+def pisces_defaults():
+    p = A.PiscesParams()
+    lib().or_pisces_defaults(C.byref(p))
+    return p
+
+
+def pisces_tendencies(p, values, aux, z, t=0.0):
+    """values: 26 tracer values (PISCES order or a dict by name), aux: 12 auxiliary values or a dict."""
+    if isinstance(values, dict):
+        values = [float(values.get(n, values.get(a, 0.0))) for n, a in zip(A.PISCES_TRACERS, A.PISCES_ASCII)]
+    if isinstance(aux, dict):
+        aux = [float(aux[n]) for n in A.PISCES_AUX]
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    a = np.ascontiguousarray(aux, dtype=np.float64)
+    G = np.zeros(A.PISCES_NUM_BGC)
+    lib().or_pisces_tendencies(C.byref(p), _dp(v), _dp(a), float(z), float(t), _dp(G))
+    return G
+
+
+def pisces_conserved_groups(p):
+    gn = (C.c_int32 * MAX_GROUPS)()
+    gs = (C.c_int32 * (MAX_GROUPS * MAX_MEMBERS))()
+    gf = (C.c_double * (MAX_GROUPS * MAX_MEMBERS))()
+    ng = lib().or_pisces_conserved_groups(C.byref(p), gn, gs, gf)
+    return _groups(ng, gn, gs, gf)
+
+
+def mixed_layer_mean(zf, C_, zmxl):
+    zf = np.ascontiguousarray(zf, dtype=np.float64)
+    C_ = np.ascontiguousarray(C_, dtype=np.float64)
+    return lib().or_mixed_layer_mean(len(C_), _dp(zf), _dp(C_), float(zmxl))
+
+
+def goc_speed(p, zc, zmxl, zeu):
+    zc = np.ascontiguousarray(zc, dtype=np.float64)
+    w = np.zeros(len(zc) + 1)
+    lib().or_pisces_goc_speed(C.byref(p), len(zc), _dp(zc), float(zmxl), float(zeu), _dp(w))
+    return w
+

@@ -57,12 +57,7 @@ def test_scale_cell_rules():
     bgc = obgc.LOBSTER(None, carbonate_system=obgc.CarbonateSystem())
     names = obgc.required_biogeochemical_tracers(bgc)
     groups = O.conserved_groups(bgc.params, names)
-    gn = np.array([len(g[0]) for g in groups], dtype=np.int32)
-    gs = np.zeros(16, dtype=np.int32)
-    gf = np.zeros(16)
-    for g, (sl, fa) in enumerate(groups):
-        gs[g * 8:g * 8 + len(sl)] = sl
-        gf[g * 8:g * 8 + len(fa)] = fa
+    gn, gs, gf = O.group_arrays(groups)
     P = O.C.POINTER
     v = np.array([1.0, 0.5, -0.1, 0.2, 0.3, -0.05, 0.1, 2000.0, 2300.0])
     ref = v.copy()
