@@ -560,6 +560,49 @@ int obgc_box_run(const obgc_npd_params* p, const obgc_npd_params* params_per_mod
  * launch of up to max_steps steps.
  * ------------------------------------------------------------------------------------- */
 /* ---------------------------------------------------------------------------------------------
+ * PISCES entry points.
+ * ------------------------------------------------------------------------------------------- */
+/* Layout of an auxiliary input (PISCES's auxiliary fields are 2-D, 3-D or constant). */
+enum obgc_pisces_field_kind {
+    OBGC_PF_CONSTANT = 0,   /* `value` everywhere                                               */
+    OBGC_PF_XY = 1,         /* (Nx, Ny) field, element i + j*stride_j                           */
+    OBGC_PF_XYZ = 2,        /* centre field with the grid's strides                              */
+    OBGC_PF_ZFACE = 3,      /* z-face field with the grid's strides, Nz+1 levels; the cell uses the
+                               mean of its two faces (the ℑz interpolation of the reference)      */
+    OBGC_PF_AUTO = 4        /* sinking velocities only: built from the parameters as the
+                               reference's setup does (constant POC speed, depth-dependent GOC) */
+};
+typedef struct obgc_pisces_field {
+    int32_t kind;
+    int32_t reserved0;
+    double value;
+    const void* data;            /* device pointer of the call's dtype                           */
+} obgc_pisces_field;
+
+/* Default parameters of PISCES(; grid) (PISCES.jl:288-340 and the component constructors). */
+int obgc_pisces_default_params(obgc_pisces_params* out);
+/* Every PISCES tendency of every interior cell in one pass: the discrete functors
+ * (bgc)(i, j, k, grid, Val(name), clock, fields, auxiliary_fields) of all 24 tracers
+ * (PISCES.jl:120-123 and the tracer files).  tracers: OBGC_PIS_NUM device fields (T and S
+ * included); aux: OBGC_PAUX_NUM inputs; G: OBGC_PIS_NUM_BGC output fields; t: model time (s). */
+int obgc_pisces_tendencies(const obgc_pisces_params* p, const obgc_grid* grid, int32_t dtype,
+                           const void* const* tracers, const obgc_pisces_field* aux, void* const* G,
+                           double t, void* stream);
+/* Host FP64 evaluation of one point: values [OBGC_PIS_NUM], aux [OBGC_PAUX_NUM] (sinking velocities
+ * already at the centre), z (m), t (s); G [OBGC_PIS_NUM_BGC]. */
+int obgc_pisces_eval_point(const obgc_pisces_params* p, const double* values, const double* aux,
+                           double z, double t, double* G);
+/* compute_mixed_layer_mean! (PISCES/mean_mixed_layer_properties.jl:10-46): the mean of a centre
+ * field above the mixed-layer depth, per column; out is an (Nx, Ny) field. */
+int obgc_mixed_layer_mean(const obgc_grid* grid, int32_t dtype, const void* field,
+                          const obgc_pisces_field* mixed_layer_depth, void* out, void* stream);
+/* compute_calcite_saturation! (PISCES/compute_calcite_saturation.jl:9-37): Ω of every cell with
+ * P = |z| g 1026 / 1e5 bar and silicate Si (NULL = 0); FP64 solve, output in dtype. */
+int obgc_pisces_calcite_saturation(const obgc_carbon_options* opt, const obgc_grid* grid, int32_t dtype,
+                                   const void* DIC, const void* Alk, const void* T, const void* S,
+                                   const void* Si, void* omega, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
  * Batched single-column runs.  Each column is the reference's one-dimensional setup
  * (examples/column.jl:41-66: RectilinearGrid(size = (1, 1, Nz)) + LOBSTER or NPZD +
  * ScalarDiffusivity(kappa(z)) with kappa(z) = 1e-2 (1 + tanh((z - MLD) / 10)) / 2 + 1e-4 at :34),

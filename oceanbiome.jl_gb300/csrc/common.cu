@@ -52,6 +52,12 @@ extern "C" int obgc_struct_layout(int32_t which, int64_t* out, int32_t cap) {
                 out[2] = offsetof(obgc_fields, u); out[3] = offsetof(obgc_fields, G); return 0;
         case 7: out[0] = sizeof(obgc_column_spec); out[1] = offsetof(obgc_column_spec, dz);
                 out[2] = offsetof(obgc_column_spec, pulse_step); out[3] = offsetof(obgc_column_spec, pulse_amount); return 0;
+        case 9: out[0] = sizeof(obgc_pisces_params); out[1] = offsetof(obgc_pisces_params, micro);
+                out[2] = offsetof(obgc_pisces_params, doc_aggregation); out[3] = offsetof(obgc_pisces_params, open_bottom); return 0;
+        case 10: out[0] = sizeof(obgc_pisces_phyto); out[1] = offsetof(obgc_pisces_phyto, exudated_fraction);
+                 out[2] = offsetof(obgc_pisces_phyto, base_growth_rate); out[3] = offsetof(obgc_pisces_phyto, silicate_half_saturation_parameter); return 0;
+        case 11: out[0] = sizeof(obgc_pisces_field); out[1] = offsetof(obgc_pisces_field, value);
+                 out[2] = offsetof(obgc_pisces_field, data); out[3] = 0; return 0;
         case 8: out[0] = sizeof(obgc_columns_desc); out[1] = offsetof(obgc_columns_desc, light);
                 out[2] = offsetof(obgc_columns_desc, arena_cells); out[3] = offsetof(obgc_columns_desc, invalid_fill_value); return 0;
     }

@@ -8,6 +8,7 @@ libobgc.so (CUDA, sm_103a); importing works without it, calling does not.
 """
 from . import _abi
 from .box import BoxModel
+from .pisces import PISCES
 from .columns import ColumnEngine
 from .service import ColumnService
 from .carbon import CarbonChemistry

@@ -191,6 +191,12 @@ class PiscesParams(C.Structure):
         int32 open_bottom, reserved0"""))
 
 
+class PiscesField(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("reserved0", C.c_int32), ("value", C.c_double), ("data", C.c_void_p)]
+
+
+PF_CONSTANT, PF_XY, PF_XYZ, PF_ZFACE, PF_AUTO = 0, 1, 2, 3, 4
+
 PISCES_TRACERS = ["P", "PChl", "PFe", "D", "DChl", "DFe", "DSi", "Z", "M", "DOC", "POC", "GOC", "SFe", "BFe", "PSi",
                   "CaCO₃", "NO₃", "NH₄", "PO₄", "Fe", "Si", "DIC", "Alk", "O₂", "T", "S"]
 PISCES_ASCII = ["P", "PChl", "PFe", "D", "DChl", "DFe", "DSi", "Z", "M", "DOC", "POC", "GOC", "SFe", "BFe", "PSi",
@@ -310,6 +316,11 @@ def load():
     _sig(lib, "obgc_columns_read", C.c_int, VP, I64, P(D))
     _sig(lib, "obgc_columns_remove", C.c_int, VP, I64)
     _sig(lib, "obgc_columns_autotune", C.c_int, VP, I32, P(I32), P(I32), VP)
+    _sig(lib, "obgc_pisces_default_params", C.c_int, P(PiscesParams))
+    _sig(lib, "obgc_pisces_eval_point", C.c_int, P(PiscesParams), P(D), P(D), D, D, P(D))
+    _sig(lib, "obgc_pisces_tendencies", C.c_int, P(PiscesParams), P(Grid), I32, P(VP), P(PiscesField), P(VP), D, VP)
+    _sig(lib, "obgc_mixed_layer_mean", C.c_int, P(Grid), I32, VP, P(PiscesField), VP, VP)
+    _sig(lib, "obgc_pisces_calcite_saturation", C.c_int, P(CarbonOptions), P(Grid), I32, VP, VP, VP, VP, VP, VP, VP)
     _sig(lib, "obgc_service_create", C.c_int, P(ServiceDesc), P(VP))
     _sig(lib, "obgc_service_destroy", C.c_int, VP)
     _sig(lib, "obgc_service_submit", C.c_int, VP, P(ColumnSpec), P(D), P(D), P(I64))
@@ -337,4 +348,6 @@ EXPORTED = [
     "obgc_columns_autotune", "obgc_npd_conserved_tracers", "obgc_scale_negatives", "obgc_zero_negatives",
     "obgc_service_create", "obgc_service_destroy", "obgc_service_submit", "obgc_service_wait", "obgc_service_drain",
     "obgc_service_get_stats", "obgc_service_reset_stats", "obgc_service_engine",
+    "obgc_pisces_default_params", "obgc_pisces_eval_point", "obgc_pisces_tendencies", "obgc_mixed_layer_mean",
+    "obgc_pisces_calcite_saturation",
 ]
