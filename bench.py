@@ -653,9 +653,147 @@ def run_carbon(args):
     return 0
 
 
+# ----------------------------------------------------------------------------- PISCES 3-D
+PIS_SHAPE = (128, 128, 48)
+PIS_EXTENT = (100_000.0, 100_000.0, 1000.0)
+PIS_DT = 1200.0
+PIS_SURFACE_PAR = 100.0
+PIS_WORKLOAD = ("PISCES 3-D, 128x128x48 (100 km x 100 km x 1000 m), 26 tracers, MultiBand PAR (3 bands, surface "
+                "100 W/m2), WENO5 + POC/GOC sinking + RK3, calcite saturation FP64, dt=1200 s")
+
+
+def pisces_cpu_baseline(threads=None, steps=None):
+    """The oracle's FP64 PISCES model (or_pisces_step3d) on a 64x64x48 sub-domain, all host threads."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import obgc
+    from obgc import _abi as A
+    from obgc.light import MultiBandPhotosyntheticallyActiveRadiation
+    threads = threads or (os.cpu_count() or 1)
+    shape = (64, 64, 48)
+    g = obgc.RectilinearGrid(shape, (PIS_EXTENT[0] * shape[0] / PIS_SHAPE[0], PIS_EXTENT[1] * shape[1] / PIS_SHAPE[1],
+                                     PIS_EXTENT[2]), ("Periodic", "Periodic", "Bounded"))
+    bgc = obgc.PISCES(g)
+    light = MultiBandPhotosyntheticallyActiveRadiation(grid=g, surface_PAR=PIS_SURFACE_PAR)
+    m = O.pisces3d(bgc.params, g.c_grid(), light, -50.0, surface_kind=A.SURFACE_CONSTANT, surface_value=PIS_SURFACE_PAR)
+    init = obgc.pisces_initial_conditions(g, seed=5)
+    st = np.ascontiguousarray(np.stack([init[n] for n in A.PISCES_ASCII]).reshape(26, -1))
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=0, device="cpu")
+    u = u.numpy().ravel().copy()
+    v = v.numpy().ravel().copy()
+    O.pisces_step3d(m, st, u=u, v=v, t=0.0, dt=PIS_DT, nsteps=1, threads=threads)   # warm
+    if steps is None:
+        t0 = time.perf_counter()
+        O.pisces_step3d(m, st, u=u, v=v, t=PIS_DT, dt=PIS_DT, nsteps=1, threads=threads)
+        one = time.perf_counter() - t0
+        steps = max(1, min(30, int(15.0 / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    O.pisces_step3d(m, st, u=u, v=v, t=2 * PIS_DT, dt=PIS_DT, nsteps=steps, threads=threads)
+    el = time.perf_counter() - t0
+    return {"value": 26 * g.N * steps / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{steps} RK3 steps of a 64x64x48 PISCES sub-domain (26 tracers), FP64, {el:.1f} s"}, el / steps
+
+
+def run_pisces(args):
+    """26-tracer PISCES 3-D model: update_biogeochemical_state! (MultiBand light, euphotic depth,
+    mixed-layer PAR, calcite saturation) + the PISCES functor + the fused WENO5/sinking/RK3 substep,
+    three stages per step, state resident in HBM."""
+    import numpy as np
+    import torch
+    import obgc
+    from obgc import _abi as A
+    torch.cuda.set_device(0)
+    lib = A.load()
+    prec = args.precision if args.precision != "f64" else "mixed"
+    shape = tuple(args.shape) if args.shape else PIS_SHAPE
+    g = obgc.RectilinearGrid(shape, (PIS_EXTENT[0] * shape[0] / PIS_SHAPE[0], PIS_EXTENT[1] * shape[1] / PIS_SHAPE[1],
+                                     PIS_EXTENT[2]), ("Periodic", "Periodic", "Bounded"),
+                             dtype="f32" if prec == "f32" else "f64")
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=7)
+    model = obgc.PiscesModel(g, biogeochemistry=obgc.PISCES(g), velocities=(u, v), precision=prec,
+                             mixed_layer_depth=-50.0, surface_PAR=PIS_SURFACE_PAR)
+    model.set_(**obgc.pisces_initial_conditions(g, seed=5))
+    for _ in range(max(args.warmup, 3)):
+        model.time_step(PIS_DT)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    model.set_profiling(True)
+    l0 = lib.obgc_kernel_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clocks:
+        e0.record(stream)
+        model.time_step(PIS_DT, nsteps=args.steps, stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = lib.obgc_kernel_launch_count() - l0
+    phases = model.last_timing()
+    model.set_profiling(False)
+    value = 26 * g.N * args.steps / (ms / 1e3)
+    finite = all(bool(torch.isfinite(model.tracers[n]).all()) for n in A.PISCES_TRACERS)
+
+    # e2e: pinned host state in, one step, state out, through the public model call
+    host = {n: torch.empty(g.shape, dtype=model.dtype, pin_memory=True) for n in A.PISCES_TRACERS}
+    for n in A.PISCES_TRACERS:
+        host[n].copy_(model.tracers[n])
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 10))
+    h2d = sum(h.numel() * h.element_size() for h in host.values())
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        for n in A.PISCES_TRACERS:
+            model.tracers[n].copy_(host[n], non_blocking=True)
+        model.time_step(PIS_DT, stream=stream.cuda_stream)
+        for n in A.PISCES_TRACERS:
+            host[n].copy_(model.tracers[n], non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+
+    # roofline of the dominant phase (algorithmic bytes per cell of one stage, state precision s,
+    # tendency precision 4): functor reads 26 tracers + PAR x4 + Omega and writes 24 tendencies;
+    # substep reads 26 tracers + 24 functor tendencies + 26 previous tendencies + u, v and writes
+    # 26 tracers + 26 tendencies; calcite reads DIC Alk T S Si + H (f64) and writes Omega + H
+    s = 4 if prec == "f32" else 8
+    per_cell = {"functor": 31 * s + 24 * 4, "substep": 54 * s + 76 * 4, "calcite": 6 * s + 16,
+                "light": 0}
+    stages = max(phases["stages"], 1)
+    dom = max(("functor", "substep", "calcite", "light"), key=lambda k: phases[k])
+    avg_ms = phases[dom] / stages
+    peak, peak_kind = peaks()
+    achieved = per_cell[dom] * g.N / (avg_ms / 1e3) / 1e9 if per_cell[dom] else 0.0
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu, _ = pisces_cpu_baseline()
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if prec == "f32" else "f64-state/f32-compute",
+        "data": "synthetic (seeded PISCES depth profiles with 5% correlated lognormal noise, random-streamfunction velocity)",
+        "config": {"workload": PIS_WORKLOAD if shape == PIS_SHAPE else PIS_WORKLOAD.replace("128x128x48", "x".join(map(str, shape))),
+                   "grid": list(shape), "tracers": 26, "dt_s": PIS_DT, "precision": prec,
+                   "l2": "state (%.0f MB) larger than L2 (129 MB)" % (26 * g.N * s / 1e6), "finite": finite,
+                   "phase_ms_per_step": {k: phases[k] / args.steps for k in ("light", "calcite", "functor", "substep")}},
+        "e2e": {"value": 26 * g.N / (e2e_ms / 1e3), "unit": METRIC, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": h2d, "ms_per_step": e2e_ms},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_kind, "kernel": {"functor": "pisces_kernel",
+                     "substep": "substep_kernel<V_EXTERNAL,26>", "calcite": "pisces_omega_kernel",
+                     "light": "multiband light"}[dom], "algorithmic_bytes_per_launch": per_cell[dom] * g.N,
+                     "avg_launch_ms": avg_ms},
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="lobster3d", choices=["lobster3d", "columns", "service", "carbon", "accuracy"])
+    ap.add_argument("--workload", default="lobster3d", choices=["lobster3d", "columns", "service", "carbon", "accuracy",
+                                                                    "pisces"])
     ap.add_argument("--rates", type=float, nargs="*", default=None, help="service: Poisson arrival rates (1/s)")
     ap.add_argument("--arrival-seconds", type=float, default=2.0, help="service: seconds of arrivals per rate")
     ap.add_argument("--chunk", type=int, default=32, help="service: steps per launch")
@@ -676,6 +814,8 @@ def main():
         return run_columns(args)
     if args.workload == "carbon":
         return run_carbon(args)
+    if args.workload == "pisces":
+        return run_pisces(args)
     if args.workload == "accuracy":
         return run_accuracy(args)
     if args.workload == "service":

@@ -565,12 +565,15 @@ int obgc_box_run(const obgc_npd_params* p, const obgc_npd_params* params_per_mod
 /* Layout of an auxiliary input (PISCES's auxiliary fields are 2-D, 3-D or constant). */
 enum obgc_pisces_field_kind {
     OBGC_PF_CONSTANT = 0,   /* `value` everywhere                                               */
-    OBGC_PF_XY = 1,         /* (Nx, Ny) field, element i + j*stride_j                           */
+    OBGC_PF_XY = 1,         /* (Nx, Ny) field, dense: element i + j*Nx                          */
     OBGC_PF_XYZ = 2,        /* centre field with the grid's strides                              */
     OBGC_PF_ZFACE = 3,      /* z-face field with the grid's strides, Nz+1 levels; the cell uses the
                                mean of its two faces (the ℑz interpolation of the reference)      */
-    OBGC_PF_AUTO = 4        /* sinking velocities only: built from the parameters as the
-                               reference's setup does (constant POC speed, depth-dependent GOC) */
+    OBGC_PF_AUTO = 4,       /* sinking velocities only: built from the parameters as the
+                               reference's setup does (constant POC speed, depth-dependent GOC
+                               from the zmxl and zeu inputs)                                     */
+    OBGC_PF_ZPROFILE = 5    /* Nz+1 face values shared by every column; the cell uses the mean of
+                               its two faces                                                     */
 };
 typedef struct obgc_pisces_field {
     int32_t kind;
@@ -601,6 +604,52 @@ int obgc_mixed_layer_mean(const obgc_grid* grid, int32_t dtype, const void* fiel
 int obgc_pisces_calcite_saturation(const obgc_carbon_options* opt, const obgc_grid* grid, int32_t dtype,
                                    const void* DIC, const void* Alk, const void* T, const void* S,
                                    const void* Si, void* omega, void* stream);
+
+/* A 3-D PISCES model stepped on the device: every RK3 stage runs update_biogeochemical_state!
+ * (PISCES/update_state.jl:1-17 after the MultiBand light of src/Light/multi_band.jl:147-185: PAR
+ * bands from PChl + DChl, euphotic depth, mixed-layer PAR, calcite saturation), then all 24
+ * tendencies, then one fused kernel for WENO5 advection of the 26 tracers, the sinking of POC, SFe
+ * (POC speed) and GOC, BFe, PSi, CaCO3 (GOC speed) and the RK3 update. */
+typedef struct obgc_pisces_model obgc_pisces_model;
+typedef struct obgc_pisces_model_desc {
+    obgc_pisces_params pisces;
+    obgc_grid grid;
+    int32_t precision;           /* OBGC_PREC_F32 or OBGC_PREC_MIXED                          */
+    int32_t advection;           /* enum obgc_advection                                        */
+    int32_t nbands;              /* MultiBand bands: 3 (PISCES reads PAR₁, PAR₂, PAR₃)           */
+    int32_t negatives;           /* OBGC_NEGATIVES_NONE or _SCALE (conserved_tracers(::PISCES)) */
+    double kw[4], e[4], chi[4], division[4];   /* band means (obgc_multiband_coefficients)     */
+    obgc_surface surface;        /* OBGC_SURFACE_PAR_DEFAULT or _CONSTANT                      */
+    double mixed_layer_depth;    /* prescribed, uniform (m, negative)                          */
+    double mean_kappa;           /* mean mixed-layer diffusivity (the reference sets 1 when the
+                                    model has no closure, PISCES.jl:360-362)                   */
+    double invalid_fill_value;
+    obgc_carbon_options carbon;
+} obgc_pisces_model_desc;
+
+enum obgc_pisces_model_field {
+    OBGC_PMF_PAR = 0, OBGC_PMF_PAR1, OBGC_PMF_PAR2, OBGC_PMF_PAR3,   /* centre fields              */
+    OBGC_PMF_ZEU = 4, OBGC_PMF_MLPAR = 5,                            /* (Nx, Ny), dense            */
+    OBGC_PMF_OMEGA = 6                                               /* centre field               */
+};
+
+int obgc_pisces_model_create(const obgc_pisces_model_desc* desc, obgc_pisces_model** out);
+int obgc_pisces_model_destroy(obgc_pisces_model* m);
+/* tracers: OBGC_PIS_NUM device fields with the grid's strides (state precision: FP32 for
+ * OBGC_PREC_F32, FP64 for OBGC_PREC_MIXED); u, v as for obgc_bind_fields, or NULL. */
+int obgc_pisces_model_bind(obgc_pisces_model* m, void* const* tracers, const void* u, const void* v);
+int obgc_pisces_model_update_state(obgc_pisces_model* m, double t, void* stream);
+int obgc_pisces_model_step(obgc_pisces_model* m, double t, double dt, int32_t nsteps, void* stream);
+/* Device pointer of an auxiliary field the model keeps (state precision). */
+int obgc_pisces_model_field(obgc_pisces_model* m, int32_t which, void** ptr);
+/* Host FP64 copy of an auxiliary field: (Nx, Ny) dense, or [Nz][Ny][Nx] dense for centre fields. */
+int obgc_pisces_model_read_field(obgc_pisces_model* m, int32_t which, double* out);
+/* CUDA events around each stage's phases of the next obgc_pisces_model_step calls (on: nonzero). */
+int obgc_pisces_model_set_profiling(obgc_pisces_model* m, int32_t on);
+/* Device milliseconds of the last profiled step call, summed over its stages: ms[0] negatives +
+ * light + euphotic depth + mixed-layer PAR, ms[1] calcite saturation, ms[2] the PISCES functor,
+ * ms[3] the fused advection/RK3 substep.  *stages = RK3 stages timed. */
+int obgc_pisces_model_last_timing(obgc_pisces_model* m, double* ms, int32_t* stages);
 
 /* ---------------------------------------------------------------------------------------------
  * Batched single-column runs.  Each column is the reference's one-dimensional setup

@@ -11,9 +11,9 @@
 
 namespace obgc {
 
-constexpr int NEG_MAX_GROUPS = 2;
-constexpr int NEG_MAX_MEMBERS = 8;
-constexpr int NEG_MAX_FIELDS = 16;
+constexpr int NEG_MAX_GROUPS = 5;
+constexpr int NEG_MAX_MEMBERS = 10;
+constexpr int NEG_MAX_FIELDS = 32;
 
 struct NegativesSpec {
     int mode;                                    // OBGC_NEGATIVES_*

@@ -60,7 +60,9 @@ struct NPDVals {
 };
 
 // Compile-time variants of the fused kernels: {nutrients, detritus, carbonate, oxygen, q10}.
-enum Variant { V_RUNTIME = -1, V_LOBSTER = 0, V_LOBSTER_C = 1, V_LOBSTER_CO = 2, V_NPZD = 3, V_LOBSTER_O = 4 };
+// V_EXTERNAL: the fused substep takes its BGC tendencies from arrays computed by another kernel
+// (PISCES), keeping the advection, sinking and RK3 update.
+enum Variant { V_RUNTIME = -1, V_LOBSTER = 0, V_LOBSTER_C = 1, V_LOBSTER_CO = 2, V_NPZD = 3, V_LOBSTER_O = 4, V_EXTERNAL = 5 };
 __host__ __device__ constexpr int vnut(int V) { return V == V_NPZD ? OBGC_NUT_NUTRIENT : OBGC_NUT_NITRATE_AMMONIA; }
 __host__ __device__ constexpr int vdet(int V) { return V == V_NPZD ? OBGC_DET_SINGLE : OBGC_DET_TWO_PARTICLE; }
 __host__ __device__ constexpr int vcarb(int V) { return (V == V_LOBSTER_C || V == V_LOBSTER_CO) ? 1 : 0; }

@@ -36,23 +36,29 @@ struct AuxField {
     const void* data;
 };
 
-template <typename T>
+// Tracers and auxiliary fields in the state precision TS, tendencies in the compute precision TC.
+template <typename TS, typename TC>
 struct PiscesFields {
-    const T* tr[OBGC_PIS_NUM];
-    T* G[OBGC_PIS_NUM_BGC];
+    const TS* tr[OBGC_PIS_NUM];
+    TC* G[OBGC_PIS_NUM_BGC];
     AuxField aux[OBGC_PAUX_NUM];
 };
 
-template <typename T>
-__device__ __forceinline__ T aux_at(const AuxField& f, int64_t oxy, int64_t o, int64_t sk) {
+// xy: dense (Nx, Ny) index i + j Nx; o: the cell with the grid's strides; k: level.
+template <typename TS, typename TC>
+__device__ __forceinline__ TC aux_at(const AuxField& f, int64_t xy, int64_t o, int64_t sk, int k) {
     switch (f.kind) {
-        case OBGC_PF_XY: return static_cast<const T*>(f.data)[oxy];
-        case OBGC_PF_XYZ: return static_cast<const T*>(f.data)[o];
+        case OBGC_PF_XY: return TC(static_cast<const TS*>(f.data)[xy]);
+        case OBGC_PF_XYZ: return TC(static_cast<const TS*>(f.data)[o]);
         case OBGC_PF_ZFACE: {
-            const T* w = static_cast<const T*>(f.data);
-            return T(0.5) * (w[o] + w[o + sk]);
+            const TS* w = static_cast<const TS*>(f.data);
+            return TC(TS(0.5) * (w[o] + w[o + sk]));
         }
-        default: return T(f.value);
+        case OBGC_PF_ZPROFILE: {
+            const TS* w = static_cast<const TS*>(f.data);
+            return TC(TS(0.5) * (w[k] + w[k + 1]));
+        }
+        default: return TC(f.value);
     }
 }
 
@@ -71,21 +77,21 @@ __device__ __forceinline__ T goc_face(const PiscesT<T>& p, int f, int Nz, T dz, 
     return -p.w_goc_min + (p.w_goc_max - p.w_goc_min) * jmin(T(0), zc - jmin(zmxl, zeu)) / T(5000);
 }
 
-template <typename T>
+template <typename TS, typename T>
 __global__ void __launch_bounds__(128) pisces_kernel(const __grid_constant__ PiscesT<T> p,
-                                                    const __grid_constant__ PiscesFields<T> F, int Nx, int Ny, int Nz,
+                                                    const __grid_constant__ PiscesFields<TS, T> F, int Nx, int Ny, int Nz,
                                                     int64_t sj, int64_t sk, T dz, T Lz, const PiscesClock<T> clk) {
     const int64_t N = (int64_t)Nx * Ny * Nz;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(c % Nx);
         const int64_t r = c / Nx;
         const int j = (int)(r % Ny), k = (int)(r / Ny);
-        const int64_t oxy = i + j * sj, o = oxy + k * sk;
+        const int64_t xy = i + (int64_t)j * Nx, o = i + j * sj + k * sk;
         T v[OBGC_PIS_NUM], a[OBGC_PAUX_NUM], G[OBGC_PIS_NUM_BGC];
 #pragma unroll
-        for (int q = 0; q < OBGC_PIS_NUM; q++) v[q] = F.tr[q][o];
+        for (int q = 0; q < OBGC_PIS_NUM; q++) v[q] = T(F.tr[q][o]);
 #pragma unroll
-        for (int q = 0; q < OBGC_PAUX_NUM; q++) a[q] = aux_at<T>(F.aux[q], oxy, o, sk);
+        for (int q = 0; q < OBGC_PAUX_NUM; q++) a[q] = aux_at<TS, T>(F.aux[q], xy, o, sk, k);
         if (F.aux[OBGC_PAUX_WPOC].kind == OBGC_PF_AUTO)
             a[OBGC_PAUX_WPOC] = T(0.5) * (poc_face(p, k, Nz) + poc_face(p, k + 1, Nz));
         if (F.aux[OBGC_PAUX_WGOC].kind == OBGC_PF_AUTO)
@@ -105,8 +111,8 @@ __global__ void mixed_layer_mean_kernel(const T* __restrict__ C, AuxField zmxl, 
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= (int64_t)Nx * Ny) return;
     const int i = (int)(c % Nx), j = (int)(c / Nx);
-    const int64_t oxy = i + j * sj;
-    const T zm = zmxl.kind == OBGC_PF_XY ? static_cast<const T*>(zmxl.data)[oxy] : T(zmxl.value);
+    const int64_t oxy = i + j * sj;   // the column in the centre field
+    const T zm = zmxl.kind == OBGC_PF_XY ? static_cast<const T*>(zmxl.data)[c] : T(zmxl.value);
     T sum = T(0), depth = T(0);
     for (int k = Nz - 1; k >= 0; k--) {
         const T zk = -Lz + T(k) * dz, zk1 = -Lz + T(k + 1) * dz;
@@ -116,14 +122,14 @@ __global__ void mixed_layer_mean_kernel(const T* __restrict__ C, AuxField zmxl, 
         sum += C[oxy + k * sk] * d;
         depth += d;
     }
-    out[oxy] = sum / depth;
+    out[c] = sum / depth;   // (Nx, Ny) output, dense
 }
 
 // _compute_calcite_saturation! (compute_calcite_saturation.jl:23-36): P from the depth of the cell.
 template <typename T>
 __global__ void __launch_bounds__(128) pisces_omega_kernel(obgc_carbon_options o, const T* DIC, const T* Alk, const T* Tc,
                                                           const T* S, const T* Si, T* out, int Nx, int Ny, int Nz, int64_t sj,
-                                                          int64_t sk, double dz, double Lz, int* failures) {
+                                                          int64_t sk, double dz, double Lz, double* H_inout, int* failures) {
     const int64_t N = (int64_t)Nx * Ny * Nz;
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= N) return;
@@ -136,9 +142,10 @@ __global__ void __launch_bounds__(128) pisces_omega_kernel(obgc_carbon_options o
     double H;
     int it;
     bool ok;
-    const double H0 = exp(-2.302585092994046 * o.initial_pH_guess);
+    const double H0 = (H_inout && H_inout[c] > 0) ? H_inout[c] : exp(-2.302585092994046 * o.initial_pH_guess);
     out[off] = T(carbon_cell(o, (double)DIC[off], (double)Alk[off], (double)Tc[off], (double)S[off], Si ? (double)Si[off] : 0.0,
                              0.0, P, 0.0, H0, &H, &it, &ok));
+    if (H_inout) H_inout[c] = H;
     if (!ok) atomicAdd(failures, 1);
 }
 
@@ -259,14 +266,18 @@ namespace {
 bool valid_field(const obgc_pisces_field& f, int q) {
     if (f.kind == OBGC_PF_AUTO) return q == OBGC_PAUX_WPOC || q == OBGC_PAUX_WGOC;
     if (f.kind == OBGC_PF_CONSTANT) return true;
-    return f.kind >= OBGC_PF_XY && f.kind <= OBGC_PF_ZFACE && f.data != nullptr;
+    return f.kind >= OBGC_PF_XY && f.kind <= OBGC_PF_ZPROFILE && f.kind != OBGC_PF_AUTO && f.data != nullptr;
 }
 
-template <typename T>
+}  // namespace
+
+namespace obgc {
+
+template <typename TS, typename T>
 int launch_pisces(const obgc_pisces_params* p, const obgc_grid* g, const void* const* tracers, const obgc_pisces_field* aux,
                   void* const* G, double t, cudaStream_t st) {
-    PiscesFields<T> F;
-    for (int q = 0; q < OBGC_PIS_NUM; q++) F.tr[q] = static_cast<const T*>(tracers[q]);
+    PiscesFields<TS, T> F;
+    for (int q = 0; q < OBGC_PIS_NUM; q++) F.tr[q] = static_cast<const TS*>(tracers[q]);
     for (int q = 0; q < OBGC_PIS_NUM_BGC; q++) F.G[q] = static_cast<T*>(G[q]);
     for (int q = 0; q < OBGC_PAUX_NUM; q++) F.aux[q] = {aux[q].kind, aux[q].value, aux[q].data};
     const PiscesClock<double> c64 = pisces_clock(*p, t);
@@ -277,13 +288,40 @@ int launch_pisces(const obgc_pisces_params* p, const obgc_grid* g, const void* c
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t want = (N + 127) / 128;
     const unsigned blocks = (unsigned)(want < (int64_t)sms * 16 ? want : (int64_t)sms * 16);
-    pisces_kernel<T><<<blocks, 128, 0, st>>>(make_pisces<T>(*p), F, g->Nx, g->Ny, g->Nz, g->stride_j, g->stride_k,
-                                             T(g->Lz / g->Nz), T(g->Lz), clk);
+    pisces_kernel<TS, T><<<blocks, 128, 0, st>>>(make_pisces<T>(*p), F, g->Nx, g->Ny, g->Nz, g->stride_j, g->stride_k,
+                                                 T(g->Lz / g->Nz), T(g->Lz), clk);
     OBGC_LAUNCHED("pisces_kernel");
     return OBGC_OK;
 }
+template int launch_pisces<float, float>(const obgc_pisces_params*, const obgc_grid*, const void* const*,
+                                         const obgc_pisces_field*, void* const*, double, cudaStream_t);
+template int launch_pisces<double, float>(const obgc_pisces_params*, const obgc_grid*, const void* const*,
+                                          const obgc_pisces_field*, void* const*, double, cudaStream_t);
+template int launch_pisces<double, double>(const obgc_pisces_params*, const obgc_grid*, const void* const*,
+                                           const obgc_pisces_field*, void* const*, double, cudaStream_t);
 
-}  // namespace
+// Calcite saturation of every cell with the depth pressure, FP64 solve warm-started from H_inout.
+template <typename T>
+int launch_pisces_omega(const obgc_carbon_options* opt, const obgc_grid* grid, const void* DIC, const void* Alk,
+                        const void* Tc, const void* S, const void* Si, void* Omega, double* H_inout, int* fails,
+                        cudaStream_t st) {
+    obgc_carbon_options o = *opt;
+    o.output = OBGC_OUT_OMEGA_CALCITE;
+    o.ph_given = 0;
+    o.has_pressure = 1;
+    const int64_t N = (int64_t)grid->Nx * grid->Ny * grid->Nz;
+    pisces_omega_kernel<T><<<(unsigned)((N + 127) / 128), 128, 0, st>>>(
+        o, (const T*)DIC, (const T*)Alk, (const T*)Tc, (const T*)S, (const T*)Si, (T*)Omega, grid->Nx, grid->Ny, grid->Nz,
+        grid->stride_j, grid->stride_k, grid->Lz / grid->Nz, grid->Lz, H_inout, fails);
+    OBGC_LAUNCHED("pisces_omega_kernel");
+    return OBGC_OK;
+}
+template int launch_pisces_omega<float>(const obgc_carbon_options*, const obgc_grid*, const void*, const void*, const void*,
+                                        const void*, const void*, void*, double*, int*, cudaStream_t);
+template int launch_pisces_omega<double>(const obgc_carbon_options*, const obgc_grid*, const void*, const void*, const void*,
+                                         const void*, const void*, void*, double*, int*, cudaStream_t);
+
+}  // namespace obgc
 
 extern "C" int obgc_pisces_tendencies(const obgc_pisces_params* p, const obgc_grid* grid, int32_t dtype,
                                       const void* const* tracers, const obgc_pisces_field* aux, void* const* G, double t,
@@ -297,8 +335,8 @@ extern "C" int obgc_pisces_tendencies(const obgc_pisces_params* p, const obgc_gr
     for (int q = 0; q < OBGC_PAUX_NUM; q++)
         if (!valid_field(aux[q], q)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_pisces_tendencies: bad auxiliary field");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    return dtype == OBGC_F32 ? launch_pisces<float>(p, grid, tracers, aux, G, t, st)
-                             : launch_pisces<double>(p, grid, tracers, aux, G, t, st);
+    return dtype == OBGC_F32 ? launch_pisces<float, float>(p, grid, tracers, aux, G, t, st)
+                             : launch_pisces<double, double>(p, grid, tracers, aux, G, t, st);
 }
 
 extern "C" int obgc_mixed_layer_mean(const obgc_grid* grid, int32_t dtype, const void* field, const obgc_pisces_field* zmxl,
@@ -340,12 +378,12 @@ extern "C" int obgc_pisces_calcite_saturation(const obgc_carbon_options* opt, co
     if (dtype == OBGC_F32)
         pisces_omega_kernel<float><<<blocks, 128, 0, st>>>(o, (const float*)DIC, (const float*)Alk, (const float*)T, (const float*)S,
                                                            (const float*)Si, (float*)Omega, grid->Nx, grid->Ny, grid->Nz,
-                                                           grid->stride_j, grid->stride_k, grid->Lz / grid->Nz, grid->Lz, fails);
+                                                           grid->stride_j, grid->stride_k, grid->Lz / grid->Nz, grid->Lz, nullptr, fails);
     else
         pisces_omega_kernel<double><<<blocks, 128, 0, st>>>(o, (const double*)DIC, (const double*)Alk, (const double*)T,
                                                             (const double*)S, (const double*)Si, (double*)Omega, grid->Nx,
                                                             grid->Ny, grid->Nz, grid->stride_j, grid->stride_k,
-                                                            grid->Lz / grid->Nz, grid->Lz, fails);
+                                                            grid->Lz / grid->Nz, grid->Lz, nullptr, fails);
     OBGC_LAUNCHED("pisces_omega_kernel");
     int h = 0;
     OBGC_CUDA(cudaMemcpyAsync(&h, fails, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -24,12 +24,13 @@ namespace obgc {
 
 constexpr int STEP_BX = 32;
 constexpr int STEP_BY = 8;
-constexpr int MAX_NT = 12;
+constexpr int MAX_NT = 26;
 
 // Tracer slot order of the fused variants: the reference's required_biogeochemical_tracers order,
 // then T and S when they are carried without a BGC tendency.
 __host__ __device__ constexpr int n_bgc(int V) {
-    return V == V_NPZD ? 5 : (V == V_LOBSTER ? 7 : (V == V_LOBSTER_C ? 9 : (V == V_LOBSTER_CO ? 10 : 8)));
+    return V == V_EXTERNAL ? 24
+         : V == V_NPZD ? 5 : (V == V_LOBSTER ? 7 : (V == V_LOBSTER_C ? 9 : (V == V_LOBSTER_CO ? 10 : 8)));
 }
 __host__ __device__ constexpr int slot_name(int V, int s) {
     // NPZD: N P Z T D ; LOBSTER: NO3 NH4 P Z sPOM bPOM DOM [DIC Alk] [O2]
@@ -55,6 +56,7 @@ struct SubstepArgs {
     const TS* in[MAX_NT];
     TS* out[MAX_NT];
     TC* G[MAX_NT];
+    const TC* ext[MAX_NT];    // V_EXTERNAL: the BGC tendency of slot t (t < n_bgc)
     const TS* u;
     const TS* v;
     const TS* w;
@@ -188,7 +190,7 @@ __device__ __forceinline__ TC vertical_flux(const SubstepArgs<TS, TC>& a, const 
 }
 
 template <int V, int NT, typename TS, typename TC>
-__global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 3 : 1)
+__global__ void __launch_bounds__(STEP_BX * STEP_BY, (sizeof(TC) == 4 && NT <= 12) ? 3 : 1)
     substep_kernel(const __grid_constant__ SubstepArgs<TS, TC> a) {
     constexpr int NB = n_bgc(V);
     constexpr int SP = slot_of_P(V);
@@ -208,15 +210,18 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 3 : 1)
     // Sinking tracers advance their vertical stencil in a register window (one new load per
     // level); two window slots per variant (LOBSTER: sPOM, bPOM; NPZD: P, D).  Any other
     // vertically advected tracer, and every tracer when a model w is given, takes the generic path.
-    constexpr int WA = V == V_NPZD ? 1 : 4, WB = V == V_NPZD ? 4 : 5;
+    // PISCES (V_EXTERNAL): POC and GOC, the other four sinking tracers take the generic path.
+    constexpr int WA = V == V_NPZD ? 1 : V == V_EXTERNAL ? 10 : 4, WB = V == V_NPZD ? 4 : V == V_EXTERNAL ? 11 : 5;
     const bool winA = a.w == nullptr && ((a.drift_mask >> WA) & 1u);
     const bool winB = a.w == nullptr && ((a.drift_mask >> WB) & 1u);
     const uint32_t gen_mask = a.w != nullptr ? 0xffffffffu : (a.drift_mask & ~((1u << WA) | (1u << WB)));
     const bool any_generic = (gen_mask & ((1u << NT) - 1u)) != 0u;
 
-    TC PAR0;
-    if (a.surf_kind == OBGC_SURFACE_PAR_DEFAULT) PAR0 = TC(default_surface_par(*a.d_time + a.c_stage * a.dt_d));
-    else PAR0 = a.surf_value;
+    TC PAR0 = TC(0);
+    if constexpr (V != V_EXTERNAL) {
+        if (a.surf_kind == OBGC_SURFACE_PAR_DEFAULT) PAR0 = TC(default_surface_par(*a.d_time + a.c_stage * a.dt_d));
+        else PAR0 = a.surf_value;
+    }
 
     for (int item = blockIdx.x; item < a.n_items; item += gridDim.x) {
         const int seg = item % a.nseg;                       // top segment first
@@ -229,7 +234,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 3 : 1)
         const bool active = i < a.Nx && j < a.Ny;
         const int ic = min(i, a.Nx - 1), jc = min(j, a.Ny - 1);
         const int64_t col = ic + (int64_t)jc * a.sj;
-        const TC P0 = a.surf_kind == OBGC_SURFACE_PAR_FIELD ? TC(a.surf_field[ic + (int64_t)jc * a.Nx]) : PAR0;
+        const TC P0 = (V != V_EXTERNAL && a.surf_kind == OBGC_SURFACE_PAR_FIELD) ? TC(a.surf_field[ic + (int64_t)jc * a.Nx])
+                                                                                 : PAR0;
 
         // horizontal offsets of the tile elements this thread stages (the same for every level
         // and tracer of the work item)
@@ -244,12 +250,14 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 3 : 1)
 
         // chlorophyll integral of the cells above the segment
         TC Sr = TC(0), Sb = TC(0);
+        if constexpr (V != V_EXTERNAL) {
 #pragma unroll 1
-        for (int k = a.Nz - 1; k > k_top; --k) {
-            TC fr, fb;
-            twoband_terms(a.light, ld<TS, TC>(a.in[SP], col + (int64_t)k * a.sk), fr, fb);
-            Sr += fr;
-            Sb += fb;
+            for (int k = a.Nz - 1; k > k_top; --k) {
+                TC fr, fb;
+                twoband_terms(a.light, ld<TS, TC>(a.in[SP], col + (int64_t)k * a.sk), fr, fb);
+                Sr += fr;
+                Sb += fb;
+            }
         }
 
         // vertical flux through the face above the segment (k_top + 1), carried per thread in smem
@@ -390,21 +398,24 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 3 : 1)
                 if (winB) wB[0] = ld<TS, TC>(a.in[WB], nk);
             }
 
-            // PAR at this cell (2band.jl:26-31)
-            TC fr, fb;
-            twoband_terms(a.light, c[SP], fr, fb);
-            const TC z = -a.Lz + (TC(k) + TC(0.5)) * a.dz;
-            const TC PAR = twoband_par(a.light, P0, z, a.dz, Sr, Sb, fr, fb);
-            Sr += fr;
-            Sb += fb;
+            TC g[V == V_EXTERNAL ? 1 : OBGC_NUM_NAMED];
+            if constexpr (V != V_EXTERNAL) {
+                // PAR at this cell (2band.jl:26-31)
+                TC fr, fb;
+                twoband_terms(a.light, c[SP], fr, fb);
+                const TC z = -a.Lz + (TC(k) + TC(0.5)) * a.dz;
+                const TC PAR = twoband_par(a.light, P0, z, a.dz, Sr, Sb, fr, fb);
+                Sr += fr;
+                Sb += fb;
 
-            // named values for the BGC functors
-            TC vals[OBGC_NUM_NAMED], g[OBGC_NUM_NAMED];
+                // named values for the BGC functors
+                TC vals[OBGC_NUM_NAMED];
 #pragma unroll
-            for (int n = 0; n < OBGC_NUM_NAMED; n++) { vals[n] = TC(0); g[n] = TC(0); }
+                for (int n = 0; n < OBGC_NUM_NAMED; n++) { vals[n] = TC(0); g[n] = TC(0); }
 #pragma unroll
-            for (int s = 0; s < NB; s++) vals[slot_name(V, s)] = c[s];
-            npd_tendencies<V, TC>(a.bgc, vals, PAR, g);
+                for (int s = 0; s < NB; s++) vals[slot_name(V, s)] = c[s];
+                npd_tendencies<V, TC>(a.bgc, vals, PAR, g);
+            }
 
 #pragma unroll
             for (int t = 0; t < NT; t++) {
@@ -414,7 +425,13 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) == 4 ? 3 : 1)
                 if (any_generic) adv += vdv[t * NTH + tid];
                 if (t == WA) adv += vdA;
                 if (t == WB) adv += vdB;
-                const TC Gt = (t < NB ? g[slot_name(V, t)] : TC(0)) - adv;
+                TC Gb = TC(0);
+                if constexpr (V == V_EXTERNAL) {
+                    if (t < NB) Gb = a.ext[t][idx];
+                } else {
+                    if (t < NB) Gb = g[slot_name(V, t)];
+                }
+                const TC Gt = Gb - adv;
                 if (active) {
                     TC Un;
                     if (a.first_stage) {

@@ -8,7 +8,7 @@ libobgc.so (CUDA, sm_103a); importing works without it, calling does not.
 """
 from . import _abi
 from .box import BoxModel
-from .pisces import PISCES
+from .pisces import PISCES, PiscesModel
 from .columns import ColumnEngine
 from .service import ColumnService
 from .carbon import CarbonChemistry
@@ -23,6 +23,7 @@ from .models import (LOBSTER, NPZD, CarbonateSystem, Detritus, NitrateAmmonia, N
                      biogeochemical_drift_velocity, conserved_tracers, eval_point, preset,
                      required_biogeochemical_auxiliary_fields, required_biogeochemical_tracers)
 from .synthetic import (lobster_column_request, lobster_initial_conditions, mixed_layer_diffusivity,
+                        pisces_initial_conditions,
                         npzd_column_ensemble, npzd_front_initial_conditions, random_streamfunction_velocity)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

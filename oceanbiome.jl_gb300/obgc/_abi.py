@@ -195,7 +195,15 @@ class PiscesField(C.Structure):
     _fields_ = [("kind", C.c_int32), ("reserved0", C.c_int32), ("value", C.c_double), ("data", C.c_void_p)]
 
 
-PF_CONSTANT, PF_XY, PF_XYZ, PF_ZFACE, PF_AUTO = 0, 1, 2, 3, 4
+PF_CONSTANT, PF_XY, PF_XYZ, PF_ZFACE, PF_AUTO, PF_ZPROFILE = 0, 1, 2, 3, 4, 5
+
+
+class PiscesModelDesc(C.Structure):
+    _fields_ = [("pisces", PiscesParams), ("grid", Grid), ("precision", C.c_int32), ("advection", C.c_int32),
+                ("nbands", C.c_int32), ("negatives", C.c_int32), ("kw", C.c_double * 4), ("e", C.c_double * 4),
+                ("chi", C.c_double * 4), ("division", C.c_double * 4), ("surface", Surface),
+                ("mixed_layer_depth", C.c_double), ("mean_kappa", C.c_double), ("invalid_fill_value", C.c_double),
+                ("carbon", CarbonOptions)]
 
 PISCES_TRACERS = ["P", "PChl", "PFe", "D", "DChl", "DFe", "DSi", "Z", "M", "DOC", "POC", "GOC", "SFe", "BFe", "PSi",
                   "CaCO₃", "NO₃", "NH₄", "PO₄", "Fe", "Si", "DIC", "Alk", "O₂", "T", "S"]
@@ -321,6 +329,15 @@ def load():
     _sig(lib, "obgc_pisces_tendencies", C.c_int, P(PiscesParams), P(Grid), I32, P(VP), P(PiscesField), P(VP), D, VP)
     _sig(lib, "obgc_mixed_layer_mean", C.c_int, P(Grid), I32, VP, P(PiscesField), VP, VP)
     _sig(lib, "obgc_pisces_calcite_saturation", C.c_int, P(CarbonOptions), P(Grid), I32, VP, VP, VP, VP, VP, VP, VP)
+    _sig(lib, "obgc_pisces_model_create", C.c_int, P(PiscesModelDesc), P(VP))
+    _sig(lib, "obgc_pisces_model_destroy", C.c_int, VP)
+    _sig(lib, "obgc_pisces_model_bind", C.c_int, VP, P(VP), VP, VP)
+    _sig(lib, "obgc_pisces_model_update_state", C.c_int, VP, D, VP)
+    _sig(lib, "obgc_pisces_model_step", C.c_int, VP, D, D, I32, VP)
+    _sig(lib, "obgc_pisces_model_field", C.c_int, VP, I32, P(VP))
+    _sig(lib, "obgc_pisces_model_read_field", C.c_int, VP, I32, P(D))
+    _sig(lib, "obgc_pisces_model_set_profiling", C.c_int, VP, I32)
+    _sig(lib, "obgc_pisces_model_last_timing", C.c_int, VP, P(D), P(I32))
     _sig(lib, "obgc_service_create", C.c_int, P(ServiceDesc), P(VP))
     _sig(lib, "obgc_service_destroy", C.c_int, VP)
     _sig(lib, "obgc_service_submit", C.c_int, VP, P(ColumnSpec), P(D), P(D), P(I64))
@@ -349,5 +366,7 @@ EXPORTED = [
     "obgc_service_create", "obgc_service_destroy", "obgc_service_submit", "obgc_service_wait", "obgc_service_drain",
     "obgc_service_get_stats", "obgc_service_reset_stats", "obgc_service_engine",
     "obgc_pisces_default_params", "obgc_pisces_eval_point", "obgc_pisces_tendencies", "obgc_mixed_layer_mean",
-    "obgc_pisces_calcite_saturation",
+    "obgc_pisces_calcite_saturation", "obgc_pisces_model_create", "obgc_pisces_model_destroy", "obgc_pisces_model_bind",
+    "obgc_pisces_model_update_state", "obgc_pisces_model_step", "obgc_pisces_model_field",
+    "obgc_pisces_model_read_field", "obgc_pisces_model_set_profiling", "obgc_pisces_model_last_timing",
 ]

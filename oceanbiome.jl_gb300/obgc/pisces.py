@@ -4,6 +4,8 @@ saturation).  Tracers follow required_biogeochemical_tracers(::PISCES) (PISCES.j
 import ctypes as C
 import math
 
+import numpy as np
+
 from . import _abi as A
 
 
@@ -98,3 +100,96 @@ def calcite_saturation(grid, DIC, Alk, T, S, Si, out, carbon_chemistry=None, str
                                                     None if Si is None else Si.data_ptr(), out.data_ptr(),
                                                     C.c_void_p(stream)), "obgc_pisces_calcite_saturation")
     return out
+
+
+class PiscesModel:
+    """A 3-D PISCES model on the device: NonhydrostaticModel(grid; biogeochemistry = PISCES(...))
+    with MultiBand light (3 bands), a prescribed uniform mixed-layer depth, prescribed velocities and
+    WENO5 advection; time_step runs update_biogeochemical_state! and the fused RK3 substeps."""
+
+    def __init__(self, grid, biogeochemistry=None, velocities=None, precision="f32", mixed_layer_depth=-50.0,
+                 mean_kappa=1.0, surface_PAR=None, light=None, advection=True, device="cuda"):
+        import torch
+        from .light import MultiBandPhotosyntheticallyActiveRadiation
+        from .carbon import CarbonChemistry
+        self.grid = grid
+        self.bgc = bgc = biogeochemistry or PISCES(grid)
+        self.precision = precision
+        self.dtype = torch.float32 if precision == "f32" else torch.float64
+        self.light = light or MultiBandPhotosyntheticallyActiveRadiation(grid=grid, surface_PAR=surface_PAR)
+        d = A.PiscesModelDesc()
+        d.pisces = bgc.params
+        d.grid = grid.c_grid()
+        d.precision = A.PREC_F32 if precision == "f32" else A.PREC_MIXED
+        d.advection = A.ADVECTION_WENO5 if advection else A.ADVECTION_NONE
+        d.nbands = len(self.light.kw)
+        d.negatives = A.NEGATIVES_SCALE if bgc.scale_negatives else A.NEGATIVES_NONE
+        for b in range(d.nbands):
+            d.kw[b], d.e[b], d.chi[b], d.division[b] = self.light.kw[b], self.light.e[b], self.light.chi[b], self.light.division[b]
+        d.surface = self.light.surface
+        d.mixed_layer_depth = float(mixed_layer_depth)
+        d.mean_kappa = float(mean_kappa)
+        d.invalid_fill_value = float(bgc.invalid_fill_value)
+        d.carbon = CarbonChemistry().options
+        self.desc = d
+        self._lib = lib = A.load()
+        h = C.c_void_p()
+        A.check(lib.obgc_pisces_model_create(C.byref(d), C.byref(h)), "obgc_pisces_model_create")
+        self._h = h
+        self.tracers = {n: torch.zeros(grid.shape, dtype=self.dtype, device=device) for n in A.PISCES_TRACERS}
+        u, v = (velocities or (None, None))[:2]
+        self.velocities = tuple(None if x is None else x.to(device=device, dtype=self.dtype).contiguous() for x in (u, v))
+        ptrs = (C.c_void_p * 26)(*[self.tracers[n].data_ptr() for n in A.PISCES_TRACERS])
+        A.check(lib.obgc_pisces_model_bind(h, ptrs, *(None if x is None else x.data_ptr() for x in self.velocities)),
+                "obgc_pisces_model_bind")
+        self.time = 0.0
+
+    def close(self):
+        if self._h:
+            self._lib.obgc_pisces_model_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_(self, **values):
+        import torch
+        for k, v in values.items():
+            name = A.PISCES_TRACERS[A.PISCES_INDEX[k]]
+            self.tracers[name].copy_(torch.as_tensor(v, dtype=self.dtype).expand(self.grid.shape))
+
+    def state_array(self):
+        import torch
+        return torch.stack([self.tracers[n] for n in A.PISCES_TRACERS])
+
+    def update_state(self, t=None, stream=0):
+        A.check(self._lib.obgc_pisces_model_update_state(self._h, float(self.time if t is None else t), C.c_void_p(stream)),
+                "obgc_pisces_model_update_state")
+
+    def time_step(self, dt, nsteps=1, stream=0):
+        A.check(self._lib.obgc_pisces_model_step(self._h, float(self.time), float(dt), int(nsteps), C.c_void_p(stream)),
+                "obgc_pisces_model_step")
+        self.time += dt * nsteps
+
+    def field(self, which):
+        """"PAR", "PAR1".."PAR3", "zeu", "mixed_layer_PAR", "Omega": a host FP64 copy of the model's buffer."""
+        idx = {"PAR": 0, "PAR1": 1, "PAR2": 2, "PAR3": 3, "zeu": 4, "mixed_layer_PAR": 5, "Omega": 6}[which]
+        shape = (self.grid.Ny, self.grid.Nx) if idx in (4, 5) else self.grid.shape
+        out = np.empty(shape, dtype=np.float64)
+        A.check(self._lib.obgc_pisces_model_read_field(self._h, idx, out.ctypes.data_as(C.POINTER(C.c_double))),
+                "obgc_pisces_model_read_field")
+        return out
+
+    def set_profiling(self, on=True):
+        A.check(self._lib.obgc_pisces_model_set_profiling(self._h, int(bool(on))), "obgc_pisces_model_set_profiling")
+
+    def last_timing(self):
+        """Device ms of the last profiled time_step, summed over its RK3 stages, by phase."""
+        ms = (C.c_double * 4)()
+        n = C.c_int32()
+        A.check(self._lib.obgc_pisces_model_last_timing(self._h, ms, C.byref(n)), "obgc_pisces_model_last_timing")
+        return dict(light=ms[0], calcite=ms[1], functor=ms[2], substep=ms[3], stages=n.value)
+

@@ -87,6 +87,40 @@ def lobster_initial_conditions(grid, seed=0, correlated=True):
     }
 
 
+# PISCES_INITIAL_VALUES of the reference's PISCES tests (test/test_PISCES.jl:8-16): the surface
+# value of each profile below
+PISCES_SURFACE_VALUES = dict(P=0.5, PChl=0.02, PFe=0.005, D=0.1, DChl=0.004, DFe=0.001, DSi=0.01, Z=0.1, M=0.7,
+                             DOC=2.1, POC=7.8, SFe=0.206, GOC=38, BFe=1.1, PSi=0.1, CaCO3=1e-10, NO3=2.3, NH4=0.9,
+                             PO4=0.6, Fe=0.13, Si=8.5, DIC=2205, Alk=2566, O2=317, T=10, S=35)
+
+
+def pisces_initial_conditions(grid, seed=0, noise=0.05):
+    """Depth profiles for the 26 PISCES tracers with spatially correlated lognormal noise of the
+    given relative size on every tracer but T and S: living and particulate pools decay below the
+    surface over 100 m to 5% of their surface value, nutrients grow fourfold over ~250 m, DIC and
+    Alk rise by 100 and 20 umol/kg, O2 falls to 60% and T from 18 to 4 C over ~200 m."""
+    rng = np.random.default_rng(seed)
+    shp = grid.shape
+    z = grid.znodes()[:, None, None] * np.ones(shp)
+    v = PISCES_SURFACE_VALUES
+    surf = 0.05 + 0.95 * np.exp(z / 100)
+    deep = 1 + 3 * (1 - np.exp(z / 250))
+    out = {}
+    for n in ("P", "PChl", "PFe", "D", "DChl", "DFe", "DSi", "Z", "M", "DOC", "POC", "SFe", "GOC", "BFe", "PSi", "CaCO3"):
+        out[n] = v[n] * surf
+    for n in ("NO3", "PO4", "Si", "Fe"):
+        out[n] = v[n] * deep
+    out["NH4"] = v["NH4"] * (0.2 + 0.8 * np.exp(z / 100))
+    out["DIC"] = v["DIC"] + 100 * (1 - np.exp(z / 300))
+    out["Alk"] = v["Alk"] + 20 * (1 - np.exp(z / 300))
+    out["O2"] = v["O2"] * (0.6 + 0.4 * np.exp(z / 200))
+    for n in list(out):
+        out[n] = out[n] * np.exp(noise * correlated_normal(shp, rng))
+    out["T"] = 4 + 14 * np.exp(z / 200)
+    out["S"] = np.full(shp, 35.0)
+    return out
+
+
 def npzd_front_initial_conditions(grid):
     """README.md:46-52 (the buoyancy-front example): N = 2.5 - 2 tanh((x - 7000 + 4z)/500),
     T = 9 + 0.05 tanh(...), P = Z = 0.03 above -50 m and 0.01 below, D = 0."""

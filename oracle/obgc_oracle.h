@@ -134,6 +134,29 @@ void or_pisces_goc_speed(const obgc_pisces_params* p, int Nz, const double* zc, 
 double or_mixed_layer_mean(int Nz, const double* zf, const double* C, double zmxl);
 int or_pisces_conserved_groups(const obgc_pisces_params* p, int32_t* gn, int32_t* gslot, double* gfac);
 
+/* 3-D PISCES with MultiBand light, WENO5 advection of all 26 tracers, the six sinking tracers and
+ * RK3; update_biogeochemical_state! before every stage (PISCES/update_state.jl:1-17: MultiBand PAR
+ * from PChl + DChl, euphotic depth, mixed-layer PAR, calcite saturation). */
+typedef struct or_pisces3d {
+    obgc_pisces_params p;
+    obgc_grid grid;              /* strides ignored: arrays are dense [Nz][Ny][Nx] */
+    int32_t nbands, surface_kind;   /* surface: OBGC_SURFACE_PAR_DEFAULT or _CONSTANT */
+    double kw[4], e[4], chi[4], division[4];
+    double surface_value;
+    double mixed_layer_depth;    /* constant zmxl (m, negative)                       */
+    double mean_kappa;           /* mean mixed-layer vertical diffusivity               */
+    int32_t advection, negatives;
+    double invalid_fill_value;
+    obgc_carbon_options carbon;
+} or_pisces3d;
+/* state [26][N]; u, v [N] or NULL. */
+void or_pisces_step3d(const or_pisces3d* m, double* state, const double* u, const double* v, double t, double dt,
+                      int nsteps, int nthreads);
+/* The auxiliary fields of the last update (for tests): PAR bands and total [4][N], zeu and mixed-layer
+ * PAR [2][Nx*Ny], Omega [N]. */
+void or_pisces_update_state3d(const or_pisces3d* m, const double* state, double t, double* par4, double* xy2,
+                              double* omega, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,6 +28,14 @@ class Model3D(C.Structure):
                 ("zero_exclude_mask", C.c_int32), ("invalid_fill_value", C.c_double)]
 
 
+class Pisces3D(C.Structure):
+    _fields_ = [("p", A.PiscesParams), ("grid", A.Grid), ("nbands", C.c_int32), ("surface_kind", C.c_int32),
+                ("kw", C.c_double * 4), ("e", C.c_double * 4), ("chi", C.c_double * 4), ("division", C.c_double * 4),
+                ("surface_value", C.c_double), ("mixed_layer_depth", C.c_double), ("mean_kappa", C.c_double),
+                ("advection", C.c_int32), ("negatives", C.c_int32), ("invalid_fill_value", C.c_double),
+                ("carbon", A.CarbonOptions)]
+
+
 NEG_NONE, NEG_SCALE, NEG_ZERO = 0, 1, 2
 MAX_GROUPS, MAX_MEMBERS = 5, 10      # OR_MAX_GROUPS, OR_MAX_GROUP
 
@@ -94,6 +102,8 @@ def lib():
         L.or_mixed_layer_mean.argtypes = [C.c_int, P(D), P(D), D]
         L.or_mixed_layer_mean.restype = D
         L.or_pisces_conserved_groups.argtypes = [P(A.PiscesParams), P(I32), P(I32), P(D)]
+        L.or_pisces_step3d.argtypes = [P(Pisces3D), P(D), VP, VP, D, D, C.c_int, C.c_int]
+        L.or_pisces_update_state3d.argtypes = [P(Pisces3D), P(D), D, P(D), P(D), P(D), C.c_int]
         L.or_conserved_groups.argtypes = [P(A.NPDParams), C.c_int, P(I32), P(I32), P(I32), P(D)]
         L.or_scale_cell.argtypes = [P(D), C.c_long, C.c_int, P(I32), P(I32), P(D), D]
         _lib = L
@@ -365,4 +375,42 @@ def goc_speed(p, zc, zmxl, zeu):
     w = np.zeros(len(zc) + 1)
     lib().or_pisces_goc_speed(C.byref(p), len(zc), _dp(zc), float(zmxl), float(zeu), _dp(w))
     return w
+
+
+def pisces3d(p, grid, light, mixed_layer_depth, mean_kappa=1.0, surface_kind=A.SURFACE_DEFAULT, surface_value=0.0,
+             advection=1, negatives=NEG_NONE, invalid_fill_value=float("nan")):
+    m = Pisces3D()
+    m.p = p
+    m.grid = grid
+    m.nbands = len(light.kw)
+    m.surface_kind = surface_kind
+    for b in range(m.nbands):
+        m.kw[b], m.e[b], m.chi[b], m.division[b] = light.kw[b], light.e[b], light.chi[b], light.division[b]
+    m.surface_value = surface_value
+    m.mixed_layer_depth = mixed_layer_depth
+    m.mean_kappa = mean_kappa
+    m.advection = advection
+    m.negatives = negatives
+    m.invalid_fill_value = invalid_fill_value
+    m.carbon = carbon_options()
+    return m
+
+
+def pisces_step3d(m, state, u=None, v=None, t=0.0, dt=1.0, nsteps=1, threads=None):
+    """state: float64 (26, Nz, Ny, Nx), stepped in place."""
+    assert state.dtype == np.float64 and state.flags.c_contiguous
+    lib().or_pisces_step3d(C.byref(m), _dp(state), _opt(u), _opt(v), t, dt, nsteps, threads or nthreads())
+    return state
+
+
+def pisces_update_state3d(m, state, t, threads=None):
+    g = m.grid
+    N = g.Nx * g.Ny * g.Nz
+    par4 = np.zeros(4 * N)
+    xy2 = np.zeros(2 * g.Nx * g.Ny)
+    omega = np.zeros(N)
+    lib().or_pisces_update_state3d(C.byref(m), _dp(np.ascontiguousarray(state, dtype=np.float64)), t, _dp(par4),
+                                   _dp(xy2), _dp(omega), threads or nthreads())
+    shp = (g.Nz, g.Ny, g.Nx)
+    return par4.reshape((4,) + shp), xy2.reshape(2, g.Ny, g.Nx), omega.reshape(shp)
 

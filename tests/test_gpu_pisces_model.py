@@ -1,0 +1,97 @@
+"""The 3-D PISCES model on the GPU against the oracle's FP64 model (or_pisces_step3d): the
+update_biogeochemical_state! fields (MultiBand PAR, euphotic depth, mixed-layer PAR, calcite
+saturation) and a few RK3 steps of all 26 tracers with WENO5 advection and POC/GOC sinking."""
+import numpy as np
+import pytest
+
+import obgc
+import oracle as O
+from obgc import _abi as A
+from obgc import pisces as PI
+from gpuhelp import cuda, rel_err
+from test_oracle_pisces import INITIAL
+
+pytestmark = pytest.mark.gpu
+
+
+def pisces_model(precision, shape=(16, 12, 10), extent=(16e3, 12e3, 400.0), seed=3, negatives=False):
+    torch = cuda()
+    g = obgc.RectilinearGrid(shape, extent, ("Periodic", "Periodic", "Bounded"),
+                             dtype="f32" if precision == "f32" else "f64")
+    bgc = PI.PISCES(g, scale_negatives=negatives)
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=seed)
+    model = PI.PiscesModel(g, biogeochemistry=bgc, velocities=(u, v), precision=precision, mixed_layer_depth=-60.0)
+    rng = np.random.default_rng(seed)
+    zc = g.znodes()[:, None, None]
+    init = {}
+    for n in A.PISCES_ASCII:
+        base = INITIAL[n]
+        init[n] = base * np.exp(rng.normal(0, 0.2, g.shape)) if n not in ("T", "S") else np.full(g.shape, base)
+    init["T"] = 4 + 10 * np.exp(zc / 80) * np.ones(g.shape)
+    model.set_(**init)
+    return torch, g, bgc, model, (u, v)
+
+
+def oracle_model(g, bgc, model, negatives=False):
+    return O.pisces3d(bgc.params, g.c_grid(), model.light, model.desc.mixed_layer_depth,
+                      mean_kappa=model.desc.mean_kappa, negatives=O.NEG_SCALE if negatives else O.NEG_NONE)
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-12), ("f32", 2e-5)])
+def test_update_state_fields_match_oracle(precision, tol):
+    torch, g, bgc, model, vel = pisces_model(precision)
+    t = 2 * 86400.0 + 3600.0          # daytime: default_surface_PAR(t) = 100 max(0, cos(pi t / 12 h)) > 0
+    model.update_state(t)
+    torch.cuda.synchronize()
+    s0 = model.state_array().double().cpu().numpy()
+    par4, xy2, omega = O.pisces_update_state3d(oracle_model(g, bgc, model), s0, t)
+    for q, name in enumerate(("PAR", "PAR1", "PAR2", "PAR3")):
+        assert rel_err(model.field(name), par4[q]) < tol, name
+    assert rel_err(model.field("zeu"), xy2[0]) < tol
+    assert rel_err(model.field("mixed_layer_PAR"), xy2[1]) < tol
+    # the carbonate solve is FP64 from the stored state in both precisions (warm-started on the
+    # device); FP32 storage rounds the result
+    assert rel_err(model.field("Omega"), omega) < (1e-8 if precision == "mixed" else 2e-7)
+    zeu = model.field("zeu")
+    assert np.all(zeu < 0) and np.any(zeu > -400.0)
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("f32", 1e-5)])
+def test_pisces_steps_match_oracle(precision, tol):
+    # tracers relative to their own magnitude after three 20-minute RK3 steps: the tendencies are
+    # FP32 arithmetic in both precisions, so the error is the FP32 rounding of the step's changes
+    torch, g, bgc, model, vel = pisces_model(precision)
+    s0 = model.state_array().double().cpu().numpy()
+    # daytime stages: with zero PAR and the growth rate's day length at zero (the reference evaluates
+    # it with latitude and time swapped), GrowthRespirationLimitedProduction's light limitation is
+    # 0/0 (growth_rate.jl:117-123) in the reference and here alike
+    dt, nsteps, t0 = 1200.0, 3, 3 * 86400.0 + 3600.0
+    model.time = t0
+    model.time_step(dt, nsteps=nsteps)
+    torch.cuda.synchronize()
+    got = model.state_array().double().cpu().numpy()
+    ref = np.ascontiguousarray(s0.reshape(26, -1).copy())
+    u, v = (x.double().cpu().numpy().ravel().copy() for x in vel)
+    O.pisces_step3d(oracle_model(g, bgc, model), ref, u=u, v=v, t=t0, dt=dt, nsteps=nsteps)
+    ref = ref.reshape(got.shape)
+    errs = {n: rel_err(got[q], ref[q]) for q, n in enumerate(A.PISCES_ASCII)}
+    assert max(errs.values()) < tol, errs
+    # the step changed every biogeochemical tracer, and the changes agree with the oracle's
+    moved = np.max(np.abs(ref - s0).reshape(26, -1), axis=1)
+    assert np.all(moved[:24] > 0)
+    change_err = np.max(np.abs((got - s0) - (ref - s0)).reshape(26, -1), axis=1) / np.maximum(moved, 1e-300)
+    assert np.max(change_err[:24]) < (1e-3 if precision == "mixed" else 0.5), dict(zip(A.PISCES_ASCII, change_err))
+
+
+def test_pisces_scale_negatives_conserves_groups():
+    # a state with negative phytoplankton carbon: ScaleNegativeTracers over the five conserved groups
+    # makes every member of every group non-negative after a step (coupling_utils.jl:11-33)
+    torch, g, bgc, model, vel = pisces_model("mixed", negatives=True)
+    P = model.tracers["P"]
+    P[:, :2, :3] = -0.05
+    model.time_step(600.0, nsteps=1)
+    torch.cuda.synchronize()
+    got = model.state_array().double().cpu().numpy()
+    assert np.all(np.isfinite(got))
+    for name in ("P", "D", "Z", "M", "DOC", "POC", "GOC", "DIC"):
+        assert got[A.PISCES_INDEX[name]].min() >= 0, name
