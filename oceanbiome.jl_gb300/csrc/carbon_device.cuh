@@ -37,19 +37,37 @@ __host__ __device__ inline double density_eos80(double T, double S, double p) {
     return rho0 / (1 - p / (K0 + Ap * p + Bp * p * p));
 }
 
-// PressureCorrection (equilibrium_constants.jl:11-40)
-__host__ __device__ inline double pressure_correction(double a0, double a1, double a2, double b0, double b1,
-                                                      double Tk, double P) {
+// PressureCorrection (equilibrium_constants.jl:11-40): the log of the factor, so that a constant
+// and its correction take one exp between them.
+__host__ __device__ inline double pressure_log(double a0, double a1, double a2, double b0, double b1, double Tk, double P) {
     const double Tc = Tk - 273.15;
     const double dV = a0 + a1 * Tc + a2 * (Tc * Tc);
     const double dk = b0 + b1 * Tc;
-    return exp((-dV + 0.5 * dk * P) * P / (83.14472 * Tk));
+    return (-dV + 0.5 * dk * P) * P / (83.14472 * Tk);
+}
+__host__ __device__ inline double pressure_correction(double a0, double a1, double a2, double b0, double b1,
+                                                      double Tk, double P) {
+    return exp(pressure_log(a0, a1, a2, b0, b1, Tk, P));
 }
 
 struct CarbConsts {
     double DIC, Alk, boron, sulfate, fluoride, silicate, phosphate;
     double K1, K2, KB, KW, KS, KF, KP1, KP2, KP3, KSi, K0;
+    // H-independent pieces of the residual (prepare_residual)
+    double sd, isd, iKB, iKSi, KSsd, K1K2, KP12, KP123, PKK;
 };
+
+__host__ __device__ inline void prepare_residual(CarbConsts& p) {
+    p.sd = 1 + p.sulfate / p.KS;
+    p.isd = 1.0 / p.sd;
+    p.iKB = 1.0 / p.KB;
+    p.iKSi = 1.0 / p.KSi;
+    p.KSsd = p.KS * p.sd;
+    p.K1K2 = p.K1 * p.K2;
+    p.KP12 = p.KP1 * p.KP2;
+    p.KP123 = p.KP12 * p.KP3;
+    p.PKK = p.phosphate * p.KP12;
+}
 
 // All equilibrium constants at (Tk, S[, P]) with logs and roots shared between them.
 __host__ __device__ inline void equilibrium_constants(double Tk, double S, bool hasP, double P, CarbConsts& c) {
@@ -57,64 +75,64 @@ __host__ __device__ inline void equilibrium_constants(double Tk, double S, bool 
     const double Is = 19.924 * S / (1000.0 + -1.005 * S);
     const double sIs = sqrt(Is);
     const double LN10 = 2.302585092994046;
-    const double pK1 = hasP ? pressure_correction(-25.50, 0.1271, 0.0, -0.00308, 0.0000877, Tk, P) : 1.0;
-    const double pK2 = hasP ? pressure_correction(-15.82, -0.0219, 0.0, 0.00113, -0.0001475, Tk, P) : 1.0;
-    const double pKB = hasP ? pressure_correction(-29.48, 0.1622, -0.0026080, -0.00284, 0.0, Tk, P) : 1.0;
-    const double pKW = hasP ? pressure_correction(-20.02, 0.1119, -0.001409, -0.00513, 0.0000794, Tk, P) : 1.0;
-    const double pKS = hasP ? pressure_correction(-18.03, 0.0466, 0.000316, -0.00453, 0.00009, Tk, P) : 1.0;
-    const double pKF = hasP ? pressure_correction(-9.78, -0.0090, -0.000942, -0.00391, 0.000054, Tk, P) : 1.0;
-    const double pP1 = hasP ? pressure_correction(-14.51, 0.1211, -0.000321, -0.00267, 0.0000427, Tk, P) : 1.0;
-    const double pP2 = hasP ? pressure_correction(-23.12, 0.1758, -0.002647, -0.00515, 0.00009, Tk, P) : 1.0;
-    const double pP3 = hasP ? pressure_correction(-26.57, 0.2020, -0.0030420, -0.00408, 0.0000714, Tk, P) : 1.0;
+    const double pK1 = hasP ? pressure_log(-25.50, 0.1271, 0.0, -0.00308, 0.0000877, Tk, P) : 0.0;
+    const double pK2 = hasP ? pressure_log(-15.82, -0.0219, 0.0, 0.00113, -0.0001475, Tk, P) : 0.0;
+    const double pKB = hasP ? pressure_log(-29.48, 0.1622, -0.0026080, -0.00284, 0.0, Tk, P) : 0.0;
+    const double pKW = hasP ? pressure_log(-20.02, 0.1119, -0.001409, -0.00513, 0.0000794, Tk, P) : 0.0;
+    const double pKS = hasP ? pressure_log(-18.03, 0.0466, 0.000316, -0.00453, 0.00009, Tk, P) : 0.0;
+    const double pKF = hasP ? pressure_log(-9.78, -0.0090, -0.000942, -0.00391, 0.000054, Tk, P) : 0.0;
+    const double pP1 = hasP ? pressure_log(-14.51, 0.1211, -0.000321, -0.00267, 0.0000427, Tk, P) : 0.0;
+    const double pP2 = hasP ? pressure_log(-23.12, 0.1758, -0.002647, -0.00515, 0.00009, Tk, P) : 0.0;
+    const double pP3 = hasP ? pressure_log(-26.57, 0.2020, -0.0030420, -0.00408, 0.0000714, Tk, P) : 0.0;
     // K1, K2: Lueker et al. (2000), log10 form (:103-172)
-    c.K1 = pK1 * exp(LN10 * (61.2172 + -3633.86 * iT + -9.67770 * lT + 0.011555 * S + -0.0001152 * (S * S)));
-    c.K2 = pK2 * exp(LN10 * (-25.9290 + -471.78 * iT + 0.01781 * S + -0.0001122 * (S * S) + 3.16967 * lT));
+    c.K1 = exp(LN10 * (61.2172 + -3633.86 * iT + -9.67770 * lT + 0.011555 * S + -0.0001152 * (S * S)) + pK1);
+    c.K2 = exp(LN10 * (-25.9290 + -471.78 * iT + 0.01781 * S + -0.0001122 * (S * S) + 3.16967 * lT) + pK2);
     // KB: Dickson (1990) (:202-250)
-    c.KB = pKB * exp(148.0248 + (-8966.90 + -2890.53 * sS + -77.942 * S + 1.728 * S * sS + -0.0996 * (S * S)) * iT +
-                     137.1942 * sS + 1.62142 * S + (-24.4344 + -25.085 * sS + -0.2474 * S) * lT + 0.053105 * sS * Tk);
+    c.KB = exp(148.0248 + (-8966.90 + -2890.53 * sS + -77.942 * S + 1.728 * S * sS + -0.0996 * (S * S)) * iT +
+               137.1942 * sS + 1.62142 * S + (-24.4344 + -25.085 * sS + -0.2474 * S) * lT + 0.053105 * sS * Tk + pKB);
     // KW: Millero (1995) (:279-313)
-    c.KW = pKW * exp(148.9652 + -13847.26 * iT + -23.6521 * lT + (-5.977 + 118.67 * iT + 1.0495 * lT) * sS + -0.01615 * S);
-    // KS: Dickson (1990) (:366-419)
-    const double KS0 = exp(141.328 + -4276.1 * iT + -23.093 * lT + (324.57 + -13856.0 * iT + -47.986 * lT) * sIs +
-                           (-771.54 + 35474.0 * iT + 114.723 * lT) * Is + -2698.0 * Is * sIs * iT + 1776.0 * (Is * Is) * iT +
-                           log(1 + -0.001005 * S));
-    c.KS = pKS * KS0;
+    c.KW = exp(148.9652 + -13847.26 * iT + -23.6521 * lT + (-5.977 + 118.67 * iT + 1.0495 * lT) * sS + -0.01615 * S + pKW);
+    // KS: Dickson (1990) (:366-419); log(1 - 0.001005 S) is shared with KSi
+    const double lS = log(1 + -0.001005 * S);
+    c.KS = exp(141.328 + -4276.1 * iT + -23.093 * lT + (324.57 + -13856.0 * iT + -47.986 * lT) * sIs +
+               (-771.54 + 35474.0 * iT + 114.723 * lT) * Is + -2698.0 * Is * sIs * iT + 1776.0 * (Is * Is) * iT + lS + pKS);
     // KF: Perez & Fraga (1987) (:451-487); log_S and log_S_KS terms are zero by default
-    c.KF = pKF * exp(-9.68 + 874.0 * iT + 0.111 * sS);
+    c.KF = exp(-9.68 + 874.0 * iT + 0.111 * sS + pKF);
     // KP1..3: Millero (1995) (:511-651)
-    c.KP1 = pP1 * exp(115.525 + -4576.752 * iT + -18.453 * lT + (0.69171 + -106.736 * iT) * sS + (-0.01844 + -0.65643 * iT) * S);
-    c.KP2 = pP2 * exp(172.0883 + -8814.715 * iT + -27.927 * lT + (1.3566 + -160.340 * iT) * sS + (-0.05778 + 0.37335 * iT) * S);
-    c.KP3 = pP3 * exp(-18.141 + -3070.75 * iT + (2.81197 + 17.27039 * iT) * sS + (-0.09984 + -44.99486 * iT) * S);
+    c.KP1 = exp(115.525 + -4576.752 * iT + -18.453 * lT + (0.69171 + -106.736 * iT) * sS + (-0.01844 + -0.65643 * iT) * S + pP1);
+    c.KP2 = exp(172.0883 + -8814.715 * iT + -27.927 * lT + (1.3566 + -160.340 * iT) * sS + (-0.05778 + 0.37335 * iT) * S + pP2);
+    c.KP3 = exp(-18.141 + -3070.75 * iT + (2.81197 + 17.27039 * iT) * sS + (-0.09984 + -44.99486 * iT) * S + pP3);
     // KSi: Millero (1995) (:674-713), no pressure correction
     c.KSi = exp(117.385 + -8904.2 * iT + -19.334 * lT + (3.5913 + -458.79 * iT) * sIs + (-1.5998 + 188.74 * iT) * Is +
-                (0.07871 + -12.1652 * iT) * (Is * Is) + log(1 + -0.001005 * S));
+                (0.07871 + -12.1652 * iT) * (Is * Is) + lS);
     // K0: Weiss (1974) (:65-80)
     c.K0 = exp(-60.2409 + (93.4517 * 100) * iT + 23.3585 * (lT - log(100.0)) +
                (0.023517 + (-0.023656 / 100) * Tk + (0.0047036 / 10000) * (Tk * Tk)) * S);
 }
 
 // Alkalinity residual and its derivative in H (alkalinity_residual.jl:18-75), sharing
-// denominators.
+// denominators; one reciprocal of H stands in for the divisions by H.
 __host__ __device__ inline void alk_residual(double H, const CarbConsts& p, double& f, double& df) {
     const double H2 = H * H, H3 = H2 * H;
-    const double cd = H2 + p.K1 * H + p.K1 * p.K2;
+    const double iH = 1.0 / H;
+    const double cd = H2 + p.K1 * H + p.K1K2;
     const double icd = 1.0 / cd;
-    const double pd = H3 + p.KP1 * H2 + p.KP1 * p.KP2 * H + p.KP1 * p.KP2 * p.KP3;
+    const double pd = H3 + p.KP1 * H2 + p.KP12 * H + p.KP123;
     const double ipd = 1.0 / pd;
-    const double sd = 1 + p.sulfate / p.KS;
-    const double qb = 1 + H / p.KB, qsi = 1 + H / p.KSi;
-    const double qh = 1 + p.KS / H * sd, qf = 1 + p.KF / H;
+    const double qb = 1 + H * p.iKB, qsi = 1 + H * p.iKSi;
+    const double qh = 1 + p.KSsd * iH, qf = 1 + p.KF * iH;
     const double iqb = 1.0 / qb, iqsi = 1.0 / qsi, iqh = 1.0 / qh, iqf = 1.0 / qf;
-    const double PKK = p.phosphate * p.KP1 * p.KP2;
-    f = p.K1 * H * p.DIC * icd + 2 * p.DIC * p.K1 * p.K2 * icd + p.boron * iqb + p.KW / H + PKK * H * ipd +
-        2 * PKK * p.KP3 * ipd + p.silicate * iqsi - H / sd - p.sulfate * iqh - p.fluoride * iqf -
+    const double PKK = p.PKK;
+    f = p.K1 * H * p.DIC * icd + 2 * p.DIC * p.K1K2 * icd + p.boron * iqb + p.KW * iH + PKK * H * ipd +
+        2 * PKK * p.KP3 * ipd + p.silicate * iqsi - H * p.isd - p.sulfate * iqh - p.fluoride * iqf -
         p.phosphate * H3 * ipd - p.Alk;
     const double dcd = 2 * H + p.K1;
-    const double dpd = 3 * H2 + 2 * p.KP1 * H + p.KP1 * p.KP2;
-    df = p.K1 * p.DIC * (p.K1 * p.K2 - H2) * icd * icd - dcd * 2 * p.DIC * p.K1 * p.K2 * icd * icd -
-         p.boron * iqb * iqb / p.KB - p.KW / H2 + PKK * ipd - dpd * PKK * H * ipd * ipd -
-         dpd * 2 * PKK * p.KP3 * ipd * ipd - p.silicate * iqsi * iqsi / p.KSi - 1 / sd +
-         p.sulfate * iqh * iqh * (-p.KS / H2 * sd) - p.fluoride * iqf * iqf * p.KF / H2 -
+    const double dpd = 3 * H2 + 2 * p.KP1 * H + p.KP12;
+    const double iH2 = iH * iH;
+    df = p.K1 * p.DIC * (p.K1K2 - H2) * icd * icd - dcd * 2 * p.DIC * p.K1K2 * icd * icd -
+         p.boron * iqb * iqb * p.iKB - p.KW * iH2 + PKK * ipd - dpd * PKK * H * ipd * ipd -
+         dpd * 2 * PKK * p.KP3 * ipd * ipd - p.silicate * iqsi * iqsi * p.iKSi - p.isd +
+         p.sulfate * iqh * iqh * (-p.KSsd * iH2) - p.fluoride * iqf * iqf * p.KF * iH2 -
          3 * p.phosphate * H2 * ipd - dpd * p.phosphate * H3 * ipd * ipd;
 }
 
@@ -140,12 +158,17 @@ __host__ __device__ inline CarbSolve solve_H(const obgc_carbon_options& o, doubl
         double fn, dfn;
         alk_residual(x - lam * d, p, fn, dfn);
         const double sf = f > 0 ? 1.0 : (f < 0 ? -1.0 : 0.0);
-        while (fabs(fn) >= fabs(f) - c * lam * f * sf && lam > lm) {
+        // A full step below 1e-9 of H is inside Newton's quadratic region: the iterate it reaches
+        // is exact to FP64 resolution (the next step would be ~1e-18 of H), and its residual is
+        // rounding noise, where the Armijo test fails at random and backtracking to the minimum
+        // damping only shortens the step.  Take it and stop.
+        const bool quadratic = lam == 1.0 && fabs(d) <= 1e-9 * fabs(x);
+        while (!quadratic && fabs(fn) >= fabs(f) - c * lam * f * sf && lam > lm) {
             lam *= o.damping;
             alk_residual(x - lam * d, p, fn, dfn);
         }
         const double xn = x - lam * d;
-        stalled = fabs(xn - x) <= 4e-16 * fabs(x);
+        stalled = quadratic || fabs(xn - x) <= 4e-16 * fabs(x);
         x = xn;
         f = fn;
         df = dfn;
@@ -197,6 +220,7 @@ __host__ __device__ inline double carbon_cell(const obgc_carbon_options& o, doub
     c.phosphate = phosphate * conv;
     c.silicate = silicate * conv;
     equilibrium_constants(Tk, S, hasP, P, c);
+    prepare_residual(c);
     double H;
     int it = 0;
     bool ok = true;
@@ -217,11 +241,11 @@ __host__ __device__ inline double carbon_cell(const obgc_carbon_options& o, doub
         const double co3 = c.DIC * c.K1 * c.K2 / d1 / d2;
         if (o.output == OBGC_OUT_CARBONATE) return co3;
         // KSP_calcite (equilibrium_constants.jl:740-805; log10(T) as in the reference)
-        const double pc = hasP ? pressure_correction(-48.76, 0.5304, -0.0, -0.01176, 0.0003692, Tk, P) : 1.0;
+        const double pc = hasP ? pressure_log(-48.76, 0.5304, -0.0, -0.01176, 0.0003692, Tk, P) : 0.0;
         const double sS = sqrt(S);
         const double lnK = -171.9065 + -0.077993 * Tk + 2839.319 / Tk + 71.595 * log10(Tk) +
                            (-0.77712 + 0.0028426 * Tk + 178.34 / Tk) * sS + -0.07711 * S + 0.0041249 * S * sS;
-        const double KSP = pc * exp(2.302585092994046 * lnK);
+        const double KSP = exp(2.302585092994046 * lnK + pc);
         return o.calcium_ion_per_salinity * S * co3 / KSP;
     }
     const double CO2 = c.DIC * (H * H) / (H * H + c.K1 * H + c.K1 * c.K2);

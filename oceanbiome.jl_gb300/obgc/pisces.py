@@ -102,6 +102,16 @@ def calcite_saturation(grid, DIC, Alk, T, S, Si, out, carbon_chemistry=None, str
     return out
 
 
+class _Tracers(dict):
+    """model.tracers: keyed by the reference's names (NO₃), also reachable by their ASCII forms (NO3)."""
+
+    def __getitem__(self, name):
+        return dict.__getitem__(self, A.PISCES_TRACERS[A.PISCES_INDEX[name]])
+
+    def __contains__(self, name):
+        return name in A.PISCES_INDEX
+
+
 class PiscesModel:
     """A 3-D PISCES model on the device: NonhydrostaticModel(grid; biogeochemistry = PISCES(...))
     with MultiBand light (3 bands), a prescribed uniform mixed-layer depth, prescribed velocities and
@@ -136,7 +146,7 @@ class PiscesModel:
         h = C.c_void_p()
         A.check(lib.obgc_pisces_model_create(C.byref(d), C.byref(h)), "obgc_pisces_model_create")
         self._h = h
-        self.tracers = {n: torch.zeros(grid.shape, dtype=self.dtype, device=device) for n in A.PISCES_TRACERS}
+        self.tracers = _Tracers((n, torch.zeros(grid.shape, dtype=self.dtype, device=device)) for n in A.PISCES_TRACERS)
         u, v = (velocities or (None, None))[:2]
         self.velocities = tuple(None if x is None else x.to(device=device, dtype=self.dtype).contiguous() for x in (u, v))
         ptrs = (C.c_void_p * 26)(*[self.tracers[n].data_ptr() for n in A.PISCES_TRACERS])

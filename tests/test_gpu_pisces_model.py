@@ -56,7 +56,7 @@ def test_update_state_fields_match_oracle(precision, tol):
     assert np.all(zeu < 0) and np.any(zeu > -400.0)
 
 
-@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("f32", 1e-5)])
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("f32", 3e-6)])
 def test_pisces_steps_match_oracle(precision, tol):
     # tracers relative to their own magnitude after three 20-minute RK3 steps: the tendencies are
     # FP32 arithmetic in both precisions, so the error is the FP32 rounding of the step's changes
@@ -74,24 +74,36 @@ def test_pisces_steps_match_oracle(precision, tol):
     u, v = (x.double().cpu().numpy().ravel().copy() for x in vel)
     O.pisces_step3d(oracle_model(g, bgc, model), ref, u=u, v=v, t=t0, dt=dt, nsteps=nsteps)
     ref = ref.reshape(got.shape)
-    errs = {n: rel_err(got[q], ref[q]) for q, n in enumerate(A.PISCES_ASCII)}
-    assert max(errs.values()) < tol, errs
-    # the step changed every biogeochemical tracer, and the changes agree with the oracle's
+    # relative error with a floor of 1% of the field's largest value: CaCO3 grows from 1e-10 to
+    # ~1e-4 in these steps, so cells it has not reached hold values far below the rounding of the rest
+    errs = {n: rel_err(got[q], ref[q], floor_frac=1e-2) for q, n in enumerate(A.PISCES_ASCII)}
+    assert max(errs.values()) < tol, sorted(errs.items(), key=lambda kv: -kv[1])[:6]
+    # the step changed every biogeochemical tracer, and the changes agree with the oracle's to the
+    # FP32 rounding of the tendencies (T and S only move by the FP32 rounding of u_x + v_y = 0)
     moved = np.max(np.abs(ref - s0).reshape(26, -1), axis=1)
     assert np.all(moved[:24] > 0)
     change_err = np.max(np.abs((got - s0) - (ref - s0)).reshape(26, -1), axis=1) / np.maximum(moved, 1e-300)
-    assert np.max(change_err[:24]) < (1e-3 if precision == "mixed" else 0.5), dict(zip(A.PISCES_ASCII, change_err))
+    assert np.max(change_err[:24]) < (3e-6 if precision == "mixed" else 1e-5), dict(zip(A.PISCES_ASCII, change_err))
 
 
-def test_pisces_scale_negatives_conserves_groups():
-    # a state with negative phytoplankton carbon: ScaleNegativeTracers over the five conserved groups
-    # makes every member of every group non-negative after a step (coupling_utils.jl:11-33)
+def test_pisces_scale_negatives_match_oracle():
+    # negative DOC and NH4 in some cells: ScaleNegativeTracers over the five conserved groups
+    # (coupling_utils.jl:11-33) before every stage and after the step, as the oracle does.  (A
+    # negative P alone would leave PChl, which no group holds, over a zero P: the chlorophyll ratio
+    # PChl / (12 P + eps(0.0)) is then infinite and the reference's tendencies NaN.)
     torch, g, bgc, model, vel = pisces_model("mixed", negatives=True)
-    P = model.tracers["P"]
-    P[:, :2, :3] = -0.05
+    model.tracers["DOC"][:, :2, :3] = -0.05
+    model.tracers["NH4"][:, 3:5, 4:6] = -0.01
+    s0 = model.state_array().double().cpu().numpy()
     model.time_step(600.0, nsteps=1)
     torch.cuda.synchronize()
     got = model.state_array().double().cpu().numpy()
+    ref = np.ascontiguousarray(s0.reshape(26, -1).copy())
+    u, v = (x.double().cpu().numpy().ravel().copy() for x in vel)
+    O.pisces_step3d(oracle_model(g, bgc, model, negatives=True), ref, u=u, v=v, t=0.0, dt=600.0, nsteps=1)
+    ref = ref.reshape(got.shape)
     assert np.all(np.isfinite(got))
-    for name in ("P", "D", "Z", "M", "DOC", "POC", "GOC", "DIC"):
+    for name in ("DOC", "NH4"):
         assert got[A.PISCES_INDEX[name]].min() >= 0, name
+    errs = {n: rel_err(got[q], ref[q], floor_frac=1e-2) for q, n in enumerate(A.PISCES_ASCII)}
+    assert max(errs.values()) < 1e-6, sorted(errs.items(), key=lambda kv: -kv[1])[:6]
