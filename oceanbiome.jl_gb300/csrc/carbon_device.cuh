@@ -39,20 +39,19 @@ __host__ __device__ inline double density_eos80(double T, double S, double p) {
 
 // PressureCorrection (equilibrium_constants.jl:11-40): the log of the factor, so that a constant
 // and its correction take one exp between them.
-__host__ __device__ inline double pressure_log(double a0, double a1, double a2, double b0, double b1, double Tk, double P) {
+// iRT = 1 / (R Tk), shared by every constant of a cell.
+__host__ __device__ inline double pressure_log(double a0, double a1, double a2, double b0, double b1, double Tk, double P,
+                                               double iRT) {
     const double Tc = Tk - 273.15;
     const double dV = a0 + a1 * Tc + a2 * (Tc * Tc);
     const double dk = b0 + b1 * Tc;
-    return (-dV + 0.5 * dk * P) * P / (83.14472 * Tk);
-}
-__host__ __device__ inline double pressure_correction(double a0, double a1, double a2, double b0, double b1,
-                                                      double Tk, double P) {
-    return exp(pressure_log(a0, a1, a2, b0, b1, Tk, P));
+    return (-dV + 0.5 * dk * P) * P * iRT;
 }
 
 struct CarbConsts {
     double DIC, Alk, boron, sulfate, fluoride, silicate, phosphate;
     double K1, K2, KB, KW, KS, KF, KP1, KP2, KP3, KSi, K0;
+    double lT, iT, sS, iRT;      // log(Tk), 1/Tk, sqrt(S), 1/(R Tk), kept for the outputs
     // H-independent pieces of the residual (prepare_residual)
     double sd, isd, iKB, iKSi, KSsd, K1K2, KP12, KP123, PKK;
 };
@@ -61,7 +60,7 @@ __host__ __device__ inline void prepare_residual(CarbConsts& p) {
     p.sd = 1 + p.sulfate / p.KS;
     p.isd = 1.0 / p.sd;
     p.iKB = 1.0 / p.KB;
-    p.iKSi = 1.0 / p.KSi;
+    p.iKSi = p.KSi != 0.0 ? 1.0 / p.KSi : 0.0;   // KSi is left at zero without silicate
     p.KSsd = p.KS * p.sd;
     p.K1K2 = p.K1 * p.K2;
     p.KP12 = p.KP1 * p.KP2;
@@ -69,21 +68,25 @@ __host__ __device__ inline void prepare_residual(CarbConsts& p) {
     p.PKK = p.phosphate * p.KP12;
 }
 
-// All equilibrium constants at (Tk, S[, P]) with logs and roots shared between them.
-__host__ __device__ inline void equilibrium_constants(double Tk, double S, bool hasP, double P, CarbConsts& c) {
+// The equilibrium constants at (Tk, S[, P]) with logs and roots shared between them.  A constant
+// whose species is absent (phosphate or silicate zero) or whose output is not asked for (K0 outside
+// fCO2 / pCO2) is left at zero: every term it enters is then multiplied by that zero concentration.
+__host__ __device__ inline void equilibrium_constants(double Tk, double S, bool hasP, double P, bool need_K0, CarbConsts& c) {
     const double lT = log(Tk), iT = 1.0 / Tk, sS = sqrt(S);
+    const double iRT = iT * (1.0 / 83.14472);
+    c.lT = lT; c.iT = iT; c.sS = sS; c.iRT = iRT;
     const double Is = 19.924 * S / (1000.0 + -1.005 * S);
     const double sIs = sqrt(Is);
     const double LN10 = 2.302585092994046;
-    const double pK1 = hasP ? pressure_log(-25.50, 0.1271, 0.0, -0.00308, 0.0000877, Tk, P) : 0.0;
-    const double pK2 = hasP ? pressure_log(-15.82, -0.0219, 0.0, 0.00113, -0.0001475, Tk, P) : 0.0;
-    const double pKB = hasP ? pressure_log(-29.48, 0.1622, -0.0026080, -0.00284, 0.0, Tk, P) : 0.0;
-    const double pKW = hasP ? pressure_log(-20.02, 0.1119, -0.001409, -0.00513, 0.0000794, Tk, P) : 0.0;
-    const double pKS = hasP ? pressure_log(-18.03, 0.0466, 0.000316, -0.00453, 0.00009, Tk, P) : 0.0;
-    const double pKF = hasP ? pressure_log(-9.78, -0.0090, -0.000942, -0.00391, 0.000054, Tk, P) : 0.0;
-    const double pP1 = hasP ? pressure_log(-14.51, 0.1211, -0.000321, -0.00267, 0.0000427, Tk, P) : 0.0;
-    const double pP2 = hasP ? pressure_log(-23.12, 0.1758, -0.002647, -0.00515, 0.00009, Tk, P) : 0.0;
-    const double pP3 = hasP ? pressure_log(-26.57, 0.2020, -0.0030420, -0.00408, 0.0000714, Tk, P) : 0.0;
+    const double pK1 = hasP ? pressure_log(-25.50, 0.1271, 0.0, -0.00308, 0.0000877, Tk, P, iRT) : 0.0;
+    const double pK2 = hasP ? pressure_log(-15.82, -0.0219, 0.0, 0.00113, -0.0001475, Tk, P, iRT) : 0.0;
+    const double pKB = hasP ? pressure_log(-29.48, 0.1622, -0.0026080, -0.00284, 0.0, Tk, P, iRT) : 0.0;
+    const double pKW = hasP ? pressure_log(-20.02, 0.1119, -0.001409, -0.00513, 0.0000794, Tk, P, iRT) : 0.0;
+    const double pKS = hasP ? pressure_log(-18.03, 0.0466, 0.000316, -0.00453, 0.00009, Tk, P, iRT) : 0.0;
+    const double pKF = hasP ? pressure_log(-9.78, -0.0090, -0.000942, -0.00391, 0.000054, Tk, P, iRT) : 0.0;
+    const double pP1 = hasP ? pressure_log(-14.51, 0.1211, -0.000321, -0.00267, 0.0000427, Tk, P, iRT) : 0.0;
+    const double pP2 = hasP ? pressure_log(-23.12, 0.1758, -0.002647, -0.00515, 0.00009, Tk, P, iRT) : 0.0;
+    const double pP3 = hasP ? pressure_log(-26.57, 0.2020, -0.0030420, -0.00408, 0.0000714, Tk, P, iRT) : 0.0;
     // K1, K2: Lueker et al. (2000), log10 form (:103-172)
     c.K1 = exp(LN10 * (61.2172 + -3633.86 * iT + -9.67770 * lT + 0.011555 * S + -0.0001152 * (S * S)) + pK1);
     c.K2 = exp(LN10 * (-25.9290 + -471.78 * iT + 0.01781 * S + -0.0001122 * (S * S) + 3.16967 * lT) + pK2);
@@ -99,40 +102,52 @@ __host__ __device__ inline void equilibrium_constants(double Tk, double S, bool 
     // KF: Perez & Fraga (1987) (:451-487); log_S and log_S_KS terms are zero by default
     c.KF = exp(-9.68 + 874.0 * iT + 0.111 * sS + pKF);
     // KP1..3: Millero (1995) (:511-651)
+    c.KP1 = c.KP2 = c.KP3 = c.KSi = c.K0 = 0.0;
+    if (c.phosphate != 0.0) {
     c.KP1 = exp(115.525 + -4576.752 * iT + -18.453 * lT + (0.69171 + -106.736 * iT) * sS + (-0.01844 + -0.65643 * iT) * S + pP1);
     c.KP2 = exp(172.0883 + -8814.715 * iT + -27.927 * lT + (1.3566 + -160.340 * iT) * sS + (-0.05778 + 0.37335 * iT) * S + pP2);
     c.KP3 = exp(-18.141 + -3070.75 * iT + (2.81197 + 17.27039 * iT) * sS + (-0.09984 + -44.99486 * iT) * S + pP3);
+    }
     // KSi: Millero (1995) (:674-713), no pressure correction
+    if (c.silicate != 0.0)
     c.KSi = exp(117.385 + -8904.2 * iT + -19.334 * lT + (3.5913 + -458.79 * iT) * sIs + (-1.5998 + 188.74 * iT) * Is +
                 (0.07871 + -12.1652 * iT) * (Is * Is) + lS);
     // K0: Weiss (1974) (:65-80)
+    if (need_K0)
     c.K0 = exp(-60.2409 + (93.4517 * 100) * iT + 23.3585 * (lT - log(100.0)) +
                (0.023517 + (-0.023656 / 100) * Tk + (0.0047036 / 10000) * (Tk * Tk)) * S);
 }
 
-// Alkalinity residual and its derivative in H (alkalinity_residual.jl:18-75), sharing
-// denominators; one reciprocal of H stands in for the divisions by H.
+// Alkalinity residual and its derivative in H (alkalinity_residual.jl:18-75).  The seven
+// denominators (H, the carbonate and phosphate polynomials, KB + H, KSi + H, H + KS(1 + ST/KS),
+// H + KF) are inverted with one division: prefix products, one reciprocal of the full product,
+// and a backward sweep (the product stays above 1e-120 for H in [1e-14, 1]).
 __host__ __device__ inline void alk_residual(double H, const CarbConsts& p, double& f, double& df) {
     const double H2 = H * H, H3 = H2 * H;
-    const double iH = 1.0 / H;
-    const double cd = H2 + p.K1 * H + p.K1K2;
-    const double icd = 1.0 / cd;
-    const double pd = H3 + p.KP1 * H2 + p.KP12 * H + p.KP123;
-    const double ipd = 1.0 / pd;
-    const double qb = 1 + H * p.iKB, qsi = 1 + H * p.iKSi;
-    const double qh = 1 + p.KSsd * iH, qf = 1 + p.KF * iH;
-    const double iqb = 1.0 / qb, iqsi = 1.0 / qsi, iqh = 1.0 / qh, iqf = 1.0 / qf;
+    const double a0 = H;
+    const double a1 = H2 + p.K1 * H + p.K1K2;                       // carbonate denominator
+    const double a2 = H3 + p.KP1 * H2 + p.KP12 * H + p.KP123;       // phosphate denominator
+    const double a3 = p.KB + H, a4 = p.KSi + H, a5 = H + p.KSsd, a6 = H + p.KF;
+    const double q1 = a0 * a1, q2 = q1 * a2, q3 = q2 * a3, q4 = q3 * a4, q5 = q4 * a5, q6 = q5 * a6;
+    double r = 1.0 / q6;
+    const double r6 = r * q5; r *= a6;
+    const double r5 = r * q4; r *= a5;
+    const double r4 = r * q3; r *= a4;
+    const double r3 = r * q2; r *= a3;
+    const double ipd = r * q1; r *= a2;
+    const double icd = r * a0;
+    const double iH = r * a1;
+    const double iqb = p.KB * r3, iqsi = p.KSi * r4, iqh = H * r5, iqf = H * r6;
     const double PKK = p.PKK;
     f = p.K1 * H * p.DIC * icd + 2 * p.DIC * p.K1K2 * icd + p.boron * iqb + p.KW * iH + PKK * H * ipd +
         2 * PKK * p.KP3 * ipd + p.silicate * iqsi - H * p.isd - p.sulfate * iqh - p.fluoride * iqf -
         p.phosphate * H3 * ipd - p.Alk;
     const double dcd = 2 * H + p.K1;
     const double dpd = 3 * H2 + 2 * p.KP1 * H + p.KP12;
-    const double iH2 = iH * iH;
     df = p.K1 * p.DIC * (p.K1K2 - H2) * icd * icd - dcd * 2 * p.DIC * p.K1K2 * icd * icd -
-         p.boron * iqb * iqb * p.iKB - p.KW * iH2 + PKK * ipd - dpd * PKK * H * ipd * ipd -
-         dpd * 2 * PKK * p.KP3 * ipd * ipd - p.silicate * iqsi * iqsi * p.iKSi - p.isd +
-         p.sulfate * iqh * iqh * (-p.KSsd * iH2) - p.fluoride * iqf * iqf * p.KF * iH2 -
+         p.boron * iqb * iqb * p.iKB - p.KW * (iH * iH) + PKK * ipd - dpd * PKK * H * ipd * ipd -
+         dpd * 2 * PKK * p.KP3 * ipd * ipd - p.silicate * iqsi * iqsi * p.iKSi - p.isd -
+         p.sulfate * p.KSsd * (r5 * r5) - p.fluoride * p.KF * (r6 * r6) -
          3 * p.phosphate * H2 * ipd - dpd * p.phosphate * H3 * ipd * ipd;
 }
 
@@ -219,7 +234,7 @@ __host__ __device__ inline double carbon_cell(const obgc_carbon_options& o, doub
     c.DIC = DIC * conv;
     c.phosphate = phosphate * conv;
     c.silicate = silicate * conv;
-    equilibrium_constants(Tk, S, hasP, P, c);
+    equilibrium_constants(Tk, S, hasP, P, o.output == OBGC_OUT_FCO2 || o.output == OBGC_OUT_PCO2, c);
     prepare_residual(c);
     double H;
     int it = 0;
@@ -241,10 +256,9 @@ __host__ __device__ inline double carbon_cell(const obgc_carbon_options& o, doub
         const double co3 = c.DIC * c.K1 * c.K2 / d1 / d2;
         if (o.output == OBGC_OUT_CARBONATE) return co3;
         // KSP_calcite (equilibrium_constants.jl:740-805; log10(T) as in the reference)
-        const double pc = hasP ? pressure_log(-48.76, 0.5304, -0.0, -0.01176, 0.0003692, Tk, P) : 0.0;
-        const double sS = sqrt(S);
-        const double lnK = -171.9065 + -0.077993 * Tk + 2839.319 / Tk + 71.595 * log10(Tk) +
-                           (-0.77712 + 0.0028426 * Tk + 178.34 / Tk) * sS + -0.07711 * S + 0.0041249 * S * sS;
+        const double pc = hasP ? pressure_log(-48.76, 0.5304, -0.0, -0.01176, 0.0003692, Tk, P, c.iRT) : 0.0;
+        const double lnK = -171.9065 + -0.077993 * Tk + 2839.319 * c.iT + 71.595 * (c.lT * 0.4342944819032518) +
+                           (-0.77712 + 0.0028426 * Tk + 178.34 * c.iT) * c.sS + -0.07711 * S + 0.0041249 * S * c.sS;
         const double KSP = exp(2.302585092994046 * lnK + pc);
         return o.calcium_ion_per_salinity * S * co3 / KSP;
     }

@@ -39,29 +39,31 @@ __global__ void __launch_bounds__(128) twoband_kernel(TwoBandT<T> L, int surf_ki
 }
 
 constexpr int MAX_BANDS = 8;
-template <typename T>
+// Fields in the storage type TS, arithmetic in T (FP32 for a model whose state is FP64 and whose
+// light runs in FP32).
+template <typename T, typename TS = T>
 struct BandsT {
     int n;
     T kw[MAX_BANDS], e[MAX_BANDS], chi[MAX_BANDS], div[MAX_BANDS];
-    T* out[MAX_BANDS];
+    TS* out[MAX_BANDS];
 };
 
-template <typename T>
-__global__ void __launch_bounds__(128) multiband_kernel(BandsT<T> B, int surf_kind, T surf_value,
-                                                        const T* __restrict__ surf_field, int Nx, int Ny,
+template <typename T, typename TS = T>
+__global__ void __launch_bounds__(128) multiband_kernel(BandsT<T, TS> B, int surf_kind, T surf_value,
+                                                        const TS* __restrict__ surf_field, int Nx, int Ny,
                                                         int Nz, int64_t sj, int64_t sk, T Lz,
-                                                        const T* __restrict__ Chl, T* __restrict__ total) {
+                                                        const TS* __restrict__ Chl, TS* __restrict__ total) {
     const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= (int64_t)Nx * Ny) return;
     const int i = (int)(col % Nx), j = (int)(col / Nx);
     const T dz = Lz / T(Nz);
-    const T PAR0 = surface_value(surf_kind, surf_value, surf_field, col);
+    const T PAR0 = surf_kind == OBGC_SURFACE_PAR_FIELD ? T(surf_field[col]) : surf_value;
     const int64_t base = i + (int64_t)j * sj;
     T prev[MAX_BANDS];
     T zprev = T(0);
     for (int k = Nz - 1; k >= 0; --k) {
         const int64_t idx = base + (int64_t)k * sk;
-        const T chl = Chl[idx];
+        const T chl = T(Chl[idx]);
         const T z = -Lz + (T(k) + T(0.5)) * dz;
         T sum = T(0);
 #pragma unroll
@@ -71,11 +73,11 @@ __global__ void __launch_bounds__(128) multiband_kernel(BandsT<T> B, int surf_ki
                 // multi_band.jl:156 (top cell) and :160-161 (cells below)
                 const T v = (k == Nz - 1) ? PAR0 * B.div[b] * t_exp(z * att) : prev[b] * t_exp((z - zprev) * att);
                 prev[b] = v;
-                B.out[b][idx] = v;
+                B.out[b][idx] = TS(v);
                 sum += v;
             }
         }
-        if (total) total[idx] = sum;
+        if (total) total[idx] = TS(sum);
         zprev = z;
     }
 }
@@ -121,21 +123,21 @@ static int launch_twoband(const obgc_twoband_params* lp, const obgc_surface* s, 
     return OBGC_OK;
 }
 
-template <typename T>
+template <typename T, typename TS = T>
 static int launch_multiband(int nb, const double* kw, const double* e, const double* chi, const double* dv,
                             const obgc_surface* s, const obgc_grid* g, const void* Chl,
                             void* const* bands, void* total, double t, cudaStream_t st) {
-    BandsT<T> B;
+    BandsT<T, TS> B;
     B.n = nb;
     for (int b = 0; b < nb; b++) {
         B.kw[b] = T(kw[b]); B.e[b] = T(e[b]); B.chi[b] = T(chi[b]); B.div[b] = T(dv[b]);
-        B.out[b] = (T*)bands[b];
+        B.out[b] = (TS*)bands[b];
     }
     const int64_t ncol = (int64_t)g->Nx * g->Ny;
     const int blocks = (int)((ncol + 127) / 128);
     const double v = s->kind == OBGC_SURFACE_PAR_DEFAULT ? default_surface_par(t) : s->value;
-    multiband_kernel<T><<<blocks, 128, 0, st>>>(B, s->kind, T(v), (const T*)s->field, g->Nx, g->Ny, g->Nz,
-                                                g->stride_j, g->stride_k, T(g->Lz), (const T*)Chl, (T*)total);
+    multiband_kernel<T, TS><<<blocks, 128, 0, st>>>(B, s->kind, T(v), (const TS*)s->field, g->Nx, g->Ny, g->Nz,
+                                                    g->stride_j, g->stride_k, T(g->Lz), (const TS*)Chl, (TS*)total);
     OBGC_LAUNCHED("multiband_kernel");
     return OBGC_OK;
 }
@@ -227,3 +229,13 @@ extern "C" int obgc_euphotic_depth(const obgc_surface* surface, const obgc_grid*
     if (dtype == OBGC_F64) return launch_euphotic<double>(surface, grid, PAR, zeu, cutoff, t, st);
     return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_euphotic_depth: bad dtype");
 }
+
+namespace obgc {
+// FP64 fields, FP32 arithmetic: the MultiBand light of a model whose state is FP64 and whose light
+// runs in FP32 (OBGC_PREC_MIXED).  Arguments as obgc_multiband_par, already validated.
+int multiband_par_mixed(int nb, const double* kw, const double* e, const double* chi, const double* dv,
+                        const obgc_surface* s, const obgc_grid* g, const void* Chl, void* const* bands, void* total,
+                        double t, cudaStream_t st) {
+    return launch_multiband<float, double>(nb, kw, e, chi, dv, s, g, Chl, bands, total, t, st);
+}
+}  // namespace obgc

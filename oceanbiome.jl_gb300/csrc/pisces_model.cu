@@ -25,6 +25,10 @@ extern "C" int obgc_mixed_layer_mean(const obgc_grid* grid, int32_t dtype, const
 
 namespace obgc {
 
+int multiband_par_mixed(int nb, const double* kw, const double* e, const double* chi, const double* dv,
+                        const obgc_surface* s, const obgc_grid* g, const void* Chl, void* const* bands, void* total,
+                        double t, cudaStream_t st);
+
 template <typename TS, typename T>
 int launch_pisces(const obgc_pisces_params* p, const obgc_grid* g, const void* const* tracers, const obgc_pisces_field* aux,
                   void* const* G, double t, cudaStream_t st);
@@ -166,8 +170,11 @@ int update_state(obgc_pisces_model* m, double t, cudaStream_t st) {
     chl_sum_kernel<TS><<<blocks, 256, 0, st>>>(PChl, DChl, static_cast<TS*>(m->chl), g.Nx, g.Ny, g.Nz, g.stride_j, g.stride_k);
     OBGC_LAUNCHED("chl_sum_kernel");
     void* bands[4] = {m->par[1], m->par[2], m->par[3], nullptr};
-    int rc = obgc_multiband_par(m->desc.nbands, m->desc.kw, m->desc.e, m->desc.chi, m->desc.division, &m->desc.surface, &g,
-                                state_dtype(m), m->chl, bands, m->par[0], t, st);
+    // light in FP32 arithmetic for both precisions (FP64 fields for the mixed path)
+    int rc = m->ts == 4 ? obgc_multiband_par(m->desc.nbands, m->desc.kw, m->desc.e, m->desc.chi, m->desc.division,
+                                             &m->desc.surface, &g, state_dtype(m), m->chl, bands, m->par[0], t, st)
+                        : multiband_par_mixed(m->desc.nbands, m->desc.kw, m->desc.e, m->desc.chi, m->desc.division,
+                                              &m->desc.surface, &g, m->chl, bands, m->par[0], t, st);
     if (rc != OBGC_OK) return rc;
     rc = obgc_euphotic_depth(&m->desc.surface, &g, state_dtype(m), m->par[0], m->zeu, 1e-3, t, st);
     if (rc != OBGC_OK) return rc;
@@ -213,7 +220,10 @@ void aux_fields(const obgc_pisces_model* m, obgc_pisces_field* a) {
 
 template <typename TS, typename TC>
 int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t st) {
-    const FusedEntry* fe = find_fused(m->desc.precision, V_EXTERNAL, PNT);
+    // the 26 tracers advect independently once their BGC tendencies are in hand: two launches of
+    // 13 tracers each hold half the shared-memory tiles and run two blocks per SM
+    constexpr int GROUP = 13;
+    const FusedEntry* fe = find_fused(m->desc.precision, V_EXTERNAL, GROUP);
     if (!fe) return fail(OBGC_ERR_UNSUPPORTED, "obgc_pisces_model_step: no fused PISCES kernel for this precision");
     const obgc_grid& g = m->desc.grid;
     SubstepArgs<TS, TC> a;
@@ -231,13 +241,9 @@ int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t 
     a.ntx = (g.Nx + STEP_BX - 1) / STEP_BX;
     a.nty = (g.Ny + STEP_BY - 1) / STEP_BY;
     a.n_items = a.ntx * a.nty * a.nseg;
-    for (int q = 0; q < PNT; q++) a.G[q] = static_cast<TC*>(m->G[q]);
-    for (int q = 0; q < OBGC_PIS_NUM_BGC; q++) a.ext[q] = static_cast<const TC*>(m->Gb[q]);
     a.u = m->desc.advection ? static_cast<const TS*>(m->u) : nullptr;
     a.v = m->desc.advection ? static_cast<const TS*>(m->v) : nullptr;
     a.w = nullptr;
-    a.drift = static_cast<const TC*>(m->drift);
-    a.drift_mask = m->desc.advection ? m->drift_mask : 0u;
     a.dt_d = dt;
     a.dt = TC(dt);
     int occ = 1;
@@ -262,13 +268,24 @@ int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t 
             rc = launch_pisces<TS, TC>(&m->desc.pisces, &g, cur, aux, m->Gb, ts, st);
             if (rc == OBGC_OK) rc = prof_mark(m, st);
             if (rc != OBGC_OK) break;
-            for (int q = 0; q < PNT; q++) { a.in[q] = static_cast<const TS*>(cur[q]); a.out[q] = static_cast<TS*>(nxt[q]); }
+            const uint32_t mask = m->desc.advection ? m->drift_mask : 0u;
             a.first_stage = stg == 0;
             a.write_G = stg < 2;
             a.gamma = TC(rk3_gamma(stg));
             a.zeta = TC(rk3_zeta(stg));
             a.c_stage = rk3_c(stg);
-            rc = fe->launch(&a, blocks, st);
+            for (int g0 = 0; g0 < PNT && rc == OBGC_OK; g0 += GROUP) {
+                for (int t = 0; t < GROUP; t++) {
+                    a.in[t] = static_cast<const TS*>(cur[g0 + t]);
+                    a.out[t] = static_cast<TS*>(nxt[g0 + t]);
+                    a.G[t] = static_cast<TC*>(m->G[g0 + t]);
+                    a.ext[t] = g0 + t < OBGC_PIS_NUM_BGC ? static_cast<const TC*>(m->Gb[g0 + t]) : nullptr;
+                }
+                a.n_ext = std::min(GROUP, OBGC_PIS_NUM_BGC - g0);
+                a.drift = static_cast<const TC*>(m->drift) + (size_t)g0 * (g.Nz + 1);
+                a.drift_mask = (mask >> g0) & ((1u << GROUP) - 1u);
+                rc = fe->launch(&a, blocks, st);
+            }
             if (rc == OBGC_OK) rc = prof_mark(m, st);
             if (rc != OBGC_OK) break;
             for (int q = 0; q < PNT; q++) { void* tmp = cur[q]; cur[q] = nxt[q]; nxt[q] = tmp; }

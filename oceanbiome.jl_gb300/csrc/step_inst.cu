@@ -27,8 +27,8 @@ typedef float TC_;
 constexpr int V_ = OBGC_INST_V;
 // tracer counts with a kernel: the BGC tracers alone, and followed by the carried T/S (PISCES
 // always carries T and S: 26 slots)
-[[maybe_unused]] constexpr int NT_A = V_ == V_EXTERNAL ? 26 : n_bgc(V_);
-[[maybe_unused]] constexpr int NT_B = V_ == V_NPZD ? 6 : V_ == V_EXTERNAL ? 26 : n_bgc(V_) + 2;
+[[maybe_unused]] constexpr int NT_A = V_ == V_EXTERNAL ? 13 : n_bgc(V_);
+[[maybe_unused]] constexpr int NT_B = V_ == V_NPZD ? 6 : V_ == V_EXTERNAL ? 13 : n_bgc(V_) + 2;
 
 template <int NT>
 int launch_fn(const void* a, int blocks, cudaStream_t st) {

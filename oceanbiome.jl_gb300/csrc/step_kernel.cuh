@@ -56,7 +56,8 @@ struct SubstepArgs {
     const TS* in[MAX_NT];
     TS* out[MAX_NT];
     TC* G[MAX_NT];
-    const TC* ext[MAX_NT];    // V_EXTERNAL: the BGC tendency of slot t (t < n_bgc)
+    const TC* ext[MAX_NT];    // V_EXTERNAL: the BGC tendency of slot t (t < n_ext)
+    int n_ext;                // V_EXTERNAL: slots of this launch with an external tendency
     const TS* u;
     const TS* v;
     const TS* w;
@@ -190,7 +191,7 @@ __device__ __forceinline__ TC vertical_flux(const SubstepArgs<TS, TC>& a, const 
 }
 
 template <int V, int NT, typename TS, typename TC>
-__global__ void __launch_bounds__(STEP_BX * STEP_BY, (sizeof(TC) == 4 && NT <= 12) ? 3 : 1)
+__global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <= 12 ? 3 : NT <= 16 ? 2 : 1)
     substep_kernel(const __grid_constant__ SubstepArgs<TS, TC> a) {
     constexpr int NB = n_bgc(V);
     constexpr int SP = slot_of_P(V);
@@ -210,7 +211,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, (sizeof(TC) == 4 && NT <= 1
     // Sinking tracers advance their vertical stencil in a register window (one new load per
     // level); two window slots per variant (LOBSTER: sPOM, bPOM; NPZD: P, D).  Any other
     // vertically advected tracer, and every tracer when a model w is given, takes the generic path.
-    // PISCES (V_EXTERNAL): POC and GOC, the other four sinking tracers take the generic path.
+    // PISCES (V_EXTERNAL, launched on tracers 0-12 and 13-25): POC and GOC in the first launch,
+    // the other four sinking tracers take the generic path.
     constexpr int WA = V == V_NPZD ? 1 : V == V_EXTERNAL ? 10 : 4, WB = V == V_NPZD ? 4 : V == V_EXTERNAL ? 11 : 5;
     const bool winA = a.w == nullptr && ((a.drift_mask >> WA) & 1u);
     const bool winB = a.w == nullptr && ((a.drift_mask >> WB) & 1u);
@@ -427,7 +429,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, (sizeof(TC) == 4 && NT <= 1
                 if (t == WB) adv += vdB;
                 TC Gb = TC(0);
                 if constexpr (V == V_EXTERNAL) {
-                    if (t < NB) Gb = a.ext[t][idx];
+                    if (t < a.n_ext) Gb = a.ext[t][idx];
                 } else {
                     if (t < NB) Gb = g[slot_name(V, t)];
                 }

@@ -13,7 +13,7 @@ inline bool fused_supported(int V, int NT) {
         case V_LOBSTER_CO: return NT == 10 || NT == 12;
         case V_LOBSTER_O: return NT == 8 || NT == 10;
         case V_NPZD: return NT == 5 || NT == 6;
-        case V_EXTERNAL: return NT == 26;
+        case V_EXTERNAL: return NT == 13;   // PISCES, in two launches of 13 tracers
     }
     return false;
 }

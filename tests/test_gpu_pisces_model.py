@@ -37,8 +37,9 @@ def oracle_model(g, bgc, model, negatives=False):
                       mean_kappa=model.desc.mean_kappa, negatives=O.NEG_SCALE if negatives else O.NEG_NONE)
 
 
-@pytest.mark.parametrize("precision,tol", [("mixed", 1e-12), ("f32", 2e-5)])
+@pytest.mark.parametrize("precision,tol", [("mixed", 2e-5), ("f32", 2e-5)])
 def test_update_state_fields_match_oracle(precision, tol):
+    # light runs in FP32 arithmetic in both precisions (FP64 fields on the mixed path)
     torch, g, bgc, model, vel = pisces_model(precision)
     t = 2 * 86400.0 + 3600.0          # daytime: default_surface_PAR(t) = 100 max(0, cos(pi t / 12 h)) > 0
     model.update_state(t)
