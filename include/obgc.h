@@ -287,6 +287,9 @@ int obgc_abi_version(void);
 const char* obgc_last_error_message(void);
 /* Number of kernels this library has launched in this process (all entry points). */
 int64_t obgc_kernel_launch_count(void);
+/* Measured FP64 FMA rate of the device (GFLOP/s, 2 per FMA): the denominator of the FP64
+ * kernels' rooflines.  Runs a few 10-ms probe launches on `stream` and synchronises it. */
+int obgc_fp64_fma_peak(double* gflops, void* stream);
 
 /* ---------------------------------------------------------------------------------------
  * NutrientsPlanktonDetritus model description (host only, no device work)

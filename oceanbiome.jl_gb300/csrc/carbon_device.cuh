@@ -161,7 +161,7 @@ __host__ __device__ inline CarbSolve solve_H(const obgc_carbon_options& o, doubl
     double x = H0, f, df;
     alk_residual(x, p, f, df);
     int N = 0;
-    bool stalled = false;
+    bool stalled = false, quadratic = false;
     const double lm = o.min_damping, c = o.armijo_constant;
     while (fabs(f) > o.atol && N < o.max_iters && !stalled) {
         const double d = f / df;
@@ -170,20 +170,25 @@ __host__ __device__ inline CarbSolve solve_H(const obgc_carbon_options& o, doubl
             const double lb = x / d;
             lam = lb < 0 ? 1.0 : (lb < 1.0 ? lb : (lb == lb ? 1.0 : lb));
         }
+        // A full step below 1e-9 of H is inside Newton's quadratic region: the iterate it reaches
+        // is exact to FP64 resolution (the next step would be ~1e-18 of H), and the residual there
+        // is rounding noise, where the Armijo test fails at random and backtracking to the minimum
+        // damping only shortens the step.  Take it and stop, without evaluating the residual again.
+        if (lam == 1.0 && fabs(d) <= 1e-9 * fabs(x)) {
+            x -= d;
+            N += 1;
+            quadratic = true;
+            break;
+        }
         double fn, dfn;
         alk_residual(x - lam * d, p, fn, dfn);
         const double sf = f > 0 ? 1.0 : (f < 0 ? -1.0 : 0.0);
-        // A full step below 1e-9 of H is inside Newton's quadratic region: the iterate it reaches
-        // is exact to FP64 resolution (the next step would be ~1e-18 of H), and its residual is
-        // rounding noise, where the Armijo test fails at random and backtracking to the minimum
-        // damping only shortens the step.  Take it and stop.
-        const bool quadratic = lam == 1.0 && fabs(d) <= 1e-9 * fabs(x);
-        while (!quadratic && fabs(fn) >= fabs(f) - c * lam * f * sf && lam > lm) {
+        while (fabs(fn) >= fabs(f) - c * lam * f * sf && lam > lm) {
             lam *= o.damping;
             alk_residual(x - lam * d, p, fn, dfn);
         }
         const double xn = x - lam * d;
-        stalled = quadratic || fabs(xn - x) <= 4e-16 * fabs(x);
+        stalled = fabs(xn - x) <= 4e-16 * fabs(x);
         x = xn;
         f = fn;
         df = dfn;
@@ -194,7 +199,7 @@ __host__ __device__ inline CarbSolve solve_H(const obgc_carbon_options& o, doubl
     r.iters = N;
     // converged: residual below atol, or the iterate stopped moving at a residual that is rounding
     // noise relative to the alkalinity scale
-    r.converged = fabs(f) <= o.atol || (stalled && fabs(f) <= 1e-12 * (fabs(p.Alk) + fabs(p.DIC)) + 1e-30);
+    r.converged = quadratic || fabs(f) <= o.atol || (stalled && fabs(f) <= 1e-12 * (fabs(p.Alk) + fabs(p.DIC)) + 1e-30);
     if (!r.converged || !(x > 0)) {
         // bisection guard on the residual, decreasing in H over [1e-14, 1]
         double lo = 1e-14, hi = 1.0, flo, fhi, dd;

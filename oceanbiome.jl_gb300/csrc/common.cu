@@ -27,6 +27,56 @@ extern "C" int obgc_abi_version(void) { return OBGC_ABI_VERSION; }
 extern "C" const char* obgc_last_error_message(void) { return obgc::g_last_error.c_str(); }
 extern "C" int64_t obgc_kernel_launch_count(void) { return obgc::g_launches.load(); }
 
+namespace obgc {
+// Eight independent FP64 FMA chains per thread: the FP64 pipe's issue rate, for the FP64 kernels'
+// rooflines.  The result is stored only if it takes an impossible value, so the chains stay live.
+__global__ void __launch_bounds__(256) fp64_fma_probe_kernel(double* out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) x[c] = 1e-3 * (threadIdx.x + c);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < 8; c++) x[c] = fma(x[c], a, b);
+    }
+    double sum = 0.0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) sum += x[c];
+    if (sum == -1.0) out[blockIdx.x] = sum;
+}
+}  // namespace obgc
+
+extern "C" int obgc_fp64_fma_peak(double* gflops, void* stream) {
+    if (!gflops) return obgc::fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_fp64_fma_peak: null output");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int dev = 0, nsm = 0;
+    OBGC_CUDA(cudaGetDevice(&dev));
+    OBGC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = nsm * 8, threads = 256, iters = 4096;
+    double* out = nullptr;
+    OBGC_CUDA(cudaMallocAsync(&out, sizeof(double) * blocks, st));
+    cudaEvent_t e0, e1;
+    OBGC_CUDA(cudaEventCreate(&e0));
+    OBGC_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    for (int r = 0; r < 4; r++) {
+        cudaEventRecord(e0, st);
+        obgc::fp64_fma_probe_kernel<<<blocks, threads, 0, st>>>(out, iters, 0.9999999, 1e-7);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0 && (best == 0.f || ms < best)) best = ms;   // the first run warms up
+    }
+    obgc::count_launches(4);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(out, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return obgc::cuda_fail(e, "obgc_fp64_fma_peak");
+    *gflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e9;
+    return OBGC_OK;
+}
+
 // Size and field offsets of the ABI structs, so a binding (ctypes, Julia) can verify its mirror.
 // which: 0 npd_params, 1 twoband, 2 surface, 3 grid, 4 carbon_options, 5 model_desc, 6 fields.
 // out[0] = sizeof, out[1..] = offsets of selected fields.

@@ -282,6 +282,7 @@ def load():
     _sig(lib, "obgc_abi_version", C.c_int)
     _sig(lib, "obgc_last_error_message", C.c_char_p)
     _sig(lib, "obgc_kernel_launch_count", I64)
+    _sig(lib, "obgc_fp64_fma_peak", C.c_int, P(D), VP)
     _sig(lib, "obgc_struct_layout", C.c_int, I32, P(I64), I32)
     _sig(lib, "obgc_npd_preset", C.c_int, I32, P(NPDParams))
     _sig(lib, "obgc_npd_required_tracers", C.c_int, P(NPDParams), P(I32), I32)
@@ -352,7 +353,7 @@ def load():
 
 # Every symbol include/obgc.h declares (checked by the CPU test suite).
 EXPORTED = [
-    "obgc_abi_version", "obgc_last_error_message", "obgc_kernel_launch_count",
+    "obgc_abi_version", "obgc_last_error_message", "obgc_kernel_launch_count", "obgc_fp64_fma_peak",
     "obgc_npd_preset", "obgc_npd_required_tracers", "obgc_npd_drift_velocity",
     "obgc_npd_eval_point", "obgc_npd_tendencies", "obgc_twoband_par", "obgc_multiband_par",
     "obgc_multiband_coefficients", "obgc_euphotic_depth", "obgc_carbon_default_options",
