@@ -305,10 +305,6 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             const bool full5 = (periodic_x || min(i, a.Nx - i) >= 3) && (periodic_y || min(j, a.Ny - j) >= 3);
             __syncthreads();
 
-            TC c[NT];
-#pragma unroll
-            for (int t = 0; t < NT; t++) c[t] = tiles[t * TILE_SZ + (ty + HALO) * TILE_W + tx + HALO];
-
             // west (x) and south (y) faces of this thread's cell for every tracer: one (not
             // unrolled) loop keeps the code inside the instruction cache; in FP32 the two
             // reconstructions run as one packed f32x2 WENO5
@@ -378,6 +374,11 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 }
             }
             __syncthreads();
+
+            // this cell's value of every tracer (read after the face loop: not live across it)
+            TC c[NT];
+#pragma unroll
+            for (int t = 0; t < NT; t++) c[t] = tiles[t * TILE_SZ + (ty + HALO) * TILE_W + tx + HALO];
 
             // window tracers: flux through the face below this cell, divergence, and slide the
             // windows down one level (the next level needs c[k-4])
