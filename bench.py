@@ -54,8 +54,8 @@ def fp64_peak():
 
 # FP64 FLOPs per cell (2 per DFMA + DMUL + DADD) from ncu's sass counters of one launch on these
 # workloads: the pH solve from a cold start (~5 Newton iterations) and PISCES' warm-started Omega
-CARBON_FLOP_PER_CELL = 1787.0
-OMEGA_FLOP_PER_CELL = 1669.0
+CARBON_FLOP_PER_CELL = 1668.0
+OMEGA_FLOP_PER_CELL = 1552.0
 
 
 def algorithmic_bytes_per_update(state_bytes, g_bytes, vel_bytes, n_tracers, n_vel):
