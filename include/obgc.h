@@ -414,6 +414,45 @@ typedef struct obgc_carbon_options {
 
 int obgc_carbon_default_options(obgc_carbon_options* out);
 
+/* ---------------------------------------------------------------------------------------
+ * Air-sea gas exchange (src/Models/GasExchange): the flux k (C_water - C_air) through the
+ * surface face of each column, positive out of the ocean (Oceananigans' top FluxBoundaryCondition,
+ * GasExchange functor gas_exchange.jl:26-39).
+ *   k = k660(u10) / sqrt(Sc(T) / 660) * solubility(T, S)       (gas_transfer_velocity.jl:30-31)
+ *   CO2: C_water = pCO2 of the surface cell's DIC, Alk, T, S (CarbonChemistry, FP64 solve;
+ *        carbon_dioxide_concentration.jl:48-60), C_air in ppmv, solubility = K0(T, S) rho(T, S) / 1000
+ *        (gas_solubility.jl:62-64), flux in mmol C / m2 / s
+ *   O2:  C_water = the surface O2, C_air = air_concentration * beta(T, S) / Tk (Wanninkhof 1992,
+ *        gas_solubility.jl:38-56, evaluated as written there), solubility = 1
+ * ------------------------------------------------------------------------------------- */
+enum obgc_gas { OBGC_GAS_CO2 = 0, OBGC_GAS_O2 = 1 };
+
+typedef struct obgc_gas_exchange {
+    int32_t gas;                 /* enum obgc_gas                                              */
+    int32_t reserved0;
+    double k660[4];              /* k660(u) = k660[0] + k660[1] u + k660[2] u^2 + k660[3] u^3
+                                  * (m/s); default Ho06: (0, 0, 0.266 / 3600 / 100, 0)         */
+    double schmidt[5];           /* Sc(T) = s0 + s1 T + s2 T^2 + s3 T^3 + s4 T^4, T in degC       */
+    double wind_speed;           /* u10 (m/s) when wind_field is NULL (default 2)              */
+    const void* wind_field;      /* (Nx, Ny) dense, grid dtype, or NULL                        */
+    double air_concentration;    /* CO2: ppmv (413); O2: mmol/m3 (9352.7)                      */
+    const void* air_field;       /* (Nx, Ny) dense, grid dtype, or NULL                        */
+    double o2_solubility[6];     /* A1 A2 A3 B1 B2 B3 (OxygenSolubility defaults)              */
+    obgc_carbon_options carbon;  /* the pCO2 solve (output is set to pCO2)                     */
+} obgc_gas_exchange;
+
+/* CarbonDioxideGasExchangeBoundaryCondition() / OxygenGasExchangeBoundaryCondition() defaults
+ * (GasExchange.jl:96-146, schmidt_number.jl, gas_transfer_velocity.jl:53-59). */
+int obgc_gas_exchange_defaults(int32_t gas, obgc_gas_exchange* out);
+/* Flux of every column (Nx, Ny dense, FP64 out) from the surface cells (k = Nz-1) of the 3-D
+ * fields T, S and DIC, Alk (CO2) or O2 (O2; the others may be NULL), of dtype `dtype`. */
+int obgc_gas_exchange_flux(const obgc_gas_exchange* g, const obgc_grid* grid, int32_t dtype, const void* T,
+                           const void* S, const void* DIC, const void* Alk, const void* O2, double* flux,
+                           void* stream);
+/* One column on the host (the same device function), e.g. for a BoxModel-style driver. */
+int obgc_gas_exchange_point(const obgc_gas_exchange* g, double T, double S, double DIC, double Alk, double O2,
+                            double u10, double air, double* flux);
+
 /*
  * Batched FP64 carbonate solve on the device: n cells.  Inputs DIC (mmol/m3), Alk (meq/m3),
  * T (degC), S (psu) of dtype `dtype`; optional (NULL = zero / absent) silicate, phosphate
@@ -500,6 +539,12 @@ int obgc_last_step_timing(const obgc_ctx* ctx, double* total_ms, double* substep
 int obgc_set_profiling(obgc_ctx* ctx, int32_t on);
 /* Vertical segment length (levels) of the fused kernel's work items (default 16). */
 int obgc_set_tiling(obgc_ctx* ctx, int32_t levels_per_item);
+/* Air-sea gas exchange as the top boundary condition of the fused step (obgc_step, obgc_step_graph):
+ * FieldBoundaryConditions(top = CarbonDioxideGasExchangeBoundaryCondition()) on DIC (g->gas CO2;
+ * the model carries DIC, Alk, T and S) or OxygenGasExchangeBoundaryCondition() on O2 (the model
+ * carries O2, T and S).  Each RK3 stage computes the flux of every column from the stage's surface
+ * cells and the surface cell's tendency loses flux / dz.  g = NULL with `gas` clears that gas. */
+int obgc_set_gas_exchange(obgc_ctx* ctx, int32_t gas, const obgc_gas_exchange* g);
 /* Size and selected field offsets of the ABI structs (which: 0 npd_params, 1 twoband,
  * 2 surface, 3 grid, 4 carbon_options, 5 model_desc, 6 fields) for binding self-checks;
  * no counterpart in the reference. */

@@ -48,6 +48,12 @@ __host__ __device__ inline double pressure_log(double a0, double a1, double a2, 
     return (-dV + 0.5 * dk * P) * P * iRT;
 }
 
+// K0 = [CO2*(aq)] / f(CO2): Weiss (1974) (equilibrium_constants.jl:65-80); lT = log(Tk), iT = 1/Tk.
+__host__ __device__ inline double weiss_k0(double Tk, double S, double lT, double iT) {
+    return exp(-60.2409 + (93.4517 * 100) * iT + 23.3585 * (lT - 4.605170185988092) +
+               (0.023517 + (-0.023656 / 100) * Tk + (0.0047036 / 10000) * (Tk * Tk)) * S);
+}
+
 struct CarbConsts {
     double DIC, Alk, boron, sulfate, fluoride, silicate, phosphate;
     double K1, K2, KB, KW, KS, KF, KP1, KP2, KP3, KSi, K0;
@@ -113,9 +119,7 @@ __host__ __device__ inline void equilibrium_constants(double Tk, double S, bool 
     c.KSi = exp(117.385 + -8904.2 * iT + -19.334 * lT + (3.5913 + -458.79 * iT) * sIs + (-1.5998 + 188.74 * iT) * Is +
                 (0.07871 + -12.1652 * iT) * (Is * Is) + lS);
     // K0: Weiss (1974) (:65-80)
-    if (need_K0)
-    c.K0 = exp(-60.2409 + (93.4517 * 100) * iT + 23.3585 * (lT - log(100.0)) +
-               (0.023517 + (-0.023656 / 100) * Tk + (0.0047036 / 10000) * (Tk * Tk)) * S);
+    if (need_K0) c.K0 = weiss_k0(Tk, S, lT, iT);
 }
 
 // Alkalinity residual and its derivative in H (alkalinity_residual.jl:18-75).  The seven

@@ -1,0 +1,89 @@
+// gas.cu — air-sea gas exchange fluxes of every column (GasExchange boundary conditions).
+#include <cstring>
+#include "gas_device.cuh"
+
+namespace obgc {
+
+// One thread per column: the surface cell (k = Nz - 1) of T, S and DIC/Alk or O2.
+template <typename T>
+__global__ void __launch_bounds__(128) gas_exchange_kernel(obgc_gas_exchange g, int Nx, int Ny, int Nz, int64_t sj,
+                                                           int64_t sk, const T* __restrict__ Tc, const T* __restrict__ S,
+                                                           const T* __restrict__ DIC, const T* __restrict__ Alk,
+                                                           const T* __restrict__ O2, const T* __restrict__ wind,
+                                                           const T* __restrict__ air, double* __restrict__ flux) {
+    const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= (int64_t)Nx * Ny) return;
+    const int i = (int)(col % Nx), j = (int)(col / Nx);
+    const int64_t o = i + (int64_t)j * sj + (int64_t)(Nz - 1) * sk;
+    const double u10 = wind ? (double)wind[col] : g.wind_speed;
+    const double ca = air ? (double)air[col] : g.air_concentration;
+    const bool co2 = g.gas == OBGC_GAS_CO2;
+    flux[col] = gas_flux_cell(g, (double)Tc[o], (double)S[o], co2 ? (double)DIC[o] : 0.0, co2 ? (double)Alk[o] : 0.0,
+                              co2 ? 0.0 : (double)O2[o], u10, ca);
+}
+
+template <typename T>
+int launch_gas_exchange(const obgc_gas_exchange* g, const obgc_grid* grid, const void* Tc, const void* S,
+                        const void* DIC, const void* Alk, const void* O2, double* flux, cudaStream_t st) {
+    const int64_t cols = (int64_t)grid->Nx * grid->Ny;
+    gas_exchange_kernel<T><<<(unsigned)((cols + 127) / 128), 128, 0, st>>>(
+        *g, grid->Nx, grid->Ny, grid->Nz, grid->stride_j, grid->stride_k, (const T*)Tc, (const T*)S, (const T*)DIC,
+        (const T*)Alk, (const T*)O2, (const T*)g->wind_field, (const T*)g->air_field, flux);
+    OBGC_LAUNCHED("gas_exchange_kernel");
+    return OBGC_OK;
+}
+template int launch_gas_exchange<float>(const obgc_gas_exchange*, const obgc_grid*, const void*, const void*,
+                                        const void*, const void*, const void*, double*, cudaStream_t);
+template int launch_gas_exchange<double>(const obgc_gas_exchange*, const obgc_grid*, const void*, const void*,
+                                         const void*, const void*, const void*, double*, cudaStream_t);
+
+bool valid_gas(const obgc_gas_exchange* g) {
+    return g && (g->gas == OBGC_GAS_CO2 || g->gas == OBGC_GAS_O2);
+}
+
+}  // namespace obgc
+
+using namespace obgc;
+
+extern "C" int obgc_gas_exchange_defaults(int32_t gas, obgc_gas_exchange* g) {
+    if (!g || (gas != OBGC_GAS_CO2 && gas != OBGC_GAS_O2)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_gas_exchange_defaults: bad argument");
+    std::memset(g, 0, sizeof(*g));
+    g->gas = gas;
+    g->k660[2] = 0.266 / 3600.0 / 100;   // Ho06 (gas_transfer_velocity.jl:53-59)
+    g->wind_speed = 2.0;
+    obgc_carbon_default_options(&g->carbon);
+    g->carbon.output = OBGC_OUT_PCO2;
+    if (gas == OBGC_GAS_CO2) {
+        // CarbonDioxidePolynomialSchmidtNumber (schmidt_number.jl:6-7); 413 ppmv (GasExchange.jl:98)
+        const double s[5] = {2116.8, -136.25, 4.7353, -0.092307, 0.0007555};
+        std::memcpy(g->schmidt, s, sizeof(s));
+        g->air_concentration = 413.0;
+    } else {
+        // OxygenPolynomialSchmidtNumber (schmidt_number.jl:14-15); OxygenSolubility
+        // (gas_solubility.jl:52-53); 9352.7 mmol O2 / m3 (GasExchange.jl:141)
+        const double s[5] = {1920.4, -135.6, 5.2122, -0.10939, 0.00093777};
+        const double a[6] = {-58.3877, 85.8079, 23.8439, -0.034892, 0.015578, -0.0019387};
+        std::memcpy(g->schmidt, s, sizeof(s));
+        std::memcpy(g->o2_solubility, a, sizeof(a));
+        g->air_concentration = 9352.7;
+    }
+    return OBGC_OK;
+}
+
+extern "C" int obgc_gas_exchange_flux(const obgc_gas_exchange* g, const obgc_grid* grid, int32_t dtype, const void* T,
+                                      const void* S, const void* DIC, const void* Alk, const void* O2, double* flux,
+                                      void* stream) {
+    if (!valid_gas(g) || !valid_grid(grid) || !T || !S || !flux || (dtype != OBGC_F32 && dtype != OBGC_F64) ||
+        (g->gas == OBGC_GAS_CO2 && (!DIC || !Alk)) || (g->gas == OBGC_GAS_O2 && !O2))
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_gas_exchange_flux: bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return dtype == OBGC_F32 ? launch_gas_exchange<float>(g, grid, T, S, DIC, Alk, O2, flux, st)
+                             : launch_gas_exchange<double>(g, grid, T, S, DIC, Alk, O2, flux, st);
+}
+
+extern "C" int obgc_gas_exchange_point(const obgc_gas_exchange* g, double T, double S, double DIC, double Alk, double O2,
+                                       double u10, double air, double* flux) {
+    if (!valid_gas(g) || !flux) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_gas_exchange_point: bad argument");
+    *flux = gas_flux_cell(*g, T, S, DIC, Alk, O2, u10, air);
+    return OBGC_OK;
+}

@@ -1,0 +1,38 @@
+// gas_device.cuh — air-sea gas exchange of one column's surface cell (host and device), FP64.
+//
+// GasExchange functor (src/Models/GasExchange/gas_exchange.jl:26-39): flux = k (C_water - C_air),
+// positive out of the ocean, with k = k660(u10) / sqrt(Sc(T) / 660) * solubility(T, S)
+// (gas_transfer_velocity.jl:30-31).
+//   CO2: C_water = pCO2 of the surface DIC, Alk, T, S with silicate = phosphate = 0
+//        (carbon_dioxide_concentration.jl:48-60), solubility = K0(T + 273.15, S) rho(T, S) / 1000
+//        with rho at zero pressure (gas_solubility.jl:58-64).
+//   O2:  C_water = O2, C_air = air * beta / Tk of Wanninkhof92Solubility evaluated as the reference
+//        writes it (gas_solubility.jl:40-50: B2 serves both salinity coefficients), solubility 1.
+#pragma once
+#include "carbon_device.cuh"
+
+namespace obgc {
+
+__host__ __device__ inline double gas_flux_cell(const obgc_gas_exchange& g, double T, double S, double DIC,
+                                                double Alk, double O2, double u10, double air) {
+    const double k660 = g.k660[0] + u10 * (g.k660[1] + u10 * (g.k660[2] + u10 * g.k660[3]));
+    const double Sc = g.schmidt[0] + T * (g.schmidt[1] + T * (g.schmidt[2] + T * (g.schmidt[3] + T * g.schmidt[4])));
+    const double kS = k660 / sqrt(Sc / 660.0);
+    if (g.gas == OBGC_GAS_CO2) {
+        const double Tk = T + 273.15;
+        const double solubility = weiss_k0(Tk, S, log(Tk), 1.0 / Tk) * density_eos80(T, S, 0.0) / 1000.0;
+        obgc_carbon_options o = g.carbon;
+        o.output = OBGC_OUT_PCO2;
+        o.ph_given = 0;
+        o.has_pressure = 0;
+        const double pCO2 = carbon_cell(o, DIC, Alk, T, S, 0.0, 0.0, 0.0, 0.0,
+                                        exp(-2.302585092994046 * o.initial_pH_guess), nullptr, nullptr, nullptr);
+        return kS * solubility * (pCO2 - air);
+    }
+    const double Tk = T + 273.15, Tk_100 = Tk / 100.0;
+    const double* A = g.o2_solubility;
+    const double beta = exp(A[0] + A[1] / Tk_100 + A[2] * log(Tk_100) + S * (A[3] + A[4] * Tk_100 + A[4] * (Tk_100 * Tk_100)));
+    return kS * (O2 - air * (beta / Tk));
+}
+
+}  // namespace obgc

@@ -9,6 +9,11 @@
 
 namespace obgc {
 
+template <typename T>
+int launch_gas_exchange(const obgc_gas_exchange* g, const obgc_grid* grid, const void* Tc, const void* S,
+                        const void* DIC, const void* Alk, const void* O2, double* flux, cudaStream_t st);
+bool valid_gas(const obgc_gas_exchange* g);
+
 // ----------------------------------------------------------------------------- registry
 static std::vector<FusedEntry>& registry() {
     static std::vector<FusedEntry> r;
@@ -122,6 +127,10 @@ struct obgc_ctx {
     void* drift = nullptr;
     uint32_t drift_mask = 0;
     NegativesSpec neg;                  // negative-tracer modifier over the slots
+    // air-sea gas exchange (top boundary condition): [0] CO2 on DIC, [1] O2 on O2
+    bool gas_on[2] = {false, false};
+    obgc_gas_exchange gas[2];
+    double* gas_flux[2] = {nullptr, nullptr};   // (Nx, Ny) per stage
     double* d_time = nullptr;
     DD* partial = nullptr;
     int n_partial = 0;
@@ -154,6 +163,8 @@ static int ctx_free(obgc_ctx* c) {
     if (c->d_time) cudaFree(c->d_time);
     if (c->partial) cudaFree(c->partial);
     if (c->d_budget) cudaFree(c->d_budget);
+    for (int q = 0; q < 2; q++)
+        if (c->gas_flux[q]) cudaFree(c->gas_flux[q]);
     if (c->ev_begin) cudaEventDestroy(c->ev_begin);
     if (c->ev_end) cudaEventDestroy(c->ev_end);
     for (auto e : c->prof_events) cudaEventDestroy(e);
@@ -269,6 +280,32 @@ extern "C" int obgc_set_profiling(obgc_ctx* c, int32_t on) {
     return OBGC_OK;
 }
 
+static int slot_named(const obgc_ctx* c, int name) {
+    for (int t = 0; t < c->NT; t++)
+        if (c->names[t] == name) return t;
+    return -1;
+}
+
+extern "C" int obgc_set_gas_exchange(obgc_ctx* c, int32_t gas, const obgc_gas_exchange* g) {
+    if (!c || (gas != OBGC_GAS_CO2 && gas != OBGC_GAS_O2) || (g && (!valid_gas(g) || g->gas != gas)))
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_gas_exchange: bad argument");
+    const int q = gas == OBGC_GAS_CO2 ? 0 : 1;
+    if (!g) {
+        c->gas_on[q] = false;
+        c->bind_version++;
+        return OBGC_OK;
+    }
+    const bool ok = slot_named(c, OBGC_T) >= 0 && slot_named(c, OBGC_S) >= 0 &&
+                    (gas == OBGC_GAS_CO2 ? slot_named(c, OBGC_DIC) >= 0 && slot_named(c, OBGC_ALK) >= 0
+                                         : slot_named(c, OBGC_O2) >= 0);
+    if (!ok) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_gas_exchange: the model does not carry the tracers this gas needs");
+    if (!c->gas_flux[q]) OBGC_CUDA(cudaMalloc(&c->gas_flux[q], sizeof(double) * (size_t)c->desc.grid.Nx * c->desc.grid.Ny));
+    c->gas[q] = *g;
+    c->gas_on[q] = true;
+    c->bind_version++;   // a captured graph holds the previous flux setup
+    return OBGC_OK;
+}
+
 extern "C" int obgc_set_tiling(obgc_ctx* c, int32_t TZ) {
     if (!c || TZ < 1) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_tiling: bad argument");
     c->TZ = TZ;
@@ -359,6 +396,16 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
             a.gamma = TC(rk3_gamma(stg));
             a.zeta = TC(rk3_zeta(stg));
             a.c_stage = rk3_c(stg);
+            for (int q = 0; q < 2; q++) {
+                a.top_slot1[q] = 0;
+                if (!c->gas_on[q]) continue;
+                auto at = [&](int name) -> const void* { const int t = slot_named(c, name); return t >= 0 ? cur[t] : nullptr; };
+                const int rg = launch_gas_exchange<TS>(&c->gas[q], &grid, at(OBGC_T), at(OBGC_S), at(OBGC_DIC), at(OBGC_ALK),
+                                                       at(OBGC_O2), c->gas_flux[q], st);
+                if (rg != OBGC_OK) return rg;
+                a.top_slot1[q] = slot_named(c, q == 0 ? OBGC_DIC : OBGC_O2) + 1;
+                a.top_flux[q] = c->gas_flux[q];
+            }
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
             int rc = fe->launch(&a, blocks, st);
             if (rc != OBGC_OK) return rc;
@@ -397,7 +444,8 @@ static int dispatch_steps(obgc_ctx* c, double dt, int nsteps, cudaStream_t st, b
 static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     const bool clock = c->desc.surface.kind == OBGC_SURFACE_PAR_DEFAULT;
     const bool neg = c->neg.mode != OBGC_NEGATIVES_NONE;
-    return (int64_t)nsteps * (3 + (clock ? 1 : 0) + (neg ? 3 : 0)) + (nsteps % 2 ? c->NT : 0) + 1 + (neg ? 1 : 0);
+    const int gases = (c->gas_on[0] ? 1 : 0) + (c->gas_on[1] ? 1 : 0);
+    return (int64_t)nsteps * (3 + (clock ? 1 : 0) + (neg ? 3 : 0) + 3 * gases) + (nsteps % 2 ? c->NT : 0) + 1 + (neg ? 1 : 0);
 }
 
 extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {

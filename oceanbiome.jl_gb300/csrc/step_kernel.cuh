@@ -58,6 +58,11 @@ struct SubstepArgs {
     TC* G[MAX_NT];
     const TC* ext[MAX_NT];    // V_EXTERNAL: the BGC tendency of slot t (t < n_ext)
     int n_ext;                // V_EXTERNAL: slots of this launch with an external tendency
+    // surface fluxes (air-sea gas exchange): slot top_slot1[q] - 1 (none when 0, so zeroed arguments
+    // carry no flux) loses top_flux[q][i + j Nx] / dz in its surface cell: the divergence of a flux
+    // through the top face, positive out of the ocean
+    int top_slot1[2];
+    const double* top_flux[2];
     const TS* u;
     const TS* v;
     const TS* w;
@@ -434,7 +439,12 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 } else {
                     if (t < NB) Gb = g[slot_name(V, t)];
                 }
-                const TC Gt = Gb - adv;
+                TC Gt = Gb - adv;
+                if (k == a.Nz - 1) {
+#pragma unroll
+                    for (int q = 0; q < 2; q++)
+                        if (t + 1 == a.top_slot1[q]) Gt -= TC(a.top_flux[q][ic + (int64_t)jc * a.Nx]) * a.inv_dz;
+                }
                 if (active) {
                     TC Un;
                     if (a.first_stage) {

@@ -108,6 +108,15 @@ class CarbonOptions(C.Structure):
                 ("min_damping", C.c_double), ("calcium_ion_per_salinity", C.c_double)]
 
 
+GAS_CO2, GAS_O2 = 0, 1
+
+
+class GasExchange(C.Structure):
+    _fields_ = [("gas", C.c_int32), ("reserved0", C.c_int32), ("k660", C.c_double * 4), ("schmidt", C.c_double * 5),
+                ("wind_speed", C.c_double), ("wind_field", C.c_void_p), ("air_concentration", C.c_double),
+                ("air_field", C.c_void_p), ("o2_solubility", C.c_double * 6), ("carbon", CarbonOptions)]
+
+
 class ModelDesc(C.Structure):
     _fields_ = [("npd", NPDParams), ("light", TwoBandParams), ("surface", Surface),
                 ("grid", Grid), ("precision", C.c_int32), ("advection", C.c_int32),
@@ -282,6 +291,10 @@ def load():
     _sig(lib, "obgc_abi_version", C.c_int)
     _sig(lib, "obgc_last_error_message", C.c_char_p)
     _sig(lib, "obgc_kernel_launch_count", I64)
+    _sig(lib, "obgc_gas_exchange_defaults", C.c_int, I32, P(GasExchange))
+    _sig(lib, "obgc_gas_exchange_flux", C.c_int, P(GasExchange), P(Grid), I32, VP, VP, VP, VP, VP, VP, VP)
+    _sig(lib, "obgc_gas_exchange_point", C.c_int, P(GasExchange), D, D, D, D, D, D, D, P(D))
+    _sig(lib, "obgc_set_gas_exchange", C.c_int, VP, I32, P(GasExchange))
     _sig(lib, "obgc_fp64_fma_peak", C.c_int, P(D), VP)
     _sig(lib, "obgc_struct_layout", C.c_int, I32, P(I64), I32)
     _sig(lib, "obgc_npd_preset", C.c_int, I32, P(NPDParams))
@@ -354,6 +367,7 @@ def load():
 # Every symbol include/obgc.h declares (checked by the CPU test suite).
 EXPORTED = [
     "obgc_abi_version", "obgc_last_error_message", "obgc_kernel_launch_count", "obgc_fp64_fma_peak",
+    "obgc_gas_exchange_defaults", "obgc_gas_exchange_flux", "obgc_gas_exchange_point", "obgc_set_gas_exchange",
     "obgc_npd_preset", "obgc_npd_required_tracers", "obgc_npd_drift_velocity",
     "obgc_npd_eval_point", "obgc_npd_tendencies", "obgc_twoband_par", "obgc_multiband_par",
     "obgc_multiband_coefficients", "obgc_euphotic_depth", "obgc_carbon_default_options",

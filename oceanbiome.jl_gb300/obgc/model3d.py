@@ -24,7 +24,10 @@ class Clock:
 
 class NonhydrostaticModel:
     def __init__(self, grid, biogeochemistry, advection="WENO5", tracers=(), velocities=None,
-                 precision="f32", clock=None, device="cuda"):
+                 precision="f32", clock=None, device="cuda", boundary_conditions=None):
+        """boundary_conditions: {"DIC": CarbonDioxideGasExchangeBoundaryCondition(...),
+        "O2": OxygenGasExchangeBoundaryCondition(...)} as top boundary conditions (the reference's
+        FieldBoundaryConditions(top = ...)); applied by time_step's fused RK3 step."""
         import torch
         self.grid = grid
         self.biogeochemistry = bgc = biogeochemistry
@@ -61,6 +64,12 @@ class NonhydrostaticModel:
         A.check(lib.obgc_create(C.byref(desc), C.byref(ctx)), "obgc_create")
         self._ctx = ctx
         self._bind()
+        self.boundary_conditions = dict(boundary_conditions or {})
+        for name, bc in self.boundary_conditions.items():
+            want = {"DIC": A.GAS_CO2, "O2": A.GAS_O2, "O₂": A.GAS_O2}.get(name)
+            if want is None or bc.gas != want:
+                raise ValueError(f"no gas exchange boundary condition of this kind for tracer {name!r}")
+            A.check(lib.obgc_set_gas_exchange(ctx, bc.gas, C.byref(bc.params)), "obgc_set_gas_exchange")
 
     def _bind(self):
         f = A.Fields()

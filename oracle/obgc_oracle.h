@@ -80,6 +80,8 @@ typedef struct or_model3d {
     int32_t negatives;           /* 0 none, 1 ScaleNegativeTracers, 2 ZeroNegativeTracers */
     int32_t zero_exclude_mask;   /* ZeroNegativeTracers: bit q set = tracer slot q excluded */
     double invalid_fill_value;   /* ScaleNegativeTracers(...; invalid_fill_value)      */
+    const obgc_gas_exchange* gas[2]; /* top boundary conditions: [0] CO2 on DIC, [1] O2 on O2, or NULL;
+                                      * constant wind speed and air concentration */
 } or_model3d;
 /* state: [n_tracers][Nz*Ny*Nx]; u, v, w: [Nz*Ny*Nx] or NULL. */
 void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,
@@ -125,6 +127,15 @@ void or_scale_negatives(int64_t n, int ntr, double* const* fields, const double*
 
 /* ---- PISCES (src/Models/AdvectedPopulations/PISCES) ---- */
 void or_pisces_defaults(obgc_pisces_params* p);
+/* ---- air-sea gas exchange (src/Models/GasExchange) ---- */
+int or_gas_exchange_defaults(int gas, obgc_gas_exchange* g);
+double or_schmidt_number(const double* c, double T);
+double or_transfer_velocity_660(const double* c, double u);
+double or_o2_solubility(const double* A, double T, double S);
+/* flux k (C_water - C_air), positive out of the ocean; u10 and air given per column */
+double or_gas_exchange_flux(const obgc_gas_exchange* g, double T, double S, double DIC, double Alk, double O2,
+                            double u10, double air);
+
 double or_cbm_day_length(double coefficient, double t, double phi);
 /* values [OBGC_PIS_NUM] in the PISCES tracer order, aux [OBGC_PAUX_NUM]; z the cell centre (m),
  * t the model time (s). */

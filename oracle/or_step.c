@@ -228,6 +228,32 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
                     G[(long)q * N + c] = tend;
                 }
             }
+            /* FieldBoundaryConditions(top = GasExchange): the surface cell loses flux / dz
+             * (gas_exchange.jl:26-39 evaluated on the stage's surface values) */
+            for (int gq = 0; gq < 2; gq++) {
+                const obgc_gas_exchange* ge = m->gas[gq];
+                if (!ge) continue;
+                int sT = -1, sS = -1, sD = -1, sA = -1, sO = -1, target = -1;
+                for (int q = 0; q < nt; q++) {
+                    if (m->names[q] == OBGC_T) sT = q;
+                    if (m->names[q] == OBGC_S) sS = q;
+                    if (m->names[q] == OBGC_DIC) sD = q;
+                    if (m->names[q] == OBGC_ALK) sA = q;
+                    if (m->names[q] == OBGC_O2) sO = q;
+                }
+                target = ge->gas == OBGC_GAS_CO2 ? sD : sO;
+                if (sT < 0 || sS < 0 || target < 0 || (ge->gas == OBGC_GAS_CO2 && sA < 0)) continue;
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+                for (long col = 0; col < NN; col++) {
+                    const long c = (long)(Nz - 1) * NN + col;
+                    const double F = or_gas_exchange_flux(ge, state[(long)sT * N + c], state[(long)sS * N + c],
+                                                          sD >= 0 ? state[(long)sD * N + c] : 0.0,
+                                                          sA >= 0 ? state[(long)sA * N + c] : 0.0,
+                                                          sO >= 0 ? state[(long)sO * N + c] : 0.0, ge->wind_speed,
+                                                          ge->air_concentration);
+                    G[(long)target * N + c] -= F / dz;
+                }
+            }
             double g = RK_G[st], z = RK_Z[st];
 #pragma omp parallel for num_threads(nthreads) schedule(static)
             for (long x = 0; x < (long)nt * N; x++) {

@@ -25,7 +25,8 @@ class Model3D(C.Structure):
     _fields_ = [("npd", A.NPDParams), ("light", A.TwoBandParams), ("surface_kind", C.c_int32),
                 ("advection", C.c_int32), ("surface_value", C.c_double), ("grid", A.Grid),
                 ("n_tracers", C.c_int32), ("names", C.c_int32 * 32), ("negatives", C.c_int32),
-                ("zero_exclude_mask", C.c_int32), ("invalid_fill_value", C.c_double)]
+                ("zero_exclude_mask", C.c_int32), ("invalid_fill_value", C.c_double),
+                ("gas", C.POINTER(A.GasExchange) * 2)]
 
 
 class Pisces3D(C.Structure):
@@ -102,6 +103,15 @@ def lib():
         L.or_mixed_layer_mean.argtypes = [C.c_int, P(D), P(D), D]
         L.or_mixed_layer_mean.restype = D
         L.or_pisces_conserved_groups.argtypes = [P(A.PiscesParams), P(I32), P(I32), P(D)]
+        L.or_gas_exchange_defaults.argtypes = [C.c_int, P(A.GasExchange)]
+        L.or_schmidt_number.argtypes = [P(D), D]
+        L.or_schmidt_number.restype = D
+        L.or_transfer_velocity_660.argtypes = [P(D), D]
+        L.or_transfer_velocity_660.restype = D
+        L.or_o2_solubility.argtypes = [P(D), D, D]
+        L.or_o2_solubility.restype = D
+        L.or_gas_exchange_flux.argtypes = [P(A.GasExchange), D, D, D, D, D, D, D]
+        L.or_gas_exchange_flux.restype = D
         L.or_pisces_step3d.argtypes = [P(Pisces3D), P(D), VP, VP, D, D, C.c_int, C.c_int]
         L.or_pisces_update_state3d.argtypes = [P(Pisces3D), P(D), D, P(D), P(D), P(D), C.c_int]
         L.or_conserved_groups.argtypes = [P(A.NPDParams), C.c_int, P(I32), P(I32), P(I32), P(D)]
@@ -259,8 +269,12 @@ def box_run(p, values, dt, nsteps, PAR_stages=None, PAR_const=0.0, t0=0.0):
 
 
 def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_value=0.0, advection=1,
-            negatives=NEG_NONE, zero_exclude=(), invalid_fill_value=float("nan")):
+            negatives=NEG_NONE, zero_exclude=(), invalid_fill_value=float("nan"), gas_exchange=()):
+    """gas_exchange: A.GasExchange structs (CO2 on DIC, O2 on O2) as top boundary conditions."""
     m = Model3D()
+    m._gas_keep = list(gas_exchange)
+    for g in gas_exchange:
+        m.gas[0 if g.gas == A.GAS_CO2 else 1] = C.pointer(g)
     m.negatives = negatives
     m.invalid_fill_value = invalid_fill_value
     m.zero_exclude_mask = sum(1 << q for q, nm in enumerate(names) if nm in zero_exclude)
@@ -413,4 +427,23 @@ def pisces_update_state3d(m, state, t, threads=None):
                                    _dp(xy2), _dp(omega), threads or nthreads())
     shp = (g.Nz, g.Ny, g.Nx)
     return par4.reshape((4,) + shp), xy2.reshape(2, g.Ny, g.Nx), omega.reshape(shp)
+
+
+def gas_exchange_defaults(gas):
+    g = A.GasExchange()
+    assert lib().or_gas_exchange_defaults(gas, C.byref(g)) == 0
+    return g
+
+
+def schmidt_number(g, T):
+    return lib().or_schmidt_number(g.schmidt, T)
+
+
+def o2_solubility(g, T, S):
+    return lib().or_o2_solubility(g.o2_solubility, T, S)
+
+
+def gas_exchange_flux(g, T, S, DIC=0.0, Alk=0.0, O2=0.0, u10=None, air=None):
+    return lib().or_gas_exchange_flux(C.byref(g), T, S, DIC, Alk, O2, g.wind_speed if u10 is None else u10,
+                                      g.air_concentration if air is None else air)
 
