@@ -364,6 +364,7 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.surf_value = TC(c->desc.surface.value);
     a.surf_field = (const TS*)c->desc.surface.field;
     a.d_time = c->d_time;
+    a.neg = c->neg;        // the modifier after every substep, fused into the substep's update
 }
 
 // Enqueue nsteps steps on stream st (no synchronisation).  The state ping-pongs between the bound
@@ -410,10 +411,6 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
             int rc = fe->launch(&a, blocks, st);
             if (rc != OBGC_OK) return rc;
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
-            if (c->neg.mode != OBGC_NEGATIVES_NONE) {
-                rc = launch_negatives(c->neg, sizeof(TS), nxt, grid, st);   // update_state! after the substep
-                if (rc != OBGC_OK) return rc;
-            }
             for (int t = 0; t < c->NT; t++) { void* tmp = cur[t]; cur[t] = nxt[t]; nxt[t] = tmp; }
         }
         if (clock) {
@@ -445,7 +442,7 @@ static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     const bool clock = c->desc.surface.kind == OBGC_SURFACE_PAR_DEFAULT;
     const bool neg = c->neg.mode != OBGC_NEGATIVES_NONE;
     const int gases = (c->gas_on[0] ? 1 : 0) + (c->gas_on[1] ? 1 : 0);
-    return (int64_t)nsteps * (3 + (clock ? 1 : 0) + (neg ? 3 : 0) + 3 * gases) + (nsteps % 2 ? c->NT : 0) + 1 + (neg ? 1 : 0);
+    return (int64_t)nsteps * (3 + (clock ? 1 : 0) + 3 * gases) + (nsteps % 2 ? c->NT : 0) + 1 + (neg ? 1 : 0);
 }
 
 extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {

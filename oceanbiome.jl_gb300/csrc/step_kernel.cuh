@@ -16,6 +16,7 @@
 // extra work is spread evenly.  Blocks loop over work items (persistent grid).
 #pragma once
 #include "light_device.cuh"
+#include "negatives.cuh"
 #include "npd_device.cuh"
 #include "weno_device.cuh"
 #include "weno_x2.cuh"
@@ -63,6 +64,9 @@ struct SubstepArgs {
     // through the top face, positive out of the ocean
     int top_slot1[2];
     const double* top_flux[2];
+    // negative-tracer modifier (update_state!) on the cell's new values, fused into the update
+    // (mode OBGC_NEGATIVES_NONE: off)
+    NegativesSpec neg;
     const TS* u;
     const TS* v;
     const TS* w;
@@ -459,6 +463,10 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (a.write_G) a.G[t][idx] = Gt;
                 }
             }
+            // ScaleNegativeTracers / ZeroNegativeTracers on the values this thread just stored,
+            // the update_state! that follows the substep (negative_tracers.jl:136-276)
+            if (a.neg.mode != OBGC_NEGATIVES_NONE && active)
+                negatives_cell<TS>(a.neg, [&](int q) -> TS& { return a.out[q][idx]; });
         }
     }
 }

@@ -69,13 +69,21 @@ def test_scale_negatives_kernel_matches_oracle(dtype):
     assert not any(np.nanmin(dev[n].cpu().numpy()) < 0 for n in names)
 
 
-def test_fused_step_with_scale_negatives_matches_oracle():
+@pytest.mark.parametrize("mode,precision,tol", [("scale", "f64", 1e-10), ("scale", "mixed", 1e-5),
+                                                ("zero", "f64", 1e-10)])
+def test_fused_step_with_scale_negatives_matches_oracle(mode, precision, tol):
+    # the modifier runs inside the substep's update (after every substep), as update_state! does
     torch = cuda()
-    g = obgc.RectilinearGrid((24, 16, 10), (2400.0, 1600.0, 100.0), ("Periodic", "Periodic", "Bounded"))
-    bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem(), scale_negatives=True)
+    g = obgc.RectilinearGrid((24, 16, 10), (2400.0, 1600.0, 100.0), ("Periodic", "Periodic", "Bounded"),
+                             dtype="f64")
+    if mode == "scale":
+        bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem(), scale_negatives=True)
+    else:
+        bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem(),
+                           modifiers=obgc.ZeroNegativeTracers(exclude=("DOM",)))
     u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=4)
     model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None),
-                                     precision="f64")
+                                     precision=precision)
     init = obgc.lobster_initial_conditions(g, seed=5)
     rng = np.random.default_rng(9)
     init["NH4"] = rng.normal(0.0, 0.05, g.shape)      # negatives to be scaled away
@@ -84,14 +92,17 @@ def test_fused_step_with_scale_negatives_matches_oracle():
     s0 = model.state_array().cpu().numpy()
     obgc.time_step(model, 200.0, nsteps=3)
     got = model.state_array().cpu().numpy()
-    m = O.model3d(bgc.params, g.c_grid(), model.tracer_names, negatives=O.NEG_SCALE)
+    m = O.model3d(bgc.params, g.c_grid(), model.tracer_names, negatives=O.NEG_SCALE if mode == "scale" else O.NEG_ZERO,
+                  zero_exclude=("DOM",) if mode == "zero" else ())
     ref = np.ascontiguousarray(s0.astype(np.float64))
     O.step3d(m, ref, u=u.double().cpu().numpy().ravel().copy(), v=v.double().cpu().numpy().ravel().copy(),
              t=0.0, dt=200.0, nsteps=3)
     nh4 = model.tracer_names.index("NH4")
     assert np.min(got[nh4]) >= 0 and np.min(s0[nh4]) < 0
+    if mode == "zero":
+        assert np.min(got[model.tracer_names.index("DOM")]) < 0      # excluded from zeroing
     errs = {n: rel_err(got[q], ref[q], floor_frac=1e-3) for q, n in enumerate(model.tracer_names)}
-    assert max(errs.values()) < 1e-10, errs
+    assert max(errs.values()) < tol, errs
 
 
 @pytest.mark.parametrize("precision,eps,floor", [("f64", 2.0 ** -53, 1e-12), ("f32", 2.0 ** -24, 1e-4),
