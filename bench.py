@@ -58,6 +58,40 @@ CARBON_FLOP_PER_CELL = 1668.0
 OMEGA_FLOP_PER_CELL = 1552.0
 
 
+def e2e_steps_ms(step, dev, host, nsteps, stream):
+    """End-to-end steps through the public API: every step copies each field in from pinned host
+    memory, steps, and copies each result back.  The read-back runs on a second stream so that a
+    field's read-back overlaps the next step's copy-in of the fields already read back (the two
+    directions of the host link run concurrently); a field is copied in only after its previous
+    read-back.  Returns ms per step (CUDA events on the launching stream, which joins the copy
+    stream before the end event)."""
+    import torch
+    names = list(dev)
+    out_stream = torch.cuda.Stream()
+    done = {n: torch.cuda.Event() for n in names}
+    stepped = torch.cuda.Event()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(nsteps):
+        for n in names:
+            if k > 0:
+                stream.wait_event(done[n])
+            dev[n].copy_(host[n], non_blocking=True)
+        step()
+        stepped.record(stream)
+        out_stream.wait_event(stepped)
+        with torch.cuda.stream(out_stream):
+            for n in names:
+                host[n].copy_(dev[n], non_blocking=True)
+                done[n].record(out_stream)
+    for n in names:
+        stream.wait_event(done[n])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / nsteps
+
+
 def algorithmic_bytes_per_update(state_bytes, g_bytes, vel_bytes, n_tracers, n_vel):
     """Per tracer-cell update (3 substeps): U read x3 + U write x3 (state precision), G write x2 +
     G- read x2 (tendency precision), and n_vel velocity components read x3 shared by all tracers."""
@@ -237,17 +271,9 @@ def run_gpu(args):
     barrier()
     e2e_steps = max(1, min(args.steps, 20))
     h2d = sum(h.numel() * h.element_size() for h in host.values())
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(e2e_steps):
-        for n in names:
-            model.tracers[n].copy_(host[n], non_blocking=True)
-        obgc.time_step(model, DT, nsteps=1, graph=True)
-        for n in names:
-            host[n].copy_(model.tracers[n], non_blocking=True)
-    e1.record(stream)
+    e2e_ms = e2e_steps_ms(lambda: obgc.time_step(model, DT, nsteps=1, graph=True),
+                          {n: model.tracers[n] for n in names}, host, e2e_steps, stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
     e2e_value = N_TRACERS * g.N * world / (e2e_ms / 1e3)
 
     # ---- roofline of the fused substep kernel
@@ -757,16 +783,8 @@ def run_pisces(args):
     torch.cuda.synchronize()
     e2e_steps = max(1, min(args.steps, 10))
     h2d = sum(h.numel() * h.element_size() for h in host.values())
-    e0.record(stream)
-    for _ in range(e2e_steps):
-        for n in A.PISCES_TRACERS:
-            model.tracers[n].copy_(host[n], non_blocking=True)
-        model.time_step(PIS_DT, stream=stream.cuda_stream)
-        for n in A.PISCES_TRACERS:
-            host[n].copy_(model.tracers[n], non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_ms = e2e_steps_ms(lambda: model.time_step(PIS_DT, stream=stream.cuda_stream),
+                          {n: model.tracers[n] for n in A.PISCES_TRACERS}, host, e2e_steps, stream)
 
     # roofline of the dominant phase (algorithmic bytes per cell of one stage, state precision s,
     # tendency precision 4): functor reads 26 tracers + PAR x4 + Omega and writes 24 tendencies;

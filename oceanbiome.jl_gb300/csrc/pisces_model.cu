@@ -236,7 +236,7 @@ int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t 
     a.sj = g.stride_j; a.sk = g.stride_k;
     a.dx = TC(g.Lx / g.Nx); a.dy = TC(g.Ly / g.Ny); a.dz = TC(g.Lz / g.Nz); a.Lz = TC(g.Lz);
     a.inv_dx = TC(g.Nx / g.Lx); a.inv_dy = TC(g.Ny / g.Ly); a.inv_dz = TC(g.Nz / g.Lz);
-    a.TZ = g.Nz < 16 ? g.Nz : 16;
+    a.TZ = g.Nz < 8 ? g.Nz : 8;
     a.nseg = (g.Nz + a.TZ - 1) / a.TZ;
     a.ntx = (g.Nx + STEP_BX - 1) / STEP_BX;
     a.nty = (g.Ny + STEP_BY - 1) / STEP_BY;

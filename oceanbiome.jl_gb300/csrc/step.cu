@@ -135,7 +135,7 @@ struct obgc_ctx {
     DD* partial = nullptr;
     int n_partial = 0;
     double* d_budget = nullptr;
-    int TZ = 16;
+    int TZ = 8;                         // levels per work item (measured best at 256x256x64)
     int blocks = 0;
     bool bound = false;
     // graph replay
