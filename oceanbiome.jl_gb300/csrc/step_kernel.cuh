@@ -382,12 +382,12 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     fy[t][STEP_BY][cc] = Fe;
                 }
             }
-            __syncthreads();
-
-            // this cell's value of every tracer (read after the face loop: not live across it)
+            // this cell's value of every tracer: read after the face loop (not live across it) and
+            // before the barrier that lets the next level's staging overwrite the tiles
             TC c[NT];
 #pragma unroll
             for (int t = 0; t < NT; t++) c[t] = tiles[t * TILE_SZ + (ty + HALO) * TILE_W + tx + HALO];
+            __syncthreads();
 
             // window tracers: flux through the face below this cell, divergence, and slide the
             // windows down one level (the next level needs c[k-4])
