@@ -86,6 +86,19 @@ struct SubstepArgs {
 template <typename TS, typename TC>
 __device__ __forceinline__ TC ld(const TS* p, int64_t i) { return TC(__ldg(p + i)); }
 
+// Asynchronous global -> shared copy of one 4- or 8-byte element (cp.async, sm_80+): no register
+// staging; completed by cp_async_wait_all() before the barrier that publishes the shared data.
+template <typename E>
+__device__ __forceinline__ void cp_async_elem(E* smem, const E* gmem) {
+    static_assert(sizeof(E) == 4 || sizeof(E) == 8, "cp.async element of 4 or 8 bytes");
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (sizeof(E) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // WENO5 of the upwind stencil: the five values are selected by the velocity sign first, so lanes
 // of a warp with opposite signs still run one reconstruction.
 template <typename TC>
@@ -227,6 +240,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     const bool winB = a.w == nullptr && ((a.drift_mask >> WB) & 1u);
     const uint32_t gen_mask = a.w != nullptr ? 0xffffffffu : (a.drift_mask & ~((1u << WA) | (1u << WB)));
     const bool any_generic = (gen_mask & ((1u << NT) - 1u)) != 0u;
+    // previous-stage tendencies staged in shared memory (the generic-drift buffer, when unused)
+    const bool gm_smem = !any_generic && !a.first_stage;
 
     TC PAR0 = TC(0);
     if constexpr (V != V_EXTERNAL) {
@@ -296,15 +311,23 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
         for (int k = k_top; k >= k_bot; --k) {
             const int64_t idx = col + (int64_t)k * a.sk;
             const int64_t kofs = (int64_t)k * a.sk;
-            // stage every tracer's tile and halo for this level: all loads in flight together
+            // stage every tracer's tile and halo for this level: all loads in flight together (FP32:
+            // asynchronous copies, no registers), and, from the second stage on, the cell's previous
+            // tendencies into the generic-drift buffer when no tracer uses it
 #pragma unroll
             for (int t = 0; t < NT; t++) {
                 const TS* __restrict__ base = a.in[t] + kofs;
                 TC* tl = tiles + t * TILE_SZ;
 #pragma unroll
                 for (int q = 0; q < TILE_LOADS; q++)
-                    if (q < TILE_LOADS - 1 || tid + q * NTH < TILE_SZ) tl[tid + q * NTH] = ld<TS, TC>(base, toff[q]);
+                    if (q < TILE_LOADS - 1 || tid + q * NTH < TILE_SZ) {
+                        if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) cp_async_elem(tl + tid + q * NTH, base + toff[q]);
+                        else tl[tid + q * NTH] = ld<TS, TC>(base, toff[q]);
+                    }
+                if (gm_smem) cp_async_elem<TC>(vdv + t * NTH + tid, a.G[t] + idx);
             }
+            if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) cp_async_wait_all();
+            else if (gm_smem) cp_async_wait_all();
             const int64_t rowb = (int64_t)jc * a.sj + kofs;
             const int64_t cb = ic + kofs;
             const bool xok = !a.flat_x && i <= a.Nx && j < a.Ny;
@@ -454,7 +477,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (a.first_stage) {
                         Un = a.dt * a.gamma * Gt;
                     } else {
-                        const TC Gm = a.G[t][idx];
+                        const TC Gm = gm_smem ? vdv[t * NTH + tid] : a.G[t][idx];
                         Un = a.dt * (a.gamma * Gt + a.zeta * Gm);
                     }
                     // accumulate in the storage precision (FP64 for the mixed path)
