@@ -95,6 +95,10 @@ __device__ __forceinline__ void cp_async_elem(E* smem, const E* gmem) {
     if constexpr (sizeof(E) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
     else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
 }
+// The same with the shared-space address given directly (constant offsets fold into the instruction).
+__device__ __forceinline__ void cp_async4_at(unsigned smem_addr, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
@@ -242,6 +246,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     const bool any_generic = (gen_mask & ((1u << NT) - 1u)) != 0u;
     // previous-stage tendencies staged in shared memory (the generic-drift buffer, when unused)
     const bool gm_smem = !any_generic && !a.first_stage;
+    // shared-space address of this thread's first tile element
+    const unsigned tiles_s = (unsigned)__cvta_generic_to_shared(tiles) + 4u * (unsigned)tid;
 
     TC PAR0 = TC(0);
     if constexpr (V != V_EXTERNAL) {
@@ -321,7 +327,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 #pragma unroll
                 for (int q = 0; q < TILE_LOADS; q++)
                     if (q < TILE_LOADS - 1 || tid + q * NTH < TILE_SZ) {
-                        if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) cp_async_elem(tl + tid + q * NTH, base + toff[q]);
+                        if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4)
+                            cp_async4_at(tiles_s + 4u * (unsigned)(t * TILE_SZ + q * NTH), base + toff[q]);
                         else tl[tid + q * NTH] = ld<TS, TC>(base, toff[q]);
                     }
                 if (gm_smem) cp_async_elem<TC>(vdv + t * NTH + tid, a.G[t] + idx);
