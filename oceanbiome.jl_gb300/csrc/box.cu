@@ -22,13 +22,20 @@ __global__ void __launch_bounds__(128) box_kernel(obgc_npd_params p0, const obgc
         Gm[q] = T(0);
     }
     int rec = 0;
+    // Q10^(T/10): recomputed only when the box's temperature changes (it has no tendency, so never
+    // within a run unless the caller changes it between runs) — the same value, without a pow per stage
+    T Tlast = v[OBGC_T], Lt = p.q10 ? t_pow(p.Q10, Tlast / T(10)) : T(1);
     for (int s = 0; s < nsteps; s++) {
 #pragma unroll
         for (int stg = 0; stg < 3; stg++) {
             const T par = PAR ? T(PAR[(int64_t)(3 * s + stg) * n + m]) : T(par_const);
 #pragma unroll
             for (int q = 0; q < OBGC_NUM_NAMED; q++) G[q] = T(0);
-            npd_tendencies<V_RUNTIME, T>(p, v, par, G);
+            if (v[OBGC_T] != Tlast) {
+                Tlast = v[OBGC_T];
+                Lt = p.q10 ? t_pow(p.Q10, Tlast / T(10)) : T(1);
+            }
+            npd_tendencies<V_RUNTIME, T>(p, v, par, G, &Lt);
             const T g = T(rk3_gamma(stg)), z = T(rk3_zeta(stg));
 #pragma unroll
             for (int q = 0; q < OBGC_NUM_NAMED; q++) {

@@ -91,8 +91,10 @@ __host__ __device__ __forceinline__ T qdiv(T a, T b) {
     return a / b;
 }
 
+// Lt_given: the temperature factor Q10^(T/10) already evaluated for this v[OBGC_T] (a caller whose
+// temperature does not change between calls, such as a box model, saves the pow), or NULL.
 template <int V, typename T>
-__host__ __device__ inline void npd_tendencies(const NPDParamsT<T>& p, const T* v, T PAR, T* G) {
+__host__ __device__ inline void npd_tendencies(const NPDParamsT<T>& p, const T* v, T PAR, T* G, const T* Lt_given = nullptr) {
     const int nut = V >= 0 ? vnut(V) : p.nutrients;
     const int det = V >= 0 ? vdet(V) : p.detritus;
     const int carb = V >= 0 ? vcarb(V) : p.carbonate_system;
@@ -139,7 +141,7 @@ __host__ __device__ inline void npd_tendencies(const NPDParamsT<T>& p, const T* 
     }
     const T Ll = p.light_limitation == OBGC_LIGHT_MONDO ? qdiv(PAR, p.kPAR + PAR)
                                                           : PAR / t_sqrt(PAR * PAR + p.kPAR * p.kPAR);
-    const T Lt = q10 ? t_pow(p.Q10, v[OBGC_T] / T(10)) : one;
+    const T Lt = q10 ? (Lt_given ? *Lt_given : t_pow(p.Q10, v[OBGC_T] / T(10))) : one;
     const T muP = p.mu0 * Ll * Ln * Lt * P;
 
     // wastes (plankton.jl:292-349)
