@@ -264,6 +264,11 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
         const int k_bot = max(0, k_top - a.TZ + 1);
         const int i = i0 + tx, j = j0 + ty;
         const bool active = i < a.Nx && j < a.Ny;
+        // tile rows past the grid (a 2-D grid with Flat y uses one of the eight) skip the arithmetic
+        // (warp-uniform: a warp is one row); the row just past the last cell row still owns the y
+        // faces of the tile's northern edge
+        const bool row_cells = j < a.Ny;
+        const bool row_faces = row_cells || (j == a.Ny && !a.flat_y);
         const int ic = min(i, a.Nx - 1), jc = min(j, a.Ny - 1);
         const int64_t col = ic + (int64_t)jc * a.sj;
         const TC P0 = (V != V_EXTERNAL && a.surf_kind == OBGC_SURFACE_PAR_FIELD) ? TC(a.surf_field[ic + (int64_t)jc * a.Nx])
@@ -348,7 +353,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             // unrolled) loop keeps the code inside the instruction cache; in FP32 the two
             // reconstructions run as one packed f32x2 WENO5
 #pragma unroll 1
-            for (int t = 0; t < NT; t++) {
+            for (int t = 0; t < (row_faces ? NT : 0); t++) {
                 const TC* tl = tiles + t * TILE_SZ;
                 const TC* xs = tl + (ty + HALO) * TILE_W + tx;   // c[i-3 .. i+2] along x
                 const TC* ys = tl + ty * TILE_W + tx + HALO;     // c[j-3 .. j+2] along y
@@ -418,6 +423,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 #pragma unroll
             for (int t = 0; t < NT; t++) c[t] = tiles[t * TILE_SZ + (ty + HALO) * TILE_W + tx + HALO];
             __syncthreads();
+            if (!row_cells) continue;   // no cell on this row: nothing below reads its registers
 
             // window tracers: flux through the face below this cell, divergence, and slide the
             // windows down one level (the next level needs c[k-4])
