@@ -853,6 +853,8 @@ def run_front(args):
     g = obgc.RectilinearGrid((160, 32), (10000.0, 500.0), ("Bounded", "Flat", "Bounded"))
     bgc = obgc.NPZD(g)
     model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, precision="f64")
+    if args.tz:
+        model.set_tiling(args.tz)
     init = obgc.npzd_front_initial_conditions(g)
     dt, nsteps = 50.0, 2000
     obgc.set_(model, **init)

@@ -537,7 +537,7 @@ int obgc_last_step_timing(const obgc_ctx* ctx, double* total_ms, double* substep
                           int64_t* launches);
 /* Bracket every fused substep launch of obgc_step with CUDA events (off by default). */
 int obgc_set_profiling(obgc_ctx* ctx, int32_t on);
-/* Vertical segment length (levels) of the fused kernel's work items (default 8). */
+/* Vertical segment length (levels) of the fused kernel's work items (default: chosen per grid, 8 when the grid has enough tiles to fill the GPU, down to 2). */
 int obgc_set_tiling(obgc_ctx* ctx, int32_t levels_per_item);
 /* Air-sea gas exchange as the top boundary condition of the fused step (obgc_step, obgc_step_graph):
  * FieldBoundaryConditions(top = CarbonDioxideGasExchangeBoundaryCondition()) on DIC (g->gas CO2;

@@ -135,7 +135,7 @@ struct obgc_ctx {
     DD* partial = nullptr;
     int n_partial = 0;
     double* d_budget = nullptr;
-    int TZ = 8;                         // levels per work item (measured best at 256x256x64)
+    int TZ = 0;                         // levels per work item; 0: chosen per grid (fill_args)
     int blocks = 0;
     bool bound = false;
     // graph replay
@@ -347,7 +347,16 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.sj = g.stride_j; a.sk = g.stride_k;
     a.dx = TC(g.Lx / g.Nx); a.dy = TC(g.Ly / g.Ny); a.dz = TC(g.Lz / g.Nz); a.Lz = TC(g.Lz);
     a.inv_dx = TC(g.Nx / g.Lx); a.inv_dy = TC(g.Ny / g.Ly); a.inv_dz = TC(g.Nz / g.Lz);
-    a.TZ = c->TZ < g.Nz ? c->TZ : g.Nz;
+    if (c->TZ > 0) {
+        a.TZ = c->TZ < g.Nz ? c->TZ : g.Nz;
+    } else {
+        // 8 levels per item (best at 256x256x64), fewer when the grid has too few tiles to fill the
+        // GPU: a 160x32 2-D grid has 5 tiles, and 2-level items gave it the shortest step
+        const int tiles = ((g.Nx + STEP_BX - 1) / STEP_BX) * ((g.Ny + STEP_BY - 1) / STEP_BY);
+        int tz = 8;
+        while (tz > 2 && (int64_t)tiles * ((g.Nz + tz - 1) / tz) < c->blocks) tz /= 2;
+        a.TZ = tz < g.Nz ? tz : g.Nz;
+    }
     a.nseg = (g.Nz + a.TZ - 1) / a.TZ;
     a.ntx = (g.Nx + STEP_BX - 1) / STEP_BX;
     a.nty = (g.Ny + STEP_BY - 1) / STEP_BY;
