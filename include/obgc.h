@@ -410,6 +410,10 @@ typedef struct obgc_carbon_options {
     double armijo_constant;      /* 0.5                                                       */
     double min_damping;          /* 0.5^10                                                    */
     double calcium_ion_per_salinity; /* 0.0103/35 (calcite_concentration.jl:78)             */
+    int32_t saturation_mineral;  /* Omega's solubility product (the CarbonChemistry's
+                                  * calcite_solubility): 0 KSP_calcite, 1 KSP_aragonite
+                                  * (equilibrium_constants.jl:740-850)                         */
+    int32_t reserved0;
 } obgc_carbon_options;
 
 int obgc_carbon_default_options(obgc_carbon_options* out);

@@ -264,10 +264,13 @@ __host__ __device__ inline double carbon_cell(const obgc_carbon_options& o, doub
         const double d2 = 1.0 + c.K1 * c.K2 / d1;
         const double co3 = c.DIC * c.K1 * c.K2 / d1 / d2;
         if (o.output == OBGC_OUT_CARBONATE) return co3;
-        // KSP_calcite (equilibrium_constants.jl:740-805; log10(T) as in the reference)
-        const double pc = hasP ? pressure_log(-48.76, 0.5304, -0.0, -0.01176, 0.0003692, Tk, P, c.iRT) : 0.0;
-        const double lnK = -171.9065 + -0.077993 * Tk + 2839.319 * c.iT + 71.595 * (c.lT * 0.4342944819032518) +
-                           (-0.77712 + 0.0028426 * Tk + 178.34 * c.iT) * c.sS + -0.07711 * S + 0.0041249 * S * c.sS;
+        // KSP_calcite / KSP_aragonite (equilibrium_constants.jl:740-850; log10(T) as in the reference)
+        const bool arag = o.saturation_mineral == 1;
+        const double pc = hasP ? pressure_log(arag ? -45.96 : -48.76, 0.5304, -0.0, -0.01176, 0.0003692, Tk, P, c.iRT) : 0.0;
+        const double lnK = arag ? -171.945 + -0.077993 * Tk + 2903.293 * c.iT + 71.595 * (c.lT * 0.4342944819032518) +
+                                      (-0.068393 + 0.0017276 * Tk + 88.135 * c.iT) * c.sS + -0.10018 * S + 0.0059415 * S * c.sS
+                                : -171.9065 + -0.077993 * Tk + 2839.319 * c.iT + 71.595 * (c.lT * 0.4342944819032518) +
+                                      (-0.77712 + 0.0028426 * Tk + 178.34 * c.iT) * c.sS + -0.07711 * S + 0.0041249 * S * c.sS;
         const double KSP = exp(2.302585092994046 * lnK + pc);
         return o.calcium_ion_per_salinity * S * co3 / KSP;
     }

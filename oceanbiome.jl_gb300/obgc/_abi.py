@@ -105,7 +105,8 @@ class CarbonOptions(C.Structure):
                 ("ph_given", C.c_int32), ("max_iters", C.c_int32), ("warm_start", C.c_int32),
                 ("density_value", C.c_double), ("initial_pH_guess", C.c_double),
                 ("atol", C.c_double), ("damping", C.c_double), ("armijo_constant", C.c_double),
-                ("min_damping", C.c_double), ("calcium_ion_per_salinity", C.c_double)]
+                ("min_damping", C.c_double), ("calcium_ion_per_salinity", C.c_double),
+                ("saturation_mineral", C.c_int32), ("reserved0", C.c_int32)]
 
 
 GAS_CO2, GAS_O2 = 0, 1

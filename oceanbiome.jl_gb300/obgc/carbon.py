@@ -17,7 +17,9 @@ _OUTPUTS = {"fCO2": A.OUT_FCO2, "fCOâ‚‚": A.OUT_FCO2, "pCO2": A.OUT_PCO2, "pCOâ‚
 class CarbonChemistry:
     """Carbon chemistry model; `density` is None for EOS-80 or a constant density (kg/m3)."""
 
-    def __init__(self, density=None, max_iters=100, atol=1e-20, initial_pH_guess=8.0):
+    def __init__(self, density=None, max_iters=100, atol=1e-20, initial_pH_guess=8.0, calcite_solubility="calcite"):
+        """calcite_solubility: "calcite" (KSP_calcite, the default) or "aragonite" (KSP_aragonite):
+        the solubility product of the saturation state Omega."""
         lib = A.load()
         self.options = A.CarbonOptions()
         A.check(lib.obgc_carbon_default_options(C.byref(self.options)), "obgc_carbon_default_options")
@@ -26,6 +28,9 @@ class CarbonChemistry:
         self.options.initial_pH_guess = initial_pH_guess
         if density is not None:
             self.options.density, self.options.density_value = A.DENSITY_CONSTANT, float(density)
+        if calcite_solubility not in ("calcite", "aragonite"):
+            raise ValueError("calcite_solubility is 'calcite' or 'aragonite'")
+        self.options.saturation_mineral = int(calcite_solubility == "aragonite")
 
     def __repr__(self):
         return "`CarbonChemistry` model which solves for pCOâ‚‚ and pH"

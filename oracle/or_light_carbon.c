@@ -352,7 +352,8 @@ int or_carbon_chemistry(const obgc_carbon_options* o, double DIC, double Alk, do
         double d2 = 1.0 + p.K1 * p.K2 / d1;
         double co3 = DIC * p.K1 * p.K2 / d1 / d2;
         if (o->output == OBGC_OUT_CARBONATE) { *out = co3; return 0; }
-        double KSP = or_equilibrium_constant(OR_KSP_CALCITE, T_c + 273.15, S, hasP, P);
+        double KSP = or_equilibrium_constant(o->saturation_mineral == 1 ? OR_KSP_ARAGONITE : OR_KSP_CALCITE, T_c + 273.15, S,
+                                             hasP, P);
         double Ca = 0.0103 * S / 35;
         *out = Ca * co3 / KSP;
         return 0;

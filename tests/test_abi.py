@@ -36,7 +36,7 @@ def test_every_declared_symbol_is_exported():
     (1, A.TwoBandParams, ["chlorophyll_red_exponent", "pigment_ratio", "phytoplankton_chlorophyll_ratio"]),
     (2, A.Surface, ["value", "field", None]),
     (3, A.Grid, ["Lx", "stride_j", "stride_k"]),
-    (4, A.CarbonOptions, ["density_value", "atol", "calcium_ion_per_salinity"]),
+    (4, A.CarbonOptions, ["density_value", "atol", "saturation_mineral"]),
     (5, A.ModelDesc, ["surface", "grid", "invalid_fill_value"]),
     (6, A.Fields, ["passive", "u", "G"]),
     (7, A.ColumnSpec, ["dz", "pulse_step", "pulse_amount"]),

@@ -112,3 +112,21 @@ def test_multiband_coefficients_match_oracle():
         np.testing.assert_allclose(a, b, rtol=1e-15)
     with pytest.raises(ValueError):
         obgc.MultiBandPhotosyntheticallyActiveRadiation(surface_PAR_division=[0.5, 0.2, 0.2])
+
+
+def test_aragonite_saturation_matches_oracle():
+    # CarbonChemistry(calcite_solubility = KSP_aragonite()): Omega against aragonite, with and without
+    # the depth pressure; the aragonite / calcite ratio is KSP_calcite / KSP_aragonite
+    import oracle as O
+    cc_a = obgc.CarbonChemistry(calcite_solubility="aragonite")
+    cc_c = obgc.CarbonChemistry()
+    for (DIC, Alk, T, S, P) in [(2100.0, 2350.0, 12.0, 35.0, None), (2200.0, 2400.0, 4.0, 34.5, 150.0)]:
+        oa = cc_a(DIC, T, S, Alk=Alk, P=P, output="Omega")
+        oc = cc_c(DIC, T, S, Alk=Alk, P=P, output="Omega")
+        ref = O.carbon_chemistry(DIC, T, S, Alk=Alk, P=P, output=A.OUT_OMEGA, saturation_mineral=1)
+        assert oa == pytest.approx(ref, rel=1e-12)
+        Tk = T + 273.15
+        ratio = O.K(O.KSP_CALCITE, Tk, S, P) / O.K(O.KSP_ARAGONITE, Tk, S, P)
+        assert oa / oc == pytest.approx(ratio, rel=1e-12)
+    with pytest.raises(ValueError):
+        obgc.CarbonChemistry(calcite_solubility="dolomite")
