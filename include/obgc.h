@@ -549,6 +549,12 @@ int obgc_set_tiling(obgc_ctx* ctx, int32_t levels_per_item);
  * carries O2, T and S).  Each RK3 stage computes the flux of every column from the stage's surface
  * cells and the surface cell's tendency loses flux / dz.  g = NULL with `gas` clears that gas. */
 int obgc_set_gas_exchange(obgc_ctx* ctx, int32_t gas, const obgc_gas_exchange* g);
+/* closure = ScalarDiffusivity(κ) (explicit time discretization) on every tracer of the fused step:
+ * a horizontal diffusivity kappa_h (m2/s, x and y faces) and a vertical one, kappa_z constant or
+ * kappa_z_faces[Nz + 1] (face f below cell f; the bottom and top faces are walls and carry no
+ * flux), added to the advective face fluxes (VerticalScalarDiffusivity: kappa_h = 0;
+ * HorizontalScalarDiffusivity: kappa_z = 0).  Zero everywhere switches it off. */
+int obgc_set_diffusivity(obgc_ctx* ctx, double kappa_h, double kappa_z, const double* kappa_z_faces);
 /* Size and selected field offsets of the ABI structs (which: 0 npd_params, 1 twoband,
  * 2 surface, 3 grid, 4 carbon_options, 5 model_desc, 6 fields) for binding self-checks;
  * no counterpart in the reference. */

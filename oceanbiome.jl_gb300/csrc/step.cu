@@ -131,6 +131,10 @@ struct obgc_ctx {
     bool gas_on[2] = {false, false};
     obgc_gas_exchange gas[2];
     double* gas_flux[2] = {nullptr, nullptr};   // (Nx, Ny) per stage
+    // ScalarDiffusivity (explicit): horizontal kappa, and kappa / dz^2 at the Nz + 1 faces (device,
+    // compute precision), or nullptr
+    double kappa_h = 0.0;
+    void* kzz = nullptr;
     double* d_time = nullptr;
     DD* partial = nullptr;
     int n_partial = 0;
@@ -165,6 +169,7 @@ static int ctx_free(obgc_ctx* c) {
     if (c->d_budget) cudaFree(c->d_budget);
     for (int q = 0; q < 2; q++)
         if (c->gas_flux[q]) cudaFree(c->gas_flux[q]);
+    if (c->kzz) cudaFree(c->kzz);
     if (c->ev_begin) cudaEventDestroy(c->ev_begin);
     if (c->ev_end) cudaEventDestroy(c->ev_end);
     for (auto e : c->prof_events) cudaEventDestroy(e);
@@ -306,6 +311,34 @@ extern "C" int obgc_set_gas_exchange(obgc_ctx* c, int32_t gas, const obgc_gas_ex
     return OBGC_OK;
 }
 
+extern "C" int obgc_set_diffusivity(obgc_ctx* c, double kappa_h, double kappa_z, const double* kappa_z_faces) {
+    if (!c || !(kappa_h >= 0) || !(kappa_z >= 0)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_diffusivity: bad argument");
+    const obgc_grid& g = c->desc.grid;
+    const int Nz = g.Nz;
+    std::vector<double> k(Nz + 1, 0.0);
+    bool any = false;
+    const double idz2 = (double)Nz * Nz / (g.Lz * g.Lz);
+    for (int f = 1; f < Nz; f++) {   // the bottom (0) and top (Nz) faces are walls
+        const double kf = kappa_z_faces ? kappa_z_faces[f] : kappa_z;
+        if (!(kf >= 0)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_diffusivity: negative diffusivity");
+        k[f] = kf * idz2;
+        any = any || kf > 0;
+    }
+    if (c->kzz) { cudaFree(c->kzz); c->kzz = nullptr; }
+    if (any) {
+        OBGC_CUDA(cudaMalloc(&c->kzz, c->tc * (Nz + 1)));
+        if (c->tc == 4) {
+            std::vector<float> kf(k.begin(), k.end());
+            OBGC_CUDA(cudaMemcpy(c->kzz, kf.data(), 4 * (Nz + 1), cudaMemcpyHostToDevice));
+        } else {
+            OBGC_CUDA(cudaMemcpy(c->kzz, k.data(), 8 * (Nz + 1), cudaMemcpyHostToDevice));
+        }
+    }
+    c->kappa_h = kappa_h;
+    c->bind_version++;
+    return OBGC_OK;
+}
+
 extern "C" int obgc_set_tiling(obgc_ctx* c, int32_t TZ) {
     if (!c || TZ < 1) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_tiling: bad argument");
     c->TZ = TZ;
@@ -374,6 +407,9 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.surf_field = (const TS*)c->desc.surface.field;
     a.d_time = c->d_time;
     a.neg = c->neg;        // the modifier after every substep, fused into the substep's update
+    a.kh_dx = g.topology_x == OBGC_FLAT ? TC(0) : TC(c->kappa_h * g.Nx / g.Lx);
+    a.kh_dy = g.topology_y == OBGC_FLAT ? TC(0) : TC(c->kappa_h * g.Ny / g.Ly);
+    a.kzz = (const TC*)c->kzz;
 }
 
 // Enqueue nsteps steps on stream st (no synchronisation).  The state ping-pongs between the bound

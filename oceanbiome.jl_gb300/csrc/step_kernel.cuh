@@ -67,6 +67,11 @@ struct SubstepArgs {
     // negative-tracer modifier (update_state!) on the cell's new values, fused into the update
     // (mode OBGC_NEGATIVES_NONE: off)
     NegativesSpec neg;
+    // ScalarDiffusivity with explicit time stepping: horizontal kh / dx and kh / dy fold a diffusive
+    // flux -kh dc/dx into every x / y face flux (zero at Bounded walls); vertical: kzz[f] = kappa_f /
+    // dz^2 at the Nz + 1 faces (zero at the bottom and top walls), or NULL for none
+    TC kh_dx, kh_dy;
+    const TC* kzz;
     const TS* u;
     const TS* v;
     const TS* w;
@@ -180,6 +185,14 @@ __device__ __forceinline__ TC tile_face_flux(const TC* s, int st, bool periodic,
     else if (b == 1) r = pos ? s[2 * st] : s[3 * st];
     else r = TC(0);
     return U * r;
+}
+
+// Diffusive flux -coef (c[f] - c[f-1]) through face f of a line of N cells (s as in tile_face_flux:
+// s[2 st] = c[f-1], s[3 st] = c[f]); zero at the walls of a bounded line.
+template <typename TC>
+__device__ __forceinline__ TC tile_diff_flux(const TC* s, int st, bool periodic, int f, int N, TC coef) {
+    if (coef == TC(0) || (!periodic && (f <= 0 || f >= N))) return TC(0);
+    return -coef * (s[3 * st] - s[2 * st]);
 }
 
 // Vertical face flux from a window w0..w5 = c[f-3 .. f+2] (same order reduction and wall rule as
@@ -372,15 +385,21 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                         up2(r, rx, ry);
                         Fx = Ux == TC(0) ? TC(0) : Ux * rx;
                         Fy = Uy == TC(0) ? TC(0) : Uy * ry;
+                        if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
+                        if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
                     } else {
                         Fx = tile_face_flux<TC>(xs, 1, periodic_x, i, a.Nx, Ux);
                         Fy = tile_face_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, Uy);
+                        if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
+                        if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
                     }
                 } else
 #endif
                 {
                     Fx = tile_face_flux<TC>(xs, 1, periodic_x, i, a.Nx, Ux);
                     Fy = tile_face_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, Uy);
+                    if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
+                    if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
                 }
                 fx[t][ty][tx] = Fx;
                 fy[t][ty][tx] = Fy;
@@ -403,7 +422,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (!a.flat_x && jr < a.Ny && f <= a.Nx) {
                         const int64_t rb = (int64_t)jr * a.sj + kofs;
                         Fe = tile_face_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx,
-                                                face_velocity<TS, TC>(a.u, rb, 1, a.Nx, periodic_x, f));
+                                                face_velocity<TS, TC>(a.u, rb, 1, a.Nx, periodic_x, f)) +
+                             tile_diff_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx, a.kh_dx);
                     }
                     fx[t][r][STEP_BX] = Fe;
                 } else {
@@ -412,7 +432,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (!a.flat_y && ix < a.Nx && f <= a.Ny) {
                         const int64_t cb2 = ix + kofs;
                         Fe = tile_face_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny,
-                                                face_velocity<TS, TC>(a.v, cb2, a.sj, a.Ny, periodic_y, f));
+                                                face_velocity<TS, TC>(a.v, cb2, a.sj, a.Ny, periodic_y, f)) +
+                             tile_diff_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny, a.kh_dy);
                     }
                     fy[t][STEP_BY][cc] = Fe;
                 }
@@ -480,6 +501,12 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (t < NB) Gb = g[slot_name(V, t)];
                 }
                 TC Gt = Gb - adv;
+                if (a.kzz) {
+                    // d/dz (kappa dc/dz), zero flux through the bottom and top walls
+                    const TC cu = k + 1 < a.Nz ? ld<TS, TC>(a.in[t], idx + a.sk) : c[t];
+                    const TC cd = k > 0 ? ld<TS, TC>(a.in[t], idx - a.sk) : c[t];
+                    Gt += a.kzz[k + 1] * (cu - c[t]) - a.kzz[k] * (c[t] - cd);
+                }
                 if (k == a.Nz - 1) {
 #pragma unroll
                     for (int q = 0; q < 2; q++)

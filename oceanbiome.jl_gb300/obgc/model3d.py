@@ -22,9 +22,33 @@ class Clock:
         self.iteration = iteration
 
 
+class ScalarDiffusivity:
+    """ScalarDiffusivity(κ = ...) with explicit time stepping (Oceananigans' default): κ a number, or
+    f(z) sampled at the cell faces for the vertical part.  `horizontal` / `vertical` select
+    HorizontalScalarDiffusivity / VerticalScalarDiffusivity."""
+
+    def __init__(self, κ=0.0, ν=None, horizontal=True, vertical=True, kappa=None):
+        self.kappa = κ if kappa is None else kappa
+        self.horizontal, self.vertical = horizontal, vertical
+
+    def face_values(self, grid):
+        import numpy as np
+        zf = -grid.Lz + grid.Lz / grid.Nz * np.arange(grid.Nz + 1)
+        k = self.kappa
+        return np.array([float(k(z)) for z in zf]) if callable(k) else np.full(grid.Nz + 1, float(k))
+
+
+def VerticalScalarDiffusivity(κ=0.0, ν=None):
+    return ScalarDiffusivity(κ, horizontal=False)
+
+
+def HorizontalScalarDiffusivity(κ=0.0, ν=None):
+    return ScalarDiffusivity(κ, vertical=False)
+
+
 class NonhydrostaticModel:
     def __init__(self, grid, biogeochemistry, advection="WENO5", tracers=(), velocities=None,
-                 precision="f32", clock=None, device="cuda", boundary_conditions=None):
+                 precision="f32", clock=None, device="cuda", boundary_conditions=None, closure=None):
         """boundary_conditions: {"DIC": CarbonDioxideGasExchangeBoundaryCondition(...),
         "O2": OxygenGasExchangeBoundaryCondition(...)} as top boundary conditions (the reference's
         FieldBoundaryConditions(top = ...)); applied by time_step's fused RK3 step."""
@@ -70,6 +94,14 @@ class NonhydrostaticModel:
             if want is None or bc.gas != want:
                 raise ValueError(f"no gas exchange boundary condition of this kind for tracer {name!r}")
             A.check(lib.obgc_set_gas_exchange(ctx, bc.gas, C.byref(bc.params)), "obgc_set_gas_exchange")
+        self.closure = closure
+        if closure is not None:
+            if closure.horizontal and callable(closure.kappa):
+                raise ValueError("a horizontal diffusivity is a constant here")
+            kh = float(closure.kappa) if closure.horizontal else 0.0
+            kz = closure.face_values(grid) if closure.vertical else None
+            arr = None if kz is None else (C.c_double * len(kz))(*kz)
+            A.check(lib.obgc_set_diffusivity(ctx, kh, 0.0, arr), "obgc_set_diffusivity")
 
     def _bind(self):
         f = A.Fields()

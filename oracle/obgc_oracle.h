@@ -82,6 +82,9 @@ typedef struct or_model3d {
     double invalid_fill_value;   /* ScaleNegativeTracers(...; invalid_fill_value)      */
     const obgc_gas_exchange* gas[2]; /* top boundary conditions: [0] CO2 on DIC, [1] O2 on O2, or NULL;
                                       * constant wind speed and air concentration */
+    double kappa_h;                  /* ScalarDiffusivity: horizontal diffusivity (m2/s)         */
+    const double* kappa_z_faces;     /* vertical diffusivity at the Nz + 1 faces, or NULL; the
+                                      * bottom and top faces are walls (no flux)                  */
 } or_model3d;
 /* state: [n_tracers][Nz*Ny*Nx]; u, v, w: [Nz*Ny*Nx] or NULL. */
 void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,

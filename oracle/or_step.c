@@ -225,6 +225,31 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
                         }
                         tend -= adv;
                     }
+                    if (m->kappa_h > 0.0 || m->kappa_z_faces) {
+                        /* ScalarDiffusivity, explicit: -div(-kappa grad c) with no flux through walls */
+                        const double* cq = state + (long)q * N;
+                        const int fx = g->topology_x == OBGC_FLAT, fy = g->topology_y == OBGC_FLAT || Ny == 1;
+                        double d = 0.0;
+                        if (!fx && m->kappa_h > 0.0) {
+                            const long row = (long)k * NN + (long)j * Nx;
+                            const double cm = (px || i > 0) ? cq[row + (i + Nx - 1) % Nx] : cq[row + i];
+                            const double cp = (px || i < Nx - 1) ? cq[row + (i + 1) % Nx] : cq[row + i];
+                            d += m->kappa_h * (cp - 2 * cq[row + i] + cm) / (dx * dx);
+                        }
+                        if (!fy && m->kappa_h > 0.0) {
+                            const long base = (long)k * NN + i;
+                            const double cm = (py || j > 0) ? cq[base + (long)((j + Ny - 1) % Ny) * Nx] : cq[base + (long)j * Nx];
+                            const double cp = (py || j < Ny - 1) ? cq[base + (long)((j + 1) % Ny) * Nx] : cq[base + (long)j * Nx];
+                            d += m->kappa_h * (cp - 2 * cq[base + (long)j * Nx] + cm) / (dy * dy);
+                        }
+                        if (m->kappa_z_faces) {
+                            const double cc = cq[c];
+                            const double up = k + 1 < Nz ? m->kappa_z_faces[k + 1] * (cq[c + NN] - cc) : 0.0;
+                            const double dn = k > 0 ? m->kappa_z_faces[k] * (cc - cq[c - NN]) : 0.0;
+                            d += (up - dn) / (dz * dz);
+                        }
+                        tend += d;
+                    }
                     G[(long)q * N + c] = tend;
                 }
             }

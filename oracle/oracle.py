@@ -26,7 +26,8 @@ class Model3D(C.Structure):
                 ("advection", C.c_int32), ("surface_value", C.c_double), ("grid", A.Grid),
                 ("n_tracers", C.c_int32), ("names", C.c_int32 * 32), ("negatives", C.c_int32),
                 ("zero_exclude_mask", C.c_int32), ("invalid_fill_value", C.c_double),
-                ("gas", C.POINTER(A.GasExchange) * 2)]
+                ("gas", C.POINTER(A.GasExchange) * 2), ("kappa_h", C.c_double),
+                ("kappa_z_faces", C.POINTER(C.c_double))]
 
 
 class Pisces3D(C.Structure):
@@ -269,9 +270,15 @@ def box_run(p, values, dt, nsteps, PAR_stages=None, PAR_const=0.0, t0=0.0):
 
 
 def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_value=0.0, advection=1,
-            negatives=NEG_NONE, zero_exclude=(), invalid_fill_value=float("nan"), gas_exchange=()):
-    """gas_exchange: A.GasExchange structs (CO2 on DIC, O2 on O2) as top boundary conditions."""
+            negatives=NEG_NONE, zero_exclude=(), invalid_fill_value=float("nan"), gas_exchange=(), kappa_h=0.0,
+            kappa_z_faces=None):
+    """gas_exchange: A.GasExchange structs (CO2 on DIC, O2 on O2) as top boundary conditions;
+    kappa_h, kappa_z_faces[Nz + 1]: ScalarDiffusivity (explicit)."""
     m = Model3D()
+    m.kappa_h = kappa_h
+    if kappa_z_faces is not None:
+        m._kz = np.ascontiguousarray(kappa_z_faces, dtype=np.float64)
+        m.kappa_z_faces = m._kz.ctypes.data_as(C.POINTER(C.c_double))
     m._gas_keep = list(gas_exchange)
     for g in gas_exchange:
         m.gas[0 if g.gas == A.GAS_CO2 else 1] = C.pointer(g)
