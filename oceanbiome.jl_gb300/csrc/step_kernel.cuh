@@ -257,6 +257,9 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     const bool winB = a.w == nullptr && ((a.drift_mask >> WB) & 1u);
     const uint32_t gen_mask = a.w != nullptr ? 0xffffffffu : (a.drift_mask & ~((1u << WA) | (1u << WB)));
     const bool any_generic = (gen_mask & ((1u << NT) - 1u)) != 0u;
+    // explicit ScalarDiffusivity (rare: off in the common configurations)
+    const bool hdiff = __builtin_expect(a.kh_dx != TC(0) || a.kh_dy != TC(0), 0);
+    const bool vdiff = __builtin_expect(a.kzz != nullptr, 0);
     // previous-stage tendencies staged in shared memory (the generic-drift buffer, when unused)
     const bool gm_smem = !any_generic && !a.first_stage;
     // shared-space address of this thread's first tile element
@@ -385,21 +388,27 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                         up2(r, rx, ry);
                         Fx = Ux == TC(0) ? TC(0) : Ux * rx;
                         Fy = Uy == TC(0) ? TC(0) : Uy * ry;
-                        if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
-                        if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
+                        if (hdiff) {
+                            if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
+                            if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
+                        }
                     } else {
                         Fx = tile_face_flux<TC>(xs, 1, periodic_x, i, a.Nx, Ux);
                         Fy = tile_face_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, Uy);
-                        if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
-                        if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
+                        if (hdiff) {
+                            if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
+                            if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
+                        }
                     }
                 } else
 #endif
                 {
                     Fx = tile_face_flux<TC>(xs, 1, periodic_x, i, a.Nx, Ux);
                     Fy = tile_face_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, Uy);
-                    if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
-                    if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
+                    if (hdiff) {
+                        if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
+                        if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
+                    }
                 }
                 fx[t][ty][tx] = Fx;
                 fy[t][ty][tx] = Fy;
@@ -422,8 +431,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (!a.flat_x && jr < a.Ny && f <= a.Nx) {
                         const int64_t rb = (int64_t)jr * a.sj + kofs;
                         Fe = tile_face_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx,
-                                                face_velocity<TS, TC>(a.u, rb, 1, a.Nx, periodic_x, f)) +
-                             tile_diff_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx, a.kh_dx);
+                                                face_velocity<TS, TC>(a.u, rb, 1, a.Nx, periodic_x, f));
+                        if (hdiff) Fe += tile_diff_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx, a.kh_dx);
                     }
                     fx[t][r][STEP_BX] = Fe;
                 } else {
@@ -432,8 +441,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (!a.flat_y && ix < a.Nx && f <= a.Ny) {
                         const int64_t cb2 = ix + kofs;
                         Fe = tile_face_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny,
-                                                face_velocity<TS, TC>(a.v, cb2, a.sj, a.Ny, periodic_y, f)) +
-                             tile_diff_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny, a.kh_dy);
+                                                face_velocity<TS, TC>(a.v, cb2, a.sj, a.Ny, periodic_y, f));
+                        if (hdiff) Fe += tile_diff_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny, a.kh_dy);
                     }
                     fy[t][STEP_BY][cc] = Fe;
                 }
@@ -501,7 +510,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (t < NB) Gb = g[slot_name(V, t)];
                 }
                 TC Gt = Gb - adv;
-                if (a.kzz) {
+                if (vdiff) {
                     // d/dz (kappa dc/dz), zero flux through the bottom and top walls
                     const TC cu = k + 1 < a.Nz ? ld<TS, TC>(a.in[t], idx + a.sk) : c[t];
                     const TC cd = k > 0 ? ld<TS, TC>(a.in[t], idx - a.sk) : c[t];

@@ -144,30 +144,32 @@ def test_zero_state_stays_zero(precision):
 
 @pytest.mark.parametrize("precision,tol", [("f64", 1e-11), ("mixed", 1e-5)])
 def test_fused_step_with_scalar_diffusivity_matches_oracle(precision, tol):
-    # closure = ScalarDiffusivity(κ) explicit: horizontal 5 m2/s and a mixed-layer profile kappa(z)
-    # through the faces, Bounded x walls (no flux) and periodic y
+    # closure = HorizontalScalarDiffusivity(κ = 5 m2/s), VerticalScalarDiffusivity(κ(z)) with a
+    # mixed-layer profile through the faces, and an isotropic ScalarDiffusivity(κ = 0.05 m2/s), all
+    # explicit (stable at these steps), with Bounded x walls (no flux) and periodic y
     torch = cuda()
     g = obgc.RectilinearGrid((24, 16, 12), (2400.0, 1600.0, 120.0), ("Bounded", "Periodic", "Bounded"),
                              dtype="f64")
     bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem())
-    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.05, seed=8)
-    u[:, :, 0] = 0.0                                      # no normal velocity through the x walls
+    # a divergence-free shear flow: no x velocity (Bounded walls), v varying with x only
+    u = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    xc = (np.arange(g.Nx) + 0.5) / g.Nx
+    v = torch.as_tensor(np.broadcast_to(0.05 * np.sin(2 * np.pi * xc), g.shape).copy(), dtype=torch.float64,
+                        device="cuda")
     kz = lambda z: 1e-2 * (1 + math.tanh((z + 40.0) / 10.0)) / 2 + 1e-4   # noqa: E731
-    closure = obgc.ScalarDiffusivity(κ=5.0)
-    model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None),
-                                     precision=precision, closure=closure)
-    model_v = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None),
-                                       precision=precision, closure=obgc.VerticalScalarDiffusivity(κ=kz))
-    init = obgc.lobster_initial_conditions(g, seed=9)
-    for mdl in (model, model_v):
-        obgc.set_(mdl, **init)
-    s0 = model.state_array().double().cpu().numpy()
-    dt, nsteps = 200.0, 3
-    obgc.time_step(model, dt, nsteps=nsteps)
-    obgc.time_step(model_v, dt, nsteps=nsteps)
-    uo, vo = (x.double().cpu().numpy().ravel().copy() for x in (u, v))
     zf = -g.Lz + g.Lz / g.Nz * np.arange(g.Nz + 1)
-    for mdl, kh, kzf in ((model, 5.0, np.full(g.Nz + 1, 5.0)), (model_v, 0.0, np.array([kz(z) for z in zf]))):
+    cases = [(obgc.HorizontalScalarDiffusivity(κ=5.0), 5.0, None),
+             (obgc.VerticalScalarDiffusivity(κ=kz), 0.0, np.array([kz(z) for z in zf])),
+             (obgc.ScalarDiffusivity(κ=0.05), 0.05, np.full(g.Nz + 1, 0.05))]
+    init = obgc.lobster_initial_conditions(g, seed=9)
+    uo, vo = (x.double().cpu().numpy().ravel().copy() for x in (u, v))
+    dt, nsteps = 200.0, 3
+    for closure, kh, kzf in cases:
+        mdl = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None),
+                                       precision=precision, closure=closure)
+        obgc.set_(mdl, **init)
+        s0 = mdl.state_array().double().cpu().numpy()
+        obgc.time_step(mdl, dt, nsteps=nsteps)
         got = mdl.state_array().double().cpu().numpy()
         m = O.model3d(bgc.params, g.c_grid(), mdl.tracer_names, kappa_h=kh, kappa_z_faces=kzf)
         ref = np.ascontiguousarray(s0.copy())
