@@ -219,13 +219,16 @@ __device__ __forceinline__ int wrap_or_clamp(int x, int N, bool periodic) {
     return min(max(x, 0), N - 1);
 }
 
-// Flux of tracer line `line` through vertical face f (model w and the tracer's drift velocity).
+// Flux of tracer line `line` through vertical face f: advective (model w and the tracer's drift
+// velocity, when `adv`) plus the explicit vertical diffusion -kappa_f dc/dz (none at the walls).
 template <typename TS, typename TC>
 __device__ __forceinline__ TC vertical_flux(const SubstepArgs<TS, TC>& a, const TS* __restrict__ line, int64_t col,
-                                            int t, int f) {
+                                            int t, int f, bool adv = true) {
     TC F = TC(0);
-    if (a.w) F += face_flux<TS, TC>(line, a.sk, a.Nz, false, f, face_velocity<TS, TC>(a.w, col, a.sk, a.Nz, false, f));
-    if ((a.drift_mask >> t) & 1u) F += face_flux<TS, TC>(line, a.sk, a.Nz, false, f, a.drift[t * (a.Nz + 1) + f]);
+    if (adv && a.w) F += face_flux<TS, TC>(line, a.sk, a.Nz, false, f, face_velocity<TS, TC>(a.w, col, a.sk, a.Nz, false, f));
+    if (adv && ((a.drift_mask >> t) & 1u)) F += face_flux<TS, TC>(line, a.sk, a.Nz, false, f, a.drift[t * (a.Nz + 1) + f]);
+    if (a.kzz && f > 0 && f < a.Nz)
+        F -= a.kzz[f] * a.dz * (ld<TS, TC>(line, (int64_t)f * a.sk) - ld<TS, TC>(line, (int64_t)(f - 1) * a.sk));
     return F;
 }
 
@@ -255,11 +258,13 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     constexpr int WA = V == V_NPZD ? 1 : V == V_EXTERNAL ? 10 : 4, WB = V == V_NPZD ? 4 : V == V_EXTERNAL ? 11 : 5;
     const bool winA = a.w == nullptr && ((a.drift_mask >> WA) & 1u);
     const bool winB = a.w == nullptr && ((a.drift_mask >> WB) & 1u);
-    const uint32_t gen_mask = a.w != nullptr ? 0xffffffffu : (a.drift_mask & ~((1u << WA) | (1u << WB)));
+    // tracers whose vertical advection takes the generic path, and those whose vertical face flux
+    // does (the generic advection set, plus every tracer under explicit vertical diffusion)
+    const uint32_t adv_mask = a.w != nullptr ? 0xffffffffu : (a.drift_mask & ~((1u << WA) | (1u << WB)));
+    const uint32_t gen_mask = a.kzz != nullptr ? 0xffffffffu : adv_mask;
     const bool any_generic = (gen_mask & ((1u << NT) - 1u)) != 0u;
-    // explicit ScalarDiffusivity (rare: off in the common configurations)
+    // explicit horizontal diffusivity (rare: off in the common configurations)
     const bool hdiff = __builtin_expect(a.kh_dx != TC(0) || a.kh_dy != TC(0), 0);
-    const bool vdiff = __builtin_expect(a.kzz != nullptr, 0);
     // previous-stage tendencies staged in shared memory (the generic-drift buffer, when unused)
     const bool gm_smem = !any_generic && !a.first_stage;
     // shared-space address of this thread's first tile element
@@ -318,7 +323,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 #pragma unroll 1
             for (int t = 0; t < NT; t++) {
                 const bool vert = (gen_mask >> t) & 1u;
-                fzu[t * NTH + tid] = vert ? vertical_flux(a, a.in[t] + col, col, t, k_top + 1) : TC(0);
+                fzu[t * NTH + tid] = vert ? vertical_flux(a, a.in[t] + col, col, t, k_top + 1, (adv_mask >> t) & 1u) : TC(0);
                 vdv[t * NTH + tid] = TC(0);
             }
         }
@@ -413,7 +418,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 fx[t][ty][tx] = Fx;
                 fy[t][ty][tx] = Fy;
                 if ((gen_mask >> t) & 1u) {
-                    const TC Fz = vertical_flux(a, a.in[t] + col, col, t, k);   // face below this cell
+                    const TC Fz = vertical_flux(a, a.in[t] + col, col, t, k, (adv_mask >> t) & 1u);   // face below this cell
                     vdv[t * NTH + tid] = (fzu[t * NTH + tid] - Fz) * a.inv_dz;
                     fzu[t * NTH + tid] = Fz;
                 }
@@ -510,12 +515,6 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (t < NB) Gb = g[slot_name(V, t)];
                 }
                 TC Gt = Gb - adv;
-                if (vdiff) {
-                    // d/dz (kappa dc/dz), zero flux through the bottom and top walls
-                    const TC cu = k + 1 < a.Nz ? ld<TS, TC>(a.in[t], idx + a.sk) : c[t];
-                    const TC cd = k > 0 ? ld<TS, TC>(a.in[t], idx - a.sk) : c[t];
-                    Gt += a.kzz[k + 1] * (cu - c[t]) - a.kzz[k] * (c[t] - cd);
-                }
                 if (k == a.Nz - 1) {
 #pragma unroll
                     for (int q = 0; q < 2; q++)
