@@ -393,27 +393,15 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                         up2(r, rx, ry);
                         Fx = Ux == TC(0) ? TC(0) : Ux * rx;
                         Fy = Uy == TC(0) ? TC(0) : Uy * ry;
-                        if (hdiff) {
-                            if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
-                            if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
-                        }
                     } else {
                         Fx = tile_face_flux<TC>(xs, 1, periodic_x, i, a.Nx, Ux);
                         Fy = tile_face_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, Uy);
-                        if (hdiff) {
-                            if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
-                            if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
-                        }
                     }
                 } else
 #endif
                 {
                     Fx = tile_face_flux<TC>(xs, 1, periodic_x, i, a.Nx, Ux);
                     Fy = tile_face_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, Uy);
-                    if (hdiff) {
-                        if (xok) Fx += tile_diff_flux<TC>(xs, 1, periodic_x, i, a.Nx, a.kh_dx);
-                        if (yok) Fy += tile_diff_flux<TC>(ys, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
-                    }
                 }
                 fx[t][ty][tx] = Fx;
                 fy[t][ty][tx] = Fy;
@@ -421,6 +409,15 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     const TC Fz = vertical_flux(a, a.in[t] + col, col, t, k, (adv_mask >> t) & 1u);   // face below this cell
                     vdv[t * NTH + tid] = (fzu[t * NTH + tid] - Fz) * a.inv_dz;
                     fzu[t * NTH + tid] = Fz;
+                }
+            }
+            // explicit horizontal diffusion: -kappa dc/dx and -kappa dc/dy added to this thread's faces
+            if (hdiff && row_faces) {
+#pragma unroll 1
+                for (int t = 0; t < NT; t++) {
+                    const TC* tl = tiles + t * TILE_SZ;
+                    if (xok) fx[t][ty][tx] += tile_diff_flux<TC>(tl + (ty + HALO) * TILE_W + tx, 1, periodic_x, i, a.Nx, a.kh_dx);
+                    if (yok) fy[t][ty][tx] += tile_diff_flux<TC>(tl + ty * TILE_W + tx + HALO, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
                 }
             }
             // the tile's east (8 per tracer) and north (32 per tracer) edge faces, spread over
