@@ -232,7 +232,15 @@ __device__ __forceinline__ TC vertical_flux(const SubstepArgs<TS, TC>& a, const 
     return F;
 }
 
-template <int V, int NT, typename TS, typename TC>
+// Whether a launch uses any of the optional terms (diffusivity closure, surface fluxes, the fused
+// negative-tracer modifier); without them the lean instantiation (EXT = false) runs.
+template <typename TS, typename TC>
+__host__ __device__ inline bool substep_needs_ext(const SubstepArgs<TS, TC>& a) {
+    return a.kh_dx != TC(0) || a.kh_dy != TC(0) || a.kzz != nullptr || a.top_slot1[0] != 0 || a.top_slot1[1] != 0 ||
+           a.neg.mode != OBGC_NEGATIVES_NONE;
+}
+
+template <int V, int NT, typename TS, typename TC, bool EXT>
 __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <= 12 ? 3 : NT <= 16 ? 2 : 1)
     substep_kernel(const __grid_constant__ SubstepArgs<TS, TC> a) {
     constexpr int NB = n_bgc(V);
@@ -261,10 +269,10 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     // tracers whose vertical advection takes the generic path, and those whose vertical face flux
     // does (the generic advection set, plus every tracer under explicit vertical diffusion)
     const uint32_t adv_mask = a.w != nullptr ? 0xffffffffu : (a.drift_mask & ~((1u << WA) | (1u << WB)));
-    const uint32_t gen_mask = a.kzz != nullptr ? 0xffffffffu : adv_mask;
+    const uint32_t gen_mask = (EXT && a.kzz != nullptr) ? 0xffffffffu : adv_mask;
     const bool any_generic = (gen_mask & ((1u << NT) - 1u)) != 0u;
     // explicit horizontal diffusivity (rare: off in the common configurations)
-    const bool hdiff = __builtin_expect(a.kh_dx != TC(0) || a.kh_dy != TC(0), 0);
+    const bool hdiff = EXT && (a.kh_dx != TC(0) || a.kh_dy != TC(0));
     // previous-stage tendencies staged in shared memory (the generic-drift buffer, when unused)
     const bool gm_smem = !any_generic && !a.first_stage;
     // shared-space address of this thread's first tile element
@@ -512,10 +520,12 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (t < NB) Gb = g[slot_name(V, t)];
                 }
                 TC Gt = Gb - adv;
-                if (k == a.Nz - 1) {
+                if constexpr (EXT) {
+                    if (k == a.Nz - 1) {
 #pragma unroll
-                    for (int q = 0; q < 2; q++)
-                        if (t + 1 == a.top_slot1[q]) Gt -= TC(a.top_flux[q][ic + (int64_t)jc * a.Nx]) * a.inv_dz;
+                        for (int q = 0; q < 2; q++)
+                            if (t + 1 == a.top_slot1[q]) Gt -= TC(a.top_flux[q][ic + (int64_t)jc * a.Nx]) * a.inv_dz;
+                    }
                 }
                 if (active) {
                     TC Un;
@@ -533,8 +543,10 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             }
             // ScaleNegativeTracers / ZeroNegativeTracers on the values this thread just stored,
             // the update_state! that follows the substep (negative_tracers.jl:136-276)
-            if (a.neg.mode != OBGC_NEGATIVES_NONE && active)
-                negatives_cell<TS>(a.neg, [&](int q) -> TS& { return a.out[q][idx]; });
+            if constexpr (EXT) {
+                if (a.neg.mode != OBGC_NEGATIVES_NONE && active)
+                    negatives_cell<TS>(a.neg, [&](int q) -> TS& { return a.out[q][idx]; });
+            }
         }
     }
 }

@@ -18,11 +18,11 @@ inline bool fused_supported(int V, int NT) {
     return false;
 }
 
-template <int V, int NT, typename TS, typename TC>
+template <int V, int NT, typename TS, typename TC, bool EXT>
 int ensure_configured() {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(substep_kernel<V, NT, TS, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(substep_kernel<V, NT, TS, TC, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)substep_smem_bytes<TC, NT>());
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(substep_kernel)");
         configured = true;
@@ -30,21 +30,36 @@ int ensure_configured() {
     return OBGC_OK;
 }
 
+// The lean instantiation unless the launch uses an optional term (substep_needs_ext).
 template <int V, int NT, typename TS, typename TC>
 int launch_one(const SubstepArgs<TS, TC>& a, int blocks, cudaStream_t st) {
-    const int rc = ensure_configured<V, NT, TS, TC>();
-    if (rc != OBGC_OK) return rc;
-    substep_kernel<V, NT, TS, TC><<<blocks, dim3(STEP_BX, STEP_BY), substep_smem_bytes<TC, NT>(), st>>>(a);
+    if (substep_needs_ext(a)) {
+        const int rc = ensure_configured<V, NT, TS, TC, true>();
+        if (rc != OBGC_OK) return rc;
+        substep_kernel<V, NT, TS, TC, true><<<blocks, dim3(STEP_BX, STEP_BY), substep_smem_bytes<TC, NT>(), st>>>(a);
+    } else {
+        const int rc = ensure_configured<V, NT, TS, TC, false>();
+        if (rc != OBGC_OK) return rc;
+        substep_kernel<V, NT, TS, TC, false><<<blocks, dim3(STEP_BX, STEP_BY), substep_smem_bytes<TC, NT>(), st>>>(a);
+    }
     OBGC_LAUNCHED("substep_kernel");
     return OBGC_OK;
 }
 
+// Blocks per SM (both instantiations share the launch bounds and shared memory; the larger one's
+// figure is the one the persistent grid is sized by).
 template <int V, int NT, typename TS, typename TC>
 int occupancy_one(int* blocks_per_sm) {
-    const int rc = ensure_configured<V, NT, TS, TC>();
+    int rc = ensure_configured<V, NT, TS, TC, true>();
+    if (rc == OBGC_OK) rc = ensure_configured<V, NT, TS, TC, false>();
     if (rc != OBGC_OK) return rc;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, substep_kernel<V, NT, TS, TC>,
+    int lean = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lean, substep_kernel<V, NT, TS, TC, false>,
                                                                   STEP_BX * STEP_BY, substep_smem_bytes<TC, NT>());
+    if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, substep_kernel<V, NT, TS, TC, true>,
+                                                      STEP_BX * STEP_BY, substep_smem_bytes<TC, NT>());
+    if (*blocks_per_sm > lean) *blocks_per_sm = lean;
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     return OBGC_OK;
 }
