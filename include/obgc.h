@@ -555,6 +555,17 @@ int obgc_set_gas_exchange(obgc_ctx* ctx, int32_t gas, const obgc_gas_exchange* g
  * flux), added to the advective face fluxes (VerticalScalarDiffusivity: kappa_h = 0;
  * HorizontalScalarDiffusivity: kappa_z = 0).  Zero everywhere switches it off. */
 int obgc_set_diffusivity(obgc_ctx* ctx, double kappa_h, double kappa_z, const double* kappa_z_faces);
+/* sediment = InstantRemineralisationSediment(grid; sinking_tracers, remineralisation_reciever,
+ * burial_efficiency_constant1 = a (0.013), _constant2 = b (0.53), _half_saturation = k (7/6.56))
+ * (src/Models/Sediments/instant_remineralisation.jl): per RK3 stage the sinking fluxes of the
+ * named tracers (enum obgc_tracer) through the bottom face deposit F per column, e = a + b (F/(k+F))^2
+ * of it is buried in the column's storage (stepped with the same RK3 stages) and (1 - e) F / dz is
+ * returned to the receiver's bottom cell.  n_sinking = 0 removes it. */
+int obgc_set_sediment(obgc_ctx* ctx, int32_t n_sinking, const int32_t* sinking_names, int32_t receiver_name,
+                      double a, double b, double k);
+/* The sediment storage of every column (Ny x Nx dense, FP64 on the host): `set` (optional) replaces
+ * it, then `get` (optional) receives it.  Synchronises the device. */
+int obgc_sediment_storage(obgc_ctx* ctx, const double* set, double* get);
 /* Size and selected field offsets of the ABI structs (which: 0 npd_params, 1 twoband,
  * 2 surface, 3 grid, 4 carbon_options, 5 model_desc, 6 fields) for binding self-checks;
  * no counterpart in the reference. */

@@ -135,6 +135,13 @@ struct obgc_ctx {
     // compute precision), or nullptr
     double kappa_h = 0.0;
     void* kzz = nullptr;
+    // InstantRemineralisation sediment: receiver slot (-1: none), sinking slots, parameters, and the
+    // storage (state precision) and previous-stage burial (compute precision) of every column
+    int sed_recv = -1;
+    uint32_t sed_mask = 0;
+    double sed_a = 0, sed_b = 0, sed_k = 0;
+    void* sed_storage = nullptr;
+    void* sed_G = nullptr;
     double* d_time = nullptr;
     DD* partial = nullptr;
     int n_partial = 0;
@@ -170,6 +177,8 @@ static int ctx_free(obgc_ctx* c) {
     for (int q = 0; q < 2; q++)
         if (c->gas_flux[q]) cudaFree(c->gas_flux[q]);
     if (c->kzz) cudaFree(c->kzz);
+    if (c->sed_storage) cudaFree(c->sed_storage);
+    if (c->sed_G) cudaFree(c->sed_G);
     if (c->ev_begin) cudaEventDestroy(c->ev_begin);
     if (c->ev_end) cudaEventDestroy(c->ev_end);
     for (auto e : c->prof_events) cudaEventDestroy(e);
@@ -339,6 +348,61 @@ extern "C" int obgc_set_diffusivity(obgc_ctx* c, double kappa_h, double kappa_z,
     return OBGC_OK;
 }
 
+extern "C" int obgc_set_sediment(obgc_ctx* c, int32_t n_sinking, const int32_t* sinking_names, int32_t receiver_name,
+                                 double a, double b, double k) {
+    if (!c || n_sinking < 0 || (n_sinking > 0 && !sinking_names)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_sediment: bad argument");
+    if (n_sinking == 0) {   // no sediment
+        c->sed_recv = -1;
+        c->sed_mask = 0;
+        c->bind_version++;
+        return OBGC_OK;
+    }
+    uint32_t mask = 0;
+    for (int q = 0; q < n_sinking; q++) {
+        const int t = slot_named(c, sinking_names[q]);
+        if (t < 0) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_sediment: a sinking tracer is not carried by the model");
+        mask |= 1u << t;
+    }
+    const int r = slot_named(c, receiver_name);
+    if (r < 0) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_sediment: the receiver is not carried by the model");
+    const size_t cols = (size_t)c->desc.grid.Nx * c->desc.grid.Ny;
+    if (!c->sed_storage) {
+        OBGC_CUDA(cudaMalloc(&c->sed_storage, c->ts * cols));
+        OBGC_CUDA(cudaMemset(c->sed_storage, 0, c->ts * cols));
+        OBGC_CUDA(cudaMalloc(&c->sed_G, c->tc * cols));
+        OBGC_CUDA(cudaMemset(c->sed_G, 0, c->tc * cols));
+    }
+    c->sed_recv = r;
+    c->sed_mask = mask;
+    c->sed_a = a; c->sed_b = b; c->sed_k = k;
+    c->bind_version++;
+    return OBGC_OK;
+}
+
+extern "C" int obgc_sediment_storage(obgc_ctx* c, const double* set, double* get) {
+    if (!c || !c->sed_storage) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_sediment_storage: no sediment");
+    const size_t cols = (size_t)c->desc.grid.Nx * c->desc.grid.Ny;
+    OBGC_CUDA(cudaDeviceSynchronize());
+    if (set) {
+        if (c->ts == 4) {
+            std::vector<float> h(set, set + cols);
+            OBGC_CUDA(cudaMemcpy(c->sed_storage, h.data(), 4 * cols, cudaMemcpyHostToDevice));
+        } else {
+            OBGC_CUDA(cudaMemcpy(c->sed_storage, set, 8 * cols, cudaMemcpyHostToDevice));
+        }
+    }
+    if (get) {
+        if (c->ts == 4) {
+            std::vector<float> h(cols);
+            OBGC_CUDA(cudaMemcpy(h.data(), c->sed_storage, 4 * cols, cudaMemcpyDeviceToHost));
+            for (size_t q = 0; q < cols; q++) get[q] = h[q];
+        } else {
+            OBGC_CUDA(cudaMemcpy(get, c->sed_storage, 8 * cols, cudaMemcpyDeviceToHost));
+        }
+    }
+    return OBGC_OK;
+}
+
 extern "C" int obgc_set_tiling(obgc_ctx* c, int32_t TZ) {
     if (!c || TZ < 1) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_tiling: bad argument");
     c->TZ = TZ;
@@ -410,6 +474,11 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.kh_dx = g.topology_x == OBGC_FLAT ? TC(0) : TC(c->kappa_h * g.Nx / g.Lx);
     a.kh_dy = g.topology_y == OBGC_FLAT ? TC(0) : TC(c->kappa_h * g.Ny / g.Ly);
     a.kzz = (const TC*)c->kzz;
+    a.sed_recv1 = c->sed_recv >= 0 ? c->sed_recv + 1 : 0;
+    a.sed_sink_mask = c->sed_mask;
+    a.sed_a = TC(c->sed_a); a.sed_b = TC(c->sed_b); a.sed_k = TC(c->sed_k);
+    a.sed_storage = (TS*)c->sed_storage;
+    a.sed_G = (TC*)c->sed_G;
 }
 
 // Enqueue nsteps steps on stream st (no synchronisation).  The state ping-pongs between the bound

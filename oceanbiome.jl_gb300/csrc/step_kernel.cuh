@@ -72,6 +72,15 @@ struct SubstepArgs {
     // dz^2 at the Nz + 1 faces (zero at the bottom and top walls), or NULL for none
     TC kh_dx, kh_dy;
     const TC* kzz;
+    // InstantRemineralisation sediment (src/Models/Sediments/instant_remineralisation.jl): the
+    // sinking fluxes of the slots in sed_sink_mask through the bottom face deposit F per column; a
+    // fraction e = a + b (F / (k + F))^2 is buried in sed_storage[i + j Nx] (RK3, previous-stage
+    // burial in sed_G), the rest returns to slot sed_recv1 - 1 in the bottom cell (0: no sediment)
+    int sed_recv1;
+    uint32_t sed_sink_mask;
+    TC sed_a, sed_b, sed_k;
+    TS* sed_storage;
+    TC* sed_G;
     const TS* u;
     const TS* v;
     const TS* w;
@@ -237,7 +246,7 @@ __device__ __forceinline__ TC vertical_flux(const SubstepArgs<TS, TC>& a, const 
 template <typename TS, typename TC>
 __host__ __device__ inline bool substep_needs_ext(const SubstepArgs<TS, TC>& a) {
     return a.kh_dx != TC(0) || a.kh_dy != TC(0) || a.kzz != nullptr || a.top_slot1[0] != 0 || a.top_slot1[1] != 0 ||
-           a.neg.mode != OBGC_NEGATIVES_NONE;
+           a.neg.mode != OBGC_NEGATIVES_NONE || a.sed_recv1 != 0;
 }
 
 template <int V, int NT, typename TS, typename TC, bool EXT>
@@ -478,6 +487,31 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 vdB = (FzB - F) * a.inv_dz;
                 FzB = F;
             }
+            // the sediment: deposition through the bottom face, its burial and the remineralised rest
+            TC sed_remin = TC(0);
+            if constexpr (EXT) {
+                if (a.sed_recv1 != 0 && k == 0) {
+                    TC dep = TC(0);
+#pragma unroll 1
+                    for (int t = 0; t < NT; t++) {
+                        if (!((a.sed_sink_mask >> t) & 1u)) continue;
+                        const TC Fb = t == WA && winA ? FzA : t == WB && winB ? FzB
+                                    : ((gen_mask >> t) & 1u) ? fzu[t * NTH + tid] : TC(0);
+                        dep -= Fb;   // downward (negative) flux deposits
+                    }
+                    const TC r = dep / (a.sed_k + dep);
+                    const TC e = a.sed_a + a.sed_b * (r * r);
+                    sed_remin = (TC(1) - e) * dep * a.inv_dz;
+                    if (active) {
+                        const int64_t c2 = ic + (int64_t)jc * a.Nx;
+                        const TC burial = e * dep;
+                        const TC upd = a.first_stage ? a.dt * a.gamma * burial
+                                                     : a.dt * (a.gamma * burial + a.zeta * a.sed_G[c2]);
+                        a.sed_storage[c2] += TS(upd);
+                        if (a.write_G) a.sed_G[c2] = burial;
+                    }
+                }
+            }
             if (k > k_bot) {
                 const int64_t nk = col + (int64_t)max(k - 4, 0) * a.sk;
 #pragma unroll
@@ -521,6 +555,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 }
                 TC Gt = Gb - adv;
                 if constexpr (EXT) {
+                    if (t + 1 == a.sed_recv1) Gt += sed_remin;   // zero above the bottom cell
                     if (k == a.Nz - 1) {
 #pragma unroll
                         for (int q = 0; q < 2; q++)

@@ -19,6 +19,7 @@ from .light import (MultiBandPhotosyntheticallyActiveRadiation, PrescribedPhotos
 from .model3d import (Clock, HorizontalScalarDiffusivity, NonhydrostaticModel, ScalarDiffusivity,
                       VerticalScalarDiffusivity, compute_tendencies, set_, time_step, update_biogeochemical_state)
 from .negatives import ScaleNegativeTracers, ZeroNegativeTracers
+from .sediments import InstantRemineralisationSediment
 from .models import (LOBSTER, NPZD, CarbonateSystem, Detritus, NitrateAmmonia, NitrateAmmoniaIron, Nutrient,
                      NutrientsPlanktonDetritus, Oxygen, PhytoZoo, TwoParticleAndDissolved, VariableRedfieldDetritus,
                      biogeochemical_drift_velocity, conserved_tracers, eval_point, preset,

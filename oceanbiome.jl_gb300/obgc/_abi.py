@@ -297,6 +297,8 @@ def load():
     _sig(lib, "obgc_gas_exchange_point", C.c_int, P(GasExchange), D, D, D, D, D, D, D, P(D))
     _sig(lib, "obgc_set_gas_exchange", C.c_int, VP, I32, P(GasExchange))
     _sig(lib, "obgc_set_diffusivity", C.c_int, VP, D, D, P(D))
+    _sig(lib, "obgc_set_sediment", C.c_int, VP, I32, P(I32), I32, D, D, D)
+    _sig(lib, "obgc_sediment_storage", C.c_int, VP, P(D), P(D))
     _sig(lib, "obgc_fp64_fma_peak", C.c_int, P(D), VP)
     _sig(lib, "obgc_struct_layout", C.c_int, I32, P(I64), I32)
     _sig(lib, "obgc_npd_preset", C.c_int, I32, P(NPDParams))
@@ -370,7 +372,7 @@ def load():
 EXPORTED = [
     "obgc_abi_version", "obgc_last_error_message", "obgc_kernel_launch_count", "obgc_fp64_fma_peak",
     "obgc_gas_exchange_defaults", "obgc_gas_exchange_flux", "obgc_gas_exchange_point", "obgc_set_gas_exchange",
-    "obgc_set_diffusivity",
+    "obgc_set_diffusivity", "obgc_set_sediment", "obgc_sediment_storage",
     "obgc_npd_preset", "obgc_npd_required_tracers", "obgc_npd_drift_velocity",
     "obgc_npd_eval_point", "obgc_npd_tendencies", "obgc_twoband_par", "obgc_multiband_par",
     "obgc_multiband_coefficients", "obgc_euphotic_depth", "obgc_carbon_default_options",

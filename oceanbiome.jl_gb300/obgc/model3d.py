@@ -94,6 +94,15 @@ class NonhydrostaticModel:
             if want is None or bc.gas != want:
                 raise ValueError(f"no gas exchange boundary condition of this kind for tracer {name!r}")
             A.check(lib.obgc_set_gas_exchange(ctx, bc.gas, C.byref(bc.params)), "obgc_set_gas_exchange")
+        sed = getattr(bgc, "sediment", None)
+        self.sediment = sed
+        if sed is not None:
+            from .sediments import InstantRemineralisationSediment
+            if not isinstance(sed, InstantRemineralisationSediment):
+                raise NotImplementedError(f"sediment model {type(sed).__name__} in the fused step")
+            names = (C.c_int32 * len(sed.sinking_tracers))(*[A.NAME_INDEX[n] for n in sed.sinking_tracers])
+            A.check(lib.obgc_set_sediment(ctx, len(sed.sinking_tracers), names, A.NAME_INDEX[sed.remineralisation_reciever],
+                                          sed.a, sed.b, sed.k), "obgc_set_sediment")
         self.closure = closure
         if closure is not None:
             if closure.horizontal and callable(closure.kappa):
@@ -133,6 +142,17 @@ class NonhydrostaticModel:
 
     def set_profiling(self, on):
         A.check(self._lib.obgc_set_profiling(self._ctx, int(on)), "obgc_set_profiling")
+
+    def sediment_storage(self, set=None):
+        """The sediment's storage field (Ny, Nx) as FP64 numpy; `set` replaces it first."""
+        import numpy as np
+        g = self.grid
+        out = np.empty((g.Ny, g.Nx), dtype=np.float64)
+        src = None if set is None else np.ascontiguousarray(np.broadcast_to(set, (g.Ny, g.Nx)), dtype=np.float64)
+        P = C.POINTER(C.c_double)
+        A.check(self._lib.obgc_sediment_storage(self._ctx, None if src is None else src.ctypes.data_as(P),
+                                                out.ctypes.data_as(P)), "obgc_sediment_storage")
+        return out
 
     def set_tiling(self, levels):
         A.check(self._lib.obgc_set_tiling(self._ctx, int(levels)), "obgc_set_tiling")

@@ -122,8 +122,12 @@ class NutrientsPlanktonDetritus:
     def __init__(self, grid=None, nutrients=None, plankton=None, detritus=None, carbonate_system=None,
                  oxygen=None, light_attenuation=None, sediment=None, scale_negatives=False,
                  invalid_fill_value=float("nan"), particles=None, modifiers=None, _base="LOBSTER"):
-        if sediment is not None or particles is not None:
-            raise NotImplementedError("sediment and particles are outside this engine's path")
+        if particles is not None:
+            raise NotImplementedError("particles are outside this engine's path")
+        from .sediments import InstantRemineralisationSediment
+        if sediment is not None and not isinstance(sediment, InstantRemineralisationSediment):
+            raise NotImplementedError(f"sediment model {type(sediment).__name__}: only InstantRemineralisationSediment")
+        self.sediment = sediment
         p = preset(_base)
         if nutrients is not None:
             p.nutrients = nutrients.kind

@@ -85,6 +85,10 @@ typedef struct or_model3d {
     double kappa_h;                  /* ScalarDiffusivity: horizontal diffusivity (m2/s)         */
     const double* kappa_z_faces;     /* vertical diffusivity at the Nz + 1 faces, or NULL; the
                                       * bottom and top faces are walls (no flux)                  */
+    int32_t sed_receiver;            /* InstantRemineralisation: receiver tracer slot, or -1    */
+    uint32_t sed_sink_mask;          /* sinking tracer slots                                     */
+    double sed_a, sed_b, sed_k;      /* burial efficiency constants and half saturation          */
+    double* sed_storage;             /* [Ny*Nx] storage, stepped with the tracers' RK3           */
 } or_model3d;
 /* state: [n_tracers][Nz*Ny*Nx]; u, v, w: [Nz*Ny*Nx] or NULL. */
 void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,

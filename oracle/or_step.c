@@ -158,6 +158,7 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
     double* PAR = malloc(sizeof(double) * N);
     double* drift = calloc((size_t)nt * (Nz + 1), sizeof(double));
     int* has_drift = calloc(nt, sizeof(int));
+    double* sed_Gm = calloc((size_t)NN, sizeof(double));
     int32_t req[32];
     int nreq = or_npd_required_tracers(&m->npd, req, 32);
     int is_bgc[32] = {0};
@@ -279,6 +280,28 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
                     G[(long)target * N + c] -= F / dz;
                 }
             }
+            /* InstantRemineralisationSediment (instant_remineralisation.jl:96-120; tracer_coupling.jl,
+             * tracked_fields.jl): the sinking fluxes through the bottom face deposit F, a fraction
+             * e = a + b (F/(k+F))^2 is buried, the rest returns to the receiver's bottom cell */
+            if (m->sed_receiver >= 0 && m->sed_storage) {
+                const double gs = RK_G[st], zs = RK_Z[st];
+                for (long col = 0; col < NN; col++) {
+                    double dep = 0.0;
+                    for (int q = 0; q < nt; q++) {
+                        if (!((m->sed_sink_mask >> q) & 1u) || !has_drift[q]) continue;
+                        const double W0 = drift[(long)q * (Nz + 1)];
+                        const double* zline = state + (long)q * N + col;
+                        const double F0 = W0 != 0.0 ? W0 * face_value(zline, NN, Nz, 0, 0, W0) : 0.0;
+                        dep -= F0;
+                    }
+                    const double r = dep / (m->sed_k + dep);
+                    const double e = m->sed_a + m->sed_b * (r * r);
+                    G[(long)m->sed_receiver * N + col] += (1.0 - e) * dep / dz;
+                    const double burial = e * dep;
+                    m->sed_storage[col] += st == 0 ? dt * gs * burial : dt * (gs * burial + zs * sed_Gm[col]);
+                    sed_Gm[col] = burial;
+                }
+            }
             double g = RK_G[st], z = RK_Z[st];
 #pragma omp parallel for num_threads(nthreads) schedule(static)
             for (long x = 0; x < (long)nt * N; x++) {
@@ -290,7 +313,7 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
         }
         t += dt;
     }
-    free(G); free(Gm); free(PAR); free(drift); free(has_drift);
+    free(G); free(Gm); free(PAR); free(drift); free(has_drift); free(sed_Gm);
 }
 
 /* ------------------------------------------------------------------ negative tracers -- */

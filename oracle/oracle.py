@@ -27,7 +27,9 @@ class Model3D(C.Structure):
                 ("n_tracers", C.c_int32), ("names", C.c_int32 * 32), ("negatives", C.c_int32),
                 ("zero_exclude_mask", C.c_int32), ("invalid_fill_value", C.c_double),
                 ("gas", C.POINTER(A.GasExchange) * 2), ("kappa_h", C.c_double),
-                ("kappa_z_faces", C.POINTER(C.c_double))]
+                ("kappa_z_faces", C.POINTER(C.c_double)), ("sed_receiver", C.c_int32), ("sed_sink_mask", C.c_uint32),
+                ("sed_a", C.c_double), ("sed_b", C.c_double), ("sed_k", C.c_double),
+                ("sed_storage", C.POINTER(C.c_double))]
 
 
 class Pisces3D(C.Structure):
@@ -271,10 +273,21 @@ def box_run(p, values, dt, nsteps, PAR_stages=None, PAR_const=0.0, t0=0.0):
 
 def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_value=0.0, advection=1,
             negatives=NEG_NONE, zero_exclude=(), invalid_fill_value=float("nan"), gas_exchange=(), kappa_h=0.0,
-            kappa_z_faces=None):
+            kappa_z_faces=None, sediment=None):
     """gas_exchange: A.GasExchange structs (CO2 on DIC, O2 on O2) as top boundary conditions;
-    kappa_h, kappa_z_faces[Nz + 1]: ScalarDiffusivity (explicit)."""
+    kappa_h, kappa_z_faces[Nz + 1]: ScalarDiffusivity (explicit).  sediment=(sinking names, receiver,
+    a, b, k, storage array [Ny, Nx] float64) for InstantRemineralisation."""
     m = Model3D()
+    m.sed_receiver = -1
+    if sediment is not None:
+        sinking, receiver, sa, sb, sk, storage = sediment
+        nm = [A.NAME_INDEX[n] if isinstance(n, str) else n for n in names]
+        m.sed_receiver = nm.index(A.NAME_INDEX[receiver])
+        m.sed_sink_mask = sum(1 << nm.index(A.NAME_INDEX[n]) for n in sinking)
+        m.sed_a, m.sed_b, m.sed_k = sa, sb, sk
+        assert storage.dtype == np.float64 and storage.flags.c_contiguous
+        m._storage = storage
+        m.sed_storage = storage.ctypes.data_as(C.POINTER(C.c_double))
     m.kappa_h = kappa_h
     if kappa_z_faces is not None:
         m._kz = np.ascontiguousarray(kappa_z_faces, dtype=np.float64)

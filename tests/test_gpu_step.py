@@ -107,7 +107,7 @@ def test_budget_is_compensated_sum():
     torch = cuda()
     g, bgc, model, vel = lobster_model(seed=13)
     got = model.budget("nitrogen")
-    names = obgc.conserved_tracers(bgc)[0]
+    names = obgc.conserved_tracers(bgc, labeled=True)["nitrogen"]
     ref = math.fsum(float(x) for n in names for x in model.tracers[n].cpu().numpy().ravel())
     assert abs(got - ref) <= 1e-15 * abs(ref)
 
@@ -181,3 +181,45 @@ def test_fused_step_with_scalar_diffusivity_matches_oracle(precision, tol):
         ref0 = np.ascontiguousarray(s0.copy())
         O.step3d(m0, ref0, u=uo, v=vo, t=0.0, dt=dt, nsteps=nsteps)
         assert max(per_tracer_err(mdl, ref0, ref).values()) > 100 * tol
+
+
+@pytest.mark.parametrize("base,precision,tol", [("NPZD", "f64", 1e-11), ("LOBSTER", "f64", 1e-11),
+                                                ("LOBSTER", "mixed", 1e-5)])
+def test_instant_remineralisation_sediment(base, precision, tol):
+    # InstantRemineralisationSediment: the GPU step against the oracle (tracers and storage), and
+    # nitrogen conserved between the water and the sediment (the reference's
+    # test/test_sediments.jl:58-80 statement), with an open bottom
+    torch = cuda()
+    g = obgc.RectilinearGrid((8, 8, 20), (800.0, 800.0, 200.0), ("Periodic", "Periodic", "Bounded"), dtype="f64")
+    if base == "NPZD":
+        sed = obgc.InstantRemineralisationSediment(g)
+        bgc = obgc.NPZD(g, sediment=sed)
+        init = dict(N=10.0, P=0.5, Z=0.1, D=1.0, T=12.0)
+    else:
+        sed = obgc.InstantRemineralisationSediment(g, sinking_tracers=("sPOM", "bPOM"), remineralisation_reciever="NH4")
+        bgc = obgc.LOBSTER(g, sediment=sed)
+        init = dict(NO3=10.0, NH4=0.5, P=0.5, Z=0.1, sPOM=1.0, bPOM=1.0, DOM=0.1)
+    bgc.params.open_bottom = 1
+    model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, precision=precision)   # no velocity: sinking only
+    obgc.set_(model, **{k: v for k, v in init.items() if k in model.tracers})
+    s0 = model.state_array().double().cpu().numpy()
+    dt, nsteps = 300.0, 12
+    obgc.time_step(model, dt, nsteps=nsteps)
+    got = model.state_array().double().cpu().numpy()
+    storage = model.sediment_storage()
+    ref = np.ascontiguousarray(s0.copy())
+    ref_storage = np.zeros((g.Ny, g.Nx))
+    m = O.model3d(bgc.params, g.c_grid(), model.tracer_names,
+                  sediment=(sed.sinking_tracers, sed.remineralisation_reciever, sed.a, sed.b, sed.k, ref_storage))
+    O.step3d(m, ref, t=0.0, dt=dt, nsteps=nsteps)
+    errs = per_tracer_err(model, got, ref)
+    assert max(errs.values()) < tol, errs
+    assert rel_err(storage, ref_storage) < tol
+    assert np.all(storage > 0)
+    # nitrogen: the volume integral of the tracers' nitrogen plus the area integral of the storage
+    names = obgc.conserved_tracers(bgc)[0]
+    dV, dA = g.Lx * g.Ly * g.Lz / g.N, g.Lx * g.Ly / (g.Nx * g.Ny)
+    def total(state, st):
+        return sum(state[model.tracer_names.index(n)].sum() for n in names) * dV + st.sum() * dA
+    assert abs(total(got, storage) - total(s0, np.zeros_like(storage))) / total(s0, np.zeros_like(storage)) < \\
+        (1e-13 if precision == "f64" else 1e-6)
