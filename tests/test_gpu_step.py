@@ -217,7 +217,7 @@ def test_instant_remineralisation_sediment(base, precision, tol):
     assert rel_err(storage, ref_storage) < tol
     assert np.all(storage > 0)
     # nitrogen: the volume integral of the tracers' nitrogen plus the area integral of the storage
-    names = obgc.conserved_tracers(bgc)[0]
+    names = obgc.conserved_tracers(bgc, labeled=True)["nitrogen"]
     dV, dA = g.Lx * g.Ly * g.Lz / g.N, g.Lx * g.Ly / (g.Nx * g.Ny)
     def total(state, st):
         return sum(state[model.tracer_names.index(n)].sum() for n in names) * dV + st.sum() * dA
