@@ -234,8 +234,11 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
                 }
             }
             __syncthreads();
-            // 4. implicit vertical diffusion, one Thomas solve per (column, tracer)
-            for (int it = tid; it < ncol * NT; it += nth) {
+            // 4. implicit vertical diffusion: one warp per (column, tracer).  The two Thomas sweeps are
+            // first-order linear recurrences, d_k = a_k d_(k-1) + b_k forward and x_k = -cp_k x_(k+1)
+            // + d_k backward, so each 32-level chunk composes its lanes' affine maps with a shuffle
+            // scan and applies the composite to the carry from the chunk before.
+            for (int it = warp; it < ncol * NT; it += nwarp) {
                 const int c = it / NT, q = it - c * NT;
                 if (s >= cst[c]) continue;
                 const int Nz = cnz[c];
@@ -244,16 +247,42 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
                 const TS* cp = th + (2 * st) * cap + coff[c];
                 const TS* idn = th + (2 * st + 1) * cap + coff[c];
                 TS* x = U + q * cap + coff[c];
-                TS d = x[0] * idn[0];
-                x[0] = d;
-                for (int k = 1; k < Nz; k++) {
-                    d = (x[k] + r * kf[k] * d) * idn[k];   // (x_k - lo_k d_{k-1}) / den_k, lo_k = -r kappa_k
-                    x[k] = d;
+                TS carry = TS(0);
+                for (int k0 = 0; k0 < Nz; k0 += 32) {
+                    const int k = k0 + lane;
+                    TS A = TS(1), B = TS(0);   // identity past the column
+                    if (k < Nz) {
+                        A = k == 0 ? TS(0) : r * kf[k] * idn[k];
+                        B = x[k] * idn[k];
+                    }
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const TS Ap = __shfl_up_sync(0xffffffffu, A, o), Bp = __shfl_up_sync(0xffffffffu, B, o);
+                        if (lane >= o) { B = A * Bp + B; A = A * Ap; }
+                    }
+                    const TS d = A * carry + B;
+                    if (k < Nz) x[k] = d;
+                    carry = __shfl_sync(0xffffffffu, d, 31);
                 }
-                for (int k = Nz - 2; k >= 0; k--) {
-                    d = x[k] - cp[k] * d;
-                    x[k] = d;
+                __syncwarp();
+                carry = x[Nz - 1];
+                for (int k0 = 0; k0 < Nz - 1; k0 += 32) {
+                    const int k = Nz - 2 - (k0 + lane);
+                    TS A = TS(1), B = TS(0);
+                    if (k >= 0) {
+                        A = -cp[k];
+                        B = x[k];
+                    }
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const TS Ap = __shfl_up_sync(0xffffffffu, A, o), Bp = __shfl_up_sync(0xffffffffu, B, o);
+                        if (lane >= o) { B = A * Bp + B; A = A * Ap; }
+                    }
+                    const TS v = A * carry + B;
+                    if (k >= 0) x[k] = v;
+                    carry = __shfl_sync(0xffffffffu, v, 31);
                 }
+                __syncwarp();
             }
             __syncthreads();
             // 5. update_state! after the substep: the negative-tracer modifier
