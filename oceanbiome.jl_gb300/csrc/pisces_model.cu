@@ -220,11 +220,17 @@ void aux_fields(const obgc_pisces_model* m, obgc_pisces_field* a) {
 
 template <typename TS, typename TC>
 int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t st) {
-    // the 26 tracers advect independently once their BGC tendencies are in hand: two launches of
-    // 13 tracers each hold half the shared-memory tiles and run two blocks per SM
-    constexpr int GROUP = 13;
-    const FusedEntry* fe = find_fused(m->desc.precision, V_EXTERNAL, GROUP);
-    if (!fe) return fail(OBGC_ERR_UNSUPPORTED, "obgc_pisces_model_step: no fused PISCES kernel for this precision");
+    // the 26 tracers advect independently once their BGC tendencies are in hand: launches on tracers
+    // 0-8, 9-17 (POC and GOC, slots 1 and 2 of the group, keep their register windows) and 18-25
+    // hold a third of the shared-memory tiles each and run three blocks per SM
+    constexpr int NGROUP = 3;
+    const int g_first[NGROUP] = {0, 9, 18}, g_size[NGROUP] = {9, 9, 8};
+    const FusedEntry* fes[NGROUP];
+    for (int q = 0; q < NGROUP; q++) {
+        fes[q] = find_fused(m->desc.precision, V_EXTERNAL, g_size[q]);
+        if (!fes[q]) return fail(OBGC_ERR_UNSUPPORTED, "obgc_pisces_model_step: no fused PISCES kernel for this precision");
+    }
+    const FusedEntry* fe = fes[0];
     const obgc_grid& g = m->desc.grid;
     SubstepArgs<TS, TC> a;
     std::memset(&a, 0, sizeof(a));
@@ -274,17 +280,18 @@ int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t 
             a.gamma = TC(rk3_gamma(stg));
             a.zeta = TC(rk3_zeta(stg));
             a.c_stage = rk3_c(stg);
-            for (int g0 = 0; g0 < PNT && rc == OBGC_OK; g0 += GROUP) {
-                for (int t = 0; t < GROUP; t++) {
+            for (int q = 0; q < NGROUP && rc == OBGC_OK; q++) {
+                const int g0 = g_first[q], gn = g_size[q];
+                for (int t = 0; t < gn; t++) {
                     a.in[t] = static_cast<const TS*>(cur[g0 + t]);
                     a.out[t] = static_cast<TS*>(nxt[g0 + t]);
                     a.G[t] = static_cast<TC*>(m->G[g0 + t]);
                     a.ext[t] = g0 + t < OBGC_PIS_NUM_BGC ? static_cast<const TC*>(m->Gb[g0 + t]) : nullptr;
                 }
-                a.n_ext = std::min(GROUP, OBGC_PIS_NUM_BGC - g0);
+                a.n_ext = std::max(0, std::min(gn, OBGC_PIS_NUM_BGC - g0));
                 a.drift = static_cast<const TC*>(m->drift) + (size_t)g0 * (g.Nz + 1);
-                a.drift_mask = (mask >> g0) & ((1u << GROUP) - 1u);
-                rc = fe->launch(&a, blocks, st);
+                a.drift_mask = (mask >> g0) & ((1u << gn) - 1u);
+                rc = fes[q]->launch(&a, blocks, st);
             }
             if (rc == OBGC_OK) rc = prof_mark(m, st);
             if (rc != OBGC_OK) break;

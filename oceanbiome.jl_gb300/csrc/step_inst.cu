@@ -25,10 +25,10 @@ typedef float TC_;
 #endif
 
 constexpr int V_ = OBGC_INST_V;
-// tracer counts with a kernel: the BGC tracers alone, and followed by the carried T/S (PISCES
-// always carries T and S: 26 slots)
-[[maybe_unused]] constexpr int NT_A = V_ == V_EXTERNAL ? 13 : n_bgc(V_);
-[[maybe_unused]] constexpr int NT_B = V_ == V_NPZD ? 6 : V_ == V_EXTERNAL ? 13 : n_bgc(V_) + 2;
+// tracer counts with a kernel: the BGC tracers alone, and followed by the carried T/S (PISCES:
+// groups of 9 and 8 of its 26 slots)
+[[maybe_unused]] constexpr int NT_A = V_ == V_EXTERNAL ? 9 : n_bgc(V_);
+[[maybe_unused]] constexpr int NT_B = V_ == V_NPZD ? 6 : V_ == V_EXTERNAL ? 8 : n_bgc(V_) + 2;
 
 template <int NT>
 int launch_fn(const void* a, int blocks, cudaStream_t st) {
@@ -37,7 +37,7 @@ int launch_fn(const void* a, int blocks, cudaStream_t st) {
 template <int NT>
 int occupancy_fn(int* bps) { return occupancy_one<V_, NT, TS_, TC_>(bps); }
 
-// 26 FP64 tiles do not fit shared memory: PISCES fuses in FP32 and mixed precision only
+// the PISCES model steps in FP32 and mixed precision only
 #if !(OBGC_INST_V == 5 && OBGC_INST_PREC == 1)
 struct Registrar {
     Registrar() {

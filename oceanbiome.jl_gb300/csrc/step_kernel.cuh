@@ -270,9 +270,9 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     // Sinking tracers advance their vertical stencil in a register window (one new load per
     // level); two window slots per variant (LOBSTER: sPOM, bPOM; NPZD: P, D).  Any other
     // vertically advected tracer, and every tracer when a model w is given, takes the generic path.
-    // PISCES (V_EXTERNAL, launched on tracers 0-12 and 13-25): POC and GOC in the first launch,
-    // the other four sinking tracers take the generic path.
-    constexpr int WA = V == V_NPZD ? 1 : V == V_EXTERNAL ? 10 : 4, WB = V == V_NPZD ? 4 : V == V_EXTERNAL ? 11 : 5;
+    // PISCES (V_EXTERNAL, launched on tracers 0-8, 9-17 and 18-25): POC and GOC are slots 1 and 2
+    // of the second launch; the other four sinking tracers take the generic path.
+    constexpr int WA = V == V_NPZD ? 1 : V == V_EXTERNAL ? 1 : 4, WB = V == V_NPZD ? 4 : V == V_EXTERNAL ? 2 : 5;
     const bool winA = a.w == nullptr && ((a.drift_mask >> WA) & 1u);
     const bool winB = a.w == nullptr && ((a.drift_mask >> WB) & 1u);
     // tracers whose vertical advection takes the generic path, and those whose vertical face flux

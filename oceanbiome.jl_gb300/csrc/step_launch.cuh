@@ -13,7 +13,7 @@ inline bool fused_supported(int V, int NT) {
         case V_LOBSTER_CO: return NT == 10 || NT == 12;
         case V_LOBSTER_O: return NT == 8 || NT == 10;
         case V_NPZD: return NT == 5 || NT == 6;
-        case V_EXTERNAL: return NT == 13;   // PISCES, in two launches of 13 tracers
+        case V_EXTERNAL: return NT == 9 || NT == 8;   // PISCES, in launches of 9, 9 and 8 tracers
     }
     return false;
 }
