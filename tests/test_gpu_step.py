@@ -223,3 +223,33 @@ def test_instant_remineralisation_sediment(base, precision, tol):
         return sum(state[model.tracer_names.index(n)].sum() for n in names) * dV + st.sum() * dA
     n0 = total(s0, np.zeros_like(storage))
     assert abs(total(got, storage) - n0) / n0 < (1e-13 if precision == "f64" else 1e-6)
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-10), ("mixed", 1e-5)])
+def test_eady_like_configuration_matches_oracle(precision, tol):
+    # the options of the reference's Eady example together (examples/eady.jl:50-73): LOBSTER with
+    # carbonates and scale_negatives, T and S, VerticalScalarDiffusivity(κ = 1e-4), and the CO2
+    # gas exchange on DIC, with a random-streamfunction flow
+    torch = cuda()
+    g = obgc.RectilinearGrid((32, 16, 12), (3200.0, 1600.0, 60.0), ("Periodic", "Periodic", "Bounded"), dtype="f64")
+    bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem(), scale_negatives=True)
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=21)
+    co2 = obgc.CarbonDioxideGasExchangeBoundaryCondition(wind_speed=8.0)
+    model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None),
+                                     precision=precision, closure=obgc.VerticalScalarDiffusivity(κ=1e-4),
+                                     boundary_conditions={"DIC": co2})
+    init = obgc.lobster_initial_conditions(g, seed=22)
+    init["NH4"] = np.random.default_rng(23).normal(0.0, 0.05, g.shape)   # negatives to scale away
+    obgc.set_(model, **{k: val for k, val in init.items() if k in model.tracers})
+    s0 = model.state_array().double().cpu().numpy()
+    dt, nsteps = 200.0, 4
+    obgc.time_step(model, dt, nsteps=nsteps, graph=True)
+    got = model.state_array().double().cpu().numpy()
+    m = O.model3d(bgc.params, g.c_grid(), model.tracer_names, negatives=O.NEG_SCALE, gas_exchange=[co2.params],
+                  kappa_z_faces=np.full(g.Nz + 1, 1e-4))
+    ref = np.ascontiguousarray(s0.copy())
+    O.step3d(m, ref, u=u.double().cpu().numpy().ravel().copy(), v=v.double().cpu().numpy().ravel().copy(),
+             t=0.0, dt=dt, nsteps=nsteps)
+    errs = {n: rel_err(got[q], ref[q], floor_frac=1e-3) for q, n in enumerate(model.tracer_names)}
+    assert max(errs.values()) < tol, errs
+    assert np.min(got[model.tracer_names.index("NH4")]) >= 0
