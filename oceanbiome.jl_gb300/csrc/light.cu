@@ -48,37 +48,50 @@ struct BandsT {
     TS* out[MAX_BANDS];
 };
 
+// One warp per column: each lane takes one level of a 32-level chunk (top first), the attenuation
+// factor of its level, and a multiplicative shuffle scan down the chunk continues the product carried
+// from the chunk above (multi_band.jl:147-185: PAR at the top cell PAR0 div exp(z att), below it
+// the cell above times exp((z - z_above) att)).
 template <typename T, typename TS = T>
 __global__ void __launch_bounds__(128) multiband_kernel(BandsT<T, TS> B, int surf_kind, T surf_value,
                                                         const TS* __restrict__ surf_field, int Nx, int Ny,
                                                         int Nz, int64_t sj, int64_t sk, T Lz,
                                                         const TS* __restrict__ Chl, TS* __restrict__ total) {
-    const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= (int64_t)Nx * Ny) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t col = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (col >= (int64_t)Nx * Ny) return;   // warp-uniform
     const int i = (int)(col % Nx), j = (int)(col / Nx);
     const T dz = Lz / T(Nz);
     const T PAR0 = surf_kind == OBGC_SURFACE_PAR_FIELD ? T(surf_field[col]) : surf_value;
     const int64_t base = i + (int64_t)j * sj;
-    T prev[MAX_BANDS];
-    T zprev = T(0);
-    for (int k = Nz - 1; k >= 0; --k) {
-        const int64_t idx = base + (int64_t)k * sk;
-        const T chl = T(Chl[idx]);
+    T carry[MAX_BANDS];
+#pragma unroll
+    for (int b = 0; b < MAX_BANDS; b++) carry[b] = T(1);
+    for (int k0 = 0; k0 < Nz; k0 += 32) {
+        const int k = Nz - 1 - (k0 + lane);
+        const bool valid = k >= 0;
+        const int64_t idx = base + (int64_t)(valid ? k : 0) * sk;
+        const T chl = valid ? T(Chl[idx]) : T(0);
         const T z = -Lz + (T(k) + T(0.5)) * dz;
         T sum = T(0);
 #pragma unroll
         for (int b = 0; b < MAX_BANDS; b++) {
             if (b < B.n) {
                 const T att = B.kw[b] + B.chi[b] * t_pow(chl, B.e[b]);
-                // multi_band.jl:156 (top cell) and :160-161 (cells below)
-                const T v = (k == Nz - 1) ? PAR0 * B.div[b] * t_exp(z * att) : prev[b] * t_exp((z - zprev) * att);
-                prev[b] = v;
-                B.out[b][idx] = TS(v);
+                T f = T(1);
+                if (valid) f = (k == Nz - 1) ? PAR0 * B.div[b] * t_exp(z * att) : t_exp(-dz * att);
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const T fp = __shfl_up_sync(0xffffffffu, f, o);
+                    if (lane >= o) f *= fp;
+                }
+                const T v = carry[b] * f;
+                if (valid) B.out[b][idx] = TS(v);
                 sum += v;
+                carry[b] = __shfl_sync(0xffffffffu, v, 31);
             }
         }
-        if (total) total[idx] = TS(sum);
-        zprev = z;
+        if (total && valid) total[idx] = TS(sum);
     }
 }
 
@@ -134,7 +147,7 @@ static int launch_multiband(int nb, const double* kw, const double* e, const dou
         B.out[b] = (TS*)bands[b];
     }
     const int64_t ncol = (int64_t)g->Nx * g->Ny;
-    const int blocks = (int)((ncol + 127) / 128);
+    const int blocks = (int)((ncol * 32 + 127) / 128);   // one warp per column
     const double v = s->kind == OBGC_SURFACE_PAR_DEFAULT ? default_surface_par(t) : s->value;
     multiband_kernel<T, TS><<<blocks, 128, 0, st>>>(B, s->kind, T(v), (const TS*)s->field, g->Nx, g->Ny, g->Nz,
                                                     g->stride_j, g->stride_k, T(g->Lz), (const TS*)Chl, (TS*)total);
