@@ -477,12 +477,34 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             // window tracers: flux through the face below this cell, divergence, and slide the
             // windows down one level (the next level needs c[k-4])
             TC vdA = TC(0), vdB = TC(0);
-            if (winA) {
+            bool win_done = false;
+#ifdef __CUDA_ARCH__
+            if constexpr (sizeof(TC) == 4) {
+                // both windows at an interior face: one packed f32x2 WENO5 (the same arithmetic per
+                // element as the scalar path below)
+                const TC UA = winA ? a.drift[WA * (a.Nz + 1) + k] : TC(0), UB = winB ? a.drift[WB * (a.Nz + 1) + k] : TC(0);
+                if (UA != TC(0) && UB != TC(0) && min(k, a.Nz - k) >= 3) {
+                    const bool pa = UA > TC(0), pb = UB > TC(0);
+                    const f32x2 r = weno5_x2(pk2(pa ? wA[0] : wA[5], pb ? wB[0] : wB[5]), pk2(pa ? wA[1] : wA[4], pb ? wB[1] : wB[4]),
+                                             pk2(pa ? wA[2] : wA[3], pb ? wB[2] : wB[3]), pk2(pa ? wA[3] : wA[2], pb ? wB[3] : wB[2]),
+                                             pk2(pa ? wA[4] : wA[1], pb ? wB[4] : wB[1]));
+                    float ra, rb;
+                    up2(r, ra, rb);
+                    const TC FA = UA * ra, FB = UB * rb;
+                    vdA = (FzA - FA) * a.inv_dz;
+                    FzA = FA;
+                    vdB = (FzB - FB) * a.inv_dz;
+                    FzB = FB;
+                    win_done = true;
+                }
+            }
+#endif
+            if (!win_done && winA) {
                 const TC F = window_face_flux(wA[0], wA[1], wA[2], wA[3], wA[4], wA[5], k, a.Nz, a.drift[WA * (a.Nz + 1) + k]);
                 vdA = (FzA - F) * a.inv_dz;
                 FzA = F;
             }
-            if (winB) {
+            if (!win_done && winB) {
                 const TC F = window_face_flux(wB[0], wB[1], wB[2], wB[3], wB[4], wB[5], k, a.Nz, a.drift[WB * (a.Nz + 1) + k]);
                 vdB = (FzB - F) * a.inv_dz;
                 FzB = F;
