@@ -440,68 +440,30 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             // the tile's east (8 per tracer) and north (32 per tracer) edge faces, spread over
             // every thread of the block
             constexpr int NEDGE = STEP_BY + STEP_BX;
-            // edge face r of tracer t: r < STEP_BY the east face of tile row r, else the north face of
-            // tile column r - STEP_BY; its stencil in the tile, velocity and destination
-            auto edge = [&](int t, int r, const TC*& sp, int& st, int& f, int& N, bool& per, TC& U, TC*& dst) {
+#pragma unroll 1
+            for (int e = tid; e < NT * NEDGE; e += NTH) {
+                const int t = e / NEDGE, r = e - t * NEDGE;
                 const TC* tl = tiles + t * TILE_SZ;
                 if (r < STEP_BY) {
-                    const int jr = j0 + r;
-                    f = i0 + STEP_BX; N = a.Nx; per = periodic_x; st = 1;
-                    sp = tl + (r + HALO) * TILE_W + STEP_BX;
-                    dst = &fx[t][r][STEP_BX];
-                    const bool ok = !a.flat_x && jr < a.Ny && f <= a.Nx;
-                    U = ok ? face_velocity<TS, TC>(a.u, (int64_t)jr * a.sj + kofs, 1, a.Nx, periodic_x, f) : TC(0);
-                    return ok;
-                }
-                const int cc = r - STEP_BY, ix = i0 + cc;
-                f = j0 + STEP_BY; N = a.Ny; per = periodic_y; st = TILE_W;
-                sp = tl + STEP_BY * TILE_W + cc + HALO;
-                dst = &fy[t][STEP_BY][cc];
-                const bool ok = !a.flat_y && ix < a.Nx && f <= a.Ny;
-                U = ok ? face_velocity<TS, TC>(a.v, ix + kofs, a.sj, a.Ny, periodic_y, f) : TC(0);
-                return ok;
-            };
-            auto edge_scalar = [&](bool ok, const TC* sp, int st, int f, int N, bool per, TC U, TC* dst, bool xdir) {
-                TC Fe = TC(0);
-                if (ok) {
-                    Fe = tile_face_flux<TC>(sp, st, per, f, N, U);
-                    if (hdiff) Fe += tile_diff_flux<TC>(sp, st, per, f, N, xdir ? a.kh_dx : a.kh_dy);
-                }
-                *dst = Fe;
-            };
-            // two faces per item: in FP32 an interior pair is one packed f32x2 WENO5
-#pragma unroll 1
-            for (int e = tid; e < NT * (NEDGE / 2); e += NTH) {
-                const int t = e / (NEDGE / 2), r0 = 2 * (e - t * (NEDGE / 2)), r1 = r0 + 1;
-                const TC *s0, *s1;
-                int st0, st1, f0, f1, N0, N1;
-                bool p0, p1;
-                TC U0, U1;
-                TC *d0, *d1;
-                const bool ok0 = edge(t, r0, s0, st0, f0, N0, p0, U0, d0);
-                const bool ok1 = edge(t, r1, s1, st1, f1, N1, p1, U1, d1);
-                bool done = false;
-#ifdef __CUDA_ARCH__
-                if constexpr (sizeof(TC) == 4) {
-                    if (ok0 && ok1 && U0 != TC(0) && U1 != TC(0) && !hdiff && (p0 || min(f0, N0 - f0) >= 3) &&
-                        (p1 || min(f1, N1 - f1) >= 3)) {
-                        const bool q0 = U0 > TC(0), q1 = U1 > TC(0);
-                        const f32x2 rr = weno5_x2(pk2(q0 ? s0[0] : s0[5 * st0], q1 ? s1[0] : s1[5 * st1]),
-                                                  pk2(q0 ? s0[st0] : s0[4 * st0], q1 ? s1[st1] : s1[4 * st1]),
-                                                  pk2(q0 ? s0[2 * st0] : s0[3 * st0], q1 ? s1[2 * st1] : s1[3 * st1]),
-                                                  pk2(q0 ? s0[3 * st0] : s0[2 * st0], q1 ? s1[3 * st1] : s1[2 * st1]),
-                                                  pk2(q0 ? s0[4 * st0] : s0[st0], q1 ? s1[4 * st1] : s1[st1]));
-                        float r0v, r1v;
-                        up2(rr, r0v, r1v);
-                        *d0 = U0 * r0v;
-                        *d1 = U1 * r1v;
-                        done = true;
+                    const int jr = j0 + r, f = i0 + STEP_BX;
+                    TC Fe = TC(0);
+                    if (!a.flat_x && jr < a.Ny && f <= a.Nx) {
+                        const int64_t rb = (int64_t)jr * a.sj + kofs;
+                        Fe = tile_face_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx,
+                                                face_velocity<TS, TC>(a.u, rb, 1, a.Nx, periodic_x, f));
+                        if (hdiff) Fe += tile_diff_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx, a.kh_dx);
                     }
-                }
-#endif
-                if (!done) {
-                    edge_scalar(ok0, s0, st0, f0, N0, p0, U0, d0, r0 < STEP_BY);
-                    edge_scalar(ok1, s1, st1, f1, N1, p1, U1, d1, r1 < STEP_BY);
+                    fx[t][r][STEP_BX] = Fe;
+                } else {
+                    const int cc = r - STEP_BY, ix = i0 + cc, f = j0 + STEP_BY;
+                    TC Fe = TC(0);
+                    if (!a.flat_y && ix < a.Nx && f <= a.Ny) {
+                        const int64_t cb2 = ix + kofs;
+                        Fe = tile_face_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny,
+                                                face_velocity<TS, TC>(a.v, cb2, a.sj, a.Ny, periodic_y, f));
+                        if (hdiff) Fe += tile_diff_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny, a.kh_dy);
+                    }
+                    fy[t][STEP_BY][cc] = Fe;
                 }
             }
             // this cell's value of every tracer: read after the face loop (not live across it) and
