@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define OBGC_ABI_VERSION 1
+#define OBGC_ABI_VERSION 2
 
 /* ---------------------------------------------------------------------------------------
  * Status codes.  Host-side errors in the reference are Julia exceptions (ArgumentError at
@@ -75,6 +75,9 @@ enum obgc_tracer {
     OBGC_NUM_NAMED
 };
 #define OBGC_MAX_PASSIVE 8
+/* Tracer codes of the 3-D context's setters (gas exchange, forcing, sediment): a name of enum
+ * obgc_tracer, or OBGC_PASSIVE(p) for passive tracer p (obgc_fields.passive[p]). */
+#define OBGC_PASSIVE(p) (OBGC_NUM_NAMED + (p))
 
 /* Component kinds of NutrientsPlanktonDetritus (NutrientsPlanktonDetritus.jl:27-33). */
 enum obgc_nutrients { OBGC_NUT_NITRATE_AMMONIA = 0, OBGC_NUT_NITRATE_AMMONIA_IRON = 1, OBGC_NUT_NUTRIENT = 2 };
@@ -491,7 +494,8 @@ typedef struct obgc_model_desc {
     obgc_grid grid;
     int32_t precision;            /* enum obgc_precision                                      */
     int32_t advection;            /* enum obgc_advection (tracer + drift advection scheme)    */
-    int32_t n_passive;            /* extra advected tracers with zero BGC tendency            */
+    int32_t n_passive;            /* extra advected tracers (obgc_fields.passive[0..n_passive)):
+                                     zero BGC tendency unless passive_tendency_of says otherwise */
     int32_t carry_T;              /* T carried as an advected tracer even if BGC ignores it   */
     int32_t carry_S;              /* S carried as an advected tracer                          */
     int32_t negatives;            /* enum obgc_negatives                                      */
@@ -499,6 +503,10 @@ typedef struct obgc_model_desc {
                                      bit 21 + p = passive tracer p                            */
     int32_t reserved1;
     double invalid_fill_value;    /* ScaleNegativeTracers(...; invalid_fill_value) (NaN)      */
+    /* CarbonateSystem(N) replicates (carbonate_system.jl:41-83): passive tracer p takes the BGC
+     * tendency of tracer passive_tendency_of[p] - 1 (OBGC_DIC or OBGC_ALK; 0: none), as DIC2..DICN
+     * and Alk2..AlkN evaluate the DIC and Alk functors.  DIC1 / Alk1 are the named DIC / Alk. */
+    int8_t passive_tendency_of[OBGC_MAX_PASSIVE];
 } obgc_model_desc;
 
 /* Fields a context works on.  Tracer arrays are device pointers of the context's state dtype
@@ -549,6 +557,21 @@ int obgc_set_tiling(obgc_ctx* ctx, int32_t levels_per_item);
  * carries O2, T and S).  Each RK3 stage computes the flux of every column from the stage's surface
  * cells and the surface cell's tendency loses flux / dz.  g = NULL with `gas` clears that gas. */
 int obgc_set_gas_exchange(obgc_ctx* ctx, int32_t gas, const obgc_gas_exchange* g);
+/* The same condition on any tracer (a code of OBGC_PASSIVE's form): g->gas CO2 with the water's
+ * CO2 from the tracers `dic` and `alk` (CarbonDioxideConcentration(; DIC = :DIC2, Alk = :Alk2),
+ * carbon_dioxide_concentration.jl:13-60), or O2 with the tracer itself as the water's O2.  Up to
+ * OBGC_MAX_GAS_CONDITIONS conditions, one per tracer; g = NULL removes the tracer's condition.
+ * obgc_set_gas_exchange(ctx, CO2, g) is obgc_set_gas_exchange_on(ctx, OBGC_DIC, g, OBGC_DIC, OBGC_ALK). */
+#define OBGC_MAX_GAS_CONDITIONS 4
+int obgc_set_gas_exchange_on(obgc_ctx* ctx, int32_t tracer, const obgc_gas_exchange* g, int32_t dic, int32_t alk);
+/* forcing = (; X = F): a prescribed source rate (tracer units per second) added to tracer X's
+ * tendency in the fused step at every RK3 stage whose time t (Oceananigans' stage clock) satisfies
+ * t_start <= t < t_end (+-INFINITY for always).  `rate` is a device field of the context's state
+ * dtype on the grid's layout; it stays the caller's and is read at every stage.  With a spatial
+ * mask it expresses the windowed release of examples/oae_experiment.jl:55-79.  Up to
+ * OBGC_MAX_FORCINGS tracers; rate = NULL removes the tracer's forcing. */
+#define OBGC_MAX_FORCINGS 4
+int obgc_set_forcing(obgc_ctx* ctx, int32_t tracer, const void* rate, double t_start, double t_end);
 /* closure = ScalarDiffusivity(κ) (explicit time discretization) on every tracer of the fused step:
  * a horizontal diffusivity kappa_h (m2/s, x and y faces) and a vertical one, kappa_z constant or
  * kappa_z_faces[Nz + 1] (face f below cell f; the bottom and top faces are walls and carry no

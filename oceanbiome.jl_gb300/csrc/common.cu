@@ -97,7 +97,7 @@ extern "C" int obgc_struct_layout(int32_t which, int64_t* out, int32_t cap) {
                 out[2] = offsetof(obgc_carbon_options, atol);
                 out[3] = offsetof(obgc_carbon_options, saturation_mineral); return 0;
         case 5: out[0] = sizeof(obgc_model_desc); out[1] = offsetof(obgc_model_desc, surface);
-                out[2] = offsetof(obgc_model_desc, grid); out[3] = offsetof(obgc_model_desc, invalid_fill_value); return 0;
+                out[2] = offsetof(obgc_model_desc, grid); out[3] = offsetof(obgc_model_desc, passive_tendency_of); return 0;
         case 6: out[0] = sizeof(obgc_fields); out[1] = offsetof(obgc_fields, passive);
                 out[2] = offsetof(obgc_fields, u); out[3] = offsetof(obgc_fields, G); return 0;
         case 7: out[0] = sizeof(obgc_column_spec); out[1] = offsetof(obgc_column_spec, dz);

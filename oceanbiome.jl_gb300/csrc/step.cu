@@ -126,11 +126,30 @@ struct obgc_ctx {
     void* G[MAX_NT] = {};
     void* drift = nullptr;
     uint32_t drift_mask = 0;
-    NegativesSpec neg;                  // negative-tracer modifier over the slots
-    // air-sea gas exchange (top boundary condition): [0] CO2 on DIC, [1] O2 on O2
-    bool gas_on[2] = {false, false};
-    obgc_gas_exchange gas[2];
-    double* gas_flux[2] = {nullptr, nullptr};   // (Nx, Ny) per stage
+    NegativesSpec neg;                  // negative-tracer modifier over the main slots
+    // passive tracers: slots NT .. NT + NP - 1 (names OBGC_PASSIVE(p)), stepped by the
+    // external-tendency kernel in launches of 4, 2 and 1 (pchunk); psrc[p]: the named tracer whose
+    // BGC tendency passive p takes (OBGC_DIC / OBGC_ALK for CarbonateSystem replicates), or -1
+    int NP = 0;
+    int psrc[OBGC_MAX_PASSIVE];
+    int nchunk = 0;
+    int pchunk[OBGC_MAX_PASSIVE];
+    int pblocks[5] = {0, 0, 0, 0, 0};   // persistent grid of the 1-, 2- and 4-tracer launches
+    NegativesSpec neg_passive;          // ZeroNegativeTracers over the passive slots (else off)
+    void* bgc_out[2] = {nullptr, nullptr};   // BGC tendencies of DIC and Alk (compute precision)
+    // air-sea gas exchange (top boundary conditions), one per target slot
+    struct GasCond {
+        bool on = false;
+        obgc_gas_exchange g;
+        int target = -1, dic = -1, alk = -1;   // slots
+        double* flux = nullptr;                 // (Nx, Ny) per stage
+    } gas[OBGC_MAX_GAS_CONDITIONS];
+    // forcings (prescribed source-rate fields), one per target slot
+    struct ForcingSpec {
+        int slot = -1;
+        const void* rate = nullptr;
+        double t0 = 0, t1 = 0;
+    } frc[OBGC_MAX_FORCINGS];
     // ScalarDiffusivity (explicit): horizontal kappa, and kappa / dz^2 at the Nz + 1 faces (device,
     // compute precision), or nullptr
     double kappa_h = 0.0;
@@ -166,7 +185,7 @@ struct obgc_ctx {
 static int ctx_free(obgc_ctx* c) {
     if (!c) return OBGC_OK;
     if (c->graph) cudaGraphExecDestroy(c->graph);
-    for (int t = 0; t < MAX_NT; t++) {
+    for (int t = 0; t < MAX_NT; t++) {   // main and passive slots
         if (c->scratch[t]) cudaFree(c->scratch[t]);
         if (c->G[t]) cudaFree(c->G[t]);
     }
@@ -174,8 +193,10 @@ static int ctx_free(obgc_ctx* c) {
     if (c->d_time) cudaFree(c->d_time);
     if (c->partial) cudaFree(c->partial);
     if (c->d_budget) cudaFree(c->d_budget);
+    for (auto& gc : c->gas)
+        if (gc.flux) cudaFree(gc.flux);
     for (int q = 0; q < 2; q++)
-        if (c->gas_flux[q]) cudaFree(c->gas_flux[q]);
+        if (c->bgc_out[q]) cudaFree(c->bgc_out[q]);
     if (c->kzz) cudaFree(c->kzz);
     if (c->sed_storage) cudaFree(c->sed_storage);
     if (c->sed_G) cudaFree(c->sed_G);
@@ -192,7 +213,8 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
     const obgc_grid& g = desc->grid;
     if (!valid_grid(&g)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: invalid grid descriptor");
     if (desc->precision < 0 || desc->precision > 2) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: bad precision");
-    if (desc->n_passive != 0) return fail(OBGC_ERR_UNSUPPORTED, "obgc_create: passive tracers are not supported");
+    if (desc->n_passive < 0 || desc->n_passive > OBGC_MAX_PASSIVE)
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: n_passive outside 0..8");
     if (desc->negatives < OBGC_NEGATIVES_NONE || desc->negatives > OBGC_NEGATIVES_ZERO)
         return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: bad negatives mode");
     int ndev = 0;
@@ -215,18 +237,48 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
     if (desc->carry_T && !hasT && nt < MAX_NT) c->names[nt++] = OBGC_T;
     if (desc->carry_S && nt < MAX_NT) c->names[nt++] = OBGC_S;
     c->NT = nt;
+    // passive slots after the main ones; a tendency source must be a carbonate tracer of the model
+    c->NP = desc->n_passive;
+    bool need_out[2] = {false, false};
+    for (int p = 0; p < c->NP; p++) {
+        const int src = desc->passive_tendency_of[p] - 1;
+        bool carried = false;
+        for (int q = 0; q < nreq; q++) carried |= req[q] == src;
+        if (src != -1 && (!(src == OBGC_DIC || src == OBGC_ALK) || !carried)) {
+            delete c;
+            return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_create: a passive tracer's tendency source must be the model's DIC or Alk");
+        }
+        c->psrc[p] = src;
+        if (src >= 0) need_out[src == OBGC_ALK] = true;
+        c->names[c->NT + p] = OBGC_PASSIVE(p);
+    }
+    for (int r = c->NP; r > 0;) {   // launches of 4, 2 and 1 passive tracers
+        const int n = r >= 4 ? 4 : r >= 2 ? 2 : 1;
+        c->pchunk[c->nchunk++] = n;
+        r -= n;
+    }
     c->extent = g.stride_k * (int64_t)g.Nz;
     int rc = negatives_spec(desc->npd, desc->negatives, c->NT, c->names, desc->zero_exclude, desc->invalid_fill_value,
                             &c->neg);
+    if (rc == OBGC_OK && c->NP > 0) {
+        // ZeroNegativeTracers reaches every tracer of the model (negative_tracers.jl:23-29); the
+        // ScaleNegativeTracers groups are named conserved tracers, none of them passive
+        int pn[OBGC_MAX_PASSIVE];
+        for (int p = 0; p < c->NP; p++) pn[p] = -1;
+        rc = negatives_spec(desc->npd, desc->negatives == OBGC_NEGATIVES_ZERO ? OBGC_NEGATIVES_ZERO : OBGC_NEGATIVES_NONE,
+                            c->NP, pn, desc->zero_exclude, desc->invalid_fill_value, &c->neg_passive);
+    }
     auto alloc = [&](void** p, size_t bytes) {
         if (rc != OBGC_OK) return;
         cudaError_t e = cudaMalloc(p, bytes);
         if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc");
     };
-    for (int t = 0; t < c->NT; t++) {
+    for (int t = 0; t < c->NT + c->NP; t++) {
         alloc(&c->scratch[t], c->ts * c->extent);
         alloc(&c->G[t], c->tc * c->extent);
     }
+    for (int q = 0; q < 2; q++)
+        if (need_out[q]) alloc(&c->bgc_out[q], c->tc * c->extent);
     // drift profiles of every slot (only non-zero ones are flagged)
     std::vector<double> prof((size_t)MAX_NT * (g.Nz + 1), 0.0);
     for (int t = 0; t < c->NT; t++) {
@@ -264,6 +316,14 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
             if (r2 != OBGC_OK) rc = r2;
         }
         c->blocks = nsm * (bps > 0 ? bps : 1);
+        for (int q = 0; q < c->nchunk && rc == OBGC_OK; q++) {
+            const int n = c->pchunk[q];
+            const FusedEntry* pe = find_fused(c->prec, V_EXTERNAL, n);
+            if (!pe) { rc = fail(OBGC_ERR_UNSUPPORTED, "obgc_create: no passive-tracer kernel for this precision"); break; }
+            int pb = 1;
+            rc = pe->occupancy(&pb);
+            c->pblocks[n] = nsm * (pb > 0 ? pb : 1);
+        }
     }
     if (rc != OBGC_OK) {
         ctx_free(c);
@@ -282,6 +342,10 @@ extern "C" int obgc_bind_fields(obgc_ctx* c, const obgc_fields* f) {
         if (!p) return fail(OBGC_ERR_INVALID_ARGUMENT, std::string("obgc_bind_fields: missing tracer slot ") + std::to_string(c->names[t]));
         c->user[t] = p;
     }
+    for (int p = 0; p < c->NP; p++) {
+        if (!f->passive[p]) return fail(OBGC_ERR_INVALID_ARGUMENT, std::string("obgc_bind_fields: missing passive tracer ") + std::to_string(p));
+        c->user[c->NT + p] = f->passive[p];
+    }
     c->fields = *f;
     c->bound = true;
     c->bind_version++;
@@ -294,29 +358,68 @@ extern "C" int obgc_set_profiling(obgc_ctx* c, int32_t on) {
     return OBGC_OK;
 }
 
+// slot of a tracer code (enum obgc_tracer or OBGC_PASSIVE(p)), or -1
 static int slot_named(const obgc_ctx* c, int name) {
-    for (int t = 0; t < c->NT; t++)
+    for (int t = 0; t < c->NT + c->NP; t++)
         if (c->names[t] == name) return t;
     return -1;
 }
 
-extern "C" int obgc_set_gas_exchange(obgc_ctx* c, int32_t gas, const obgc_gas_exchange* g) {
-    if (!c || (gas != OBGC_GAS_CO2 && gas != OBGC_GAS_O2) || (g && (!valid_gas(g) || g->gas != gas)))
-        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_gas_exchange: bad argument");
-    const int q = gas == OBGC_GAS_CO2 ? 0 : 1;
-    if (!g) {
-        c->gas_on[q] = false;
+extern "C" int obgc_set_gas_exchange_on(obgc_ctx* c, int32_t tracer, const obgc_gas_exchange* g, int32_t dic, int32_t alk) {
+    if (!c || (g && !valid_gas(g))) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_gas_exchange_on: bad argument");
+    const int target = slot_named(c, tracer);
+    if (target < 0) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_gas_exchange_on: the model does not carry the tracer");
+    obgc_ctx::GasCond* slot = nullptr;
+    for (auto& gc : c->gas)
+        if (gc.on && gc.target == target) slot = &gc;
+    if (!g) {   // remove the tracer's condition
+        if (slot) slot->on = false;
         c->bind_version++;
         return OBGC_OK;
     }
-    const bool ok = slot_named(c, OBGC_T) >= 0 && slot_named(c, OBGC_S) >= 0 &&
-                    (gas == OBGC_GAS_CO2 ? slot_named(c, OBGC_DIC) >= 0 && slot_named(c, OBGC_ALK) >= 0
-                                         : slot_named(c, OBGC_O2) >= 0);
-    if (!ok) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_gas_exchange: the model does not carry the tracers this gas needs");
-    if (!c->gas_flux[q]) OBGC_CUDA(cudaMalloc(&c->gas_flux[q], sizeof(double) * (size_t)c->desc.grid.Nx * c->desc.grid.Ny));
-    c->gas[q] = *g;
-    c->gas_on[q] = true;
+    const int sd = g->gas == OBGC_GAS_CO2 ? slot_named(c, dic) : -1, sa = g->gas == OBGC_GAS_CO2 ? slot_named(c, alk) : -1;
+    if (slot_named(c, OBGC_T) < 0 || slot_named(c, OBGC_S) < 0 || (g->gas == OBGC_GAS_CO2 && (sd < 0 || sa < 0)))
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_gas_exchange: the model does not carry the tracers this gas needs");
+    for (auto& gc : c->gas)
+        if (!slot && !gc.on) slot = &gc;
+    if (!slot) return fail(OBGC_ERR_UNSUPPORTED, "obgc_set_gas_exchange_on: more than 4 gas exchange conditions");
+    if (!slot->flux) OBGC_CUDA(cudaMalloc(&slot->flux, sizeof(double) * (size_t)c->desc.grid.Nx * c->desc.grid.Ny));
+    slot->g = *g;
+    slot->target = target;
+    slot->dic = sd;
+    slot->alk = sa;
+    slot->on = true;
     c->bind_version++;   // a captured graph holds the previous flux setup
+    return OBGC_OK;
+}
+
+extern "C" int obgc_set_gas_exchange(obgc_ctx* c, int32_t gas, const obgc_gas_exchange* g) {
+    if (!c || (gas != OBGC_GAS_CO2 && gas != OBGC_GAS_O2) || (g && g->gas != gas))
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_gas_exchange: bad argument");
+    return obgc_set_gas_exchange_on(c, gas == OBGC_GAS_CO2 ? OBGC_DIC : OBGC_O2, g, OBGC_DIC, OBGC_ALK);
+}
+
+extern "C" int obgc_set_forcing(obgc_ctx* c, int32_t tracer, const void* rate, double t_start, double t_end) {
+    if (!c || std::isnan(t_start) || std::isnan(t_end) || t_end < t_start)
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_forcing: bad argument");
+    const int t = slot_named(c, tracer);
+    if (t < 0) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_forcing: the model does not carry the tracer");
+    obgc_ctx::ForcingSpec* f = nullptr;
+    for (auto& x : c->frc)
+        if (x.rate && x.slot == t) f = &x;
+    if (!rate) {
+        if (f) *f = obgc_ctx::ForcingSpec();
+        c->bind_version++;
+        return OBGC_OK;
+    }
+    for (auto& x : c->frc)
+        if (!f && !x.rate) f = &x;
+    if (!f) return fail(OBGC_ERR_UNSUPPORTED, "obgc_set_forcing: more than 4 forced tracers");
+    f->slot = t;
+    f->rate = rate;
+    f->t0 = t_start;
+    f->t1 = t_end;
+    c->bind_version++;
     return OBGC_OK;
 }
 
@@ -357,14 +460,15 @@ extern "C" int obgc_set_sediment(obgc_ctx* c, int32_t n_sinking, const int32_t* 
         c->bind_version++;
         return OBGC_OK;
     }
+    // the sediment couples to the main launch's slots (passive tracers neither sink nor receive)
     uint32_t mask = 0;
     for (int q = 0; q < n_sinking; q++) {
         const int t = slot_named(c, sinking_names[q]);
-        if (t < 0) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_sediment: a sinking tracer is not carried by the model");
+        if (t < 0 || t >= c->NT) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_sediment: a sinking tracer is not carried by the model");
         mask |= 1u << t;
     }
     const int r = slot_named(c, receiver_name);
-    if (r < 0) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_sediment: the receiver is not carried by the model");
+    if (r < 0 || r >= c->NT) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_sediment: the receiver is not carried by the model");
     const size_t cols = (size_t)c->desc.grid.Nx * c->desc.grid.Ny;
     if (!c->sed_storage) {
         OBGC_CUDA(cudaMalloc(&c->sed_storage, c->ts * cols));
@@ -417,7 +521,9 @@ extern "C" int obgc_update_state(obgc_ctx* c, double t, void* stream) {
         // update_biogeochemical_state! runs the modifiers before the light (src/OceanBioME.jl:161-167)
         void* f[MAX_NT];
         for (int t = 0; t < c->NT; t++) f[t] = c->user[t];
-        const int rc = launch_negatives(c->neg, c->ts, f, c->desc.grid, static_cast<cudaStream_t>(stream));
+        int rc = launch_negatives(c->neg, c->ts, f, c->desc.grid, static_cast<cudaStream_t>(stream));
+        if (rc == OBGC_OK && c->neg_passive.mode != OBGC_NEGATIVES_NONE)
+            rc = launch_negatives(c->neg_passive, c->ts, &c->user[c->NT], c->desc.grid, static_cast<cudaStream_t>(stream));
         if (rc != OBGC_OK) return rc;
     }
     const void* P = c->fields.tracers[OBGC_P];
@@ -481,51 +587,120 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.sed_G = (TC*)c->sed_G;
 }
 
+// Whether the device clock (d_time) must advance with the steps: the default surface PAR and the
+// forcing windows read it.
+static bool needs_clock(const obgc_ctx* c) {
+    bool f = false;
+    for (const auto& x : c->frc) f = f || x.rate != nullptr;
+    return c->desc.surface.kind == OBGC_SURFACE_PAR_DEFAULT || f;
+}
+
+// The surface-flux and forcing slots of the launch over slots [b, b + n).
+template <typename TS, typename TC>
+static void launch_terms(const obgc_ctx* c, SubstepArgs<TS, TC>& a, int b, int n) {
+    int nt = 0, nf = 0;
+    for (int q = 0; q < MAX_TOP; q++) { a.top_slot1[q] = 0; a.top_flux[q] = nullptr; }
+    for (const auto& gc : c->gas)
+        if (gc.on && gc.target >= b && gc.target < b + n && nt < MAX_TOP) {
+            a.top_slot1[nt] = gc.target - b + 1;
+            a.top_flux[nt++] = gc.flux;
+        }
+    for (int q = 0; q < MAX_FRC; q++) { a.frc_slot1[q] = 0; a.frc[q] = nullptr; }
+    for (const auto& f : c->frc)
+        if (f.rate && f.slot >= b && f.slot < b + n && nf < MAX_FRC) {
+            a.frc_slot1[nf] = f.slot - b + 1;
+            a.frc[nf] = (const TS*)f.rate;
+            a.frc_t0[nf] = f.t0;
+            a.frc_t1[nf++] = f.t1;
+        }
+}
+
 // Enqueue nsteps steps on stream st (no synchronisation).  The state ping-pongs between the bound
 // arrays and the context's scratch buffers; after an odd number of substeps the interior is copied
-// back so the bound arrays always hold the result.
+// back so the bound arrays always hold the result.  Per RK3 stage: the gas-exchange flux of every
+// condition, the main launch (the model's tracers, T and S), then the passive launches (their BGC
+// tendency, if any, is the main launch's DIC / Alk tendency of the same stage).
 template <typename TS, typename TC>
 static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nsteps, cudaStream_t st, bool profile) {
     SubstepArgs<TS, TC> a;
     fill_args<TS, TC>(c, a);
     a.dt_d = dt;
     a.dt = TC(dt);
+    a.bgc_out[0] = (TC*)c->bgc_out[0];
+    a.bgc_out[1] = (TC*)c->bgc_out[1];
+    // the passive launches: no drift, no sediment, ZeroNegativeTracers only
+    SubstepArgs<TS, TC> ap = a;
+    ap.drift_mask = 0;
+    ap.sed_recv1 = 0;
+    ap.sed_sink_mask = 0;
+    ap.bgc_out[0] = ap.bgc_out[1] = nullptr;
+    const FusedEntry* pe[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    for (int q = 0; q < c->nchunk; q++) {
+        pe[c->pchunk[q]] = find_fused(c->prec, V_EXTERNAL, c->pchunk[q]);
+        if (!pe[c->pchunk[q]]) return fail(OBGC_ERR_UNSUPPORTED, "obgc_step: no passive-tracer kernel for this precision");
+    }
+    const int NS = c->NT + c->NP;
     void* cur[MAX_NT];
     void* nxt[MAX_NT];
-    for (int t = 0; t < c->NT; t++) { cur[t] = c->user[t]; nxt[t] = c->scratch[t]; }
-    const bool clock = c->desc.surface.kind == OBGC_SURFACE_PAR_DEFAULT;
+    for (int t = 0; t < NS; t++) { cur[t] = c->user[t]; nxt[t] = c->scratch[t]; }
+    const bool clock = needs_clock(c);
     int blocks = c->blocks < a.n_items ? c->blocks : a.n_items;
     size_t ev = 0;
     const obgc_grid& grid = c->desc.grid;
     if (c->neg.mode != OBGC_NEGATIVES_NONE) {
         // the state entering the first stage has been through update_state! (iteration 0); applying
         // the modifier again to a state it already produced changes nothing
-        const int rc = launch_negatives(c->neg, sizeof(TS), cur, grid, st);
+        int rc = launch_negatives(c->neg, sizeof(TS), cur, grid, st);
+        if (rc == OBGC_OK && c->neg_passive.mode != OBGC_NEGATIVES_NONE)
+            rc = launch_negatives(c->neg_passive, sizeof(TS), cur + c->NT, grid, st);
         if (rc != OBGC_OK) return rc;
     }
     for (int s = 0; s < nsteps; s++) {
         for (int stg = 0; stg < 3; stg++) {
-            for (int t = 0; t < c->NT; t++) { a.in[t] = (const TS*)cur[t]; a.out[t] = (TS*)nxt[t]; }
-            a.first_stage = stg == 0;
-            a.write_G = stg < 2;
-            a.gamma = TC(rk3_gamma(stg));
-            a.zeta = TC(rk3_zeta(stg));
-            a.c_stage = rk3_c(stg);
-            for (int q = 0; q < 2; q++) {
-                a.top_slot1[q] = 0;
-                if (!c->gas_on[q]) continue;
-                auto at = [&](int name) -> const void* { const int t = slot_named(c, name); return t >= 0 ? cur[t] : nullptr; };
-                const int rg = launch_gas_exchange<TS>(&c->gas[q], &grid, at(OBGC_T), at(OBGC_S), at(OBGC_DIC), at(OBGC_ALK),
-                                                       at(OBGC_O2), c->gas_flux[q], st);
+            for (const auto& gc : c->gas) {
+                if (!gc.on) continue;
+                auto at = [&](int slot) -> const void* { return slot >= 0 ? cur[slot] : nullptr; };
+                const bool co2 = gc.g.gas == OBGC_GAS_CO2;
+                const int rg = launch_gas_exchange<TS>(&gc.g, &grid, at(slot_named(c, OBGC_T)), at(slot_named(c, OBGC_S)),
+                                                       co2 ? at(gc.dic) : nullptr, co2 ? at(gc.alk) : nullptr,
+                                                       co2 ? nullptr : at(gc.target), gc.flux, st);
                 if (rg != OBGC_OK) return rg;
-                a.top_slot1[q] = slot_named(c, q == 0 ? OBGC_DIC : OBGC_O2) + 1;
-                a.top_flux[q] = c->gas_flux[q];
             }
+            for (SubstepArgs<TS, TC>* x : {&a, &ap}) {
+                x->first_stage = stg == 0;
+                x->write_G = stg < 2;
+                x->gamma = TC(rk3_gamma(stg));
+                x->zeta = TC(rk3_zeta(stg));
+                x->c_stage = rk3_c(stg);
+            }
+            for (int t = 0; t < c->NT; t++) { a.in[t] = (const TS*)cur[t]; a.out[t] = (TS*)nxt[t]; }
+            launch_terms(c, a, 0, c->NT);
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
             int rc = fe->launch(&a, blocks, st);
             if (rc != OBGC_OK) return rc;
+            for (int q = 0, b = c->NT; q < c->nchunk; b += c->pchunk[q++]) {
+                const int n = c->pchunk[q];
+                for (int t = 0; t < MAX_NT; t++) { ap.in[t] = nullptr; ap.out[t] = nullptr; ap.G[t] = nullptr; ap.ext[t] = nullptr; }
+                for (int t = 0; t < n; t++) {
+                    ap.in[t] = (const TS*)cur[b + t];
+                    ap.out[t] = (TS*)nxt[b + t];
+                    ap.G[t] = (TC*)c->G[b + t];
+                    const int src = c->psrc[b + t - c->NT];
+                    ap.ext[t] = src < 0 ? nullptr : (const TC*)c->bgc_out[src == OBGC_ALK];
+                }
+                ap.n_ext = n;
+                ap.neg = c->neg_passive;
+                if (ap.neg.mode != OBGC_NEGATIVES_NONE) {
+                    ap.neg.nt = n;
+                    ap.neg.zero_skip = (c->neg_passive.zero_skip >> (b - c->NT)) & ((1u << n) - 1u);
+                }
+                launch_terms(c, ap, b, n);
+                const int pb = c->pblocks[n] < ap.n_items ? c->pblocks[n] : ap.n_items;
+                rc = pe[n]->launch(&ap, pb, st);
+                if (rc != OBGC_OK) return rc;
+            }
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
-            for (int t = 0; t < c->NT; t++) { void* tmp = cur[t]; cur[t] = nxt[t]; nxt[t] = tmp; }
+            for (int t = 0; t < NS; t++) { void* tmp = cur[t]; cur[t] = nxt[t]; nxt[t] = tmp; }
         }
         if (clock) {
             advance_time_kernel<<<1, 1, 0, st>>>(c->d_time, dt);
@@ -535,7 +710,7 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
     if (nsteps % 2 == 1) {
         const obgc_grid& g = c->desc.grid;
         const int64_t N = (int64_t)g.Nx * g.Ny * g.Nz;
-        for (int t = 0; t < c->NT; t++) {
+        for (int t = 0; t < NS; t++) {
             copy_interior_kernel<TS><<<(unsigned)((N + 255) / 256), 256, 0, st>>>((const TS*)cur[t], (TS*)c->user[t], g.Nx,
                                                                                 g.Ny, g.Nz, g.stride_j, g.stride_k);
             OBGC_LAUNCHED("copy_interior_kernel");
@@ -553,10 +728,11 @@ static int dispatch_steps(obgc_ctx* c, double dt, int nsteps, cudaStream_t st, b
 }
 
 static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
-    const bool clock = c->desc.surface.kind == OBGC_SURFACE_PAR_DEFAULT;
-    const bool neg = c->neg.mode != OBGC_NEGATIVES_NONE;
-    const int gases = (c->gas_on[0] ? 1 : 0) + (c->gas_on[1] ? 1 : 0);
-    return (int64_t)nsteps * (3 + (clock ? 1 : 0) + 3 * gases) + (nsteps % 2 ? c->NT : 0) + 1 + (neg ? 1 : 0);
+    const bool clock = needs_clock(c);
+    const int neg = c->neg.mode == OBGC_NEGATIVES_NONE ? 0 : c->neg_passive.mode != OBGC_NEGATIVES_NONE ? 2 : 1;
+    int gases = 0;
+    for (const auto& gc : c->gas) gases += gc.on ? 1 : 0;
+    return (int64_t)nsteps * (3 * (1 + c->nchunk + gases) + (clock ? 1 : 0)) + (nsteps % 2 ? c->NT + c->NP : 0) + 1 + neg;
 }
 
 extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {

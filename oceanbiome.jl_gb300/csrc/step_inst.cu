@@ -25,8 +25,10 @@ typedef float TC_;
 #endif
 
 constexpr int V_ = OBGC_INST_V;
-// tracer counts with a kernel: the BGC tracers alone, and followed by the carried T/S (PISCES:
-// groups of 9 and 8 of its 26 slots)
+// tracer counts with a kernel: the BGC tracers alone, and followed by the carried T/S.  The
+// external-tendency variant serves the PISCES groups of 9 and 8 of its 26 slots (FP32 and mixed)
+// and the passive tracers of every model (CarbonateSystem replicates included) in launches of 4,
+// 2 and 1 tracers.
 [[maybe_unused]] constexpr int NT_A = V_ == V_EXTERNAL ? 9 : n_bgc(V_);
 [[maybe_unused]] constexpr int NT_B = V_ == V_NPZD ? 6 : V_ == V_EXTERNAL ? 8 : n_bgc(V_) + 2;
 
@@ -37,16 +39,20 @@ int launch_fn(const void* a, int blocks, cudaStream_t st) {
 template <int NT>
 int occupancy_fn(int* bps) { return occupancy_one<V_, NT, TS_, TC_>(bps); }
 
-// the PISCES model steps in FP32 and mixed precision only
-#if !(OBGC_INST_V == 5 && OBGC_INST_PREC == 1)
 struct Registrar {
     Registrar() {
+#if OBGC_INST_V == 5
+        register_fused({OBGC_INST_PREC, V_, 1, &launch_fn<1>, &occupancy_fn<1>});
+        register_fused({OBGC_INST_PREC, V_, 2, &launch_fn<2>, &occupancy_fn<2>});
+        register_fused({OBGC_INST_PREC, V_, 4, &launch_fn<4>, &occupancy_fn<4>});
+#endif
+#if !(OBGC_INST_V == 5 && OBGC_INST_PREC == 1)   // the PISCES model steps in FP32 and mixed precision
         register_fused({OBGC_INST_PREC, V_, NT_A, &launch_fn<NT_A>, &occupancy_fn<NT_A>});
         if (NT_B != NT_A) register_fused({OBGC_INST_PREC, V_, NT_B, &launch_fn<NT_B>, &occupancy_fn<NT_B>});
+#endif
     }
 };
 Registrar registrar;
-#endif
 
 }  // namespace
 }  // namespace obgc

@@ -26,6 +26,8 @@ namespace obgc {
 constexpr int STEP_BX = 32;
 constexpr int STEP_BY = 8;
 constexpr int MAX_NT = 26;
+constexpr int MAX_TOP = 4;      // surface-flux slots per launch
+constexpr int MAX_FRC = 4;      // forced slots per launch
 
 // Tracer slot order of the fused variants: the reference's required_biogeochemical_tracers order,
 // then T and S when they are carried without a BGC tendency.
@@ -57,13 +59,21 @@ struct SubstepArgs {
     const TS* in[MAX_NT];
     TS* out[MAX_NT];
     TC* G[MAX_NT];
-    const TC* ext[MAX_NT];    // V_EXTERNAL: the BGC tendency of slot t (t < n_ext)
+    const TC* ext[MAX_NT];    // V_EXTERNAL: the BGC tendency of slot t (t < n_ext; NULL: none)
     int n_ext;                // V_EXTERNAL: slots of this launch with an external tendency
     // surface fluxes (air-sea gas exchange): slot top_slot1[q] - 1 (none when 0, so zeroed arguments
     // carry no flux) loses top_flux[q][i + j Nx] / dz in its surface cell: the divergence of a flux
     // through the top face, positive out of the ocean
-    int top_slot1[2];
-    const double* top_flux[2];
+    int top_slot1[MAX_TOP];
+    const double* top_flux[MAX_TOP];
+    // forcing: slot frc_slot1[q] - 1 gains the rate frc[q][idx] while the stage time lies in
+    // [frc_t0[q], frc_t1[q])
+    int frc_slot1[MAX_FRC];
+    const TS* frc[MAX_FRC];
+    double frc_t0[MAX_FRC], frc_t1[MAX_FRC];
+    // CarbonateSystem replicates: the cell's BGC tendencies of DIC and Alk, written for the
+    // launches of the replicate tracers (NULL: not written)
+    TC* bgc_out[2];
     // negative-tracer modifier (update_state!) on the cell's new values, fused into the update
     // (mode OBGC_NEGATIVES_NONE: off)
     NegativesSpec neg;
@@ -241,12 +251,16 @@ __device__ __forceinline__ TC vertical_flux(const SubstepArgs<TS, TC>& a, const 
     return F;
 }
 
-// Whether a launch uses any of the optional terms (diffusivity closure, surface fluxes, the fused
-// negative-tracer modifier); without them the lean instantiation (EXT = false) runs.
+// Whether a launch uses any of the optional terms (diffusivity closure, surface fluxes, forcing,
+// the fused negative-tracer modifier, the sediment, replicate tendencies); without them the lean
+// instantiation (EXT = false) runs.
 template <typename TS, typename TC>
 __host__ __device__ inline bool substep_needs_ext(const SubstepArgs<TS, TC>& a) {
-    return a.kh_dx != TC(0) || a.kh_dy != TC(0) || a.kzz != nullptr || a.top_slot1[0] != 0 || a.top_slot1[1] != 0 ||
-           a.neg.mode != OBGC_NEGATIVES_NONE || a.sed_recv1 != 0;
+    bool any = a.kh_dx != TC(0) || a.kh_dy != TC(0) || a.kzz != nullptr || a.neg.mode != OBGC_NEGATIVES_NONE ||
+               a.sed_recv1 != 0 || a.bgc_out[0] != nullptr || a.bgc_out[1] != nullptr;
+    for (int q = 0; q < MAX_TOP; q++) any = any || a.top_slot1[q] != 0;
+    for (int q = 0; q < MAX_FRC; q++) any = any || a.frc_slot1[q] != 0;
+    return any;
 }
 
 template <int V, int NT, typename TS, typename TC, bool EXT>
@@ -286,6 +300,22 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     const bool gm_smem = !any_generic && !a.first_stage;
     // shared-space address of this thread's first tile element
     const unsigned tiles_s = (unsigned)__cvta_generic_to_shared(tiles) + 4u * (unsigned)tid;
+
+    // forcings switched on at this stage's time
+    bool frc_on[MAX_FRC];
+#pragma unroll
+    for (int q = 0; q < MAX_FRC; q++) frc_on[q] = false;
+    if constexpr (EXT) {
+        bool any_frc = false;
+#pragma unroll
+        for (int q = 0; q < MAX_FRC; q++) any_frc = any_frc || a.frc_slot1[q] != 0;
+        if (any_frc) {   // d_time is only required of launches with a forcing
+            const double t_stage = *a.d_time + a.c_stage * a.dt_d;
+#pragma unroll
+            for (int q = 0; q < MAX_FRC; q++)
+                frc_on[q] = a.frc_slot1[q] != 0 && t_stage >= a.frc_t0[q] && t_stage < a.frc_t1[q];
+        }
+    }
 
     TC PAR0 = TC(0);
     if constexpr (V != V_EXTERNAL) {
@@ -559,6 +589,10 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 #pragma unroll
                 for (int s = 0; s < NB; s++) vals[slot_name(V, s)] = c[s];
                 npd_tendencies<V, TC>(a.bgc, vals, PAR, g);
+                if constexpr (EXT) {
+                    if (active && a.bgc_out[0]) a.bgc_out[0][idx] = g[OBGC_DIC];
+                    if (active && a.bgc_out[1]) a.bgc_out[1][idx] = g[OBGC_ALK];
+                }
             }
 
 #pragma unroll
@@ -571,7 +605,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 if (t == WB) adv += vdB;
                 TC Gb = TC(0);
                 if constexpr (V == V_EXTERNAL) {
-                    if (t < a.n_ext) Gb = a.ext[t][idx];
+                    if (t < a.n_ext && a.ext[t] != nullptr) Gb = a.ext[t][idx];
                 } else {
                     if (t < NB) Gb = g[slot_name(V, t)];
                 }
@@ -580,9 +614,12 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if (t + 1 == a.sed_recv1) Gt += sed_remin;   // zero above the bottom cell
                     if (k == a.Nz - 1) {
 #pragma unroll
-                        for (int q = 0; q < 2; q++)
+                        for (int q = 0; q < MAX_TOP; q++)
                             if (t + 1 == a.top_slot1[q]) Gt -= TC(a.top_flux[q][ic + (int64_t)jc * a.Nx]) * a.inv_dz;
                     }
+#pragma unroll
+                    for (int q = 0; q < MAX_FRC; q++)
+                        if (frc_on[q] && t + 1 == a.frc_slot1[q] && active) Gt += ld<TS, TC>(a.frc[q], idx);
                 }
                 if (active) {
                     TC Un;

@@ -1,22 +1,10 @@
-// step_launch.cuh — instantiation helpers for the fused substep kernel.  Each precision lives in
-// its own translation unit (step_f32.cu, step_f64.cu, step_mixed.cu) so they compile in parallel.
+// step_launch.cuh — instantiation helpers for the fused substep kernel.  Each (precision, variant)
+// slice is its own translation unit (step_inst.cu compiled once per slice) so they compile in
+// parallel.
 #pragma once
 #include "step_kernel.cuh"
 
 namespace obgc {
-
-// (variant, tracer count) pairs with a fused kernel: the BGC tracers alone, or followed by T and S.
-inline bool fused_supported(int V, int NT) {
-    switch (V) {
-        case V_LOBSTER: return NT == 7 || NT == 9;
-        case V_LOBSTER_C: return NT == 9 || NT == 11;
-        case V_LOBSTER_CO: return NT == 10 || NT == 12;
-        case V_LOBSTER_O: return NT == 8 || NT == 10;
-        case V_NPZD: return NT == 5 || NT == 6;
-        case V_EXTERNAL: return NT == 9 || NT == 8;   // PISCES, in launches of 9, 9 and 8 tracers
-    }
-    return false;
-}
 
 template <int V, int NT, typename TS, typename TC, bool EXT>
 int ensure_configured() {

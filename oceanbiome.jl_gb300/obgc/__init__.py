@@ -8,7 +8,9 @@ libobgc.so (CUDA, sm_103a); importing works without it, calling does not.
 """
 from . import _abi
 from .box import BoxModel
-from .gas import CarbonDioxideGasExchangeBoundaryCondition, GasExchange, OxygenGasExchangeBoundaryCondition
+from .forcing import Forcing
+from .gas import (CarbonDioxideConcentration, CarbonDioxideGasExchangeBoundaryCondition, GasExchange,
+                  OxygenGasExchangeBoundaryCondition)
 from .pisces import PISCES, PiscesModel
 from .columns import ColumnEngine
 from .service import ColumnService

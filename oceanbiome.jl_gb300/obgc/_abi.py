@@ -27,6 +27,13 @@ ASCII_NAMES = ["NO3", "NH4", "Fe", "N", "P", "Z", "T", "sPOM", "bPOM", "DOM", "s
                "DON", "sPOC", "bPOC", "DOC", "D", "DIC", "Alk", "O2", "S"]
 NUM_NAMED = len(TRACER_NAMES)
 MAX_PASSIVE = 8
+MAX_GAS_CONDITIONS = 4
+MAX_FORCINGS = 4
+
+
+def PASSIVE(p):
+    """Tracer code of passive tracer p (OBGC_PASSIVE)."""
+    return NUM_NAMED + p
 NAME_INDEX = {n: i for i, n in enumerate(TRACER_NAMES)}
 NAME_INDEX.update({n: i for i, n in enumerate(ASCII_NAMES)})
 for _i, _n in enumerate(ASCII_NAMES):
@@ -123,7 +130,7 @@ class ModelDesc(C.Structure):
                 ("grid", Grid), ("precision", C.c_int32), ("advection", C.c_int32),
                 ("n_passive", C.c_int32), ("carry_T", C.c_int32), ("carry_S", C.c_int32),
                 ("negatives", C.c_int32), ("zero_exclude", C.c_uint32), ("reserved1", C.c_int32),
-                ("invalid_fill_value", C.c_double)]
+                ("invalid_fill_value", C.c_double), ("passive_tendency_of", C.c_int8 * MAX_PASSIVE)]
 
 
 class Fields(C.Structure):
@@ -296,6 +303,8 @@ def load():
     _sig(lib, "obgc_gas_exchange_flux", C.c_int, P(GasExchange), P(Grid), I32, VP, VP, VP, VP, VP, VP, VP)
     _sig(lib, "obgc_gas_exchange_point", C.c_int, P(GasExchange), D, D, D, D, D, D, D, P(D))
     _sig(lib, "obgc_set_gas_exchange", C.c_int, VP, I32, P(GasExchange))
+    _sig(lib, "obgc_set_gas_exchange_on", C.c_int, VP, I32, P(GasExchange), I32, I32)
+    _sig(lib, "obgc_set_forcing", C.c_int, VP, I32, VP, D, D)
     _sig(lib, "obgc_set_diffusivity", C.c_int, VP, D, D, P(D))
     _sig(lib, "obgc_set_sediment", C.c_int, VP, I32, P(I32), I32, D, D, D)
     _sig(lib, "obgc_sediment_storage", C.c_int, VP, P(D), P(D))
@@ -372,6 +381,7 @@ def load():
 EXPORTED = [
     "obgc_abi_version", "obgc_last_error_message", "obgc_kernel_launch_count", "obgc_fp64_fma_peak",
     "obgc_gas_exchange_defaults", "obgc_gas_exchange_flux", "obgc_gas_exchange_point", "obgc_set_gas_exchange",
+    "obgc_set_gas_exchange_on", "obgc_set_forcing",
     "obgc_set_diffusivity", "obgc_set_sediment", "obgc_sediment_storage",
     "obgc_npd_preset", "obgc_npd_required_tracers", "obgc_npd_drift_velocity",
     "obgc_npd_eval_point", "obgc_npd_tendencies", "obgc_twoband_par", "obgc_multiband_par",

@@ -5,13 +5,28 @@ import ctypes as C
 from . import _abi as A
 
 
+class CarbonDioxideConcentration:
+    """CarbonDioxideConcentration(; DIC = :DIC, Alk = :Alk) (carbon_dioxide_concentration.jl:13-60):
+    the tracers whose surface values give the water's pCO2, e.g. DIC = "DIC2", Alk = "Alk2" for the
+    second replicate of CarbonateSystem(2)."""
+
+    def __init__(self, DIC="DIC", Alk="Alk", carbon_chemistry=None):
+        self.DIC, self.Alk, self.carbon_chemistry = DIC, Alk, carbon_chemistry
+
+
 class GasExchange:
     """GasExchange(gas; wind_speed, air_concentration, transfer velocity / Schmidt / solubility
-    coefficients): wind_speed and air_concentration are numbers or (Ny, Nx) device tensors."""
+    coefficients): wind_speed and air_concentration are numbers or (Ny, Nx) device tensors.
+    water_concentration: a CarbonDioxideConcentration (CO2; default DIC and Alk)."""
 
     def __init__(self, gas, wind_speed=None, air_concentration=None, k660=None, schmidt=None, o2_solubility=None,
-                 carbon_chemistry=None):
+                 carbon_chemistry=None, water_concentration=None):
         self.gas = gas
+        if water_concentration is not None and gas != A.GAS_CO2:
+            raise ValueError("water_concentration: the O2 condition reads its own tracer")
+        self.water_concentration = water_concentration or (CarbonDioxideConcentration() if gas == A.GAS_CO2 else None)
+        if carbon_chemistry is None and self.water_concentration is not None:
+            carbon_chemistry = self.water_concentration.carbon_chemistry
         self.params = A.GasExchange()
         A.check(A.load().obgc_gas_exchange_defaults(gas, C.byref(self.params)), "obgc_gas_exchange_defaults")
         self._keep = []

@@ -38,6 +38,13 @@ class RectilinearGrid:
         zf = -self.Lz + self.dz * np.arange(self.Nz + 1)
         return zf if loc == "face" else zf[:-1] + self.dz / 2
 
+    def nodes(self):
+        """Cell-centre coordinates (z, y, x): x in (0, Lx), y in (0, Ly), z in (-Lz, 0), as
+        Oceananigans places a grid of the given extent; a Flat direction gives 0."""
+        x = (np.arange(self.Nx) + 0.5) * (self.Lx / self.Nx) if self.topology[0] != "Flat" else np.zeros(1)
+        y = (np.arange(self.Ny) + 0.5) * (self.Ly / self.Ny) if self.topology[1] != "Flat" else np.zeros(1)
+        return self.znodes(), y, x
+
     def c_grid(self, stride_j=None, stride_k=None):
         g = A.Grid()
         g.Nx, g.Ny, g.Nz = self.Nx, self.Ny, self.Nz

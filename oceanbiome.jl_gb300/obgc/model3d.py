@@ -11,7 +11,7 @@ import numpy as np
 
 from . import _abi as A
 from .negatives import negatives_config
-from .models import required_biogeochemical_tracers
+from .models import replicate_of, required_biogeochemical_tracers
 
 _PREC = {"f32": A.PREC_F32, "f64": A.PREC_F64, "mixed": A.PREC_MIXED}
 
@@ -48,10 +48,13 @@ def HorizontalScalarDiffusivity(κ=0.0, ν=None):
 
 class NonhydrostaticModel:
     def __init__(self, grid, biogeochemistry, advection="WENO5", tracers=(), velocities=None,
-                 precision="f32", clock=None, device="cuda", boundary_conditions=None, closure=None):
+                 precision="f32", clock=None, device="cuda", boundary_conditions=None, closure=None, forcing=None):
         """boundary_conditions: {"DIC": CarbonDioxideGasExchangeBoundaryCondition(...),
         "O2": OxygenGasExchangeBoundaryCondition(...)} as top boundary conditions (the reference's
-        FieldBoundaryConditions(top = ...)); applied by time_step's fused RK3 step."""
+        FieldBoundaryConditions(top = ...)); applied by time_step's fused RK3 step.  With
+        CarbonateSystem(N) the keys are DIC1..DICN, each condition naming its DIC / Alk through a
+        CarbonDioxideConcentration.  tracers: T and S, and any passive tracer names (at most 8
+        passive tracers, CarbonateSystem replicates 2..N included).  forcing: {name: Forcing(...)}."""
         import torch
         self.grid = grid
         self.biogeochemistry = bgc = biogeochemistry
@@ -61,17 +64,41 @@ class NonhydrostaticModel:
         self.state_dtype = torch.float32 if precision == "f32" else torch.float64
         bgc_names = list(required_biogeochemical_tracers(bgc))
         extra = [t for t in tracers if t not in bgc_names]
+        # tracer codes of the C ABI: named slots; replicates 2..N of DIC / Alk and every extra tracer
+        # but T and S are passive tracers (the replicates take the DIC / Alk tendency)
+        self._code, source = {}, []
+        for n in bgc_names:
+            base = replicate_of(n)
+            if base == n or n in ("DIC1", "Alk1"):
+                self._code[n] = A.NAME_INDEX[base]
+            else:
+                self._code[n] = A.PASSIVE(len(source))
+                source.append(A.NAME_INDEX[base] + 1)
+        carried = [t for t in ("T", "S") if t in extra]
         for t in extra:
-            if t not in ("T", "S"):
-                raise ValueError(f"extra tracer {t!r}: only T and S can be carried alongside the BGC tracers")
-        self.tracer_names = bgc_names + [t for t in ("T", "S") if t in extra]
+            if t not in carried:
+                self._code[t] = A.PASSIVE(len(source))
+                source.append(0)
+        for t in carried:
+            self._code[t] = A.NAME_INDEX[t]
+        if len(source) > A.MAX_PASSIVE:
+            raise ValueError(f"at most {A.MAX_PASSIVE} passive tracers (replicates included)")
+        self.tracer_names = bgc_names + carried + [t for t in extra if t not in carried]
         self.tracers = {n: torch.zeros(grid.shape, dtype=self.state_dtype, device=device) for n in self.tracer_names}
         if velocities is None:
             velocities = (None, None, None)
         self.velocities = tuple(None if v is None else v.to(device=device, dtype=self.state_dtype).contiguous()
                                 for v in velocities)
         self.PAR = torch.zeros(grid.shape, dtype=self.state_dtype, device=device)
-        self.G = {n: torch.zeros(grid.shape, dtype=self.state_dtype, device=device) for n in bgc_names}
+        # mode (i) tendencies: one array per named tracer; a replicate shares its DIC / Alk array
+        # (the functors are the same)
+        self.G = {}
+        for n in bgc_names:
+            if self._code[n] < A.NUM_NAMED:
+                self.G[n] = torch.zeros(grid.shape, dtype=self.state_dtype, device=device)
+        for n in bgc_names:
+            if self._code[n] >= A.NUM_NAMED:
+                self.G[n] = self.G[replicate_of(n) + "1"]
         light = bgc.light_attenuation
         desc = A.ModelDesc()
         desc.npd = bgc.params
@@ -82,7 +109,10 @@ class NonhydrostaticModel:
         desc.advection = A.ADVECTION_WENO5 if advection else A.ADVECTION_NONE
         desc.carry_T = int("T" in extra)
         desc.carry_S = int("S" in extra)
-        desc.negatives, desc.zero_exclude, desc.invalid_fill_value = negatives_config(bgc)
+        desc.n_passive = len(source)
+        for p, src in enumerate(source):
+            desc.passive_tendency_of[p] = src
+        desc.negatives, desc.zero_exclude, desc.invalid_fill_value = negatives_config(bgc, self.code)
         self._lib = lib = A.load()
         ctx = C.c_void_p()
         A.check(lib.obgc_create(C.byref(desc), C.byref(ctx)), "obgc_create")
@@ -90,18 +120,29 @@ class NonhydrostaticModel:
         self._bind()
         self.boundary_conditions = dict(boundary_conditions or {})
         for name, bc in self.boundary_conditions.items():
-            want = {"DIC": A.GAS_CO2, "O2": A.GAS_O2, "O₂": A.GAS_O2}.get(name)
-            if want is None or bc.gas != want:
+            name = "O2" if name == "O₂" else name
+            want = A.GAS_CO2 if replicate_of(name) == "DIC" else A.GAS_O2 if name == "O2" else None
+            if want is None or bc.gas != want or name not in self._code:
                 raise ValueError(f"no gas exchange boundary condition of this kind for tracer {name!r}")
-            A.check(lib.obgc_set_gas_exchange(ctx, bc.gas, C.byref(bc.params)), "obgc_set_gas_exchange")
+            wc = bc.water_concentration
+            dic, alk = (self.code(wc.DIC), self.code(wc.Alk)) if want == A.GAS_CO2 else (0, 0)
+            A.check(lib.obgc_set_gas_exchange_on(ctx, self._code[name], C.byref(bc.params), dic, alk),
+                    "obgc_set_gas_exchange_on")
+        self.forcing = dict(forcing or {})
+        self._forcing_fields = {}
+        for name, f in self.forcing.items():
+            rate = f.field(grid, self.state_dtype, device)
+            self._forcing_fields[name] = rate
+            A.check(lib.obgc_set_forcing(ctx, self.code(name), C.c_void_p(rate.data_ptr()), f.start_time, f.end_time),
+                    "obgc_set_forcing")
         sed = getattr(bgc, "sediment", None)
         self.sediment = sed
         if sed is not None:
             from .sediments import InstantRemineralisationSediment
             if not isinstance(sed, InstantRemineralisationSediment):
                 raise NotImplementedError(f"sediment model {type(sed).__name__} in the fused step")
-            names = (C.c_int32 * len(sed.sinking_tracers))(*[A.NAME_INDEX[n] for n in sed.sinking_tracers])
-            A.check(lib.obgc_set_sediment(ctx, len(sed.sinking_tracers), names, A.NAME_INDEX[sed.remineralisation_reciever],
+            names = (C.c_int32 * len(sed.sinking_tracers))(*[self.code(n) for n in sed.sinking_tracers])
+            A.check(lib.obgc_set_sediment(ctx, len(sed.sinking_tracers), names, self.code(sed.remineralisation_reciever),
                                           sed.a, sed.b, sed.k), "obgc_set_sediment")
         self.closure = closure
         if closure is not None:
@@ -112,17 +153,28 @@ class NonhydrostaticModel:
             arr = None if kz is None else (C.c_double * len(kz))(*kz)
             A.check(lib.obgc_set_diffusivity(ctx, kh, 0.0, arr), "obgc_set_diffusivity")
 
+    def code(self, name):
+        """The C ABI tracer code of a tracer of this model (a named slot or OBGC_PASSIVE(p))."""
+        if name not in self._code:
+            raise ValueError(f"name {name} not found in model.tracers.")
+        return self._code[name]
+
     def _bind(self):
         f = A.Fields()
         for n, t in self.tracers.items():
-            f.tracers[A.NAME_INDEX[n]] = t.data_ptr()
+            c = self._code[n]
+            if c < A.NUM_NAMED:
+                f.tracers[c] = t.data_ptr()
+            else:
+                f.passive[c - A.NUM_NAMED] = t.data_ptr()
         u, v, w = self.velocities
         f.u = None if u is None else u.data_ptr()
         f.v = None if v is None else v.data_ptr()
         f.w = None if w is None else w.data_ptr()
         f.PAR = self.PAR.data_ptr()
         for n, t in self.G.items():
-            f.G[A.NAME_INDEX[n]] = t.data_ptr()
+            if self._code[n] < A.NUM_NAMED:
+                f.G[self._code[n]] = t.data_ptr()
         A.check(self._lib.obgc_bind_fields(self._ctx, C.byref(f)), "obgc_bind_fields")
 
     def __del__(self):

@@ -59,11 +59,14 @@ class Detritus(_Component):
 
 
 class CarbonateSystem(_Component):
-    """carbonate_system.jl:39-47 — DIC and Alk (one replicate)."""
+    """carbonate_system.jl:39-83 — DIC and Alk; with N > 1 replicates the tracers DIC1..DICN and
+    Alk1..AlkN, each evolving under the DIC / Alk tendency (they differ through their boundary
+    conditions and forcing, e.g. an alkalinity release in one of them)."""
 
     def __init__(self, replicates=1):
-        if replicates != 1:
-            raise ValueError("CarbonateSystem: only one replicate is supported")
+        if int(replicates) < 1 or int(replicates) > 1 + A.MAX_PASSIVE // 2:
+            raise ValueError(f"CarbonateSystem: 1 to {1 + A.MAX_PASSIVE // 2} replicates")
+        self.replicates = int(replicates)
         super().__init__()
 
 
@@ -140,6 +143,7 @@ class NutrientsPlanktonDetritus:
         else:
             p.detritus = A.DET_NONE          # detritus = nothing: instant remineralisation
         p.carbonate_system = int(carbonate_system is not None)
+        self.carbonate_replicates = carbonate_system.replicates if carbonate_system is not None else 0
         p.oxygen = int(oxygen is not None)
         if oxygen is not None:
             _apply(p, oxygen.overrides, "oxygen")
@@ -198,7 +202,21 @@ def required_biogeochemical_tracers(bgc):
     n = lib.obgc_npd_required_tracers(C.byref(bgc.params), buf, 32)
     if n < 0:
         raise A.ObgcError(-n, "obgc_npd_required_tracers")
-    return tuple(A.ASCII_NAMES[buf[i]] for i in range(n))
+    names = [A.ASCII_NAMES[buf[i]] for i in range(n)]
+    R = getattr(bgc, "carbonate_replicates", 1)
+    if R > 1:   # (DIC1, ..., DICN, Alk1, ..., AlkN) in place of (DIC, Alk) (carbonate_system.jl:47-48)
+        q = names.index("DIC")
+        names[q:q + 2] = [f"DIC{r}" for r in range(1, R + 1)] + [f"Alk{r}" for r in range(1, R + 1)]
+    return tuple(names)
+
+
+def replicate_of(name):
+    """The carbonate tracer a replicate name evaluates ("DIC2" -> "DIC", "Alk1" -> "Alk"), else the
+    name itself."""
+    for base in ("DIC", "Alk"):
+        if name.startswith(base) and name[len(base):].isdigit():
+            return base
+    return name
 
 
 def required_biogeochemical_auxiliary_fields(bgc):
@@ -212,7 +230,7 @@ def biogeochemical_drift_velocity(bgc, name, Nz=None):
     lib = A.load()
     Nz = Nz or bgc.grid.Nz
     w = np.zeros(Nz + 1)
-    r = lib.obgc_npd_drift_velocity(C.byref(bgc.params), A.NAME_INDEX[name], Nz,
+    r = lib.obgc_npd_drift_velocity(C.byref(bgc.params), A.NAME_INDEX[replicate_of(name)], Nz,
                                     w.ctypes.data_as(C.POINTER(C.c_double)))
     if r < 0:
         raise A.ObgcError(-r, "obgc_npd_drift_velocity")
@@ -245,9 +263,9 @@ def eval_point(bgc, name, values, PAR, x=0.0, y=0.0, z=0.0, t=0.0):
     lib = A.load()
     v = np.zeros(A.NUM_NAMED)
     for k, x_ in values.items():
-        v[A.NAME_INDEX[k]] = x_
+        v[A.NAME_INDEX[replicate_of(k)]] = x_
     out = C.c_double(0)
-    A.check(lib.obgc_npd_eval_point(C.byref(bgc.params), A.NAME_INDEX[name], x, y, z, t,
+    A.check(lib.obgc_npd_eval_point(C.byref(bgc.params), A.NAME_INDEX[replicate_of(name)], x, y, z, t,
                                     v.ctypes.data_as(C.POINTER(C.c_double)), PAR, C.byref(out)),
             "obgc_npd_eval_point")
     return out.value

@@ -54,9 +54,10 @@ class ZeroNegativeTracers:
                 "obgc_zero_negatives")
 
 
-def negatives_config(bgc):
+def negatives_config(bgc, code=None):
     """(mode, zero_exclude mask, invalid_fill_value) of a biogeochemistry's modifier for the engine:
-    scale_negatives = true scales conserved_tracers(bgc); a ZeroNegativeTracers modifier zeroes."""
+    scale_negatives = true scales conserved_tracers(bgc); a ZeroNegativeTracers modifier zeroes.
+    code: a model's tracer-name -> C ABI code map (passive tracers have bits 21 + p)."""
     if getattr(bgc, "scale_negatives", False):
         return A.NEGATIVES_SCALE, 0, float(getattr(bgc, "invalid_fill_value", math.nan))
     mods = getattr(bgc, "modifiers", None)
@@ -65,7 +66,7 @@ def negatives_config(bgc):
         if isinstance(m, ZeroNegativeTracers):
             mask = 0
             for n in m.exclude:
-                mask |= 1 << A.NAME_INDEX[n]
+                mask |= 1 << (code(n) if code is not None else A.NAME_INDEX[n])
             return A.NEGATIVES_ZERO, mask, math.nan
         if isinstance(m, ScaleNegativeTracers):
             raise NotImplementedError("a custom ScaleNegativeTracers group as a model modifier: use scale_negatives=True "

@@ -68,6 +68,7 @@ void or_box_run(const obgc_npd_params* p, double* v, const double* PAR_stages, d
                 double t0, double dt, int nsteps);
 
 /* ---- 3-D fused model: WENO5 + drift + BGC + TwoBand light + RK3 ---- */
+#define OR_MAX_GAS 4
 typedef struct or_model3d {
     obgc_npd_params npd;
     obgc_twoband_params light;
@@ -80,8 +81,11 @@ typedef struct or_model3d {
     int32_t negatives;           /* 0 none, 1 ScaleNegativeTracers, 2 ZeroNegativeTracers */
     int32_t zero_exclude_mask;   /* ZeroNegativeTracers: bit q set = tracer slot q excluded */
     double invalid_fill_value;   /* ScaleNegativeTracers(...; invalid_fill_value)      */
-    const obgc_gas_exchange* gas[2]; /* top boundary conditions: [0] CO2 on DIC, [1] O2 on O2, or NULL;
-                                      * constant wind speed and air concentration */
+    const obgc_gas_exchange* gas[OR_MAX_GAS]; /* top boundary conditions (NULL: none), with
+                                      * constant wind speed and air concentration: gas[q] takes
+                                      * the flux out of slot gas_target[q]; CO2 reads the water's
+                                      * DIC / Alk from slots gas_dic[q] / gas_alk[q], O2 the target */
+    int32_t gas_target[OR_MAX_GAS], gas_dic[OR_MAX_GAS], gas_alk[OR_MAX_GAS];
     double kappa_h;                  /* ScalarDiffusivity: horizontal diffusivity (m2/s)         */
     const double* kappa_z_faces;     /* vertical diffusivity at the Nz + 1 faces, or NULL; the
                                       * bottom and top faces are walls (no flux)                  */
@@ -89,6 +93,10 @@ typedef struct or_model3d {
     uint32_t sed_sink_mask;          /* sinking tracer slots                                     */
     double sed_a, sed_b, sed_k;      /* burial efficiency constants and half saturation          */
     double* sed_storage;             /* [Ny*Nx] storage, stepped with the tracers' RK3           */
+    int32_t tendency_of[32];         /* passive slots (names -1): enum obgc_tracer + 1 whose BGC
+                                      * tendency the slot takes (CarbonateSystem replicates), 0 none */
+    const double* forcing[32];       /* per slot: a source rate [Nz*Ny*Nx] (per second) or NULL,  */
+    double forcing_t0[32], forcing_t1[32]; /* added at stage times t0 <= t < t1              */
 } or_model3d;
 /* state: [n_tracers][Nz*Ny*Nx]; u, v, w: [Nz*Ny*Nx] or NULL. */
 void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,

@@ -187,7 +187,12 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
                 double vals[OBGC_NUM_NAMED] = {0};
                 for (int q = 0; q < nt; q++) if (m->names[q] >= 0) vals[m->names[q]] = state[(long)q * N + c];
                 for (int q = 0; q < nt; q++) {
-                    double tend = is_bgc[q] ? or_npd_tendency(&m->npd, m->names[q], vals, PAR[c]) : 0.0;
+                    /* a replicate (DIC2, Alk2, ...) evaluates the DIC / Alk functor
+                     * (carbonate_system.jl:70-83); a forcing adds its rate at the stage time */
+                    double tend = is_bgc[q] ? or_npd_tendency(&m->npd, m->names[q], vals, PAR[c])
+                                : m->tendency_of[q] > 0 ? or_npd_tendency(&m->npd, m->tendency_of[q] - 1, vals, PAR[c])
+                                : 0.0;
+                    if (m->forcing[q] && ts >= m->forcing_t0[q] && ts < m->forcing_t1[q]) tend += m->forcing[q][c];
                     if (m->advection) {
                         const double* cq = state + (long)q * N;
                         double adv = 0.0;
@@ -256,19 +261,18 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
             }
             /* FieldBoundaryConditions(top = GasExchange): the surface cell loses flux / dz
              * (gas_exchange.jl:26-39 evaluated on the stage's surface values) */
-            for (int gq = 0; gq < 2; gq++) {
+            for (int gq = 0; gq < OR_MAX_GAS; gq++) {
                 const obgc_gas_exchange* ge = m->gas[gq];
                 if (!ge) continue;
-                int sT = -1, sS = -1, sD = -1, sA = -1, sO = -1, target = -1;
+                int sT = -1, sS = -1;
                 for (int q = 0; q < nt; q++) {
                     if (m->names[q] == OBGC_T) sT = q;
                     if (m->names[q] == OBGC_S) sS = q;
-                    if (m->names[q] == OBGC_DIC) sD = q;
-                    if (m->names[q] == OBGC_ALK) sA = q;
-                    if (m->names[q] == OBGC_O2) sO = q;
                 }
-                target = ge->gas == OBGC_GAS_CO2 ? sD : sO;
-                if (sT < 0 || sS < 0 || target < 0 || (ge->gas == OBGC_GAS_CO2 && sA < 0)) continue;
+                const int target = m->gas_target[gq];
+                const int co2 = ge->gas == OBGC_GAS_CO2;
+                const int sD = co2 ? m->gas_dic[gq] : -1, sA = co2 ? m->gas_alk[gq] : -1, sO = co2 ? -1 : target;
+                if (sT < 0 || sS < 0 || target < 0 || (co2 && (sA < 0 || sD < 0))) continue;
 #pragma omp parallel for num_threads(nthreads) schedule(static)
                 for (long col = 0; col < NN; col++) {
                     const long c = (long)(Nz - 1) * NN + col;

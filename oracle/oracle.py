@@ -26,10 +26,12 @@ class Model3D(C.Structure):
                 ("advection", C.c_int32), ("surface_value", C.c_double), ("grid", A.Grid),
                 ("n_tracers", C.c_int32), ("names", C.c_int32 * 32), ("negatives", C.c_int32),
                 ("zero_exclude_mask", C.c_int32), ("invalid_fill_value", C.c_double),
-                ("gas", C.POINTER(A.GasExchange) * 2), ("kappa_h", C.c_double),
+                ("gas", C.POINTER(A.GasExchange) * 4), ("gas_target", C.c_int32 * 4), ("gas_dic", C.c_int32 * 4),
+                ("gas_alk", C.c_int32 * 4), ("kappa_h", C.c_double),
                 ("kappa_z_faces", C.POINTER(C.c_double)), ("sed_receiver", C.c_int32), ("sed_sink_mask", C.c_uint32),
                 ("sed_a", C.c_double), ("sed_b", C.c_double), ("sed_k", C.c_double),
-                ("sed_storage", C.POINTER(C.c_double))]
+                ("sed_storage", C.POINTER(C.c_double)), ("tendency_of", C.c_int32 * 32),
+                ("forcing", C.POINTER(C.c_double) * 32), ("forcing_t0", C.c_double * 32), ("forcing_t1", C.c_double * 32)]
 
 
 class Pisces3D(C.Structure):
@@ -273,11 +275,36 @@ def box_run(p, values, dt, nsteps, PAR_stages=None, PAR_const=0.0, t0=0.0):
 
 def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_value=0.0, advection=1,
             negatives=NEG_NONE, zero_exclude=(), invalid_fill_value=float("nan"), gas_exchange=(), kappa_h=0.0,
-            kappa_z_faces=None, sediment=None):
-    """gas_exchange: A.GasExchange structs (CO2 on DIC, O2 on O2) as top boundary conditions;
-    kappa_h, kappa_z_faces[Nz + 1]: ScalarDiffusivity (explicit).  sediment=(sinking names, receiver,
-    a, b, k, storage array [Ny, Nx] float64) for InstantRemineralisation."""
+            kappa_z_faces=None, sediment=None, tendency_of=None, forcing=None):
+    """gas_exchange: top boundary conditions, each an A.GasExchange struct (CO2 on DIC with DIC and
+    Alk, O2 on O2) or a tuple (struct, target, dic, alk) of tracer names or slots (None for passive
+    entries of `names`); kappa_h, kappa_z_faces[Nz + 1]: ScalarDiffusivity (explicit).
+    sediment=(sinking names, receiver, a, b, k, storage array [Ny, Nx] float64) for
+    InstantRemineralisation.  tendency_of={slot: "DIC" | "Alk"}: passive slots taking that BGC
+    tendency (CarbonateSystem replicates).  forcing={slot: (rate array [Nz, Ny, Nx], t0, t1)}."""
     m = Model3D()
+    nm_all = [-1 if n is None else (A.NAME_INDEX[n] if isinstance(n, str) else n) for n in names]
+
+    def slot(x):   # a slot index, or a tracer name
+        return x if isinstance(x, int) else nm_all.index(A.NAME_INDEX[x])
+    m._gas_keep = []
+    for q, g in enumerate(gas_exchange):
+        if not isinstance(g, tuple):
+            g = (g, "DIC", "DIC", "Alk") if g.gas == A.GAS_CO2 else (g, "O2", None, None)
+        ge, target, dic, alk = g
+        m._gas_keep.append(ge)
+        m.gas[q] = C.pointer(ge)
+        m.gas_target[q] = slot(target)
+        m.gas_dic[q] = slot(dic) if dic is not None else -1
+        m.gas_alk[q] = slot(alk) if alk is not None else -1
+    for q, src in (tendency_of or {}).items():
+        m.tendency_of[q] = A.NAME_INDEX[src] + 1
+    m._forcing_keep = []
+    for q, (rate, t0, t1) in (forcing or {}).items():
+        r = np.ascontiguousarray(rate, dtype=np.float64)
+        m._forcing_keep.append(r)
+        m.forcing[q] = r.ctypes.data_as(C.POINTER(C.c_double))
+        m.forcing_t0[q], m.forcing_t1[q] = t0, t1
     m.sed_receiver = -1
     if sediment is not None:
         sinking, receiver, sa, sb, sk, storage = sediment
@@ -292,9 +319,6 @@ def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_
     if kappa_z_faces is not None:
         m._kz = np.ascontiguousarray(kappa_z_faces, dtype=np.float64)
         m.kappa_z_faces = m._kz.ctypes.data_as(C.POINTER(C.c_double))
-    m._gas_keep = list(gas_exchange)
-    for g in gas_exchange:
-        m.gas[0 if g.gas == A.GAS_CO2 else 1] = C.pointer(g)
     m.negatives = negatives
     m.invalid_fill_value = invalid_fill_value
     m.zero_exclude_mask = sum(1 << q for q, nm in enumerate(names) if nm in zero_exclude)

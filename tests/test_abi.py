@@ -19,7 +19,7 @@ def declared_functions():
 
 def test_library_loads_and_version():
     lib = A.load()
-    assert lib.obgc_abi_version() == 1
+    assert lib.obgc_abi_version() == 2
 
 
 def test_every_declared_symbol_is_exported():
@@ -37,7 +37,7 @@ def test_every_declared_symbol_is_exported():
     (2, A.Surface, ["value", "field", None]),
     (3, A.Grid, ["Lx", "stride_j", "stride_k"]),
     (4, A.CarbonOptions, ["density_value", "atol", "saturation_mineral"]),
-    (5, A.ModelDesc, ["surface", "grid", "invalid_fill_value"]),
+    (5, A.ModelDesc, ["surface", "grid", "passive_tendency_of"]),
     (6, A.Fields, ["passive", "u", "G"]),
     (7, A.ColumnSpec, ["dz", "pulse_step", "pulse_amount"]),
     (8, A.ColumnsDesc, ["light", "arena_cells", "invalid_fill_value"]),

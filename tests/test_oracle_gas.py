@@ -39,3 +39,16 @@ def test_transfer_velocity_ho06_and_sign():
     # supersaturated water outgasses (positive, out of the ocean)
     assert O.gas_exchange_flux(g, T, S, O2=2 * air, u10=u) > 0
     assert O.gas_exchange_flux(g, T, S, O2=0.5 * air, u10=u) < 0
+
+
+@pytest.mark.parametrize("air", [413.1, 413.0])
+def test_replicated_carbonate_systems_surface_flux(air):
+    # test/test_gasexchange_carbon_chem.jl:21-67: T = 15, S = 35, the default wind; DIC 2220 / Alk
+    # 2500 gives a surface flux of -8e-6 +- 1e-6 (into the ocean), and the second replicate (2221 /
+    # 2501) another value of the same size
+    g = O.gas_exchange_defaults(A.GAS_CO2)
+    f1 = O.gas_exchange_flux(g, 15.0, 35.0, DIC=2220.0, Alk=2500.0, air=air)
+    f2 = O.gas_exchange_flux(g, 15.0, 35.0, DIC=2221.0, Alk=2501.0, air=air)
+    assert f1 == pytest.approx(-8e-6, abs=1e-6)
+    assert f2 == pytest.approx(-8e-6, abs=1e-6)
+    assert f1 != f2
