@@ -34,7 +34,8 @@ def oracle_layout(model):
 
 def oae_model(precision, shape=(24, 16, 8), seed=5, with_bcs=True, with_forcing=True, modifiers=None):
     torch = cuda()
-    g = obgc.RectilinearGrid(shape, (500.0, 400.0, 15.0), dtype="f32" if precision == "f32" else "f64")
+    # 208 m cells: the flow (0.27 m/s at most) moves under 0.4 cells per 300 s step
+    g = obgc.RectilinearGrid(shape, (5000.0, 4000.0, 15.0), dtype="f32" if precision == "f32" else "f64")
     bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem(2), modifiers=modifiers)
     u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=seed)
     bcs = {}
@@ -45,7 +46,7 @@ def oae_model(precision, shape=(24, 16, 8), seed=5, with_bcs=True, with_forcing=
     forcing = {}
     if with_forcing:
         z, y, x = g.nodes()
-        mask = ((x[None, None, :] - 250) ** 2 + (y[None, :, None] - 200) ** 2 < 100.0 ** 2) & (z[:, None, None] > -4)
+        mask = ((x[None, None, :] - 2500) ** 2 + (y[None, :, None] - 2000) ** 2 < 1000.0 ** 2) & (z[:, None, None] > -4)
         rate = np.where(mask, 0.05, 0.0) * np.ones(g.shape)
         forcing["Alk2"] = obgc.Forcing(rate, start_time=400.0, end_time=1000.0)
     model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S", "C"), velocities=(u, v, None),
@@ -74,7 +75,7 @@ def oracle_run(model, bgc, g, vel, s0, dt, nsteps, bcs=None, forcing=None):
 
 def test_tracer_order_and_codes():
     cuda()
-    g = obgc.RectilinearGrid((8, 8, 4), (100.0, 100.0, 10.0))
+    g = obgc.RectilinearGrid((8, 8, 4), (1000.0, 1000.0, 10.0))
     bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem(2))
     model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S", "C"))
     assert model.tracer_names[7:] == ["DIC1", "DIC2", "Alk1", "Alk2", "T", "S", "C"]
