@@ -15,6 +15,9 @@ from obgc import _abi as A
 from gpuhelp import cuda, rel_err
 
 pytestmark = pytest.mark.gpu
+# C starts as noise of both signs: its error is measured against 1 % of its largest magnitude where
+# it crosses zero (the other tracers keep one sign)
+FLOOR = {"C": 1e-2}
 
 
 def oracle_layout(model):
@@ -92,8 +95,9 @@ def test_oae_replicates_with_gas_exchange_and_release_match_oracle(precision, to
     obgc.time_step(model, dt, nsteps=nsteps)
     got = model.state_array().double().cpu().numpy()
     ref = oracle_run(model, bgc, g, vel, s0, dt, nsteps, bcs=bcs, forcing=forcing)
-    errs = {n: rel_err(got[q], ref[q]) for q, n in enumerate(model.tracer_names)}
-    assert max(errs.values()) < tol, errs
+    errs = {n: rel_err(got[q], ref[q], floor_frac=FLOOR.get(n, 1e-6)) for q, n in enumerate(model.tracer_names)}
+    worst = max(errs, key=errs.get)
+    assert errs[worst] < tol, (worst, errs)
     # the release added alkalinity to Alk2 only (six stages fall inside [400, 1000) s: times 460,
     # 500, 600, 760, 800 and 900 of steps 1-3), so the excess of Alk2 over Alk1 grew
     q1, q2 = model.tracer_names.index("Alk1"), model.tracer_names.index("Alk2")
@@ -110,7 +114,7 @@ def test_forcing_window_releases_its_integral():
     g, bgc, model, vel, bcs, forcing = oae_model("f64", with_bcs=False, with_forcing=False)
     rate = np.zeros(g.shape)
     rate[-1, 4:9, 6:12] = 0.02
-    model2 = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S", "C"), velocities=vel, precision="f64",
+    model2 = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S", "C"), velocities=vel + (None,), precision="f64",
                                       forcing={"Alk2": obgc.Forcing(rate, start_time=300.0, end_time=900.0)})
     obgc.set_(model2, **{n: model.tracers[n] for n in model.tracer_names})
     s0 = model2.state_array().double().cpu().numpy()
@@ -138,7 +142,8 @@ def test_replicates_without_conditions_track_each_other(precision):
 @pytest.mark.parametrize("precision,tol", [("f64", 1e-11), ("mixed", 1e-5)])
 def test_zero_negative_tracers_reach_passive_tracers(precision, tol):
     mods = obgc.ZeroNegativeTracers(exclude=("Alk2",))
-    g, bgc, model, vel, bcs, forcing = oae_model(precision, with_forcing=False, modifiers=mods)
+    # no gas exchange here: a negative Alk2 would make its pCO2 meaningless
+    g, bgc, model, vel, bcs, forcing = oae_model(precision, with_bcs=False, with_forcing=False, modifiers=mods)
     obgc.set_(model, Alk2=-np.abs(model.tracers["Alk2"].double().cpu().numpy()))
     s0 = model.state_array().double().cpu().numpy()
     obgc.time_step(model, 300.0, nsteps=3)
@@ -153,8 +158,9 @@ def test_zero_negative_tracers_reach_passive_tracers(precision, tol):
     ref = np.ascontiguousarray(s0.copy())
     u, v = (x.double().cpu().numpy().ravel().copy() for x in vel)
     O.step3d(m, ref, u=u, v=v, t=0.0, dt=300.0, nsteps=3)
-    errs = {n: rel_err(got[q], ref[q]) for q, n in enumerate(model.tracer_names)}
-    assert max(errs.values()) < tol, errs
+    errs = {n: rel_err(got[q], ref[q], floor_frac=FLOOR.get(n, 1e-6)) for q, n in enumerate(model.tracer_names)}
+    worst = max(errs, key=errs.get)
+    assert errs[worst] < tol, (worst, errs)
     C = got[model.tracer_names.index("C")]
     assert C.min() >= 0.0 and C.max() > 0.0                 # the passive tracer was zeroed where negative
     assert got[model.tracer_names.index("Alk2")].min() < 0  # the excluded one was not
