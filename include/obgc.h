@@ -391,7 +391,10 @@ enum obgc_carbon_output {
     OBGC_OUT_CARBONATE = 6,/* carbonate_concentration (calcite_concentration.jl:1-53) */
     OBGC_OUT_OMEGA_CALCITE = 7 /* calcite_saturation (calcite_concentration.jl:55-80)  */
 };
-enum obgc_density { OBGC_DENSITY_EOS80 = 0, OBGC_DENSITY_CONSTANT = 1 };
+/* Seawater density of the unit conversions: the reference's default teos10_polynomial_approximation
+ * (src/Models/seawater_density.jl:33-39, the Roquet et al. 2015 TEOS-10 polynomial fed as the
+ * reference feeds it), UNESCO EOS-80, or a constant. */
+enum obgc_density { OBGC_DENSITY_EOS80 = 0, OBGC_DENSITY_CONSTANT = 1, OBGC_DENSITY_TEOS10_POLYNOMIAL = 2 };
 
 /*
  * Options of a batched carbonate solve, mirroring the keyword arguments of

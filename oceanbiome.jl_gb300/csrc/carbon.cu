@@ -66,8 +66,9 @@ static int launch_carbon(const obgc_carbon_options* o, int64_t n, const void* DI
 }
 
 static bool valid_options(const obgc_carbon_options* o) {
-    return o && o->output >= 0 && o->output <= OBGC_OUT_OMEGA_CALCITE && (o->density == 0 || o->density == 1) &&
-           o->max_iters >= 0 && (o->density == 0 || o->density_value > 0);
+    return o && o->output >= 0 && o->output <= OBGC_OUT_OMEGA_CALCITE && o->density >= OBGC_DENSITY_EOS80 &&
+           o->density <= OBGC_DENSITY_TEOS10_POLYNOMIAL && o->max_iters >= 0 &&
+           (o->density != OBGC_DENSITY_CONSTANT || o->density_value > 0);
 }
 
 }  // namespace obgc
@@ -78,7 +79,7 @@ extern "C" int obgc_carbon_default_options(obgc_carbon_options* o) {
     if (!o) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_carbon_default_options: null");
     std::memset(o, 0, sizeof(*o));
     o->output = OBGC_OUT_FCO2;
-    o->density = OBGC_DENSITY_EOS80;
+    o->density = OBGC_DENSITY_TEOS10_POLYNOMIAL;
     o->max_iters = 100;
     o->initial_pH_guess = 8.0;
     o->atol = 1e-20;

@@ -16,8 +16,48 @@
 
 namespace obgc {
 
-// UNESCO EOS-80 (Millero & Poisson 1981; Millero et al. 1980 secant bulk modulus), p in bar.
-// Stands in for SeawaterPolynomials.TEOS10._rho (a third-party polynomial absent here).
+// Seawater density of the default CarbonChemistry, teos10_polynomial_approximation
+// (src/Models/seawater_density.jl:33-39): the 55-term TEOS-10 polynomial of Roquet, Madec,
+// McDougall & Barker (2015, Ocean Modelling 90:29-43) for in-situ density as a function of
+// conservative temperature, absolute salinity and depth, rho = r0(zeta) + rho'(tau, s, zeta) with
+// tau = T / 40, s = sqrt((S + 32) / (40 x 35.16504 / 35)) and zeta = -Z / 1e4.  The reference feeds
+// it T as the conservative temperature, S as the absolute salinity and Z = +10 m per bar of P
+// (positive: the polynomial's Z is a height, so zeta = -P / 1000 places the cell above the sea
+// surface); this function does the same.  Horner form in zeta, then tau, then s.
+__host__ __device__ inline double density_teos10_poly(double T, double S, double Pbar) {
+    const double z = -(10.0 * Pbar) * 1e-4;
+    const double t = T * 0.025;
+    const double s = sqrt((S + 32.0) * (35.0 / (40.0 * 35.16504)));
+    // zeta^0: coefficients of tau^0 .. tau^6, each a polynomial in s
+    const double a0 = (((((-6.0579916612e+01 * s + 4.3227585684e+02) * s - 1.2849161071e+03) * s + 2.0375295546e+03) * s -
+                        1.7864682637e+03) * s + 8.6672408165e+02) * s + 8.0189615746e+02;
+    const double a1 = ((((-1.9193502195 * s + 1.7681814114e+01) * s - 5.6888046321e+01) * s + 8.1770425108e+01) * s -
+                       6.5281885265e+01) * s + 2.6010145068e+01;
+    const double a2 = (((-5.4723692739 * s + 2.9130021253e+01) * s - 6.0362551501e+01) * s + 6.1548258127e+01) * s -
+                      3.7074170417e+01;
+    const double a3 = ((-3.1742946532 * s + 1.9717078466e+01) * s - 3.3449108469e+01) * s + 2.1661789529e+01;
+    const double a4 = (-5.3563304045 * s + 1.1311538584e+01) * s - 8.3627885467;
+    const double a5 = 4.8169980163e-01 * s + 5.4048723791e-01;
+    const double p0 = (((((-1.9083568888e-01 * t + a5) * t + a4) * t + a3) * t + a2) * t + a1) * t + a0;
+    // zeta^1
+    const double b0 = (((6.6051753097 * s - 3.0938076334e+01) * s + 5.0774768218e+01) * s - 4.2549998214e+01) * s +
+                      1.9681925209e+01;
+    const double b1 = ((-6.5399043664e-01 * s + 5.0042598061) * s - 4.4870114575) * s - 1.3336301113e+01;
+    const double b2 = (-1.8795372996 * s + 3.5063081279) * s + 6.7080479603;
+    const double b3 = -5.5077101279e-01 * s - 2.4649669534;
+    const double p1 = (((5.5927935970e-01 * t + b3) * t + b2) * t + b1) * t + b0;
+    // zeta^2 and zeta^3
+    const double p2 = (-1.2419983026 * t + (-2.1311365518e-01 * s + 2.0564311499)) * t +
+                      ((2.5019633244 * s - 4.9527603989) * s + 2.0660924175);
+    const double p3 = 3.7969820455e-01 * t - 1.8507636718e-02 * s - 2.3342758797e-02;
+    // reference profile r0(zeta)
+    const double r0 = z * (4.6494977072e+01 + z * (-5.2099962525 + z * (2.2601900708e-01 + z * (6.4326772569e-02 +
+                      z * (1.5616995503e-02 + z * -1.7243708991e-03)))));
+    return r0 + (p0 + z * (p1 + z * (p2 + z * p3)));
+}
+
+// UNESCO EOS-80 (Millero & Poisson 1981; Millero et al. 1980 secant bulk modulus), p in bar: the
+// OBGC_DENSITY_EOS80 option.
 __host__ __device__ inline double density_eos80(double T, double S, double p) {
     const double T2 = T * T, T3 = T2 * T, T4 = T3 * T, T5 = T4 * T;
     const double rw = 999.842594 + 6.793952e-2 * T - 9.095290e-3 * T2 + 1.001685e-4 * T3 - 1.120083e-6 * T4 +
@@ -35,6 +75,13 @@ __host__ __device__ inline double density_eos80(double T, double S, double p) {
     const double Ap = Aw + (2.2838e-3 - 1.0981e-5 * T - 1.6078e-6 * T2) * S + 1.91075e-4 * S15;
     const double Bp = Bw + (-9.9348e-7 + 2.0816e-8 * T + 9.1697e-10 * T2) * S;
     return rho0 / (1 - p / (K0 + Ap * p + Bp * p * p));
+}
+
+// The density a CarbonChemistry's options select, at P bar.
+__host__ __device__ inline double seawater_density(const obgc_carbon_options& o, double T, double S, double Pbar) {
+    return o.density == OBGC_DENSITY_CONSTANT ? o.density_value
+         : o.density == OBGC_DENSITY_EOS80   ? density_eos80(T, S, Pbar)
+                                              : density_teos10_poly(T, S, Pbar);
 }
 
 // PressureCorrection (equilibrium_constants.jl:11-40): the log of the factor, so that a constant
@@ -232,7 +279,7 @@ __host__ __device__ inline double carbon_cell(const obgc_carbon_options& o, doub
     const bool carbonate_path = o.output == OBGC_OUT_CARBONATE || o.output == OBGC_OUT_OMEGA_CALCITE;
     const bool hasP = o.has_pressure != 0;
     const double Pd = hasP ? P : (carbonate_path ? 0.0 : 1.0);
-    const double rho = o.density == OBGC_DENSITY_CONSTANT ? o.density_value : density_eos80(T, S, Pd);
+    const double rho = seawater_density(o, T, S, Pd);
     CarbConsts c;
     c.boron = 0.000232 / 10.811 * S / 1.80655;
     c.sulfate = 0.14 / 96.06 * S / 1.80655;

@@ -5,7 +5,8 @@
 // (gas_transfer_velocity.jl:30-31).
 //   CO2: C_water = pCO2 of the surface DIC, Alk, T, S with silicate = phosphate = 0
 //        (carbon_dioxide_concentration.jl:48-60), solubility = K0(T + 273.15, S) rho(T, S) / 1000
-//        with rho at zero pressure (gas_solubility.jl:58-64).
+//        with the carbon chemistry's density function at zero pressure (gas_solubility.jl:58-65,
+//        GasExchange.jl:110).
 //   O2:  C_water = O2, C_air = air * beta / Tk of Wanninkhof92Solubility evaluated as the reference
 //        writes it (gas_solubility.jl:40-50: B2 serves both salinity coefficients), solubility 1.
 #pragma once
@@ -20,7 +21,7 @@ __host__ __device__ inline double gas_flux_cell(const obgc_gas_exchange& g, doub
     const double kS = k660 / sqrt(Sc / 660.0);
     if (g.gas == OBGC_GAS_CO2) {
         const double Tk = T + 273.15;
-        const double solubility = weiss_k0(Tk, S, log(Tk), 1.0 / Tk) * density_eos80(T, S, 0.0) / 1000.0;
+        const double solubility = weiss_k0(Tk, S, log(Tk), 1.0 / Tk) * seawater_density(g.carbon, T, S, 0.0) / 1000.0;
         obgc_carbon_options o = g.carbon;
         o.output = OBGC_OUT_PCO2;
         o.ph_given = 0;

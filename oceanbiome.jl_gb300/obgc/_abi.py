@@ -48,7 +48,7 @@ SURFACE_DEFAULT, SURFACE_CONSTANT, SURFACE_FIELD = 0, 1, 2
 PERIODIC, BOUNDED, FLAT = 0, 1, 2
 ADVECTION_NONE, ADVECTION_WENO5 = 0, 1
 OUT_FCO2, OUT_PCO2, OUT_PH_FREE, OUT_PH_TOTAL, OUT_PH_SWS, OUT_H, OUT_CARBONATE, OUT_OMEGA = range(8)
-DENSITY_EOS80, DENSITY_CONSTANT = 0, 1
+DENSITY_EOS80, DENSITY_CONSTANT, DENSITY_TEOS10_POLYNOMIAL = 0, 1, 2
 
 
 # ----------------------------------------------------------------------------- structs

@@ -15,7 +15,9 @@ _OUTPUTS = {"fCO2": A.OUT_FCO2, "fCOâ‚‚": A.OUT_FCO2, "pCO2": A.OUT_PCO2, "pCOâ‚
 
 
 class CarbonChemistry:
-    """Carbon chemistry model; `density` is None for EOS-80 or a constant density (kg/m3)."""
+    """Carbon chemistry model.  `density`: None for the reference's default
+    teos10_polynomial_approximation (the TEOS-10 polynomial of Roquet et al. 2015), "eos80" for
+    UNESCO EOS-80, or a constant density (kg/m3)."""
 
     def __init__(self, density=None, max_iters=100, atol=1e-20, initial_pH_guess=8.0, calcite_solubility="calcite"):
         """calcite_solubility: "calcite" (KSP_calcite, the default) or "aragonite" (KSP_aragonite):
@@ -26,7 +28,9 @@ class CarbonChemistry:
         self.options.max_iters = max_iters
         self.options.atol = atol
         self.options.initial_pH_guess = initial_pH_guess
-        if density is not None:
+        if density == "eos80":
+            self.options.density = A.DENSITY_EOS80
+        elif density is not None:
             self.options.density, self.options.density_value = A.DENSITY_CONSTANT, float(density)
         if calcite_solubility not in ("calcite", "aragonite"):
             raise ValueError("calcite_solubility is 'calcite' or 'aragonite'")

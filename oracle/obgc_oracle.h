@@ -49,6 +49,8 @@ double or_pressure_correction(int which, double Tk, double P);
 double or_first_virial(double Tk);
 double or_cross_virial(double Tk);
 double or_density_eos80(double T, double S, double Pbar);
+double or_density_teos10_polynomial(double T, double S, double Pbar);
+double or_density(const obgc_carbon_options* o, double T, double S, double Pbar);
 int or_carbon_default_options(obgc_carbon_options* o);
 int or_carbon_chemistry(const obgc_carbon_options* o, double DIC, double Alk, double T, double S,
                         double silicate, double phosphate, double P, double pH, double* out,

@@ -64,7 +64,8 @@ double or_gas_exchange_flux(const obgc_gas_exchange* g, double T, double S, doub
     const double k660 = or_transfer_velocity_660(g->k660, u10);
     const double Sc = or_schmidt_number(g->schmidt, T);
     if (g->gas == OBGC_GAS_CO2) {
-        const double solubility = or_equilibrium_constant(OR_K0, T + 273.15, S, 0, 0.0) * or_density_eos80(T, S, 0.0) / 1000.0;
+        /* the carbon chemistry's density function at zero pressure (gas_solubility.jl:58-65) */
+        const double solubility = or_equilibrium_constant(OR_K0, T + 273.15, S, 0, 0.0) * or_density(&g->carbon, T, S, 0.0) / 1000.0;
         const double k = k660 / sqrt(Sc / 660.0) * solubility;
         obgc_carbon_options o = g->carbon;
         o.output = OBGC_OUT_PCO2;

@@ -4,10 +4,13 @@
  *   src/Models/CarbonChemistry/{carbon_chemistry.jl, alkalinity_residual.jl,
  *     equilibrium_constants.jl, virial_coefficients.jl, calcite_concentration.jl}
  *   src/Utils/solvers.jl (all four solvers) and the test functions of test/test_solvers.jl:8-25.
- * Seawater density: the reference evaluates SeawaterPolynomials.TEOS10._ρ (a third-party package,
- * SeawaterPolynomials 0.3.x, absent here).  The oracle offers the published UNESCO EOS-80
- * (Millero & Poisson 1981 one-atmosphere density, Millero et al. 1980 secant bulk modulus) or a
- * constant density; the doctest digits are pinned with the constant density they imply.
+ * Seawater density: the reference evaluates SeawaterPolynomials.TEOS10._ρ (SeawaterPolynomials
+ * 0.3.x, a third-party package absent here) through teos10_polynomial_approximation
+ * (src/Models/seawater_density.jl:33-39).  That is the published 55-term polynomial of Roquet et al.
+ * (2015, Ocean Modelling 90:29-43), restated below from the paper's coefficients as a plain sum
+ * over its (s, tau, zeta) exponents; the CarbonChemistry doctest digits pin it
+ * (carbon_chemistry.jl:55-62).  UNESCO EOS-80 (Millero & Poisson 1981, Millero et al. 1980) and a
+ * constant density are the other options.
  */
 #include <math.h>
 #include <float.h>
@@ -88,6 +91,47 @@ double or_euphotic_depth_column(int Nz, const double* zc, const double* PAR, dou
 }
 
 /* ------------------------------------------------------------------ density ---------- */
+/* Roquet et al. (2015): rho = r0(zeta) + sum R_ijk s^i tau^j zeta^k, tau = T / 40,
+ * s = sqrt((S_A + 32) / S_u), S_u = 40 x 35.16504 / 35, zeta = -Z / 1e4 with Z the height (m).
+ * teos10_polynomial_approximation (seawater_density.jl:33-39) passes T, S_A = S and Z = +10 Pbar. */
+static const struct { int i, j, k; double c; } ROQUET[] = {
+    {0,0,0, 8.0189615746e+02}, {1,0,0, 8.6672408165e+02}, {2,0,0,-1.7864682637e+03}, {3,0,0, 2.0375295546e+03},
+    {4,0,0,-1.2849161071e+03}, {5,0,0, 4.3227585684e+02}, {6,0,0,-6.0579916612e+01},
+    {0,1,0, 2.6010145068e+01}, {1,1,0,-6.5281885265e+01}, {2,1,0, 8.1770425108e+01}, {3,1,0,-5.6888046321e+01},
+    {4,1,0, 1.7681814114e+01}, {5,1,0,-1.9193502195e+00},
+    {0,2,0,-3.7074170417e+01}, {1,2,0, 6.1548258127e+01}, {2,2,0,-6.0362551501e+01}, {3,2,0, 2.9130021253e+01},
+    {4,2,0,-5.4723692739e+00},
+    {0,3,0, 2.1661789529e+01}, {1,3,0,-3.3449108469e+01}, {2,3,0, 1.9717078466e+01}, {3,3,0,-3.1742946532e+00},
+    {0,4,0,-8.3627885467e+00}, {1,4,0, 1.1311538584e+01}, {2,4,0,-5.3563304045e+00},
+    {0,5,0, 5.4048723791e-01}, {1,5,0, 4.8169980163e-01}, {0,6,0,-1.9083568888e-01},
+    {0,0,1, 1.9681925209e+01}, {1,0,1,-4.2549998214e+01}, {2,0,1, 5.0774768218e+01}, {3,0,1,-3.0938076334e+01},
+    {4,0,1, 6.6051753097e+00},
+    {0,1,1,-1.3336301113e+01}, {1,1,1,-4.4870114575e+00}, {2,1,1, 5.0042598061e+00}, {3,1,1,-6.5399043664e-01},
+    {0,2,1, 6.7080479603e+00}, {1,2,1, 3.5063081279e+00}, {2,2,1,-1.8795372996e+00},
+    {0,3,1,-2.4649669534e+00}, {1,3,1,-5.5077101279e-01}, {0,4,1, 5.5927935970e-01},
+    {0,0,2, 2.0660924175e+00}, {1,0,2,-4.9527603989e+00}, {2,0,2, 2.5019633244e+00},
+    {0,1,2, 2.0564311499e+00}, {1,1,2,-2.1311365518e-01}, {0,2,2,-1.2419983026e+00},
+    {0,0,3,-2.3342758797e-02}, {1,0,3,-1.8507636718e-02}, {0,1,3, 3.7969820455e-01},
+};
+static const double ROQUET_R0[6] = {4.6494977072e+01, -5.2099962525e+00, 2.2601900708e-01, 6.4326772569e-02,
+                                    1.5616995503e-02, -1.7243708991e-03};
+
+double or_density_teos10_polynomial(double T, double S, double Pbar) {
+    const double Z = 10.0 * Pbar;                 /* seawater_density.jl:34 */
+    const double zeta = -Z / 1e4, tau = T / 40.0, s = sqrt((S + 32.0) / (40.0 * 35.16504 / 35.0));
+    double rho = 0.0;
+    for (int n = 0; n < 6; n++) rho += ROQUET_R0[n] * pow(zeta, n + 1);
+    for (size_t q = 0; q < sizeof(ROQUET) / sizeof(ROQUET[0]); q++)
+        rho += ROQUET[q].c * pow(s, ROQUET[q].i) * pow(tau, ROQUET[q].j) * pow(zeta, ROQUET[q].k);
+    return rho;
+}
+
+double or_density(const obgc_carbon_options* o, double T, double S, double Pbar) {
+    if (o->density == OBGC_DENSITY_CONSTANT) return o->density_value;
+    if (o->density == OBGC_DENSITY_EOS80) return or_density_eos80(T, S, Pbar);
+    return or_density_teos10_polynomial(T, S, Pbar);
+}
+
 /* UNESCO EOS-80: rho(S, T, p) with p in bar (the reference passes bar and converts 10 m/bar). */
 double or_density_eos80(double T, double S, double p) {
     double T2 = T * T, T3 = T2 * T, T4 = T3 * T, T5 = T4 * T;
@@ -300,7 +344,7 @@ static double damped_newton_H(const obgc_carbon_options* o, double x0, const car
 int or_carbon_default_options(obgc_carbon_options* o) {
     memset(o, 0, sizeof(*o));
     o->output = OBGC_OUT_FCO2;
-    o->density = OBGC_DENSITY_EOS80;
+    o->density = OBGC_DENSITY_TEOS10_POLYNOMIAL;
     o->max_iters = 100;
     o->initial_pH_guess = 8.0;
     o->atol = 1e-20;
@@ -319,7 +363,7 @@ int or_carbon_chemistry(const obgc_carbon_options* o, double DIC, double Alk, do
     double T_c = T;
     /* density at P (or 1 bar for the pCO2 functor, 0 bar for carbonate_concentration) */
     double Pd = hasP ? P : (carbonate_path ? 0.0 : 1.0);
-    double rho = o->density == OBGC_DENSITY_CONSTANT ? o->density_value : or_density_eos80(T, S, Pd);
+    double rho = or_density(o, T, S, Pd);
     double boron = 0.000232 / 10.811 * S / 1.80655;
     double sulfate = 0.14 / 96.06 * S / 1.80655;
     double fluoride = 0.000067 / 18.9984 * S / 1.80655;

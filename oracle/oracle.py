@@ -86,6 +86,8 @@ def lib():
         L.or_cross_virial.restype = D
         L.or_density_eos80.argtypes = [D, D, D]
         L.or_density_eos80.restype = D
+        L.or_density_teos10_polynomial.argtypes = [D, D, D]
+        L.or_density_teos10_polynomial.restype = D
         L.or_carbon_default_options.argtypes = [P(A.CarbonOptions)]
         L.or_carbon_chemistry.argtypes = [P(A.CarbonOptions), D, D, D, D, D, D, D, D, P(D), P(C.c_int)]
         L.or_carbon_chemistry_batch.argtypes = [P(A.CarbonOptions), I64, P(D), P(D), P(D), P(D),
@@ -224,6 +226,10 @@ def density_eos80(T, S, P):
     return lib().or_density_eos80(T, S, P)
 
 
+def density_teos10_polynomial(T, S, P):
+    return lib().or_density_teos10_polynomial(T, S, P)
+
+
 def carbon_options(**kw):
     o = A.CarbonOptions()
     lib().or_carbon_default_options(C.byref(o))
@@ -235,7 +241,9 @@ def carbon_options(**kw):
 def carbon_chemistry(DIC, T, S, Alk=0.0, pH=None, P=None, silicate=0.0, phosphate=0.0,
                      output=A.OUT_FCO2, density=None, return_iters=False, **kw):
     o = carbon_options(output=output, **kw)
-    if density is not None:
+    if density == "eos80":
+        o.density = A.DENSITY_EOS80
+    elif density is not None:
         o.density, o.density_value = A.DENSITY_CONSTANT, density
     if pH is not None:
         o.ph_given = 1

@@ -95,6 +95,13 @@ def test_carbon_point_matches_oracle(output):
 
 
 def test_carbon_point_doctest_digits():
+    # the library's own TEOS-10 polynomial (Horner form), the default density, gives the three
+    # doctest digits of carbon_chemistry.jl:55-62 with no density supplied
+    cc = obgc.CarbonChemistry()
+    assert cc(2000.0, 10.0, 35.0, Alk=2000.0) == pytest.approx(1308.1474527899106, rel=1e-14)
+    assert cc(2000.0, 10.0, 35.0, Alk=2000.0, output="pHf") == pytest.approx(7.502532746463654, rel=1e-14)
+    assert cc(2000.0, 10.0, 35.0, pH=7.5) == pytest.approx(1315.7136384737507, rel=1e-14)
+    # and so does a constant density equal to the one the third digit implies
     from test_oracle_carbon import doctest_density
     rho = doctest_density()
     cc = obgc.CarbonChemistry(density=rho)

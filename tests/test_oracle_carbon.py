@@ -49,8 +49,11 @@ def test_virial_coefficients():
 
 
 def test_pco2_350():
-    # test_gasexchange_carbon_chem.jl:319-327 (EOS-80 stands in for the TEOS-10 polynomial)
+    # test_gasexchange_carbon_chem.jl:319-327
     pco2 = O.carbon_chemistry(2136.242890518708, 25.0, 35.0, Alk=2500.0, output=A.OUT_PCO2)
+    assert abs(pco2 - 350) <= 0.1
+    # and with EOS-80 standing in, as the oracle did before the polynomial was restated
+    pco2 = O.carbon_chemistry(2136.242890518708, 25.0, 35.0, Alk=2500.0, output=A.OUT_PCO2, density="eos80")
     assert abs(pco2 - 350) <= 0.1
 
 
@@ -61,6 +64,30 @@ def doctest_density():
     K1, K2, K0 = (O.K(w, Tk, 35.0) for w in (O.K1, O.K2, O.K0))
     f = 2000.0 * 1e-3 * H * H / (H * H + K1 * H + K1 * K2) / K0 * 1e6
     return f / 1315.7136384737507
+
+
+def test_doctest_digits_at_the_default_density():
+    # the default density (the TEOS-10 polynomial of Roquet et al. 2015, evaluated as
+    # seawater_density.jl:33-39 evaluates it, at the functor's default P = 1 bar) reproduces the
+    # three doctest digits of carbon_chemistry.jl:55-62
+    f1 = O.carbon_chemistry(2000.0, 10.0, 35.0, Alk=2000.0)
+    ph = O.carbon_chemistry(2000.0, 10.0, 35.0, Alk=2000.0, output=A.OUT_PH_FREE)
+    f3 = O.carbon_chemistry(2000.0, 10.0, 35.0, pH=7.5)
+    assert f1 == pytest.approx(1308.1474527899106, rel=1e-14, abs=0)
+    assert ph == pytest.approx(7.502532746463654, rel=1e-14, abs=0)
+    assert f3 == pytest.approx(1315.7136384737507, rel=1e-14, abs=0)
+    # the density itself: the one the third digit implies (fCO2 is linear in 1 / rho there)
+    assert O.density_teos10_polynomial(10.0, 35.0, 1.0) == pytest.approx(doctest_density(), rel=1e-14, abs=0)
+
+
+def test_teos10_polynomial_against_eos80():
+    # the two equations of state agree to the size of the practical / absolute salinity and
+    # temperature-scale differences (<= 0.2 kg/m3 over the ocean's range at the surface)
+    for T in (-1.0, 5.0, 15.0, 25.0, 30.0):
+        for S in (30.0, 35.0, 38.0):
+            assert abs(O.density_teos10_polynomial(T, S, 0.0) - O.density_eos80(T, S, 0.0)) < 0.2
+    # the reference's Z = +10 m per bar makes the polynomial's height positive: density falls with P
+    assert O.density_teos10_polynomial(10.0, 35.0, 100.0) < O.density_teos10_polynomial(10.0, 35.0, 0.0)
 
 
 def test_doctest_digits_with_implied_density():
