@@ -53,9 +53,10 @@ def fp64_peak():
 
 
 # FP64 FLOPs per cell (2 per DFMA + DMUL + DADD) from ncu's sass counters of one launch on these
-# workloads: the pH solve from a cold start (~5 Newton iterations) and PISCES' warm-started Omega
-CARBON_FLOP_PER_CELL = 1668.0
-OMEGA_FLOP_PER_CELL = 1552.0
+# workloads: the pH solve from a cold start (~5 Newton iterations) and PISCES' warm-started Omega,
+# both with the default TEOS-10 polynomial density
+CARBON_FLOP_PER_CELL = 1671.0
+OMEGA_FLOP_PER_CELL = 1529.0
 
 
 def e2e_steps_ms(step, dev, host, nsteps, stream):
