@@ -8,7 +8,8 @@ advanced one full RK3 step (three substeps) in one cell.
 
 Arms:
   default           the fused CUDA path through the C ABI (state resident in HBM for `value`;
-                    `e2e` copies the whole state host->device and back around every step).
+                    `e2e` copies the whole state host->device and back around every step, with
+                    two ensemble members alternating so that one's copies overlap the other's step).
   --impl reference  the CPU restatement of the reference's path (the reference itself is Julia and
                     cannot run here), all host cores, on a bounded sample of the same workload.
 Multi-GPU: each rank runs an independent replica (weak scaling, no data-path collective).
@@ -88,6 +89,51 @@ def e2e_steps_ms(step, dev, host, nsteps, stream):
                 done[n].record(out_stream)
     for n in names:
         stream.wait_event(done[n])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / nsteps
+
+
+def e2e_members_ms(members, nsteps, stream):
+    """End-to-end steps of an ensemble through the public API, the way a host drives several model
+    members on one GPU: member k % M takes step k, which copies that member's fields in from pinned
+    host memory (a copy stream), steps it on the launching stream and reads its result back (a
+    read-back stream).  A member's copy-in waits for its previous read-back, and its step for its
+    copy-in, so every step still moves its whole state both ways; the copies of one member overlap
+    the step of another.  members: [(step, dev fields, pinned host fields)].  Returns ms per step
+    (CUDA events on the launching stream, which joins both copy streams before the end event)."""
+    import torch
+    M = len(members)
+    in_stream, out_stream = torch.cuda.Stream(), torch.cuda.Stream()
+    copied = [torch.cuda.Event() for _ in range(M)]
+    stepped = [torch.cuda.Event() for _ in range(M)]
+    read = [torch.cuda.Event() for _ in range(M)]
+    start = torch.cuda.Event()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    start.record(stream)
+    in_stream.wait_event(start)
+    out_stream.wait_event(start)
+    for k in range(nsteps):
+        m = k % M
+        step, dev, host = members[m]
+        if k >= M:
+            in_stream.wait_event(read[m])
+        with torch.cuda.stream(in_stream):
+            for n in dev:
+                dev[n].copy_(host[n], non_blocking=True)
+            copied[m].record(in_stream)
+        stream.wait_event(copied[m])
+        step()
+        stepped[m].record(stream)
+        out_stream.wait_event(stepped[m])
+        with torch.cuda.stream(out_stream):
+            for n in dev:
+                host[n].copy_(dev[n], non_blocking=True)
+            read[m].record(out_stream)
+    for m in range(min(M, nsteps)):
+        stream.wait_event(read[m])
     e1.record(stream)
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / nsteps
@@ -264,18 +310,30 @@ def run_gpu(args):
     updates = N_TRACERS * g.N * args.steps * world
     value = updates / (ms / 1e3)
 
-    # ---- e2e: public API with host buffers: pinned state -> device, one step, state -> host
+    # ---- e2e: public API with host buffers: every step copies a member's whole state in from
+    # pinned host memory, steps it and copies it back; two ensemble members (two model contexts)
+    # alternate so that one member's copies overlap the other's step
     names = model.tracer_names
-    host = {n: torch.empty(g.shape, dtype=model.state_dtype, pin_memory=True) for n in names}
-    for n in names:
-        host[n].copy_(model.tracers[n])
+    member2 = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None),
+                                       precision=prec)
+    if args.tz:
+        member2.set_tiling(args.tz)
+    obgc.set_(member2, **obgc.lobster_initial_conditions(g, seed=23 + rank))
+    obgc.time_step(member2, DT, nsteps=1, graph=True)          # warm-up: builds its graph
+    members = []
+    for mdl in (model, member2):
+        host = {n: torch.empty(g.shape, dtype=mdl.state_dtype, pin_memory=True) for n in names}
+        for n in names:
+            host[n].copy_(mdl.tracers[n])
+        members.append(((lambda mdl=mdl: obgc.time_step(mdl, DT, nsteps=1, graph=True)),
+                        {n: mdl.tracers[n] for n in names}, host))
     barrier()
-    e2e_steps = max(1, min(args.steps, 20))
-    h2d = sum(h.numel() * h.element_size() for h in host.values())
-    e2e_ms = e2e_steps_ms(lambda: obgc.time_step(model, DT, nsteps=1, graph=True),
-                          {n: model.tracers[n] for n in names}, host, e2e_steps, stream)
+    e2e_steps = max(4, min(args.steps, 20))
+    h2d = sum(h.numel() * h.element_size() for h in members[0][2].values())
+    e2e_ms = e2e_members_ms(members, e2e_steps, stream)
     barrier()
     e2e_value = N_TRACERS * g.N * world / (e2e_ms / 1e3)
+    del member2, members
 
     # ---- roofline of the fused substep kernel
     s = 4 if prec == "f32" else 8
@@ -304,7 +362,9 @@ def run_gpu(args):
                        "precision": prec, "l2": "state (%.0f MB) larger than L2 (129 MB)" % (N_TRACERS * g.N * s / 1e6),
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-                    "ms_per_step": e2e_ms},
+                    "ms_per_step": e2e_ms, "steps": e2e_steps,
+                    "pipeline": "2 ensemble members alternate: each step copies its member's state in from pinned "
+                                "host memory and back; a member's copies overlap the other's step"},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
