@@ -531,7 +531,9 @@ def run_columns(args):
 
 # ----------------------------------------------------------------------------- column service
 SVC_WORKLOAD = ("column-run service: LOBSTER+carbonates columns, 8-512 levels (log-uniform), 1-30 days, dt 300-1800 s, "
-                "alkalinity pulse 0-500 at a random level and step; Poisson arrivals")
+                "alkalinity pulse 0-500 at a random level and step, air-sea CO2 exchange on DIC (surface T 2-28 degC, "
+                "S 33-37, wind 7 m/s); Poisson arrivals")
+SVC_WIND = 7.0
 
 
 def run_service(args):
@@ -543,6 +545,7 @@ def run_service(args):
     lib = A.load()
     prec = args.precision
     bgc = obgc.LOBSTER(None, carbonate_system=obgc.CarbonateSystem())
+    co2 = obgc.CarbonDioxideGasExchangeBoundaryCondition(wind_speed=SVC_WIND)
     rates = args.rates or [10.0, 100.0, 1000.0]
     rng = np.random.default_rng(99)
     sweep = []
@@ -553,7 +556,7 @@ def run_service(args):
             reqs = [obgc.lobster_column_request(rng) for _ in range(n)]
             gaps = rng.exponential(1.0 / lam, size=n)
             svc = obgc.ColumnService(bgc, precision=prec, max_columns=8192, arena_cells=4 << 20,
-                                     chunk_steps=args.chunk)
+                                     chunk_steps=args.chunk, co2_exchange=co2)
             l0 = lib.obgc_kernel_launch_count()
             t = time.perf_counter()
             for r, gap in zip(reqs, gaps):
@@ -580,8 +583,8 @@ def run_service(args):
     stream = torch.cuda.current_stream()
     for Nz in levels:
         r = obgc.lobster_column_request(np.random.default_rng(Nz), levels=(Nz, Nz), days=(1, 1))
-        e1_ = obgc.ColumnEngine(bgc, precision="f64", max_columns=1, arena_cells=Nz + 1)
-        e1_.add(r["init"], r["kappa"], r["dz"], r["dt"], 10 ** 6, surface_PAR=r["surface_PAR"])
+        e1_ = obgc.ColumnEngine(bgc, precision="f64", max_columns=1, arena_cells=Nz + 1, co2_exchange=co2)
+        e1_.add(r["init"], r["kappa"], r["dz"], r["dt"], 10 ** 6, surface_PAR=r["surface_PAR"], T=r["T"], S=r["S"])
         e1_.run(4, steps_per_launch=4, graph=False)
         torch.cuda.synchronize()
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

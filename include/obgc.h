@@ -771,6 +771,8 @@ typedef struct obgc_column_spec {
     int32_t pulse_step;      /* step at whose start pulse_amount is added to Alk (-1: none)    */
     int32_t pulse_k;         /* level of the pulse (0 = bottom)                                */
     double pulse_amount;     /* alkalinity added (meq/m3)                                      */
+    double temperature;      /* T (degC) and S of the column's surface water, read by the CO2  */
+    double salinity;         /* gas exchange (obgc_columns_desc.gas_exchange)                  */
 } obgc_column_spec;
 
 typedef struct obgc_columns_desc {
@@ -785,6 +787,14 @@ typedef struct obgc_columns_desc {
     int32_t negatives;           /* enum obgc_negatives                                        */
     uint32_t zero_exclude;       /* ZeroNegativeTracers exclude mask (bit n = enum obgc_tracer n) */
     double invalid_fill_value;   /* ScaleNegativeTracers fill for a negative group total (NaN) */
+    /* FieldBoundaryConditions(top = CarbonDioxideGasExchangeBoundaryCondition()) on DIC of every
+     * LOBSTER column (examples/column.jl:54-64): 1 on, 0 off.  `gas` (gas = OBGC_GAS_CO2, constant
+     * wind speed and air concentration: no wind or air fields) gives the condition's coefficients;
+     * each RK3 stage takes the flux from the column's surface DIC and Alk and its spec's
+     * temperature and salinity, and the surface cell loses flux / dz. */
+    int32_t gas_exchange;
+    int32_t reserved1;
+    obgc_gas_exchange gas;
 } obgc_columns_desc;
 
 int obgc_columns_create(const obgc_columns_desc* desc, obgc_columns** out);

@@ -8,7 +8,10 @@
 //      the column in chunks of 32 levels (2band.jl:15-32).
 //   2. Sinking face fluxes (WENO5 with the wall order reduction of the 3-D path) of the two
 //      drifting tracers (NPZD: P, D; LOBSTER: sPOM, bPOM).
-//   3. Every cell: BGC tendency + sinking divergence, RK3 update U += dt (gamma G + zeta G-).
+//   2b. With the CO2 gas exchange (LOBSTER columns): one thread per column takes the air-sea flux
+//      from the surface DIC and Alk and the column's T and S (FP64 pCO2 solve).
+//   3. Every cell: BGC tendency + sinking divergence (+ the surface flux / dz on DIC's top cell),
+//      RK3 update U += dt (gamma G + zeta G-).
 //   4. Vertically implicit diffusion (I - dt_s d/dz kappa d/dz) U = U*, dt_s = (gamma + zeta) dt,
 //      zero-flux walls: one Thomas solve per (column, tracer) with factors precomputed per stage.
 #include <algorithm>
@@ -17,6 +20,7 @@
 #include <map>
 #include <vector>
 #include "columns_engine.h"
+#include "gas_device.cuh"
 #include "negatives.cuh"
 #include "step_kernel.cuh"
 
@@ -38,11 +42,13 @@ struct ColArgs {
     int max_steps;
     int cap;
     NegativesSpec neg;          // modifier applied to the initial state and after every stage
+    int co2;                    // CO2 gas exchange on DIC (LOBSTER columns)
+    obgc_gas_exchange gas;
 };
 
 template <typename TS, typename TC, int NT>
 __host__ __device__ constexpr size_t col_smem_bytes(int cap) {
-    return sizeof(TS) * ((size_t)NT * cap + (cap + COL_MAXC) + 6 * (size_t)cap + 6 * COL_MAXC) +
+    return sizeof(TS) * ((size_t)NT * cap + (cap + COL_MAXC) + 6 * (size_t)cap + 8 * COL_MAXC) +
            sizeof(TC) * ((size_t)NT * cap + cap + 2 * (size_t)(cap + COL_MAXC)) + sizeof(int64_t) * COL_MAXC +
            sizeof(int) * 6 * COL_MAXC + sizeof(short) * ((size_t)2 * cap + COL_MAXC);
 }
@@ -58,7 +64,7 @@ template <int V, int NT, typename TS, typename TC>
 __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ ColArgs<TS, TC> a) {
     constexpr int SP = slot_of_P(V);
     constexpr int WA = V == V_NPZD ? 1 : 4, WB = V == V_NPZD ? 4 : 5;
-    constexpr int SALK = V == V_NPZD ? -1 : 8;
+    constexpr int SALK = V == V_NPZD ? -1 : 8, SDIC = V == V_NPZD ? -1 : 7;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const ColPack pk = a.packs[blockIdx.x];
     const int ncol = pk.count, cells = pk.cells, cap = a.cap;
@@ -72,8 +78,10 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
     TS* cP0 = cdt + COL_MAXC;
     TS* cmu = cP0 + COL_MAXC;
     TS* cpa = cmu + COL_MAXC;
-    TS* cr = cpa + COL_MAXC;                 // spare
-    TC* Gm = reinterpret_cast<TC*>(cr + COL_MAXC);
+    TS* cr = cpa + COL_MAXC;                 // the stage's air-sea flux of each column
+    TS* cT = cr + COL_MAXC;                  // surface T and S of each column
+    TS* cS = cT + COL_MAXC;
+    TC* Gm = reinterpret_cast<TC*>(cS + COL_MAXC);
     TC* PAR = Gm + NT * cap;
     TC* F = PAR + cap;                       // [2][cap + COL_MAXC] sinking fluxes
     int64_t* cbase = reinterpret_cast<int64_t*>(F + 2 * (cap + COL_MAXC));
@@ -99,6 +107,9 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
         cP0[tid] = sl.PAR0;
         cmu[tid] = sl.mu0;
         cpa[tid] = sl.pulse_amount;
+        cT[tid] = sl.temp;
+        cS[tid] = sl.sal;
+        cr[tid] = TS(0);
     }
     __syncthreads();
     if (tid == 0) {
@@ -207,6 +218,14 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
                     F[cap + COL_MAXC + fi] = TC(0);
                 }
             }
+            // 2b. air-sea CO2 flux of every column from its surface cell (gas_exchange.jl:26-39)
+            if constexpr (SDIC >= 0) {
+                if (a.co2 && tid < ncol && s < cst[tid]) {
+                    const int top = coff[tid] + cnz[tid] - 1;
+                    cr[tid] = TS(gas_flux_cell(a.gas, double(cT[tid]), double(cS[tid]), double(U[SDIC * cap + top]),
+                                               double(U[SALK * cap + top]), 0.0, a.gas.wind_speed, a.gas.air_concentration));
+                }
+            }
             __syncthreads();
             // 3. BGC + sinking divergence + RK3 update of every cell (increment in TC, sum in TS)
             const TC gam = TC(rk3_gamma(st)), zet = TC(rk3_zeta(st));
@@ -228,6 +247,7 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
                     TC G = g[slot_name(V, q)];
                     if (q == WA) G -= (F[fi + 1] - F[fi]) * idz;
                     if (q == WB) G -= (F[cap + COL_MAXC + fi + 1] - F[cap + COL_MAXC + fi]) * idz;
+                    if (q == SDIC && k == cnz[c] - 1) G -= TC(cr[c]) * idz;   // zero without the condition
                     const TC upd = st == 0 ? dt * gam * G : dt * (gam * G + zet * Gm[q * cap + i]);
                     U[q * cap + i] += TS(upd);
                     Gm[q * cap + i] = G;
@@ -311,6 +331,7 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
 
 int required_tracers(const obgc_npd_params* p, int32_t* names);
 bool drift_speed(const obgc_npd_params* p, int name, double* w0);
+bool valid_gas(const obgc_gas_exchange* g);
 
 }  // namespace obgc
 
@@ -353,6 +374,8 @@ int launch_columns(obgc_columns* e, int npacks, int max_steps, int threads, int 
     a.max_steps = max_steps;
     a.cap = cap;
     a.neg = e->neg;
+    a.co2 = e->desc.gas_exchange;
+    a.gas = e->desc.gas;
     const size_t smem = smem_for(e, cap);
     if (e->V == V_NPZD) column_kernel<V_NPZD, 5, TS, TC><<<npacks, threads, smem, st>>>(a);
     else column_kernel<V_LOBSTER_C, 9, TS, TC><<<npacks, threads, smem, st>>>(a);
@@ -412,7 +435,8 @@ int stage_slots(obgc_columns* e, int b) {
         ColSlot<T> o;
         o.cell_off = d.cell_off; o.Nz = d.Nz; o.steps_left = d.steps_left; o.steps_done = d.steps_done;
         o.pulse_step = d.pulse_step; o.pulse_k = d.pulse_k; o.live = d.live;
-        o.dz = T(d.dz); o.dt = T(d.dt); o.PAR0 = T(d.PAR0); o.mu0 = T(d.mu0); o.pulse_amount = T(d.pulse_amount); o.pad = T(0);
+        o.dz = T(d.dz); o.dt = T(d.dt); o.PAR0 = T(d.PAR0); o.mu0 = T(d.mu0); o.pulse_amount = T(d.pulse_amount);
+        o.temp = T(d.temp); o.sal = T(d.sal); o.pad = T(0);
         h[s] = o;
     }
     return n;
@@ -496,6 +520,7 @@ int reserve_column(obgc_columns* e, const obgc_column_spec* sp, int64_t* slot) {
     c.cell_off = off; c.Nz = sp->Nz; c.steps_left = sp->nsteps; c.steps_done = 0;
     c.pulse_step = sp->pulse_step; c.pulse_k = sp->pulse_k; c.live = 1;
     c.dz = sp->dz; c.dt = sp->dt; c.PAR0 = sp->surface_PAR; c.mu0 = sp->mu0; c.pulse_amount = sp->pulse_amount;
+    c.temp = sp->temperature; c.sal = sp->salinity;
     *slot = s;
     return OBGC_OK;
 }
@@ -529,6 +554,11 @@ extern "C" int obgc_columns_create(const obgc_columns_desc* d, obgc_columns** ou
     const int V = variant_of(d->npd);
     if (V != V_NPZD && V != V_LOBSTER_C)
         return fail(OBGC_ERR_UNSUPPORTED, "obgc_columns_create: columns support NPZD and LOBSTER with carbonates");
+    if (d->gas_exchange != 0 &&
+        (d->gas_exchange != 1 || V != V_LOBSTER_C || d->gas.gas != OBGC_GAS_CO2 || d->gas.wind_field || d->gas.air_field ||
+         !valid_gas(&d->gas)))
+        return fail(OBGC_ERR_INVALID_ARGUMENT,
+                    "obgc_columns_create: gas_exchange is CO2 on LOBSTER columns with a constant wind and air concentration");
     obgc_columns* e = new obgc_columns();
     e->desc = *d;
     e->V = V;

@@ -16,7 +16,7 @@ template <typename T>
 struct ColSlot {
     int64_t cell_off;           // first cell of the column's block (state at cell_off*NT, kappa at cell_off)
     int32_t Nz, steps_left, steps_done, pulse_step, pulse_k, live;
-    T dz, dt, PAR0, mu0, pulse_amount, pad;
+    T dz, dt, PAR0, mu0, pulse_amount, temp, sal, pad;   // temp / sal: surface T and S (gas exchange)
 };
 
 struct ColPack {

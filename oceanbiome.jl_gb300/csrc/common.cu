@@ -101,7 +101,7 @@ extern "C" int obgc_struct_layout(int32_t which, int64_t* out, int32_t cap) {
         case 6: out[0] = sizeof(obgc_fields); out[1] = offsetof(obgc_fields, passive);
                 out[2] = offsetof(obgc_fields, u); out[3] = offsetof(obgc_fields, G); return 0;
         case 7: out[0] = sizeof(obgc_column_spec); out[1] = offsetof(obgc_column_spec, dz);
-                out[2] = offsetof(obgc_column_spec, pulse_step); out[3] = offsetof(obgc_column_spec, pulse_amount); return 0;
+                out[2] = offsetof(obgc_column_spec, pulse_step); out[3] = offsetof(obgc_column_spec, salinity); return 0;
         case 9: out[0] = sizeof(obgc_pisces_params); out[1] = offsetof(obgc_pisces_params, micro);
                 out[2] = offsetof(obgc_pisces_params, doc_aggregation); out[3] = offsetof(obgc_pisces_params, open_bottom); return 0;
         case 10: out[0] = sizeof(obgc_pisces_phyto); out[1] = offsetof(obgc_pisces_phyto, exudated_fraction);
@@ -111,7 +111,7 @@ extern "C" int obgc_struct_layout(int32_t which, int64_t* out, int32_t cap) {
         case 12: out[0] = sizeof(obgc_gas_exchange); out[1] = offsetof(obgc_gas_exchange, wind_field);
                  out[2] = offsetof(obgc_gas_exchange, o2_solubility); out[3] = offsetof(obgc_gas_exchange, carbon); return 0;
         case 8: out[0] = sizeof(obgc_columns_desc); out[1] = offsetof(obgc_columns_desc, light);
-                out[2] = offsetof(obgc_columns_desc, arena_cells); out[3] = offsetof(obgc_columns_desc, invalid_fill_value); return 0;
+                out[2] = offsetof(obgc_columns_desc, arena_cells); out[3] = offsetof(obgc_columns_desc, gas); return 0;
     }
     return OBGC_ERR_INVALID_ARGUMENT;
 }

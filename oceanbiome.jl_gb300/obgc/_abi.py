@@ -236,14 +236,16 @@ PISCES_AUX = ["zmxl", "zeu", "Si_clim", "Omega", "kappa", "mixed_layer_PAR", "wP
 class ColumnSpec(C.Structure):
     _fields_ = [("Nz", C.c_int32), ("nsteps", C.c_int32), ("dz", C.c_double), ("dt", C.c_double),
                 ("surface_PAR", C.c_double), ("mu0", C.c_double), ("pulse_step", C.c_int32),
-                ("pulse_k", C.c_int32), ("pulse_amount", C.c_double)]
+                ("pulse_k", C.c_int32), ("pulse_amount", C.c_double), ("temperature", C.c_double),
+                ("salinity", C.c_double)]
 
 
 class ColumnsDesc(C.Structure):
     _fields_ = [("npd", NPDParams), ("light", TwoBandParams), ("precision", C.c_int32),
                 ("pack_cells", C.c_int32), ("threads", C.c_int32), ("max_columns", C.c_int32),
                 ("arena_cells", C.c_int64), ("negatives", C.c_int32), ("zero_exclude", C.c_uint32),
-                ("invalid_fill_value", C.c_double)]
+                ("invalid_fill_value", C.c_double), ("gas_exchange", C.c_int32), ("reserved1", C.c_int32),
+                ("gas", GasExchange)]
 
 
 class ServiceDesc(C.Structure):

@@ -5,8 +5,9 @@ Bounded))` with a NPZD or LOBSTER biogeochemistry, TwoBand light with a constant
 sinking of the particulate tracers (`src/Utils/sinking_velocity_fields.jl:10-35`), a
 vertically-implicit scalar diffusivity and Oceananigans' RK3 (the column examples of the
 reference, e.g. `examples/column.jl`).  Columns differ in depth, level count, dt, number of steps,
-maximum growth rate and an optional alkalinity pulse.  The engine packs whole columns into thread
-blocks and keeps each pack in shared memory for all steps of a launch.
+maximum growth rate, surface temperature and salinity, and an optional alkalinity pulse.  LOBSTER
+columns may carry the air-sea CO2 exchange of `examples/column.jl:54-64` on DIC.  The engine packs
+whole columns into thread blocks and keeps each pack in shared memory for all steps of a launch.
 """
 import ctypes as C
 
@@ -29,13 +30,16 @@ def _stream(stream):
 
 
 class ColumnEngine:
-    """ColumnEngine(biogeochemistry; precision, max_columns, arena_cells, pack_cells, threads).
+    """ColumnEngine(biogeochemistry; precision, max_columns, arena_cells, pack_cells, threads,
+    co2_exchange).
 
     `arena_cells` bounds the device memory: a column of Nz levels holds Nz + 1 cells of it
-    (state: n_tracers values per cell, plus one diffusivity per face)."""
+    (state: n_tracers values per cell, plus one diffusivity per face).  co2_exchange: a
+    CarbonDioxideGasExchangeBoundaryCondition (constant wind speed and air concentration) as the top
+    condition of every column's DIC, with each column's surface temperature and salinity."""
 
     def __init__(self, biogeochemistry, precision="f64", max_columns=1024, arena_cells=1 << 20,
-                 pack_cells=0, threads=0, light=None):
+                 pack_cells=0, threads=0, light=None, co2_exchange=None):
         lib = A.load()
         d = A.ColumnsDesc()
         d.npd = biogeochemistry.params
@@ -47,6 +51,10 @@ class ColumnEngine:
         d.max_columns = max_columns
         d.arena_cells = arena_cells
         d.negatives, d.zero_exclude, d.invalid_fill_value = negatives_config(biogeochemistry)
+        if co2_exchange is not None:
+            d.gas_exchange = 1
+            d.gas = co2_exchange.params
+        self.co2_exchange = co2_exchange
         h = C.c_void_p()
         A.check(lib.obgc_columns_create(C.byref(d), C.byref(h)), "obgc_columns_create")
         self._lib, self._h = lib, h
@@ -68,16 +76,17 @@ class ColumnEngine:
             pass
 
     def add(self, init, kappa, dz, dt, nsteps, surface_PAR=100.0, mu0=0.0, pulse_step=-1, pulse_k=-1,
-            pulse_amount=0.0):
+            pulse_amount=0.0, T=15.0, S=35.0):
         """init: [n_tracers, Nz] (bottom first), or a dict name -> [Nz]; kappa: Nz + 1 face
-        diffusivities (m^2/s).  Returns the column's slot."""
+        diffusivities (m^2/s); T, S: the surface temperature and salinity read by the CO2 exchange.
+        Returns the column's slot."""
         if isinstance(init, dict):
             init = np.stack([np.asarray(init[n], dtype=np.float64) for n in self.tracers])
         init = np.ascontiguousarray(init, dtype=np.float64)
         Nz = init.shape[1]
         kappa = np.ascontiguousarray(np.broadcast_to(np.asarray(kappa, dtype=np.float64), (Nz + 1,)))
         sp = A.ColumnSpec(Nz, int(nsteps), float(dz), float(dt), float(surface_PAR), float(mu0),
-                          int(pulse_step), int(pulse_k), float(pulse_amount))
+                          int(pulse_step), int(pulse_k), float(pulse_amount), float(T), float(S))
         slot = C.c_int64()
         A.check(self._lib.obgc_columns_add(self._h, C.byref(sp), init.ctypes.data_as(C.POINTER(C.c_double)),
                                            kappa.ctypes.data_as(C.POINTER(C.c_double)), C.byref(slot)),

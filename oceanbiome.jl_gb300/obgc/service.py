@@ -16,7 +16,9 @@ from .negatives import negatives_config
 
 class ColumnService:
     def __init__(self, biogeochemistry, precision="f32", max_columns=4096, arena_cells=1 << 20, chunk_steps=32,
-                 max_queue=0, pack_cells=0, threads=0, light=None):
+                 max_queue=0, pack_cells=0, threads=0, light=None, co2_exchange=None):
+        """co2_exchange: a CarbonDioxideGasExchangeBoundaryCondition on every LOBSTER run's DIC (the
+        uptake an alkalinity release drives), with each request's surface T and S."""
         lib = A.load()
         d = A.ServiceDesc()
         c = d.columns
@@ -29,6 +31,10 @@ class ColumnService:
         c.max_columns = max_columns
         c.arena_cells = arena_cells
         c.negatives, c.zero_exclude, c.invalid_fill_value = negatives_config(biogeochemistry)
+        if co2_exchange is not None:
+            c.gas_exchange = 1
+            c.gas = co2_exchange.params
+        self.co2_exchange = co2_exchange
         d.chunk_steps = chunk_steps
         d.max_queue = max_queue
         h = C.c_void_p()
@@ -53,14 +59,14 @@ class ColumnService:
             pass
 
     def submit(self, init, kappa, dz, dt, nsteps, surface_PAR=100.0, mu0=0.0, pulse_step=-1, pulse_k=-1,
-               pulse_amount=0.0):
+               pulse_amount=0.0, T=15.0, S=35.0):
         if isinstance(init, dict):
             init = np.stack([np.asarray(init[n], dtype=np.float64) for n in self.tracers])
         init = np.ascontiguousarray(init, dtype=np.float64)
         Nz = init.shape[1]
         kappa = np.ascontiguousarray(np.broadcast_to(np.asarray(kappa, dtype=np.float64), (Nz + 1,)))
         sp = A.ColumnSpec(Nz, int(nsteps), float(dz), float(dt), float(surface_PAR), float(mu0), int(pulse_step),
-                          int(pulse_k), float(pulse_amount))
+                          int(pulse_k), float(pulse_amount), float(T), float(S))
         rid = C.c_int64()
         A.check(self._lib.obgc_service_submit(self._h, C.byref(sp), init.ctypes.data_as(C.POINTER(C.c_double)),
                                               kappa.ctypes.data_as(C.POINTER(C.c_double)), C.byref(rid)),
@@ -72,7 +78,7 @@ class ColumnService:
         """Submit a dict as made by lobster_column_request / npzd_column_ensemble."""
         return self.submit(r["init"], r["kappa"], r["dz"], r["dt"], r["nsteps"], surface_PAR=r["surface_PAR"],
                            mu0=r.get("mu0", 0.0), pulse_step=r.get("pulse_step", -1), pulse_k=r.get("pulse_k", -1),
-                           pulse_amount=r.get("pulse_amount", 0.0))
+                           pulse_amount=r.get("pulse_amount", 0.0), T=r.get("T", 15.0), S=r.get("S", 35.0))
 
     def wait(self, rid, timeout=600.0):
         """(final state [n_tracers, Nz], latency in ms)."""

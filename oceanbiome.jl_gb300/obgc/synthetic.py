@@ -169,7 +169,8 @@ def lobster_column_request(rng, levels=(8, 512), days=(1, 30), dts=(300.0, 1800.
     random level and step.  The level thickness is U(2, 10) m but at least 1.5 w_max dt, so the
     explicit sinking of large particles stays below CFL 0.7.  Values: NO3 ~ U(5, 15), NH4 0.05,
     P, Z ~ lognormal(log 0.1, 0.5) in the mixed layer (a tenth below), sPOM = bPOM = DOM = 0.01,
-    DIC ~ U(2100, 2250), Alk ~ U(2300, 2450)."""
+    DIC ~ U(2100, 2250), Alk ~ U(2300, 2450); surface T ~ U(2, 28) degC and S ~ U(33, 37) for the
+    CO2 gas exchange."""
     Nz = int(np.exp(rng.uniform(np.log(levels[0]), np.log(levels[1] + 1))))
     Nz = max(levels[0], min(levels[1], Nz))
     dt = float(rng.uniform(*dts))
@@ -185,4 +186,5 @@ def lobster_column_request(rng, levels=(8, 512), days=(1, 30), dts=(300.0, 1800.
                      np.full(Nz, 0.01), np.full(Nz, rng.uniform(2100, 2250)), np.full(Nz, rng.uniform(2300, 2450))])
     return dict(init=init, kappa=mixed_layer_diffusivity(Nz, dz, mld), dz=dz, dt=dt, nsteps=nsteps,
                 surface_PAR=float(rng.uniform(50, 300)), mu0=0.0, pulse_step=int(rng.integers(0, nsteps)),
-                pulse_k=int(rng.integers(0, Nz)), pulse_amount=float(rng.uniform(*pulse)))
+                pulse_k=int(rng.integers(0, Nz)), pulse_amount=float(rng.uniform(*pulse)),
+                T=float(rng.uniform(2, 28)), S=float(rng.uniform(33, 37)))

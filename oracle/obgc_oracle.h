@@ -116,6 +116,7 @@ typedef struct or_column {
     int32_t pulse_step;          /* step at whose start pulse_amount is added to Alk (-1) */
     int32_t pulse_k;
     double pulse_amount;
+    double temperature, salinity; /* surface T and S of the CO2 gas exchange                   */
 } or_column;
 /* state: per column [n_tracers][Nz] (offsets given); kappa: per column Nz+1 face values.
  * negatives: 0 none, 1 ScaleNegativeTracers over conserved_tracers(bgc) (applied to the initial
@@ -124,7 +125,8 @@ void or_columns_run(const obgc_npd_params* p, const obgc_twoband_params* lp, int
                     const or_column* cols, const int64_t* state_offsets,
                     const int64_t* kappa_offsets, int n_tracers, const int32_t* names,
                     double* state, const double* kappa, double t0, double dt, int nsteps,
-                    int negatives, double invalid_fill_value, int nthreads);
+                    int negatives, double invalid_fill_value, int nthreads,
+                    const obgc_gas_exchange* gas /* CO2 on DIC, or NULL */);
 
 /* ---- negative tracers (src/Utils/negative_tracers.jl) ---- */
 #define OR_MAX_GROUPS 5

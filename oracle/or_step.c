@@ -408,7 +408,8 @@ static void implicit_diffusion(int Nz, double dz, const double* kf, double dts, 
 void or_columns_run(const obgc_npd_params* p0, const obgc_twoband_params* lp, int n_cols,
                     const or_column* cols, const int64_t* so, const int64_t* ko,
                     int nt, const int32_t* names, double* state, const double* kappa,
-                    double t0, double dt_all, int nsteps_all, int negatives, double fill, int nthreads) {
+                    double t0, double dt_all, int nsteps_all, int negatives, double fill, int nthreads,
+                    const obgc_gas_exchange* gas) {
     (void)t0;
     int32_t gn[OR_MAX_GROUPS], gslot[OR_MAX_GROUPS * OR_MAX_GROUP];
     double gfac[OR_MAX_GROUPS * OR_MAX_GROUP];
@@ -421,8 +422,11 @@ void or_columns_run(const obgc_npd_params* p0, const obgc_twoband_params* lp, in
         double dz = cols[c].dz;
         double dt = cols[c].dt > 0 ? cols[c].dt : dt_all;
         int nsteps = cols[c].nsteps > 0 ? cols[c].nsteps : nsteps_all;
-        int sAlk = -1;
-        for (int q = 0; q < nt; q++) if (names[q] == OBGC_ALK) sAlk = q;
+        int sAlk = -1, sDIC = -1;
+        for (int q = 0; q < nt; q++) {
+            if (names[q] == OBGC_ALK) sAlk = q;
+            if (names[q] == OBGC_DIC) sDIC = q;
+        }
         double* U = state + so[c];
         const double* kf = kappa + ko[c];
         double* G = calloc((size_t)nt * Nz, sizeof(double));
@@ -468,6 +472,15 @@ void or_columns_run(const obgc_npd_params* p0, const obgc_twoband_params* lp, in
                         }
                         G[(long)q * Nz + k] = tend;
                     }
+                }
+                /* FieldBoundaryConditions(top = CarbonDioxideGasExchangeBoundaryCondition()) on DIC
+                 * (examples/column.jl:54-64): the surface cell loses the stage's flux / dz */
+                if (gas && sDIC >= 0 && sAlk >= 0) {
+                    const long top = Nz - 1;
+                    const double F = or_gas_exchange_flux(gas, cols[c].temperature, cols[c].salinity,
+                                                          U[(long)sDIC * Nz + top], U[(long)sAlk * Nz + top], 0.0,
+                                                          gas->wind_speed, gas->air_concentration);
+                    G[(long)sDIC * Nz + top] -= F / dz;
                 }
                 double g = RK_G[st], z = RK_Z[st];
                 for (long x = 0; x < (long)nt * Nz; x++)

@@ -49,7 +49,8 @@ MAX_GROUPS, MAX_MEMBERS = 5, 10      # OR_MAX_GROUPS, OR_MAX_GROUP
 class Column(C.Structure):
     _fields_ = [("Nz", C.c_int32), ("nsteps", C.c_int32), ("dz", C.c_double),
                 ("surface_PAR", C.c_double), ("mu0", C.c_double), ("dt", C.c_double),
-                ("pulse_step", C.c_int32), ("pulse_k", C.c_int32), ("pulse_amount", C.c_double)]
+                ("pulse_step", C.c_int32), ("pulse_k", C.c_int32), ("pulse_amount", C.c_double),
+                ("temperature", C.c_double), ("salinity", C.c_double)]
 
 
 def build():
@@ -98,7 +99,8 @@ def lib():
         L.or_step3d.argtypes = [P(Model3D), P(D), VP, VP, VP, D, D, C.c_int, C.c_int]
         L.or_par3d.argtypes = [P(Model3D), P(D), D, P(D), C.c_int]
         L.or_columns_run.argtypes = [P(A.NPDParams), P(A.TwoBandParams), C.c_int, P(Column), P(I64),
-                                     P(I64), C.c_int, P(I32), P(D), P(D), D, D, C.c_int, C.c_int, D, C.c_int]
+                                     P(I64), C.c_int, P(I32), P(D), P(D), D, D, C.c_int, C.c_int, D, C.c_int,
+                                     P(A.GasExchange)]
         L.or_scale_negatives.argtypes = [I64, C.c_int, P(P(D)), P(D), D]
         L.or_pisces_defaults.argtypes = [P(A.PiscesParams)]
         L.or_cbm_day_length.argtypes = [D, D, D]
@@ -383,7 +385,8 @@ def group_arrays(groups):
 
 
 def columns_run(p, lp, cols, names, state, kappa, state_offsets, kappa_offsets, dt, nsteps, threads=None,
-                negatives=NEG_NONE, invalid_fill_value=float("nan")):
+                negatives=NEG_NONE, invalid_fill_value=float("nan"), gas=None):
+    """gas: an A.GasExchange (CO2) as the top boundary condition of DIC, or None."""
     n = len(cols)
     carr = (Column * n)(*cols)
     so = np.ascontiguousarray(state_offsets, dtype=np.int64)
@@ -392,7 +395,8 @@ def columns_run(p, lp, cols, names, state, kappa, state_offsets, kappa_offsets, 
     lib().or_columns_run(C.byref(p), C.byref(lp), n, carr, so.ctypes.data_as(C.POINTER(C.c_int64)),
                          ko.ctypes.data_as(C.POINTER(C.c_int64)), len(names),
                          nm.ctypes.data_as(C.POINTER(C.c_int32)), _dp(state), _dp(kappa), 0.0, dt,
-                         nsteps, negatives, invalid_fill_value, threads or nthreads())
+                         nsteps, negatives, invalid_fill_value, threads or nthreads(),
+                         None if gas is None else C.byref(gas))
     return state
 
 

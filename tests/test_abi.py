@@ -39,8 +39,8 @@ def test_every_declared_symbol_is_exported():
     (4, A.CarbonOptions, ["density_value", "atol", "saturation_mineral"]),
     (5, A.ModelDesc, ["surface", "grid", "passive_tendency_of"]),
     (6, A.Fields, ["passive", "u", "G"]),
-    (7, A.ColumnSpec, ["dz", "pulse_step", "pulse_amount"]),
-    (8, A.ColumnsDesc, ["light", "arena_cells", "invalid_fill_value"]),
+    (7, A.ColumnSpec, ["dz", "pulse_step", "salinity"]),
+    (8, A.ColumnsDesc, ["light", "arena_cells", "gas"]),
     (9, A.PiscesParams, ["micro", "doc_aggregation", "open_bottom"]),
     (10, A.PiscesPhyto, ["exudated_fraction", "base_growth_rate", "silicate_half_saturation_parameter"]),
     (11, A.PiscesField, ["value", "data", None]),

@@ -11,7 +11,7 @@ from gpuhelp import cuda, rel_err
 pytestmark = pytest.mark.gpu
 
 
-def oracle_columns(bgc, cols, names, negatives=O.NEG_NONE):
+def oracle_columns(bgc, cols, names, negatives=O.NEG_NONE, gas=None):
     """Run the columns through the oracle; returns a list of [n_tracers, Nz] arrays."""
     nt = len(names)
     so, ko, states, kaps, specs = [], [], [], [], []
@@ -25,19 +25,20 @@ def oracle_columns(bgc, cols, names, negatives=O.NEG_NONE):
         s_off += nt * Nz
         k_off += Nz + 1
         specs.append(O.Column(Nz, c["nsteps"], c["dz"], c["surface_PAR"], c.get("mu0", 0.0), c["dt"],
-                              c.get("pulse_step", -1), c.get("pulse_k", -1), c.get("pulse_amount", 0.0)))
+                              c.get("pulse_step", -1), c.get("pulse_k", -1), c.get("pulse_amount", 0.0),
+                              c.get("T", 15.0), c.get("S", 35.0)))
     state = np.ascontiguousarray(np.concatenate(states))
     kappa = np.ascontiguousarray(np.concatenate(kaps))
     O.columns_run(bgc.params, bgc.light_attenuation.params if bgc.light_attenuation else obgc._abi.default_twoband(),
                   specs, names, state, kappa, so, ko, 0.0, 0, negatives=negatives,
-                  invalid_fill_value=getattr(bgc, "invalid_fill_value", float("nan")))
+                  invalid_fill_value=getattr(bgc, "invalid_fill_value", float("nan")), gas=gas)
     return [state[so[q]:so[q] + nt * c["init"].shape[1]].reshape(nt, -1) for q, c in enumerate(cols)]
 
 
 def add_all(eng, cols):
     return [eng.add(c["init"], c["kappa"], c["dz"], c["dt"], c["nsteps"], surface_PAR=c["surface_PAR"],
                     mu0=c.get("mu0", 0.0), pulse_step=c.get("pulse_step", -1), pulse_k=c.get("pulse_k", -1),
-                    pulse_amount=c.get("pulse_amount", 0.0)) for c in cols]
+                    pulse_amount=c.get("pulse_amount", 0.0), T=c.get("T", 15.0), S=c.get("S", 35.0)) for c in cols]
 
 
 def npzd_cols(n=48, nsteps=60, seed=3):
@@ -121,6 +122,28 @@ def test_lobster_columns_with_pulses_match_oracle(precision, eps, floor):
     ref = oracle_columns(bgc, cols, eng.tracers)
     pert = oracle_columns(bgc, perturbed(cols, eps), eng.tracers)
     assert_within_envelope(got, ref, pert, floor)
+
+
+@pytest.mark.parametrize("precision,eps,floor", [("f64", 2.0 ** -53, 1e-12), ("mixed", 2.0 ** -24, 1e-4)])
+def test_lobster_columns_with_co2_exchange_match_oracle(precision, eps, floor):
+    # examples/column.jl:54-64: the CO2 gas exchange on every column's DIC, each column with its own
+    # surface T and S, a wind of 8 m/s and the air's 413 ppm; the alkalinity pulses then drive uptake
+    cuda()
+    bgc = lobster_bgc()
+    cols = lobster_cols(seed=9)
+    co2 = obgc.CarbonDioxideGasExchangeBoundaryCondition(wind_speed=8.0)
+    eng = obgc.ColumnEngine(bgc, precision=precision, max_columns=32, arena_cells=32 * 520, co2_exchange=co2)
+    slots = add_all(eng, cols)
+    while any(eng.remaining(s) for s in slots):
+        eng.advance(37)
+    got = [eng.read(s) for s in slots]
+    ref = oracle_columns(bgc, cols, eng.tracers, gas=co2.params)
+    pert = oracle_columns(bgc, perturbed(cols, eps), eng.tracers, gas=co2.params)
+    assert_within_envelope(got, ref, pert, floor)
+    # the condition moved the surface DIC (and nothing the pulses alone would)
+    plain = oracle_columns(bgc, cols, eng.tracers)
+    q = eng.tracers.index("DIC")
+    assert max(abs(r[q, -1] - p[q, -1]) for r, p in zip(ref, plain)) > 1e-2
 
 
 def test_result_is_the_same_alone_and_in_the_mix():

@@ -17,10 +17,11 @@ def requests(n, seed, days=(0.1, 0.6)):
     return [obgc.lobster_column_request(rng, levels=(8, 256), days=days) for _ in range(n)]
 
 
-def alone(bgc, r, precision):
-    eng = obgc.ColumnEngine(bgc, precision=precision, max_columns=2, arena_cells=r["init"].shape[1] + 1)
+def alone(bgc, r, precision, co2=None):
+    eng = obgc.ColumnEngine(bgc, precision=precision, max_columns=2, arena_cells=r["init"].shape[1] + 1,
+                            co2_exchange=co2)
     s = eng.add(r["init"], r["kappa"], r["dz"], r["dt"], r["nsteps"], surface_PAR=r["surface_PAR"], mu0=r["mu0"],
-                pulse_step=r["pulse_step"], pulse_k=r["pulse_k"], pulse_amount=r["pulse_amount"])
+                pulse_step=r["pulse_step"], pulse_k=r["pulse_k"], pulse_amount=r["pulse_amount"], T=r["T"], S=r["S"])
     while eng.remaining(s):
         eng.advance(97)
     out = eng.read(s)
@@ -28,12 +29,14 @@ def alone(bgc, r, precision):
     return out
 
 
-@pytest.mark.parametrize("precision", ["f32", "mixed"])
-def test_each_result_is_the_same_alone_and_in_the_mix(precision):
+@pytest.mark.parametrize("precision,with_co2", [("f32", False), ("mixed", False), ("f32", True)])
+def test_each_result_is_the_same_alone_and_in_the_mix(precision, with_co2):
     cuda()
     bgc = obgc.LOBSTER(None, carbonate_system=obgc.CarbonateSystem())
+    co2 = obgc.CarbonDioxideGasExchangeBoundaryCondition(wind_speed=7.0) if with_co2 else None
     reqs = requests(30, seed=17)
-    svc = obgc.ColumnService(bgc, precision=precision, max_columns=64, arena_cells=64 * 260, chunk_steps=16)
+    svc = obgc.ColumnService(bgc, precision=precision, max_columns=64, arena_cells=64 * 260, chunk_steps=16,
+                             co2_exchange=co2)
     ids = []
     for wave in range(3):                       # later waves arrive while earlier runs are on the GPU
         for r in reqs[wave * 10:(wave + 1) * 10]:
@@ -45,7 +48,7 @@ def test_each_result_is_the_same_alone_and_in_the_mix(precision):
     assert st["completed"] == len(reqs) and st["launches"] > 0
     for r, (got, lat) in zip(reqs, results):
         assert lat > 0
-        assert np.array_equal(got, alone(bgc, r, precision))
+        assert np.array_equal(got, alone(bgc, r, precision, co2))
 
 
 def test_admission_waits_for_the_hbm_budget():

@@ -63,3 +63,34 @@ def test_columns_are_independent_in_one_call():
     together = run(bgc, cols, names)
     for c, t in zip(cols, together):
         assert np.array_equal(run(bgc, [c], names)[0], t)
+
+
+def test_co2_exchange_column_equals_the_3d_step_of_a_single_column():
+    """The column runner's CO2 condition (examples/column.jl:54-64) against the oracle's 3-D step of a
+    1 x 1 x Nz grid carrying the same T and S as tracers, with no diffusion: the two restatements of
+    the top boundary condition agree to rounding."""
+    bgc = obgc.LOBSTER(None, carbonate_system=obgc.CarbonateSystem())
+    rng = np.random.default_rng(4)
+    c = obgc.lobster_column_request(rng, levels=(24, 24), days=(0.5, 0.5), pulse=(300.0, 300.0))
+    c["kappa"] = np.zeros_like(c["kappa"])
+    names = list(obgc.required_biogeochemical_tracers(bgc))
+    co2 = O.gas_exchange_defaults(obgc._abi.GAS_CO2)
+    co2.wind_speed = 9.0
+    Nz, nt = c["init"].shape[1], len(names)
+    spec = O.Column(Nz, c["nsteps"], c["dz"], c["surface_PAR"], 0.0, c["dt"], -1, -1, 0.0, c["T"], c["S"])
+    col = np.ascontiguousarray(c["init"].ravel().copy())
+    O.columns_run(bgc.params, obgc._abi.default_twoband(), [spec], names, col, c["kappa"], [0], [0], 0.0, 0, gas=co2)
+    g = obgc.RectilinearGrid((1, 1, Nz), (1.0, 1.0, Nz * c["dz"]), ("Flat", "Flat", "Bounded"))
+    m = O.model3d(bgc.params, g.c_grid(), names + ["T", "S"], surface_kind=obgc._abi.SURFACE_CONSTANT,
+                  surface_value=c["surface_PAR"], gas_exchange=[co2])
+    s3 = np.concatenate([c["init"], np.full((1, Nz), c["T"]), np.full((1, Nz), c["S"])]).reshape(nt + 2, Nz, 1, 1)
+    s3 = np.ascontiguousarray(s3)
+    O.step3d(m, s3, t=0.0, dt=c["dt"], nsteps=c["nsteps"])
+    col = col.reshape(nt, Nz)
+    for q in range(nt):
+        assert np.max(np.abs(col[q] - s3[q, :, 0, 0])) <= 1e-12 * np.max(np.abs(s3[q])), names[q]
+    # and the condition did something: the surface DIC differs from a run without it
+    plain = np.ascontiguousarray(c["init"].ravel().copy())
+    O.columns_run(bgc.params, obgc._abi.default_twoband(), [spec], names, plain, c["kappa"], [0], [0], 0.0, 0)
+    q = names.index("DIC")
+    assert abs(plain.reshape(nt, Nz)[q, -1] - col[q, -1]) > 1e-2
