@@ -271,6 +271,21 @@ __host__ __device__ inline CarbSolve solve_H(const obgc_carbon_options& o, doubl
     return r;
 }
 
+// pCO2 from fCO2 (carbon_chemistry.jl:170-193): the virial fugacity coefficient iterated three
+// times at total pressure Pp (Pa).
+__host__ __device__ inline double pco2_from_fco2(double fCO2, double Tk, double Pp) {
+    const double B = (-1636.75 + 12.0408 * Tk + (-3.27957 * 1e-2) * (Tk * Tk) + (3.16528 * 1e-5) * (Tk * Tk * Tk)) * 1e-6;
+    const double dl = (57.7 + -0.118 * Tk) * 1e-6;
+    const double fp = fCO2 * 0.09807;
+    double phi = 1.0, x = fp / Pp;
+    for (int n = 0; n < 3; n++) {
+        const double y = 1.0 - x;
+        phi = exp((B + 2.0 * y * y * dl) * Pp / (8.31446261815324 * Tk));
+        x = fp / (phi * Pp);
+    }
+    return fp / phi / 0.09807;
+}
+
 // One cell of (p::CarbonChemistry)(; DIC, T, S, Alk, pH, P, output, silicate, phosphate) and of
 // carbonate_concentration / calcite_saturation.  Returns the selected output.
 __host__ __device__ inline double carbon_cell(const obgc_carbon_options& o, double DIC, double Alk, double T, double S,
@@ -327,19 +342,7 @@ __host__ __device__ inline double carbon_cell(const obgc_carbon_options& o, doub
         case OBGC_OUT_FCO2: return fCO2;
         case OBGC_OUT_H: return H;
         case OBGC_OUT_PH_FREE: return -log10(H);
-        case OBGC_OUT_PCO2: {
-            const double Pp = (hasP ? P : 1.0) * 101325;
-            const double B = (-1636.75 + 12.0408 * Tk + (-3.27957 * 1e-2) * (Tk * Tk) + (3.16528 * 1e-5) * (Tk * Tk * Tk)) * 1e-6;
-            const double dl = (57.7 + -0.118 * Tk) * 1e-6;
-            const double fp = fCO2 * 0.09807;
-            double phi = 1.0, x = fp / Pp;
-            for (int n = 0; n < 3; n++) {
-                const double y = 1.0 - x;
-                phi = exp((B + 2.0 * y * y * dl) * Pp / (8.31446261815324 * Tk));
-                x = fp / (phi * Pp);
-            }
-            return fp / phi / 0.09807;
-        }
+        case OBGC_OUT_PCO2: return pco2_from_fco2(fCO2, Tk, (hasP ? P : 1.0) * 101325);
         case OBGC_OUT_PH_TOTAL: return -log10(H + c.sulfate / (1 + c.KS / H));
         case OBGC_OUT_PH_SWS: return -log10(H + c.sulfate / (1 + c.KS / H) + c.fluoride / (1 + c.KF / H));
     }

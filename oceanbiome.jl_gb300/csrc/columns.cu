@@ -53,6 +53,14 @@ __host__ __device__ constexpr size_t col_smem_bytes(int cap) {
            sizeof(int) * 6 * COL_MAXC + sizeof(short) * ((size_t)2 * cap + COL_MAXC);
 }
 
+// The CO2 condition's per-column state after the layout above (engines with the condition only):
+// the cached T/S constants and the [H+] each column's solve restarts from.
+template <typename TS, typename TC, int NT>
+__host__ __device__ constexpr size_t col_co2_offset(int cap) {
+    return (col_smem_bytes<TS, TC, NT>(cap) + 15) / 16 * 16;
+}
+constexpr size_t COL_CO2_BYTES = (sizeof(Co2Column) + sizeof(double)) * COL_MAXC;
+
 template <typename T>
 __device__ __forceinline__ T sink_w(T w0, int open_bottom, int f, int Nz) {
     // setup_velocity_fields (sinking_velocity_fields.jl:10-35); the surface face stays zero
@@ -93,6 +101,8 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
     int* cpk = cps + COL_MAXC;
     short* colid = reinterpret_cast<short*>(cpk + COL_MAXC);
     short* fcol = colid + cap;
+    Co2Column* cco2 = reinterpret_cast<Co2Column*>(smem_raw + col_co2_offset<TS, TC, NT>(cap));
+    double* cH = reinterpret_cast<double*>(cco2 + COL_MAXC);
 
     if (tid < ncol) {
         const ColSlot<TS> sl = a.slots[a.pack_slots[pk.first + tid]];
@@ -110,6 +120,12 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
         cT[tid] = sl.temp;
         cS[tid] = sl.sal;
         cr[tid] = TS(0);
+        if constexpr (SDIC >= 0) {
+            if (a.co2) {
+                co2_column_prepare(a.gas, double(sl.temp), double(sl.sal), a.gas.wind_speed, cco2[tid]);
+                cH[tid] = exp(-2.302585092994046 * a.gas.carbon.initial_pH_guess);
+            }
+        }
     }
     __syncthreads();
     if (tid == 0) {
@@ -222,8 +238,8 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
             if constexpr (SDIC >= 0) {
                 if (a.co2 && tid < ncol && s < cst[tid]) {
                     const int top = coff[tid] + cnz[tid] - 1;
-                    cr[tid] = TS(gas_flux_cell(a.gas, double(cT[tid]), double(cS[tid]), double(U[SDIC * cap + top]),
-                                               double(U[SALK * cap + top]), 0.0, a.gas.wind_speed, a.gas.air_concentration));
+                    cr[tid] = TS(co2_column_flux(a.gas, cco2[tid], double(U[SDIC * cap + top]), double(U[SALK * cap + top]),
+                                                 a.gas.air_concentration, cH[tid]));
                 }
             }
             __syncthreads();
@@ -391,10 +407,17 @@ int launch_any(obgc_columns* e, int npacks, int max_steps, int threads, int cap,
 
 size_t smem_for(const obgc_columns* e, int cap) {
     const bool npzd = e->V == V_NPZD;
-    if (e->prec == OBGC_PREC_F32) return npzd ? col_smem_bytes<float, float, 5>(cap) : col_smem_bytes<float, float, 9>(cap);
+    if (npzd) {
+        if (e->prec == OBGC_PREC_F32) return col_smem_bytes<float, float, 5>(cap);
+        if (e->prec == OBGC_PREC_F64) return col_smem_bytes<double, double, 5>(cap);
+        return col_smem_bytes<double, float, 5>(cap);
+    }
+    // LOBSTER: the CO2 condition's per-column state follows the common layout
+    const size_t co2 = e->desc.gas_exchange ? COL_CO2_BYTES : 0;
+    if (e->prec == OBGC_PREC_F32) return (co2 ? col_co2_offset<float, float, 9>(cap) : col_smem_bytes<float, float, 9>(cap)) + co2;
     if (e->prec == OBGC_PREC_F64)
-        return npzd ? col_smem_bytes<double, double, 5>(cap) : col_smem_bytes<double, double, 9>(cap);
-    return npzd ? col_smem_bytes<double, float, 5>(cap) : col_smem_bytes<double, float, 9>(cap);
+        return (co2 ? col_co2_offset<double, double, 9>(cap) : col_smem_bytes<double, double, 9>(cap)) + co2;
+    return (co2 ? col_co2_offset<double, float, 9>(cap) : col_smem_bytes<double, float, 9>(cap)) + co2;
 }
 
 // First-fit decreasing packing of the live columns into packs of `cap` cells, written to staging

@@ -36,4 +36,47 @@ __host__ __device__ inline double gas_flux_cell(const obgc_gas_exchange& g, doub
     return kS * (O2 - air * (beta / Tk));
 }
 
+// The CO2 condition of one column whose surface T and S stay fixed (the column engine): the
+// T/S-dependent parts of gas_flux_cell evaluated once (equilibrium constants, the residual's
+// H-independent terms, the density conversion, k x solubility), then per RK3 stage only the
+// unit conversion of DIC and Alk, the Newton solve started from the column's previous [H+], and
+// pCO2.  The same arithmetic as gas_flux_cell but for the starting point of the solve.
+struct Co2Column {
+    CarbConsts c;
+    double conv;       // 1e-3 / rho (mmol/m3 -> mol/kg)
+    double k_sol;      // transfer velocity x solubility
+    double Tk;
+};
+
+__host__ __device__ inline void co2_column_prepare(const obgc_gas_exchange& g, double T, double S, double u10, Co2Column& col) {
+    const double k660 = g.k660[0] + u10 * (g.k660[1] + u10 * (g.k660[2] + u10 * g.k660[3]));
+    const double Sc = g.schmidt[0] + T * (g.schmidt[1] + T * (g.schmidt[2] + T * (g.schmidt[3] + T * g.schmidt[4])));
+    const double Tk = T + 273.15;
+    col.Tk = Tk;
+    col.k_sol = k660 / sqrt(Sc / 660.0) * (weiss_k0(Tk, S, log(Tk), 1.0 / Tk) * seawater_density(g.carbon, T, S, 0.0) / 1000.0);
+    col.conv = 1e-3 / seawater_density(g.carbon, T, S, 1.0);   // the pCO2 functor's density at 1 bar
+    CarbConsts& c = col.c;
+    c.boron = 0.000232 / 10.811 * S / 1.80655;
+    c.sulfate = 0.14 / 96.06 * S / 1.80655;
+    c.fluoride = 0.000067 / 18.9984 * S / 1.80655;
+    c.DIC = c.Alk = c.phosphate = c.silicate = 0.0;
+    equilibrium_constants(Tk, S, false, 0.0, true, c);
+    prepare_residual(c);
+}
+
+// Flux (positive out of the ocean) from the surface DIC and Alk; H: the column's [H+], updated.
+__host__ __device__ inline double co2_column_flux(const obgc_gas_exchange& g, const Co2Column& col, double DIC,
+                                                  double Alk, double air, double& H) {
+    CarbConsts c = col.c;
+    c.DIC = DIC * col.conv;
+    c.Alk = Alk * col.conv;
+    obgc_carbon_options o = g.carbon;
+    o.output = OBGC_OUT_PCO2;
+    const CarbSolve r = solve_H(o, H, c);
+    H = r.H;
+    const double CO2 = c.DIC * (H * H) / (H * H + c.K1 * H + c.K1 * c.K2);
+    const double pCO2 = pco2_from_fco2((CO2 / c.K0) * 1e6, col.Tk, 101325.0);
+    return col.k_sol * (pCO2 - air);
+}
+
 }  // namespace obgc
