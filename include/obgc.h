@@ -645,6 +645,29 @@ int obgc_box_run(const obgc_npd_params* p, const obgc_npd_params* params_per_mod
                  double t0, double dt, int32_t nsteps, int32_t record_every, double* record,
                  int32_t precision, void* stream);
 
+/* Time-dependent drivers of obgc_box_run_drivers: BoxModel(; forcing, prescribed_tracers)
+ * (src/BoxModel/boxmodel.jl:65-87, timesteppers.jl:37-63), sampled at the RK3 stage times like PAR.
+ *   prescribed_tracers = (; X = f(t)): before the tendencies of stage s of step n the tracer takes
+ *     prescribed[q][(3n + s) * n_models + m] (update_state!), and after step n the value of row
+ *     3(n + 1), so a device array of (3 nsteps + 1) rows of n_models.
+ *   forcing = (; X = F): F's rate at the stage time, forcing[q][(3n + s) * n_models + m], is added
+ *     to X's tendency; 3 nsteps rows.  Forcings that read the model's fields are outside this form. */
+#define OBGC_BOX_MAX_DRIVERS 4
+typedef struct obgc_box_drivers {
+    const double* PAR;           /* as obgc_box_run                                            */
+    double par_constant;
+    int32_t n_prescribed, n_forced;             /* each <= OBGC_BOX_MAX_DRIVERS              */
+    int32_t prescribed_names[OBGC_BOX_MAX_DRIVERS];   /* enum obgc_tracer                     */
+    int32_t forced_names[OBGC_BOX_MAX_DRIVERS];
+    const double* prescribed[OBGC_BOX_MAX_DRIVERS];   /* device                               */
+    const double* forcing[OBGC_BOX_MAX_DRIVERS];      /* device                               */
+} obgc_box_drivers;
+/* obgc_box_run with prescribed tracers and forcing (drivers->n_prescribed = n_forced = 0 is
+ * obgc_box_run). */
+int obgc_box_run_drivers(const obgc_npd_params* p, const obgc_npd_params* params_per_model, int64_t n_models,
+                         double* state, const obgc_box_drivers* drivers, double t0, double dt, int32_t nsteps,
+                         int32_t record_every, double* record, int32_t precision, void* stream);
+
 /* ---------------------------------------------------------------------------------------
  * Batched uneven columns: many independent 1-D water columns (different depth, parameters,
  * step and duration) advanced together.  Each column is the reference's column configuration

@@ -248,6 +248,16 @@ class ColumnsDesc(C.Structure):
                 ("gas", GasExchange)]
 
 
+BOX_MAX_DRIVERS = 4
+
+
+class BoxDrivers(C.Structure):
+    _fields_ = [("PAR", C.c_void_p), ("par_constant", C.c_double), ("n_prescribed", C.c_int32),
+                ("n_forced", C.c_int32), ("prescribed_names", C.c_int32 * BOX_MAX_DRIVERS),
+                ("forced_names", C.c_int32 * BOX_MAX_DRIVERS), ("prescribed", C.c_void_p * BOX_MAX_DRIVERS),
+                ("forcing", C.c_void_p * BOX_MAX_DRIVERS)]
+
+
 class ServiceDesc(C.Structure):
     _fields_ = [("columns", ColumnsDesc), ("chunk_steps", C.c_int32), ("max_queue", C.c_int32)]
 
@@ -340,6 +350,7 @@ def load():
     _sig(lib, "obgc_set_profiling", C.c_int, VP, I32)
     _sig(lib, "obgc_set_tiling", C.c_int, VP, I32)
     _sig(lib, "obgc_box_run", C.c_int, P(NPDParams), VP, I64, VP, VP, D, D, D, I32, I32, VP, I32, VP)
+    _sig(lib, "obgc_box_run_drivers", C.c_int, P(NPDParams), VP, I64, VP, P(BoxDrivers), D, D, I32, I32, VP, I32, VP)
     _sig(lib, "obgc_npd_conserved_tracers", C.c_int, P(NPDParams), I32, P(I32), P(D), I32)
     _sig(lib, "obgc_scale_negatives", C.c_int, P(Grid), I32, I32, P(VP), P(D), D, VP)
     _sig(lib, "obgc_zero_negatives", C.c_int, P(Grid), I32, I32, P(VP), VP)
@@ -390,7 +401,7 @@ EXPORTED = [
     "obgc_multiband_coefficients", "obgc_euphotic_depth", "obgc_carbon_default_options",
     "obgc_carbon_chemistry", "obgc_carbon_chemistry_point", "obgc_create", "obgc_destroy",
     "obgc_bind_fields", "obgc_update_state", "obgc_compute_tendencies", "obgc_step",
-    "obgc_step_graph", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run",
+    "obgc_step_graph", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run", "obgc_box_run_drivers",
     "obgc_set_profiling", "obgc_set_tiling", "obgc_struct_layout", "obgc_tracer_budget_static",
     "obgc_columns_create", "obgc_columns_destroy", "obgc_columns_tracers", "obgc_columns_add",
     "obgc_columns_advance", "obgc_columns_run", "obgc_columns_remaining", "obgc_columns_read", "obgc_columns_remove",

@@ -66,6 +66,9 @@ double or_solve_test_function(int solver, int fid, double x0, double x1, double 
                               double pa, double pb);
 
 /* ---- BoxModel ---- */
+void or_box_run_drivers(const obgc_npd_params* p, double* v, const double* PAR_stages, double PAR_const, double dt,
+                        int nsteps, int np, const int32_t* pnames, const double* const* presc, int nf,
+                        const int32_t* fnames, const double* const* frc);
 void or_box_run(const obgc_npd_params* p, double* v, const double* PAR_stages, double PAR_const,
                 double t0, double dt, int nsteps);
 

@@ -91,6 +91,34 @@ void or_box_run(const obgc_npd_params* p, double* v, const double* PAR_stages, d
     }
 }
 
+/* BoxModel(; forcing, prescribed_tracers) (boxmodel.jl:65-87, timesteppers.jl:37-63): before
+ * the tendencies of stage st of step s, update_state! sets each prescribed tracer to its value at
+ * the stage time (row 3 s + st of presc[q]); after the step, to its value at the step's end (row
+ * 3 (s + 1)).  A forcing adds its stage-time rate (row 3 s + st of frc[q]) to the tracer's
+ * tendency.  presc[q]: [3 nsteps + 1], frc[q]: [3 nsteps]. */
+void or_box_run_drivers(const obgc_npd_params* p, double* v, const double* PAR_stages, double PAR_const, double dt,
+                        int nsteps, int np, const int32_t* pnames, const double* const* presc, int nf,
+                        const int32_t* fnames, const double* const* frc) {
+    int32_t names[32];
+    int n = or_npd_required_tracers(p, names, 32);
+    double G[OBGC_NUM_NAMED] = {0}, Gm[OBGC_NUM_NAMED] = {0};
+    for (int s = 0; s < nsteps; s++) {
+        for (int st = 0; st < 3; st++) {
+            for (int q = 0; q < np; q++) v[pnames[q]] = presc[q][3 * s + st];
+            double PAR = PAR_stages ? PAR_stages[3 * s + st] : PAR_const;
+            for (int q = 0; q < n; q++) G[names[q]] = or_npd_tendency(p, names[q], v, PAR);
+            for (int q = 0; q < nf; q++) G[fnames[q]] += frc[q][3 * s + st];
+            for (int nm = 0; nm < OBGC_NUM_NAMED; nm++) {
+                if (st == 0) v[nm] += dt * RK_G[0] * G[nm];
+                else v[nm] += dt * (RK_G[st] * G[nm] + RK_Z[st] * Gm[nm]);
+            }
+            memcpy(Gm, G, sizeof(G));
+            memset(G, 0, sizeof(G));
+        }
+        for (int q = 0; q < np; q++) v[pnames[q]] = presc[q][3 * (s + 1)];
+    }
+}
+
 /* ------------------------------------------------------------------ 3-D ---------- */
 static double surface_par(const or_model3d* m, double t) {
     return m->surface_kind == OBGC_SURFACE_PAR_CONSTANT ? m->surface_value : or_default_surface_PAR(t);

@@ -96,6 +96,8 @@ def lib():
         L.or_solve_test_function.argtypes = [C.c_int, C.c_int, D, D, D, D, D]
         L.or_solve_test_function.restype = D
         L.or_box_run.argtypes = [P(A.NPDParams), P(D), VP, D, D, D, C.c_int]
+        L.or_box_run_drivers.argtypes = [P(A.NPDParams), P(D), VP, D, D, C.c_int, C.c_int, P(I32), P(P(D)), C.c_int,
+                                         P(I32), P(P(D))]
         L.or_step3d.argtypes = [P(Model3D), P(D), VP, VP, VP, D, D, C.c_int, C.c_int]
         L.or_par3d.argtypes = [P(Model3D), P(D), D, P(D), C.c_int]
         L.or_columns_run.argtypes = [P(A.NPDParams), P(A.TwoBandParams), C.c_int, P(Column), P(I64),
@@ -280,6 +282,22 @@ def box_run(p, values, dt, nsteps, PAR_stages=None, PAR_const=0.0, t0=0.0):
         v[A.NAME_INDEX[k] if isinstance(k, str) else k] = x
     ps = None if PAR_stages is None else np.ascontiguousarray(PAR_stages, dtype=np.float64)
     lib().or_box_run(C.byref(p), _dp(v), _opt(ps), PAR_const, t0, dt, nsteps)
+    return v
+
+
+def box_run_drivers(p, values, dt, nsteps, PAR_stages=None, PAR_const=0.0, prescribed=None, forcing=None):
+    """prescribed={name: values [3 nsteps + 1]}, forcing={name: rates [3 nsteps]} at the stage times."""
+    v = np.zeros(A.NUM_NAMED)
+    for k, x in values.items():
+        v[A.NAME_INDEX[k] if isinstance(k, str) else k] = x
+    ps = None if PAR_stages is None else np.ascontiguousarray(PAR_stages, dtype=np.float64)
+    pres = [(A.NAME_INDEX[k], np.ascontiguousarray(a, dtype=np.float64)) for k, a in (prescribed or {}).items()]
+    frcs = [(A.NAME_INDEX[k], np.ascontiguousarray(a, dtype=np.float64)) for k, a in (forcing or {}).items()]
+    pn = (C.c_int32 * max(1, len(pres)))(*[q for q, _ in pres])
+    pp = (C.POINTER(C.c_double) * max(1, len(pres)))(*[_dp(a) for _, a in pres])
+    fn = (C.c_int32 * max(1, len(frcs)))(*[q for q, _ in frcs])
+    fp = (C.POINTER(C.c_double) * max(1, len(frcs)))(*[_dp(a) for _, a in frcs])
+    lib().or_box_run_drivers(C.byref(p), _dp(v), _opt(ps), PAR_const, dt, nsteps, len(pres), pn, pp, len(frcs), fn, fp)
     return v
 
 

@@ -221,3 +221,32 @@ def test_mode_i_zero_state_all_configurations(dtype):
         torch.cuda.synchronize()
         for n in names:
             assert torch.count_nonzero(Gs[n]).item() == 0
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-12), ("f32", 1e-3)])
+def test_box_model_forcing_and_prescribed_tracers_match_oracle(precision, tol):
+    # BoxModel(; forcing, prescribed_tracers) (boxmodel.jl:65-87): NPZD with a seasonal temperature
+    # prescribed as T(t) (it drives the Q10 growth) and a nutrient supply forcing N
+    torch = cuda()
+    g = obgc.BoxModelGrid()
+    bgc = obgc.NPZD(g, light_attenuation=obgc.PrescribedPhotosyntheticallyActiveRadiation(40.0))
+    temp = lambda t: 10 + 6 * math.sin(2 * math.pi * t / (20 * 86400))       # noqa: E731
+    supply = lambda t: 2e-6 * (1 + math.cos(2 * math.pi * t / (5 * 86400)))  # noqa: E731
+    n = 16
+    box = obgc.BoxModel(bgc, n_models=n, precision=precision, prescribed_tracers={"T": temp}, forcing={"N": supply})
+    box.set(N=10.0, P=0.1, Z=0.01, T=0.0)
+    dt, nsteps = 1200.0, 300
+    for _ in range(2):                      # two calls: the series continue from the model's clock
+        box.run(dt, nsteps // 2)
+    torch.cuda.synchronize()
+    got = box.state.cpu().numpy()
+    times = np.array([dt * (s + c) for s in range(nsteps + 1) for c in (0, 8 / 15, 2 / 3)])
+    ref = O.box_run_drivers(bgc.params, {"N": 10.0, "P": 0.1, "Z": 0.01, "T": 0.0}, dt, nsteps, PAR_const=40.0,
+                            prescribed={"T": [temp(t) for t in times[:3 * nsteps + 1]]},
+                            forcing={"N": [supply(t) for t in times[:3 * nsteps]]})
+    for m in (0, n - 1):
+        assert rel_err(got[m], ref, 1e-9) < tol
+    assert got[0, A.NAME_INDEX["T"]] == pytest.approx(temp(dt * nsteps), rel=1e-6)
+    # the forcing and the prescribed temperature changed the outcome
+    plain = O.box_run(bgc.params, {"N": 10.0, "P": 0.1, "Z": 0.01, "T": 0.0}, dt, nsteps, PAR_const=40.0)
+    assert abs(plain[A.NAME_INDEX["P"]] - ref[A.NAME_INDEX["P"]]) > 1e-3 * abs(ref[A.NAME_INDEX["P"]])
