@@ -23,7 +23,7 @@ __device__ __forceinline__ void box_prescribe(const BoxDrv& d, T* v, int64_t row
         if ((d.pmask >> r) & 1u) v[r] = T(d.presc[d.pslot[r]][row]);
 }
 
-template <typename T>
+template <typename T, bool DRV>
 __global__ void __launch_bounds__(128) box_kernel(obgc_npd_params p0, const obgc_npd_params* __restrict__ per_model,
                                                   int64_t n, double* __restrict__ state, const double* __restrict__ PAR,
                                                   double par_const, double dt_d, int nsteps, int record_every,
@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(128) box_kernel(obgc_npd_params p0, const obgc
         for (int stg = 0; stg < 3; stg++) {
             const int64_t row = (int64_t)(3 * s + stg) * n + m;
             const T par = PAR ? T(PAR[row]) : T(par_const);
-            if (drv.pmask) box_prescribe(drv, v, row);   // update_state! at the stage time
+            if (DRV && drv.pmask) box_prescribe(drv, v, row);   // update_state! at the stage time
 #pragma unroll
             for (int q = 0; q < OBGC_NUM_NAMED; q++) G[q] = T(0);
             if (v[OBGC_T] != Tlast) {
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(128) box_kernel(obgc_npd_params p0, const obgc
                 Lt = p.q10 ? t_pow(p.Q10, Tlast / T(10)) : T(1);
             }
             npd_tendencies<V_RUNTIME, T>(p, v, par, G, &Lt);
-            if (drv.fmask) {
+            if (DRV && drv.fmask) {
 #pragma unroll
                 for (int r = 0; r < OBGC_NUM_NAMED; r++)
                     if ((drv.fmask >> r) & 1u) G[r] += T(drv.frc[drv.fslot[r]][row]);
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(128) box_kernel(obgc_npd_params p0, const obgc
                 Gm[q] = G[q];
             }
         }
-        if (drv.pmask) box_prescribe(drv, v, (int64_t)(3 * (s + 1)) * n + m);   // update_state! at the step's end
+        if (DRV && drv.pmask) box_prescribe(drv, v, (int64_t)(3 * (s + 1)) * n + m);   // update_state! at the step's end
         if (record && record_every > 0 && (s + 1) % record_every == 0) {
 #pragma unroll
             for (int q = 0; q < OBGC_NUM_NAMED; q++) record[((int64_t)rec * n + m) * OBGC_NUM_NAMED + q] = (double)v[q];
@@ -110,14 +110,21 @@ extern "C" int obgc_box_run_drivers(const obgc_npd_params* p, const obgc_npd_par
     if (n == 0 || nsteps == 0) return OBGC_OK;
     cudaStream_t st = (cudaStream_t)stream;
     const int blocks = (int)((n + 127) / 128);
-    if (precision == OBGC_PREC_F32)
-        box_kernel<float><<<blocks, 128, 0, st>>>(*p, per_model, n, state, d->PAR, d->par_constant, dt, nsteps, record_every,
-                                                  record, drv);
-    else if (precision == OBGC_PREC_F64)
-        box_kernel<double><<<blocks, 128, 0, st>>>(*p, per_model, n, state, d->PAR, d->par_constant, dt, nsteps, record_every,
-                                                   record, drv);
-    else
+    // the driver-free instantiation keeps the plain run free of the per-stage driver checks
+    const bool any = drv.pmask != 0u || drv.fmask != 0u;
+    if (precision == OBGC_PREC_F32) {
+        if (any) box_kernel<float, true><<<blocks, 128, 0, st>>>(*p, per_model, n, state, d->PAR, d->par_constant, dt, nsteps,
+                                                                 record_every, record, drv);
+        else box_kernel<float, false><<<blocks, 128, 0, st>>>(*p, per_model, n, state, d->PAR, d->par_constant, dt, nsteps,
+                                                              record_every, record, drv);
+    } else if (precision == OBGC_PREC_F64) {
+        if (any) box_kernel<double, true><<<blocks, 128, 0, st>>>(*p, per_model, n, state, d->PAR, d->par_constant, dt, nsteps,
+                                                                  record_every, record, drv);
+        else box_kernel<double, false><<<blocks, 128, 0, st>>>(*p, per_model, n, state, d->PAR, d->par_constant, dt, nsteps,
+                                                               record_every, record, drv);
+    } else {
         return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_box_run: precision must be F32 or F64");
+    }
     OBGC_LAUNCHED("box_kernel");
     return OBGC_OK;
 }
