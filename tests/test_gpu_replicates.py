@@ -6,6 +6,8 @@ LOBSTER with CarbonateSystem(2), a CO2 gas-exchange condition on DIC1 (water CO2
 and one on DIC2 (from DIC2/Alk2), and an alkalinity release forcing Alk2 inside a region over a
 window of time.  The replicates DIC2 / Alk2 run as passive tracers taking the DIC / Alk tendency of
 the same stage; a further passive tracer C has no BGC tendency."""
+import math
+
 import numpy as np
 import pytest
 
@@ -164,3 +166,39 @@ def test_zero_negative_tracers_reach_passive_tracers(precision, tol):
     C = got[model.tracer_names.index("C")]
     assert C.min() >= 0.0 and C.max() > 0.0                 # the passive tracer was zeroed where negative
     assert got[model.tracer_names.index("Alk2")].min() < 0  # the excluded one was not
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-11), ("mixed", 1e-5)])
+def test_npzd_passive_tracers_with_diffusivity_match_oracle(precision, tol):
+    # NonhydrostaticModel(; tracers = (:T, :C1, :C2, :C3), closure = ScalarDiffusivity(κ)) with NPZD:
+    # three passive tracers (launches of 2 and 1) advected and diffused with the model's tracers,
+    # one of them forced everywhere at a constant rate
+    torch = cuda()
+    g = obgc.RectilinearGrid((24, 16, 10), (4800.0, 3200.0, 100.0), dtype="f64")
+    bgc = obgc.NPZD(g)
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=12)
+    rate = np.full(g.shape, 1e-6)
+    model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "C1", "C2", "C3"), velocities=(u, v, None),
+                                     precision=precision, closure=obgc.ScalarDiffusivity(κ=0.5),
+                                     forcing={"C2": obgc.Forcing(rate)})
+    rng = np.random.default_rng(12)
+    obgc.set_(model, C1=rng.uniform(1, 2, g.shape), C2=rng.uniform(0.5, 1, g.shape), C3=rng.uniform(3, 4, g.shape))
+    obgc.set_(model, N=7.0, P=0.1, Z=0.05, D=0.1, T=np.broadcast_to(np.linspace(8, 14, g.Nz)[:, None, None], g.shape))
+    s0 = model.state_array().double().cpu().numpy()
+    dt, nsteps = 120.0, 3
+    obgc.time_step(model, dt, nsteps=nsteps)
+    got = model.state_array().double().cpu().numpy()
+    names, src = oracle_layout(model)
+    slot = {n: q for q, n in enumerate(model.tracer_names)}
+    m = O.model3d(bgc.params, g.c_grid(), names, kappa_h=0.5, kappa_z_faces=np.full(g.Nz + 1, 0.5), tendency_of=src,
+                  forcing={slot["C2"]: (rate, -math.inf, math.inf)})
+    ref = np.ascontiguousarray(s0.copy())
+    uo, vo = (x.double().cpu().numpy().ravel().copy() for x in (u, v))
+    O.step3d(m, ref, u=uo, v=vo, t=0.0, dt=dt, nsteps=nsteps)
+    errs = {n: rel_err(got[q], ref[q]) for q, n in enumerate(model.tracer_names)}
+    worst = max(errs, key=errs.get)
+    assert errs[worst] < tol, (worst, errs)
+    # the passive tracers kept their totals (periodic, no-flux walls), C2 gained rate x dt x cells
+    for name, gain in (("C1", 0.0), ("C3", 0.0), ("C2", rate.sum() * dt * nsteps)):
+        q = slot[name]
+        assert got[q].sum() - s0[q].sum() == pytest.approx(gain, abs=(1e-9 if precision == "f64" else 1e-6) * s0[q].sum())
