@@ -202,3 +202,22 @@ def test_npzd_passive_tracers_with_diffusivity_match_oracle(precision, tol):
     for name, gain in (("C1", 0.0), ("C3", 0.0), ("C2", rate.sum() * dt * nsteps)):
         q = slot[name]
         assert got[q].sum() - s0[q].sum() == pytest.approx(gain, abs=(1e-9 if precision == "f64" else 1e-6) * s0[q].sum())
+
+
+def test_oae_release_increases_co2_uptake():
+    # examples/oae_experiment.jl in miniature: two identical carbonate systems, an alkalinity release
+    # into the second; the added alkalinity lowers the surface pCO2, so the second system takes up
+    # more CO2 from the air than the first (its DIC ends higher), while everything else stays equal
+    torch = cuda()
+    g, bgc, model, vel, bcs, forcing = oae_model("f64", with_forcing=False)
+    obgc.set_(model, DIC2=model.tracers["DIC1"], Alk2=model.tracers["Alk1"])
+    z, y, x = g.nodes()
+    mask = ((x[None, None, :] - 2500) ** 2 + (y[None, :, None] - 2000) ** 2 < 1500.0 ** 2) & (z[:, None, None] > -4)
+    release = obgc.Forcing(np.where(mask, 0.2, 0.0) * np.ones(g.shape), start_time=0.0, end_time=1800.0)
+    oae = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S", "C"), velocities=vel + (None,),
+                                   precision="f64", boundary_conditions=bcs, forcing={"Alk2": release})
+    obgc.set_(oae, **{n: model.tracers[n] for n in model.tracer_names})
+    obgc.time_step(oae, 300.0, nsteps=12)
+    t = {n: oae.tracers[n].double().cpu().numpy() for n in oae.tracer_names}
+    assert t["Alk2"].sum() > t["Alk1"].sum()
+    assert t["DIC2"].sum() > t["DIC1"].sum()
