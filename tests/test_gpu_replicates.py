@@ -221,3 +221,15 @@ def test_oae_release_increases_co2_uptake():
     t = {n: oae.tracers[n].double().cpu().numpy() for n in oae.tracer_names}
     assert t["Alk2"].sum() > t["Alk1"].sum()
     assert t["DIC2"].sum() > t["DIC1"].sum()
+
+
+def test_graph_replay_with_passive_launches_is_bit_identical():
+    # obgc_step_graph captures the passive launches, the gas-exchange flux kernels and the clock
+    # advance of the forcing windows with the main launch
+    torch = cuda()
+    runs = []
+    for graph in (False, True):
+        g, bgc, model, vel, bcs, forcing = oae_model("mixed", seed=8)
+        obgc.time_step(model, 300.0, nsteps=5, graph=graph)
+        runs.append(model.state_array().double().cpu().numpy())
+    np.testing.assert_array_equal(runs[0], runs[1])
