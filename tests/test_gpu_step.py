@@ -71,6 +71,20 @@ def test_fused_f32_and_mixed_within_tolerance(precision, tol):
         assert max(errs.values()) < tol, (precision, errs)
 
 
+@pytest.mark.parametrize("topo", [("Bounded", "Periodic", "Bounded"), ("Periodic", "Bounded", "Bounded")])
+def test_f32_full_and_ragged_tiles(topo):
+    # FP32 tiles whose 32 columns lie inside the grid stage their rows with 16-byte copies, the
+    # ragged last tile with 4-byte copies: both against the oracle, with walls in x or in y
+    g, bgc, model, vel = lobster_model(shape=(72, 20, 10), extent=(7200.0, 2000.0, 100.0), precision="f32", topo=topo,
+                                       seed=6)
+    s0 = model.state_array().double().cpu().numpy()
+    obgc.time_step(model, 300.0, nsteps=4)
+    got = model.state_array().double().cpu().numpy()
+    ref = oracle_run(g, bgc, model, vel, s0, 300.0, 4)
+    errs = per_tracer_err(model, got, ref)
+    assert max(errs.values()) < 5e-5, errs
+
+
 def test_bounded_walls_vertical_velocity_and_sinking():
     g, bgc, model, vel = lobster_model(shape=(21, 13, 17), extent=(2100.0, 1300.0, 170.0),
                                        topo=("Bounded", "Bounded", "Bounded"), w=True, carbonates=False, seed=8)
