@@ -291,7 +291,6 @@ int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t 
                 a.n_ext = std::max(0, std::min(gn, OBGC_PIS_NUM_BGC - g0));
                 a.drift = static_cast<const TC*>(m->drift) + (size_t)g0 * (g.Nz + 1);
                 a.drift_mask = (mask >> g0) & ((1u << gn) - 1u);
-                set_vec_rows(a, gn);
                 rc = fes[q]->launch(&a, blocks, st);
             }
             if (rc == OBGC_OK) rc = prof_mark(m, st);

@@ -674,7 +674,6 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
                 x->c_stage = rk3_c(stg);
             }
             for (int t = 0; t < c->NT; t++) { a.in[t] = (const TS*)cur[t]; a.out[t] = (TS*)nxt[t]; }
-            set_vec_rows(a, c->NT);
             launch_terms(c, a, 0, c->NT);
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
             int rc = fe->launch(&a, blocks, st);
@@ -690,7 +689,6 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
                     ap.ext[t] = src < 0 ? nullptr : (const TC*)c->bgc_out[src == OBGC_ALK];
                 }
                 ap.n_ext = n;
-                set_vec_rows(ap, n);
                 ap.neg = c->neg_passive;
                 if (ap.neg.mode != OBGC_NEGATIVES_NONE) {
                     ap.neg.nt = n;

@@ -105,9 +105,6 @@ struct SubstepArgs {
     double c_stage, dt_d;
     TC dt, gamma, zeta;
     int first_stage, write_G;
-    // FP32: every in[t] 16-byte aligned and the strides multiples of 4, so full-width tiles stage
-    // their rows' interiors as 16-byte copies (0: 4-byte copies only)
-    int vec_rows;
 };
 
 template <typename TS, typename TC>
@@ -125,10 +122,6 @@ __device__ __forceinline__ void cp_async_elem(E* smem, const E* gmem) {
 // The same with the shared-space address given directly (constant offsets fold into the instruction).
 __device__ __forceinline__ void cp_async4_at(unsigned smem_addr, const void* gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr), "l"(gmem) : "memory");
-}
-// 16-byte asynchronous copy (both addresses 16-byte aligned; L2 only).
-__device__ __forceinline__ void cp_async16_at(unsigned smem_addr, const void* gmem) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
@@ -190,22 +183,13 @@ template <typename TC, int NT>
 constexpr size_t substep_smem_bytes() {
     // fx, fy face fluxes, the carried vertical flux and its divergence, and every tracer's tile
     return sizeof(TC) * NT * (STEP_BY * (STEP_BX + 1) + (STEP_BY + 1) * STEP_BX + 2 * STEP_BX * STEP_BY +
-                              (STEP_BY + 6) * (STEP_BX + 8));
+                              (STEP_BY + 6) * (STEP_BX + 6));
 }
 
-// A tile row holds a pad column, the three western halo cells, the 32 cells of the block and the
-// three eastern halo cells (and a pad): the block's first cell sits at column TX = 4, so the 32
-// interior cells of a row start on a 16-byte boundary in shared memory and stage as eight 16-byte
-// copies.
 constexpr int HALO = 3;
-constexpr int TX = 4;
-constexpr int TILE_W = TX + STEP_BX + HALO + 1;
+constexpr int TILE_W = STEP_BX + 2 * HALO;
 constexpr int TILE_H = STEP_BY + 2 * HALO;
 constexpr int TILE_LOADS = (TILE_W * TILE_H + STEP_BX * STEP_BY - 1) / (STEP_BX * STEP_BY);
-constexpr int VEC_COPIES = TILE_H * (STEP_BX / 4);     // 16-byte copies of the rows' interiors
-constexpr int HALO_COPIES = TILE_H * 2 * HALO;         // 4-byte copies of the west and east halos
-static_assert(VEC_COPIES + HALO_COPIES <= STEP_BX * STEP_BY, "one copy per thread");
-static_assert(TILE_H * TILE_W == (STEP_BY + 6) * (STEP_BX + 8), "tile size in substep_smem_bytes");
 
 // Face flux from six tile values s[0], s[st], ..., s[5 st] = c[f-3 .. f+2] of a line of N cells,
 // with the Bounded-wall order reduction of face_flux.
@@ -267,16 +251,6 @@ __device__ __forceinline__ TC vertical_flux(const SubstepArgs<TS, TC>& a, const 
     return F;
 }
 
-// Set a.vec_rows for a launch over n slots: FP32 tiles, every slot's array 16-byte aligned and both
-// strides multiples of four elements (then every interior row of a full-width tile starts on a
-// 16-byte boundary at every level).
-template <typename TS, typename TC>
-inline void set_vec_rows(SubstepArgs<TS, TC>& a, int n) {
-    bool ok = sizeof(TS) == 4 && sizeof(TC) == 4 && a.sj % 4 == 0 && a.sk % 4 == 0;
-    for (int t = 0; t < n && ok; t++) ok = (reinterpret_cast<uintptr_t>(a.in[t]) & 15u) == 0;
-    a.vec_rows = ok ? 1 : 0;
-}
-
 // Whether a launch uses any of the optional terms (diffusivity closure, surface fluxes, forcing,
 // the fused negative-tracer modifier, the sediment, replicate tendencies); without them the lean
 // instantiation (EXT = false) runs.
@@ -324,9 +298,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     const bool hdiff = EXT && (a.kh_dx != TC(0) || a.kh_dy != TC(0));
     // previous-stage tendencies staged in shared memory (the generic-drift buffer, when unused)
     const bool gm_smem = !any_generic && !a.first_stage;
-    // shared-space address of the tiles, and of this thread's first tile element
-    const unsigned tiles_s0 = (unsigned)__cvta_generic_to_shared(tiles);
-    const unsigned tiles_s = tiles_s0 + 4u * (unsigned)tid;
+    // shared-space address of this thread's first tile element
+    const unsigned tiles_s = (unsigned)__cvta_generic_to_shared(tiles) + 4u * (unsigned)tid;
 
     // forcings switched on at this stage's time
     bool frc_on[MAX_FRC];
@@ -370,41 +343,14 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                                                                                  : PAR0;
 
         // horizontal offsets of the tile elements this thread stages (the same for every level
-        // and tracer of the work item): a tile whose 32 columns lie inside the grid copies each
-        // row's interior in 16-byte pieces (threads below VEC_COPIES) and its x halos in 4-byte
-        // pieces (the next HALO_COPIES threads); other tiles copy every element in 4 bytes
-        const bool vec_tile = sizeof(TS) == 4 && sizeof(TC) == 4 && a.vec_rows && i0 + STEP_BX <= a.Nx;
+        // and tracer of the work item)
         int64_t toff[TILE_LOADS];
-        unsigned vdst = 0;          // tile element of this thread's copy (vector form)
-        int vkind = 0;              // 0 none, 1 16-byte interior copy, 2 4-byte halo copy
-        if (vec_tile) {
-            int r, c;
-            if (tid < VEC_COPIES) {
-                r = tid / (STEP_BX / 4);
-                c = TX + 4 * (tid - r * (STEP_BX / 4));
-                vkind = 1;
-            } else if (tid < VEC_COPIES + HALO_COPIES) {
-                const int h = tid - VEC_COPIES;
-                r = h / (2 * HALO);
-                const int m = h - r * (2 * HALO);
-                c = m < HALO ? TX - HALO + m : TX + STEP_BX + (m - HALO);
-                vkind = 2;
-            } else {
-                r = 0;
-                c = TX;
-            }
-            vdst = (unsigned)(r * TILE_W + c);
-            toff[0] = wrap_or_clamp(i0 - TX + c, a.Nx, periodic_x) + (int64_t)wrap_or_clamp(j0 - HALO + r, a.Ny, periodic_y) * a.sj;
 #pragma unroll
-            for (int q = 1; q < TILE_LOADS; q++) toff[q] = 0;
-        } else {
-#pragma unroll
-            for (int q = 0; q < TILE_LOADS; q++) {
-                const int e = min(tid + q * NTH, TILE_H * TILE_W - 1);
-                const int r = e / TILE_W, c = e - r * TILE_W;
-                toff[q] = wrap_or_clamp(i0 - TX + c, a.Nx, periodic_x) +
-                          (int64_t)wrap_or_clamp(j0 - HALO + r, a.Ny, periodic_y) * a.sj;
-            }
+        for (int q = 0; q < TILE_LOADS; q++) {
+            const int e = min(tid + q * NTH, TILE_H * TILE_W - 1);
+            const int r = e / TILE_W, c = e - r * TILE_W;
+            toff[q] = wrap_or_clamp(i0 - HALO + c, a.Nx, periodic_x) +
+                      (int64_t)wrap_or_clamp(j0 - HALO + r, a.Ny, periodic_y) * a.sj;
         }
 
         // chlorophyll integral of the cells above the segment
@@ -451,21 +397,13 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             for (int t = 0; t < NT; t++) {
                 const TS* __restrict__ base = a.in[t] + kofs;
                 TC* tl = tiles + t * TILE_SZ;
-                if (vec_tile) {
-                    if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) {
-                        const unsigned dst = tiles_s0 + 4u * (unsigned)(t * TILE_SZ) + 4u * vdst;
-                        if (vkind == 1) cp_async16_at(dst, base + toff[0]);
-                        else if (vkind == 2) cp_async4_at(dst, base + toff[0]);
-                    }
-                } else {
 #pragma unroll
-                    for (int q = 0; q < TILE_LOADS; q++)
-                        if (q < TILE_LOADS - 1 || tid + q * NTH < TILE_SZ) {
-                            if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4)
-                                cp_async4_at(tiles_s + 4u * (unsigned)(t * TILE_SZ + q * NTH), base + toff[q]);
-                            else tl[tid + q * NTH] = ld<TS, TC>(base, toff[q]);
-                        }
-                }
+                for (int q = 0; q < TILE_LOADS; q++)
+                    if (q < TILE_LOADS - 1 || tid + q * NTH < TILE_SZ) {
+                        if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4)
+                            cp_async4_at(tiles_s + 4u * (unsigned)(t * TILE_SZ + q * NTH), base + toff[q]);
+                        else tl[tid + q * NTH] = ld<TS, TC>(base, toff[q]);
+                    }
                 if (gm_smem) cp_async_elem<TC>(vdv + t * NTH + tid, a.G[t] + idx);
             }
             if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) cp_async_wait_all();
@@ -485,8 +423,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 #pragma unroll 1
             for (int t = 0; t < (row_faces ? NT : 0); t++) {
                 const TC* tl = tiles + t * TILE_SZ;
-                const TC* xs = tl + (ty + HALO) * TILE_W + tx + (TX - HALO);   // c[i-3 .. i+2] along x
-                const TC* ys = tl + ty * TILE_W + tx + TX;                      // c[j-3 .. j+2] along y
+                const TC* xs = tl + (ty + HALO) * TILE_W + tx;   // c[i-3 .. i+2] along x
+                const TC* ys = tl + ty * TILE_W + tx + HALO;     // c[j-3 .. j+2] along y
                 TC Fx, Fy;
 #ifdef __CUDA_ARCH__
                 if constexpr (sizeof(TC) == 4) {
@@ -525,8 +463,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 #pragma unroll 1
                 for (int t = 0; t < NT; t++) {
                     const TC* tl = tiles + t * TILE_SZ;
-                    if (xok) fx[t][ty][tx] += tile_diff_flux<TC>(tl + (ty + HALO) * TILE_W + tx + (TX - HALO), 1, periodic_x, i, a.Nx, a.kh_dx);
-                    if (yok) fy[t][ty][tx] += tile_diff_flux<TC>(tl + ty * TILE_W + tx + TX, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
+                    if (xok) fx[t][ty][tx] += tile_diff_flux<TC>(tl + (ty + HALO) * TILE_W + tx, 1, periodic_x, i, a.Nx, a.kh_dx);
+                    if (yok) fy[t][ty][tx] += tile_diff_flux<TC>(tl + ty * TILE_W + tx + HALO, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
                 }
             }
             // the tile's east (8 per tracer) and north (32 per tracer) edge faces, spread over
@@ -541,9 +479,9 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     TC Fe = TC(0);
                     if (!a.flat_x && jr < a.Ny && f <= a.Nx) {
                         const int64_t rb = (int64_t)jr * a.sj + kofs;
-                        Fe = tile_face_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX + (TX - HALO), 1, periodic_x, f, a.Nx,
+                        Fe = tile_face_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx,
                                                 face_velocity<TS, TC>(a.u, rb, 1, a.Nx, periodic_x, f));
-                        if (hdiff) Fe += tile_diff_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX + (TX - HALO), 1, periodic_x, f, a.Nx, a.kh_dx);
+                        if (hdiff) Fe += tile_diff_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx, a.kh_dx);
                     }
                     fx[t][r][STEP_BX] = Fe;
                 } else {
@@ -551,9 +489,9 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     TC Fe = TC(0);
                     if (!a.flat_y && ix < a.Nx && f <= a.Ny) {
                         const int64_t cb2 = ix + kofs;
-                        Fe = tile_face_flux<TC>(tl + STEP_BY * TILE_W + cc + TX, TILE_W, periodic_y, f, a.Ny,
+                        Fe = tile_face_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny,
                                                 face_velocity<TS, TC>(a.v, cb2, a.sj, a.Ny, periodic_y, f));
-                        if (hdiff) Fe += tile_diff_flux<TC>(tl + STEP_BY * TILE_W + cc + TX, TILE_W, periodic_y, f, a.Ny, a.kh_dy);
+                        if (hdiff) Fe += tile_diff_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny, a.kh_dy);
                     }
                     fy[t][STEP_BY][cc] = Fe;
                 }
@@ -562,7 +500,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             // before the barrier that lets the next level's staging overwrite the tiles
             TC c[NT];
 #pragma unroll
-            for (int t = 0; t < NT; t++) c[t] = tiles[t * TILE_SZ + (ty + HALO) * TILE_W + tx + TX];
+            for (int t = 0; t < NT; t++) c[t] = tiles[t * TILE_SZ + (ty + HALO) * TILE_W + tx + HALO];
             __syncthreads();
             if (!row_cells) continue;   // no cell on this row: nothing below reads its registers
 

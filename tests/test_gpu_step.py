@@ -73,8 +73,7 @@ def test_fused_f32_and_mixed_within_tolerance(precision, tol):
 
 @pytest.mark.parametrize("topo", [("Bounded", "Periodic", "Bounded"), ("Periodic", "Bounded", "Bounded")])
 def test_f32_full_and_ragged_tiles(topo):
-    # FP32 tiles whose 32 columns lie inside the grid stage their rows with 16-byte copies, the
-    # ragged last tile with 4-byte copies: both against the oracle, with walls in x or in y
+    # FP32 on a grid of two full-width tiles and a ragged one in x, with walls in x or in y
     g, bgc, model, vel = lobster_model(shape=(72, 20, 10), extent=(7200.0, 2000.0, 100.0), precision="f32", topo=topo,
                                        seed=6)
     s0 = model.state_array().double().cpu().numpy()
