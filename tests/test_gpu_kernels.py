@@ -116,7 +116,7 @@ def test_carbon_batch_fp64():
         got = cc(dev(DIC), dev(T), dev(S), Alk=dev(Alk), output=out).cpu().numpy()
         ref = O.carbon_chemistry_batch(O.carbon_options(output=code), DIC, Alk, T, S)
         if out == "pHf":
-            assert np.max(np.abs(got - ref)) < 1e-10        # spec bar: 1e-8
+            assert np.max(np.abs(got - ref)) < 1e-10        # the pH statement of the path: 1e-8
         else:
             assert rel_err(got, ref) < 1e-10
 
