@@ -581,6 +581,13 @@ int obgc_set_forcing(obgc_ctx* ctx, int32_t tracer, const void* rate, double t_s
  * flux), added to the advective face fluxes (VerticalScalarDiffusivity: kappa_h = 0;
  * HorizontalScalarDiffusivity: kappa_z = 0).  Zero everywhere switches it off. */
 int obgc_set_diffusivity(obgc_ctx* ctx, double kappa_h, double kappa_z, const double* kappa_z_faces);
+/* The vertical part's time discretization: OBGC_EXPLICIT (default) or OBGC_VERTICALLY_IMPLICIT
+ * (VerticalScalarDiffusivity(VerticallyImplicitTimeDiscretization(), κ)): after each RK3 stage's
+ * explicit update U* (advection, BGC, horizontal diffusion), every column of every tracer solves
+ * (I - dt_s d/dz kappa d/dz) U = U* with dt_s = (gamma + zeta) dt and no flux through the bottom
+ * and top faces, then the negative-tracer modifier runs. */
+enum obgc_time_discretization { OBGC_EXPLICIT = 0, OBGC_VERTICALLY_IMPLICIT = 1 };
+int obgc_set_vertical_time_discretization(obgc_ctx* ctx, int32_t discretization);
 /* sediment = InstantRemineralisationSediment(grid; sinking_tracers, remineralisation_reciever,
  * burial_efficiency_constant1 = a (0.013), _constant2 = b (0.53), _half_saturation = k (7/6.56))
  * (src/Models/Sediments/instant_remineralisation.jl): per RK3 stage the sinking fluxes of the

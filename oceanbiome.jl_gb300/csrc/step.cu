@@ -42,6 +42,60 @@ void drift_profile(double w0, int open_bottom, int Nz, double* w);
 __global__ void set_time_kernel(double* t, double v) { *t = v; }
 __global__ void advance_time_kernel(double* t, double dt) { *t += dt; }
 
+// Thomas factors of the vertically implicit diffusion for the three RK3 stages (the same in every
+// column): out[(2 st) Nz + k] = c'_k and out[(2 st + 1) Nz + k] = 1 / pivot_k of
+// (I - dt_s d/dz kappa d/dz), dt_s = (gamma_st + zeta_st) dt; lo_k = -r kappa_k (face below k,
+// zero at the bottom wall), up_k = -r kappa_(k+1) (zero at the top wall), r = dt_s / dz^2.
+__global__ void thomas_factors_kernel(const double* __restrict__ kappa_faces, int Nz, double inv_dz2, double dt,
+                                      double* __restrict__ out) {
+    const int st = threadIdx.x;
+    if (st >= 3) return;
+    const double r = (rk3_gamma(st) + rk3_zeta(st)) * dt * inv_dz2;
+    double cprev = 0.0;
+    for (int k = 0; k < Nz; k++) {
+        const double lo = k > 0 ? -r * kappa_faces[k] : 0.0;
+        const double up = k < Nz - 1 ? -r * kappa_faces[k + 1] : 0.0;
+        const double den = (1.0 - lo - up) - lo * cprev;
+        cprev = up / den;
+        out[(2 * st) * Nz + k] = cprev;
+        out[(2 * st + 1) * Nz + k] = 1.0 / den;
+    }
+}
+
+template <typename TS>
+struct ImplicitFields {
+    TS* f[MAX_NT];
+};
+
+// One thread per (column, tracer): forward sweep d_k = (x_k - lo_k d_(k-1)) / pivot_k in place,
+// then x_k = d_k - c'_k x_(k+1).  Threads of a warp take neighbouring columns, so every level's
+// loads and stores are coalesced.
+template <typename TS>
+__global__ void implicit_vertical_kernel(const __grid_constant__ ImplicitFields<TS> F, int nslots, int Nx, int Ny, int Nz,
+                                         int64_t sj, int64_t sk, const double* __restrict__ kappa_faces, double inv_dz2,
+                                         double dt, int st, const double* __restrict__ factors) {
+    const int64_t NN = (int64_t)Nx * Ny;
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= NN * nslots) return;
+    const int t = (int)(g / NN);
+    const int64_t c = g - (int64_t)t * NN;
+    TS* x = F.f[t] + (c % Nx) + (c / Nx) * sj;
+    const double r = (rk3_gamma(st) + rk3_zeta(st)) * dt * inv_dz2;
+    const double* cp = factors + (2 * st) * Nz;
+    const double* ip = factors + (2 * st + 1) * Nz;
+    double d = 0.0;
+    for (int k = 0; k < Nz; k++) {
+        const double lo = k > 0 ? -r * kappa_faces[k] : 0.0;
+        d = ((double)x[k * sk] - lo * d) * ip[k];
+        x[k * sk] = TS(d);
+    }
+    double xn = d;
+    for (int k = Nz - 2; k >= 0; k--) {
+        xn = (double)x[k * sk] - cp[k] * xn;
+        x[k * sk] = TS(xn);
+    }
+}
+
 template <typename TS>
 __global__ void copy_interior_kernel(const TS* __restrict__ src, TS* __restrict__ dst, int Nx, int Ny, int Nz,
                                      int64_t sj, int64_t sk) {
@@ -154,6 +208,11 @@ struct obgc_ctx {
     // compute precision), or nullptr
     double kappa_h = 0.0;
     void* kzz = nullptr;
+    // VerticallyImplicitTimeDiscretization: kappa at the faces (FP64, device, nullptr: no vertical
+    // diffusivity) and the Thomas factors of the three stages
+    bool vimplicit = false;
+    double* kzf = nullptr;
+    double* thomas = nullptr;
     // InstantRemineralisation sediment: receiver slot (-1: none), sinking slots, parameters, and the
     // storage (state precision) and previous-stage burial (compute precision) of every column
     int sed_recv = -1;
@@ -198,6 +257,8 @@ static int ctx_free(obgc_ctx* c) {
     for (int q = 0; q < 2; q++)
         if (c->bgc_out[q]) cudaFree(c->bgc_out[q]);
     if (c->kzz) cudaFree(c->kzz);
+    if (c->kzf) cudaFree(c->kzf);
+    if (c->thomas) cudaFree(c->thomas);
     if (c->sed_storage) cudaFree(c->sed_storage);
     if (c->sed_G) cudaFree(c->sed_G);
     if (c->ev_begin) cudaEventDestroy(c->ev_begin);
@@ -437,7 +498,14 @@ extern "C" int obgc_set_diffusivity(obgc_ctx* c, double kappa_h, double kappa_z,
         any = any || kf > 0;
     }
     if (c->kzz) { cudaFree(c->kzz); c->kzz = nullptr; }
+    if (c->kzf) { cudaFree(c->kzf); c->kzf = nullptr; }
     if (any) {
+        // the faces' kappa for the implicit form (the explicit form below carries kappa / dz^2)
+        std::vector<double> kf(Nz + 1, 0.0);
+        for (int f = 1; f < Nz; f++) kf[f] = kappa_z_faces ? kappa_z_faces[f] : kappa_z;
+        OBGC_CUDA(cudaMalloc(&c->kzf, sizeof(double) * (Nz + 1)));
+        OBGC_CUDA(cudaMemcpy(c->kzf, kf.data(), sizeof(double) * (Nz + 1), cudaMemcpyHostToDevice));
+        if (!c->thomas) OBGC_CUDA(cudaMalloc(&c->thomas, sizeof(double) * 6 * Nz));
         OBGC_CUDA(cudaMalloc(&c->kzz, c->tc * (Nz + 1)));
         if (c->tc == 4) {
             std::vector<float> kf(k.begin(), k.end());
@@ -447,6 +515,14 @@ extern "C" int obgc_set_diffusivity(obgc_ctx* c, double kappa_h, double kappa_z,
         }
     }
     c->kappa_h = kappa_h;
+    c->bind_version++;
+    return OBGC_OK;
+}
+
+extern "C" int obgc_set_vertical_time_discretization(obgc_ctx* c, int32_t discretization) {
+    if (!c || (discretization != OBGC_EXPLICIT && discretization != OBGC_VERTICALLY_IMPLICIT))
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_vertical_time_discretization: bad argument");
+    c->vimplicit = discretization == OBGC_VERTICALLY_IMPLICIT;
     c->bind_version++;
     return OBGC_OK;
 }
@@ -579,7 +655,7 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.neg = c->neg;        // the modifier after every substep, fused into the substep's update
     a.kh_dx = g.topology_x == OBGC_FLAT ? TC(0) : TC(c->kappa_h * g.Nx / g.Lx);
     a.kh_dy = g.topology_y == OBGC_FLAT ? TC(0) : TC(c->kappa_h * g.Ny / g.Ly);
-    a.kzz = (const TC*)c->kzz;
+    a.kzz = c->vimplicit ? nullptr : (const TC*)c->kzz;   // the implicit form leaves the vertical part out
     a.sed_recv1 = c->sed_recv >= 0 ? c->sed_recv + 1 : 0;
     a.sed_sink_mask = c->sed_mask;
     a.sed_a = TC(c->sed_a); a.sed_b = TC(c->sed_b); a.sed_k = TC(c->sed_k);
@@ -644,6 +720,17 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
     void* nxt[MAX_NT];
     for (int t = 0; t < NS; t++) { cur[t] = c->user[t]; nxt[t] = c->scratch[t]; }
     const bool clock = needs_clock(c);
+    // VerticallyImplicitTimeDiscretization: the Thomas factors of this dt, then after every stage an
+    // implicit solve of every column and slot, followed by the negative-tracer modifier (which the
+    // substep then must not fuse: it acts on the diffused state)
+    const obgc_grid& gz = c->desc.grid;
+    const bool impl = c->vimplicit && c->kzf;
+    const double inv_dz2 = (double)gz.Nz * gz.Nz / (gz.Lz * gz.Lz);
+    if (impl) {
+        a.neg.mode = OBGC_NEGATIVES_NONE;
+        thomas_factors_kernel<<<1, 32, 0, st>>>(c->kzf, gz.Nz, inv_dz2, dt, c->thomas);
+        OBGC_LAUNCHED("thomas_factors_kernel");
+    }
     int blocks = c->blocks < a.n_items ? c->blocks : a.n_items;
     size_t ev = 0;
     const obgc_grid& grid = c->desc.grid;
@@ -690,6 +777,7 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
                 }
                 ap.n_ext = n;
                 ap.neg = c->neg_passive;
+                if (impl) ap.neg.mode = OBGC_NEGATIVES_NONE;
                 if (ap.neg.mode != OBGC_NEGATIVES_NONE) {
                     ap.neg.nt = n;
                     ap.neg.zero_skip = (c->neg_passive.zero_skip >> (b - c->NT)) & ((1u << n) - 1u);
@@ -698,6 +786,20 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
                 const int pb = c->pblocks[n] < ap.n_items ? c->pblocks[n] : ap.n_items;
                 rc = pe[n]->launch(&ap, pb, st);
                 if (rc != OBGC_OK) return rc;
+            }
+            if (impl) {
+                ImplicitFields<TS> F;
+                for (int t = 0; t < NS; t++) F.f[t] = (TS*)nxt[t];
+                const int64_t nthr = (int64_t)gz.Nx * gz.Ny * NS;
+                implicit_vertical_kernel<TS><<<(unsigned)((nthr + 127) / 128), 128, 0, st>>>(
+                    F, NS, gz.Nx, gz.Ny, gz.Nz, gz.stride_j, gz.stride_k, c->kzf, inv_dz2, dt, stg, c->thomas);
+                OBGC_LAUNCHED("implicit_vertical_kernel");
+                if (c->neg.mode != OBGC_NEGATIVES_NONE) {
+                    rc = launch_negatives(c->neg, sizeof(TS), nxt, grid, st);
+                    if (rc == OBGC_OK && c->neg_passive.mode != OBGC_NEGATIVES_NONE)
+                        rc = launch_negatives(c->neg_passive, sizeof(TS), nxt + c->NT, grid, st);
+                    if (rc != OBGC_OK) return rc;
+                }
             }
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
             for (int t = 0; t < NS; t++) { void* tmp = cur[t]; cur[t] = nxt[t]; nxt[t] = tmp; }
@@ -732,7 +834,9 @@ static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     const int neg = c->neg.mode == OBGC_NEGATIVES_NONE ? 0 : c->neg_passive.mode != OBGC_NEGATIVES_NONE ? 2 : 1;
     int gases = 0;
     for (const auto& gc : c->gas) gases += gc.on ? 1 : 0;
-    return (int64_t)nsteps * (3 * (1 + c->nchunk + gases) + (clock ? 1 : 0)) + (nsteps % 2 ? c->NT + c->NP : 0) + 1 + neg;
+    const bool impl = c->vimplicit && c->kzf;
+    const int per_stage = 1 + c->nchunk + gases + (impl ? 1 + neg : 0);
+    return (int64_t)nsteps * (3 * per_stage + (clock ? 1 : 0)) + (nsteps % 2 ? c->NT + c->NP : 0) + 1 + neg + (impl ? 1 : 0);
 }
 
 extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {

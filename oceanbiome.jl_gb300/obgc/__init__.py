@@ -18,8 +18,9 @@ from .carbon import CarbonChemistry
 from .grid import BoxModelGrid, RectilinearGrid
 from .light import (MultiBandPhotosyntheticallyActiveRadiation, PrescribedPhotosyntheticallyActiveRadiation,
                     TwoBandPhotosyntheticallyActiveRadiation, default_surface_PAR, euphotic_depth)
-from .model3d import (Clock, HorizontalScalarDiffusivity, NonhydrostaticModel, ScalarDiffusivity,
-                      VerticalScalarDiffusivity, compute_tendencies, set_, time_step, update_biogeochemical_state)
+from .model3d import (Clock, ExplicitTimeDiscretization, HorizontalScalarDiffusivity, NonhydrostaticModel,
+                      ScalarDiffusivity, VerticallyImplicitTimeDiscretization, VerticalScalarDiffusivity,
+                      compute_tendencies, set_, time_step, update_biogeochemical_state)
 from .negatives import ScaleNegativeTracers, ZeroNegativeTracers
 from .sediments import InstantRemineralisationSediment
 from .models import (LOBSTER, NPZD, CarbonateSystem, Detritus, NitrateAmmonia, NitrateAmmoniaIron, Nutrient,

@@ -28,6 +28,7 @@ ASCII_NAMES = ["NO3", "NH4", "Fe", "N", "P", "Z", "T", "sPOM", "bPOM", "DOM", "s
 NUM_NAMED = len(TRACER_NAMES)
 MAX_PASSIVE = 8
 MAX_GAS_CONDITIONS = 4
+EXPLICIT, VERTICALLY_IMPLICIT = 0, 1
 MAX_FORCINGS = 4
 
 
@@ -317,6 +318,7 @@ def load():
     _sig(lib, "obgc_set_gas_exchange", C.c_int, VP, I32, P(GasExchange))
     _sig(lib, "obgc_set_gas_exchange_on", C.c_int, VP, I32, P(GasExchange), I32, I32)
     _sig(lib, "obgc_set_forcing", C.c_int, VP, I32, VP, D, D)
+    _sig(lib, "obgc_set_vertical_time_discretization", C.c_int, VP, I32)
     _sig(lib, "obgc_set_diffusivity", C.c_int, VP, D, D, P(D))
     _sig(lib, "obgc_set_sediment", C.c_int, VP, I32, P(I32), I32, D, D, D)
     _sig(lib, "obgc_sediment_storage", C.c_int, VP, P(D), P(D))
@@ -394,7 +396,7 @@ def load():
 EXPORTED = [
     "obgc_abi_version", "obgc_last_error_message", "obgc_kernel_launch_count", "obgc_fp64_fma_peak",
     "obgc_gas_exchange_defaults", "obgc_gas_exchange_flux", "obgc_gas_exchange_point", "obgc_set_gas_exchange",
-    "obgc_set_gas_exchange_on", "obgc_set_forcing",
+    "obgc_set_gas_exchange_on", "obgc_set_forcing", "obgc_set_vertical_time_discretization",
     "obgc_set_diffusivity", "obgc_set_sediment", "obgc_sediment_storage",
     "obgc_npd_preset", "obgc_npd_required_tracers", "obgc_npd_drift_velocity",
     "obgc_npd_eval_point", "obgc_npd_tendencies", "obgc_twoband_par", "obgc_multiband_par",

@@ -22,12 +22,25 @@ class Clock:
         self.iteration = iteration
 
 
+class ExplicitTimeDiscretization:
+    """Oceananigans' default: the diffusive fluxes enter each RK3 stage's tendency."""
+
+
+class VerticallyImplicitTimeDiscretization:
+    """The vertical part is solved implicitly after each RK3 stage's explicit update."""
+
+
 class ScalarDiffusivity:
-    """ScalarDiffusivity(κ = ...) with explicit time stepping (Oceananigans' default): κ a number, or
-    f(z) sampled at the cell faces for the vertical part.  `horizontal` / `vertical` select
+    """ScalarDiffusivity([time_discretization]; κ = ...): κ a number, or f(z) sampled at the cell
+    faces for the vertical part; the time discretization is ExplicitTimeDiscretization() (default)
+    or VerticallyImplicitTimeDiscretization().  `horizontal` / `vertical` select
     HorizontalScalarDiffusivity / VerticalScalarDiffusivity."""
 
-    def __init__(self, κ=0.0, ν=None, horizontal=True, vertical=True, kappa=None):
+    def __init__(self, time_discretization=None, κ=0.0, ν=None, horizontal=True, vertical=True, kappa=None):
+        if time_discretization is not None and not isinstance(
+                time_discretization, (ExplicitTimeDiscretization, VerticallyImplicitTimeDiscretization)):
+            κ, time_discretization = time_discretization, None      # ScalarDiffusivity(κ) given positionally
+        self.time_discretization = time_discretization or ExplicitTimeDiscretization()
         self.kappa = κ if kappa is None else kappa
         self.horizontal, self.vertical = horizontal, vertical
 
@@ -38,12 +51,12 @@ class ScalarDiffusivity:
         return np.array([float(k(z)) for z in zf]) if callable(k) else np.full(grid.Nz + 1, float(k))
 
 
-def VerticalScalarDiffusivity(κ=0.0, ν=None):
-    return ScalarDiffusivity(κ, horizontal=False)
+def VerticalScalarDiffusivity(time_discretization=None, κ=0.0, ν=None):
+    return ScalarDiffusivity(time_discretization, κ=κ, horizontal=False)
 
 
 def HorizontalScalarDiffusivity(κ=0.0, ν=None):
-    return ScalarDiffusivity(κ, vertical=False)
+    return ScalarDiffusivity(κ=κ, vertical=False)
 
 
 class NonhydrostaticModel:
@@ -152,6 +165,9 @@ class NonhydrostaticModel:
             kz = closure.face_values(grid) if closure.vertical else None
             arr = None if kz is None else (C.c_double * len(kz))(*kz)
             A.check(lib.obgc_set_diffusivity(ctx, kh, 0.0, arr), "obgc_set_diffusivity")
+            if isinstance(closure.time_discretization, VerticallyImplicitTimeDiscretization):
+                A.check(lib.obgc_set_vertical_time_discretization(ctx, A.VERTICALLY_IMPLICIT),
+                        "obgc_set_vertical_time_discretization")
 
     def code(self, name):
         """The C ABI tracer code of a tracer of this model (a named slot or OBGC_PASSIVE(p))."""

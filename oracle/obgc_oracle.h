@@ -94,6 +94,8 @@ typedef struct or_model3d {
     double kappa_h;                  /* ScalarDiffusivity: horizontal diffusivity (m2/s)         */
     const double* kappa_z_faces;     /* vertical diffusivity at the Nz + 1 faces, or NULL; the
                                       * bottom and top faces are walls (no flux)                  */
+    int32_t vertical_implicit;       /* VerticallyImplicitTimeDiscretization: the vertical part is
+                                      * solved implicitly after each stage's explicit update      */
     int32_t sed_receiver;            /* InstantRemineralisation: receiver tracer slot, or -1    */
     uint32_t sed_sink_mask;          /* sinking tracer slots                                     */
     double sed_a, sed_b, sed_k;      /* burial efficiency constants and half saturation          */

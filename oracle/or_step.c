@@ -172,6 +172,8 @@ static void or_negatives3d(const or_model3d* m, double* state, long N, int ng, c
     }
 }
 
+static void implicit_diffusion(int Nz, double dz, const double* kf, double dts, double* x, double* cp, double* dp);
+
 void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,
                const double* w, double t, double dt, int nsteps, int nthreads) {
     const obgc_grid* g = &m->grid;
@@ -276,7 +278,7 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
                             const double cp = (py || j < Ny - 1) ? cq[base + (long)((j + 1) % Ny) * Nx] : cq[base + (long)j * Nx];
                             d += m->kappa_h * (cp - 2 * cq[base + (long)j * Nx] + cm) / (dy * dy);
                         }
-                        if (m->kappa_z_faces) {
+                        if (m->kappa_z_faces && !m->vertical_implicit) {
                             const double cc = cq[c];
                             const double up = k + 1 < Nz ? m->kappa_z_faces[k + 1] * (cq[c + NN] - cc) : 0.0;
                             const double dn = k > 0 ? m->kappa_z_faces[k] * (cc - cq[c - NN]) : 0.0;
@@ -339,6 +341,18 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
             for (long x = 0; x < (long)nt * N; x++) {
                 if (st == 0) state[x] += dt * g * G[x];
                 else state[x] += dt * (g * G[x] + z * Gm[x]);
+            }
+            /* VerticallyImplicitTimeDiscretization: (I - dt_s d/dz kappa d/dz) U = U* per column and
+             * tracer with dt_s = (gamma + zeta) dt, walls at the bottom and top */
+            if (m->kappa_z_faces && m->vertical_implicit) {
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+                for (long qc = 0; qc < (long)nt * NN; qc++) {
+                    const long q = qc / NN, col = qc % NN;
+                    double x[Nz], cp[Nz], dp[Nz];
+                    for (int k = 0; k < Nz; k++) x[k] = state[q * N + (long)k * NN + col];
+                    implicit_diffusion(Nz, dz, m->kappa_z_faces, (g + z) * dt, x, cp, dp);
+                    for (int k = 0; k < Nz; k++) state[q * N + (long)k * NN + col] = x[k];
+                }
             }
             if (m->negatives) or_negatives3d(m, state, N, ng, gn, gslot, gfac, nthreads);
             double* tmp = G; G = Gm; Gm = tmp;

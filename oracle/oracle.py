@@ -28,7 +28,8 @@ class Model3D(C.Structure):
                 ("zero_exclude_mask", C.c_int32), ("invalid_fill_value", C.c_double),
                 ("gas", C.POINTER(A.GasExchange) * 4), ("gas_target", C.c_int32 * 4), ("gas_dic", C.c_int32 * 4),
                 ("gas_alk", C.c_int32 * 4), ("kappa_h", C.c_double),
-                ("kappa_z_faces", C.POINTER(C.c_double)), ("sed_receiver", C.c_int32), ("sed_sink_mask", C.c_uint32),
+                ("kappa_z_faces", C.POINTER(C.c_double)), ("vertical_implicit", C.c_int32),
+                ("sed_receiver", C.c_int32), ("sed_sink_mask", C.c_uint32),
                 ("sed_a", C.c_double), ("sed_b", C.c_double), ("sed_k", C.c_double),
                 ("sed_storage", C.POINTER(C.c_double)), ("tendency_of", C.c_int32 * 32),
                 ("forcing", C.POINTER(C.c_double) * 32), ("forcing_t0", C.c_double * 32), ("forcing_t1", C.c_double * 32)]
@@ -303,7 +304,7 @@ def box_run_drivers(p, values, dt, nsteps, PAR_stages=None, PAR_const=0.0, presc
 
 def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_value=0.0, advection=1,
             negatives=NEG_NONE, zero_exclude=(), invalid_fill_value=float("nan"), gas_exchange=(), kappa_h=0.0,
-            kappa_z_faces=None, sediment=None, tendency_of=None, forcing=None):
+            kappa_z_faces=None, sediment=None, tendency_of=None, forcing=None, vertical_implicit=False):
     """gas_exchange: top boundary conditions, each an A.GasExchange struct (CO2 on DIC with DIC and
     Alk, O2 on O2) or a tuple (struct, target, dic, alk) of tracer names or slots (None for passive
     entries of `names`); kappa_h, kappa_z_faces[Nz + 1]: ScalarDiffusivity (explicit).
@@ -344,6 +345,7 @@ def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_
         m._storage = storage
         m.sed_storage = storage.ctypes.data_as(C.POINTER(C.c_double))
     m.kappa_h = kappa_h
+    m.vertical_implicit = int(bool(vertical_implicit))
     if kappa_z_faces is not None:
         m._kz = np.ascontiguousarray(kappa_z_faces, dtype=np.float64)
         m.kappa_z_faces = m._kz.ctypes.data_as(C.POINTER(C.c_double))

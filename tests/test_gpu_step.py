@@ -85,6 +85,38 @@ def test_f32_full_and_ragged_tiles(topo):
     assert max(errs.values()) < 5e-5, errs
 
 
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-11), ("mixed", 1e-5)])
+def test_vertically_implicit_diffusivity_matches_oracle(precision, tol):
+    # VerticalScalarDiffusivity(VerticallyImplicitTimeDiscretization(), κ = κ(z)) with a 0.5 m2/s
+    # mixed layer over 10 m cells at dt = 600 s (dt κ / dz^2 = 3: far beyond an explicit step), and
+    # scale_negatives = true, which then runs after the implicit solve of every stage
+    torch = cuda()
+    g = obgc.RectilinearGrid((40, 16, 12), (8000.0, 3200.0, 120.0), dtype="f32" if precision == "f32" else "f64")
+    bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem(), scale_negatives=True)
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.05, seed=3)
+    kz = lambda z: 0.5 * (1 + math.tanh((z + 50.0) / 10.0)) / 2 + 1e-4   # noqa: E731
+    model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None),
+                                     precision=precision,
+                                     closure=obgc.VerticalScalarDiffusivity(obgc.VerticallyImplicitTimeDiscretization(), κ=kz))
+    obgc.set_(model, **obgc.lobster_initial_conditions(g, seed=5))
+    s0 = model.state_array().double().cpu().numpy()
+    dt, nsteps = 600.0, 4
+    obgc.time_step(model, dt, nsteps=nsteps)
+    got = model.state_array().double().cpu().numpy()
+    zf = -g.Lz + g.Lz / g.Nz * np.arange(g.Nz + 1)
+    m = O.model3d(bgc.params, g.c_grid(), model.tracer_names, kappa_z_faces=np.array([kz(z) for z in zf]),
+                  vertical_implicit=True, negatives=O.NEG_SCALE)
+    ref = np.ascontiguousarray(s0.copy())
+    O.step3d(m, ref, u=u.double().cpu().numpy().ravel().copy(), v=v.double().cpu().numpy().ravel().copy(), t=0.0,
+             dt=dt, nsteps=nsteps)
+    errs = per_tracer_err(model, got, ref)
+    assert max(errs.values()) < tol, errs
+    # the mixed layer homogenised T (a linear profile at the start)
+    q = model.tracer_names.index("T")
+    top = got[q, -4:]
+    assert np.ptp(top) < 0.2 * np.ptp(s0[q, -4:])
+
+
 def test_bounded_walls_vertical_velocity_and_sinking():
     g, bgc, model, vel = lobster_model(shape=(21, 13, 17), extent=(2100.0, 1300.0, 170.0),
                                        topo=("Bounded", "Bounded", "Bounded"), w=True, carbonates=False, seed=8)

@@ -94,3 +94,25 @@ def test_co2_exchange_column_equals_the_3d_step_of_a_single_column():
     O.columns_run(bgc.params, obgc._abi.default_twoband(), [spec], names, plain, c["kappa"], [0], [0], 0.0, 0)
     q = names.index("DIC")
     assert abs(plain.reshape(nt, Nz)[q, -1] - col[q, -1]) > 1e-2
+
+
+def test_implicit_vertical_diffusion_of_the_3d_step_equals_the_column_runner():
+    """VerticallyImplicitTimeDiscretization in the oracle's 3-D step (a 1 x 1 x Nz grid) against the
+    column runner, whose vertical diffusion has always been implicit: equal to rounding."""
+    bgc = obgc.LOBSTER(None, carbonate_system=obgc.CarbonateSystem())
+    rng = np.random.default_rng(8)
+    c = obgc.lobster_column_request(rng, levels=(30, 30), days=(0.5, 0.5))
+    names = list(obgc.required_biogeochemical_tracers(bgc))
+    Nz, nt = c["init"].shape[1], len(names)
+    spec = O.Column(Nz, c["nsteps"], c["dz"], c["surface_PAR"], 0.0, c["dt"], -1, -1, 0.0, c["T"], c["S"])
+    col = np.ascontiguousarray(c["init"].ravel().copy())
+    O.columns_run(bgc.params, obgc._abi.default_twoband(), [spec], names, col, c["kappa"], [0], [0], 0.0, 0)
+    g = obgc.RectilinearGrid((1, 1, Nz), (1.0, 1.0, Nz * c["dz"]), ("Flat", "Flat", "Bounded"))
+    m = O.model3d(bgc.params, g.c_grid(), names, surface_kind=obgc._abi.SURFACE_CONSTANT, surface_value=c["surface_PAR"],
+                  kappa_z_faces=c["kappa"], vertical_implicit=True)
+    s3 = np.ascontiguousarray(c["init"].reshape(nt, Nz, 1, 1).copy())
+    O.step3d(m, s3, t=0.0, dt=c["dt"], nsteps=c["nsteps"])
+    col = col.reshape(nt, Nz)
+    for q in range(nt):
+        assert np.max(np.abs(col[q] - s3[q, :, 0, 0])) <= 1e-12 * np.max(np.abs(s3[q])), names[q]
+    assert np.max(np.abs(c["kappa"])) >= 1e-3      # a mixed layer: explicit steps of this dt would be unstable
