@@ -60,40 +60,6 @@ CARBON_FLOP_PER_CELL = 1671.0
 OMEGA_FLOP_PER_CELL = 1529.0
 
 
-def e2e_steps_ms(step, dev, host, nsteps, stream):
-    """End-to-end steps through the public API: every step copies each field in from pinned host
-    memory, steps, and copies each result back.  The read-back runs on a second stream so that a
-    field's read-back overlaps the next step's copy-in of the fields already read back (the two
-    directions of the host link run concurrently); a field is copied in only after its previous
-    read-back.  Returns ms per step (CUDA events on the launching stream, which joins the copy
-    stream before the end event)."""
-    import torch
-    names = list(dev)
-    out_stream = torch.cuda.Stream()
-    done = {n: torch.cuda.Event() for n in names}
-    stepped = torch.cuda.Event()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for k in range(nsteps):
-        for n in names:
-            if k > 0:
-                stream.wait_event(done[n])
-            dev[n].copy_(host[n], non_blocking=True)
-        step()
-        stepped.record(stream)
-        out_stream.wait_event(stepped)
-        with torch.cuda.stream(out_stream):
-            for n in names:
-                host[n].copy_(dev[n], non_blocking=True)
-                done[n].record(out_stream)
-    for n in names:
-        stream.wait_event(done[n])
-    e1.record(stream)
-    torch.cuda.synchronize()
-    return e0.elapsed_time(e1) / nsteps
-
-
 def e2e_members_ms(members, nsteps, stream):
     """End-to-end steps of an ensemble through the public API, the way a host drives several model
     members on one GPU: member k % M takes step k, which copies that member's fields in from pinned
