@@ -6,6 +6,7 @@ LOBSTER with CarbonateSystem(2), a CO2 gas-exchange condition on DIC1 (water CO2
 and one on DIC2 (from DIC2/Alk2), and an alkalinity release forcing Alk2 inside a region over a
 window of time.  The replicates DIC2 / Alk2 run as passive tracers taking the DIC / Alk tendency of
 the same stage; a further passive tracer C has no BGC tendency."""
+import ctypes as C
 import math
 
 import numpy as np
@@ -233,3 +234,39 @@ def test_graph_replay_with_passive_launches_is_bit_identical():
         obgc.time_step(model, 300.0, nsteps=5, graph=graph)
         runs.append(model.state_array().double().cpu().numpy())
     np.testing.assert_array_equal(runs[0], runs[1])
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-11), ("mixed", 1e-5)])
+def test_forcing_of_a_model_tracer_with_implicit_diffusion_and_a_passive_tracer(precision, tol):
+    # a forcing on NO3 (a tracer of the main launch) over a window that opens mid-step, a passive
+    # tracer, and VerticallyImplicitTimeDiscretization acting on every slot after each stage
+    torch = cuda()
+    g = obgc.RectilinearGrid((36, 12, 10), (7200.0, 2400.0, 100.0), dtype="f64")
+    bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem())
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.05, seed=21)
+    kz = np.linspace(1e-4, 0.3, g.Nz + 1)
+    rate = np.zeros(g.shape)
+    rate[-2:, 3:9, 5:20] = 5e-5
+    model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S", "C"), velocities=(u, v, None),
+                                     precision=precision, forcing={"NO3": obgc.Forcing(rate, start_time=250.0,
+                                                                                        end_time=1000.0)})
+    A.check(model._lib.obgc_set_diffusivity(model._ctx, 0.0, 0.0, (C.c_double * (g.Nz + 1))(*kz)),
+            "obgc_set_diffusivity")
+    A.check(model._lib.obgc_set_vertical_time_discretization(model._ctx, A.VERTICALLY_IMPLICIT), "vertical")
+    rng = np.random.default_rng(21)
+    obgc.set_(model, **obgc.lobster_initial_conditions(g, seed=22))
+    obgc.set_(model, C=rng.uniform(1, 2, g.shape))
+    s0 = model.state_array().double().cpu().numpy()
+    dt, nsteps = 300.0, 4
+    obgc.time_step(model, dt, nsteps=nsteps)
+    got = model.state_array().double().cpu().numpy()
+    names, src = oracle_layout(model)
+    slot = {n: q for q, n in enumerate(model.tracer_names)}
+    m = O.model3d(bgc.params, g.c_grid(), names, kappa_z_faces=kz, vertical_implicit=True, tendency_of=src,
+                  forcing={slot["NO3"]: (rate, 250.0, 1000.0)})
+    ref = np.ascontiguousarray(s0.copy())
+    O.step3d(m, ref, u=u.double().cpu().numpy().ravel().copy(), v=v.double().cpu().numpy().ravel().copy(), t=0.0,
+             dt=dt, nsteps=nsteps)
+    errs = {n: rel_err(got[q], ref[q], floor_frac=FLOOR.get(n, 1e-6)) for q, n in enumerate(model.tracer_names)}
+    worst = max(errs, key=errs.get)
+    assert errs[worst] < tol, (worst, errs)
