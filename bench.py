@@ -1063,10 +1063,74 @@ def run_box(args):
     return 0
 
 
+# ----------------------------------------------------------------------------- OAE replicates
+OAE_WORKLOAD = ("OAE experiment at the headline grid: LOBSTER + CarbonateSystem(2) (DIC1 DIC2 Alk1 Alk2) + T S, "
+                "256x256x64, a CO2 gas-exchange condition on each replicate (5 m/s), an alkalinity release into "
+                "Alk2 in a surface disc, WENO5 + sinking + TwoBand PAR + RK3, dt=300 s")
+
+
+def run_oae(args):
+    """examples/oae_experiment.jl's tracer physics at the headline grid: the replicates DIC2 / Alk2
+    run as passive launches with the DIC / Alk tendency, two gas-exchange flux kernels per stage,
+    the release as a windowed forcing field."""
+    import numpy as np
+    import torch
+    import obgc
+    from obgc import _abi as A
+    torch.cuda.set_device(0)
+    lib = A.load()
+    prec = args.precision
+    shape = tuple(args.shape) if args.shape else SHAPE
+    g = obgc.RectilinearGrid(shape, (EXTENT[0] * shape[0] / SHAPE[0], EXTENT[1] * shape[1] / SHAPE[1], EXTENT[2]),
+                             ("Periodic", "Periodic", "Bounded"), dtype="f32" if prec == "f32" else "f64")
+    bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem(2))
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=7)
+    bcs = {f"DIC{r}": obgc.CarbonDioxideGasExchangeBoundaryCondition(
+        wind_speed=5.0, water_concentration=obgc.CarbonDioxideConcentration(DIC=f"DIC{r}", Alk=f"Alk{r}")) for r in (1, 2)}
+    z, y, x = g.nodes()
+    disc = ((x[None, None, :] - g.Lx / 2) ** 2 + (y[None, :, None] - g.Ly / 2) ** 2 < (g.Lx / 10) ** 2) & (z[:, None, None] > -10)
+    release = obgc.Forcing(np.where(disc, 1e-3, 0.0) * np.ones(g.shape), start_time=1200.0, end_time=1200.0 + 3600.0)
+    model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None), precision=prec,
+                                     boundary_conditions=bcs, forcing={"Alk2": release})
+    init = obgc.lobster_initial_conditions(g, seed=11)
+    vals = {k: val for k, val in init.items() if k in model.tracers}
+    vals.update(DIC1=init["DIC"], DIC2=init["DIC"], Alk1=init["Alk"], Alk2=init["Alk"])
+    obgc.set_(model, **vals)
+    nt = len(model.tracer_names)
+    obgc.time_step(model, DT, nsteps=max(args.warmup, 3), graph=True)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    l0 = lib.obgc_kernel_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clocks:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        obgc.time_step(model, DT, nsteps=args.steps, graph=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = lib.obgc_kernel_launch_count() - l0
+    t = {n: model.tracers[n].double() for n in ("DIC1", "DIC2", "Alk1", "Alk2")}
+    line = {
+        "metric": METRIC, "value": nt * g.N * args.steps / (ms / 1e3), "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": {"f32": "f32", "mixed": "f64-state/f32-compute", "f64": "f64"}[prec],
+        "data": "synthetic (seeded LOBSTER initial conditions, both replicates equal at the start)",
+        "config": {"workload": OAE_WORKLOAD if shape == SHAPE else OAE_WORKLOAD.replace("256x256x64", "x".join(map(str, shape))),
+                   "grid": list(shape), "tracers": nt, "precision": prec, "parallelism": "1 GPU"},
+        "gpu_launches": int(launches),
+        "released_alkalinity_excess": float((t["Alk2"] - t["Alk1"]).sum().item()),
+        "dic_uptake_excess": float((t["DIC2"] - t["DIC1"]).sum().item()),
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="lobster3d", choices=["lobster3d", "columns", "service", "carbon", "accuracy",
-                                                                    "pisces", "box", "front"])
+                                                                    "pisces", "box", "front", "oae"])
     ap.add_argument("--rates", type=float, nargs="*", default=None, help="service: Poisson arrival rates (1/s)")
     ap.add_argument("--arrival-seconds", type=float, default=2.0, help="service: seconds of arrivals per rate")
     ap.add_argument("--chunk", type=int, default=32, help="service: steps per launch")
@@ -1095,6 +1159,8 @@ def main():
         return run_front(args)
     if args.workload == "accuracy":
         return run_accuracy(args)
+    if args.workload == "oae":
+        return run_oae(args)
     if args.workload == "service":
         if "--precision" not in sys.argv:
             args.precision = "mixed"
