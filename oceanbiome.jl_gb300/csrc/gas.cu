@@ -10,7 +10,8 @@ __global__ void __launch_bounds__(128) gas_exchange_kernel(obgc_gas_exchange g, 
                                                            int64_t sk, const T* __restrict__ Tc, const T* __restrict__ S,
                                                            const T* __restrict__ DIC, const T* __restrict__ Alk,
                                                            const T* __restrict__ O2, const T* __restrict__ wind,
-                                                           const T* __restrict__ air, double* __restrict__ flux) {
+                                                           const T* __restrict__ air, double* __restrict__ flux,
+                                                           double* __restrict__ H) {
     const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= (int64_t)Nx * Ny) return;
     const int i = (int)(col % Nx), j = (int)(col / Nx);
@@ -19,23 +20,23 @@ __global__ void __launch_bounds__(128) gas_exchange_kernel(obgc_gas_exchange g, 
     const double ca = air ? (double)air[col] : g.air_concentration;
     const bool co2 = g.gas == OBGC_GAS_CO2;
     flux[col] = gas_flux_cell(g, (double)Tc[o], (double)S[o], co2 ? (double)DIC[o] : 0.0, co2 ? (double)Alk[o] : 0.0,
-                              co2 ? 0.0 : (double)O2[o], u10, ca);
+                              co2 ? 0.0 : (double)O2[o], u10, ca, H ? H + col : nullptr);
 }
 
 template <typename T>
 int launch_gas_exchange(const obgc_gas_exchange* g, const obgc_grid* grid, const void* Tc, const void* S,
-                        const void* DIC, const void* Alk, const void* O2, double* flux, cudaStream_t st) {
+                        const void* DIC, const void* Alk, const void* O2, double* flux, cudaStream_t st, double* H) {
     const int64_t cols = (int64_t)grid->Nx * grid->Ny;
     gas_exchange_kernel<T><<<(unsigned)((cols + 127) / 128), 128, 0, st>>>(
         *g, grid->Nx, grid->Ny, grid->Nz, grid->stride_j, grid->stride_k, (const T*)Tc, (const T*)S, (const T*)DIC,
-        (const T*)Alk, (const T*)O2, (const T*)g->wind_field, (const T*)g->air_field, flux);
+        (const T*)Alk, (const T*)O2, (const T*)g->wind_field, (const T*)g->air_field, flux, H);
     OBGC_LAUNCHED("gas_exchange_kernel");
     return OBGC_OK;
 }
 template int launch_gas_exchange<float>(const obgc_gas_exchange*, const obgc_grid*, const void*, const void*,
-                                        const void*, const void*, const void*, double*, cudaStream_t);
+                                        const void*, const void*, const void*, double*, cudaStream_t, double*);
 template int launch_gas_exchange<double>(const obgc_gas_exchange*, const obgc_grid*, const void*, const void*,
-                                         const void*, const void*, const void*, double*, cudaStream_t);
+                                         const void*, const void*, const void*, double*, cudaStream_t, double*);
 
 bool valid_gas(const obgc_gas_exchange* g) {
     return g && (g->gas == OBGC_GAS_CO2 || g->gas == OBGC_GAS_O2);
@@ -77,8 +78,8 @@ extern "C" int obgc_gas_exchange_flux(const obgc_gas_exchange* g, const obgc_gri
         (g->gas == OBGC_GAS_CO2 && (!DIC || !Alk)) || (g->gas == OBGC_GAS_O2 && !O2))
         return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_gas_exchange_flux: bad argument");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    return dtype == OBGC_F32 ? launch_gas_exchange<float>(g, grid, T, S, DIC, Alk, O2, flux, st)
-                             : launch_gas_exchange<double>(g, grid, T, S, DIC, Alk, O2, flux, st);
+    return dtype == OBGC_F32 ? launch_gas_exchange<float>(g, grid, T, S, DIC, Alk, O2, flux, st, nullptr)
+                             : launch_gas_exchange<double>(g, grid, T, S, DIC, Alk, O2, flux, st, nullptr);
 }
 
 extern "C" int obgc_gas_exchange_point(const obgc_gas_exchange* g, double T, double S, double DIC, double Alk, double O2,

@@ -14,8 +14,11 @@
 
 namespace obgc {
 
+// H: when non-null, the Newton solve of the CO2 condition starts from *H if positive (the
+// column's [H+] of the previous evaluation) and leaves the solved [H+] there; otherwise it starts
+// from 10^-initial_pH_guess.
 __host__ __device__ inline double gas_flux_cell(const obgc_gas_exchange& g, double T, double S, double DIC,
-                                                double Alk, double O2, double u10, double air) {
+                                                double Alk, double O2, double u10, double air, double* H = nullptr) {
     const double k660 = g.k660[0] + u10 * (g.k660[1] + u10 * (g.k660[2] + u10 * g.k660[3]));
     const double Sc = g.schmidt[0] + T * (g.schmidt[1] + T * (g.schmidt[2] + T * (g.schmidt[3] + T * g.schmidt[4])));
     const double kS = k660 / sqrt(Sc / 660.0);
@@ -26,8 +29,8 @@ __host__ __device__ inline double gas_flux_cell(const obgc_gas_exchange& g, doub
         o.output = OBGC_OUT_PCO2;
         o.ph_given = 0;
         o.has_pressure = 0;
-        const double pCO2 = carbon_cell(o, DIC, Alk, T, S, 0.0, 0.0, 0.0, 0.0,
-                                        exp(-2.302585092994046 * o.initial_pH_guess), nullptr, nullptr, nullptr);
+        const double H0 = H && *H > 0.0 ? *H : exp(-2.302585092994046 * o.initial_pH_guess);
+        const double pCO2 = carbon_cell(o, DIC, Alk, T, S, 0.0, 0.0, 0.0, 0.0, H0, H, nullptr, nullptr);
         return kS * solubility * (pCO2 - air);
     }
     const double Tk = T + 273.15, Tk_100 = Tk / 100.0;

@@ -11,7 +11,7 @@ namespace obgc {
 
 template <typename T>
 int launch_gas_exchange(const obgc_gas_exchange* g, const obgc_grid* grid, const void* Tc, const void* S,
-                        const void* DIC, const void* Alk, const void* O2, double* flux, cudaStream_t st);
+                        const void* DIC, const void* Alk, const void* O2, double* flux, cudaStream_t st, double* H);
 bool valid_gas(const obgc_gas_exchange* g);
 
 // ----------------------------------------------------------------------------- registry
@@ -197,6 +197,7 @@ struct obgc_ctx {
         obgc_gas_exchange g;
         int target = -1, dic = -1, alk = -1;   // slots
         double* flux = nullptr;                 // (Nx, Ny) per stage
+        double* H = nullptr;                    // (Nx, Ny): each column's [H+] from the previous stage
     } gas[OBGC_MAX_GAS_CONDITIONS];
     // forcings (prescribed source-rate fields), one per target slot
     struct ForcingSpec {
@@ -252,8 +253,10 @@ static int ctx_free(obgc_ctx* c) {
     if (c->d_time) cudaFree(c->d_time);
     if (c->partial) cudaFree(c->partial);
     if (c->d_budget) cudaFree(c->d_budget);
-    for (auto& gc : c->gas)
+    for (auto& gc : c->gas) {
         if (gc.flux) cudaFree(gc.flux);
+        if (gc.H) cudaFree(gc.H);
+    }
     for (int q = 0; q < 2; q++)
         if (c->bgc_out[q]) cudaFree(c->bgc_out[q]);
     if (c->kzz) cudaFree(c->kzz);
@@ -444,7 +447,11 @@ extern "C" int obgc_set_gas_exchange_on(obgc_ctx* c, int32_t tracer, const obgc_
     for (auto& gc : c->gas)
         if (!slot && !gc.on) slot = &gc;
     if (!slot) return fail(OBGC_ERR_UNSUPPORTED, "obgc_set_gas_exchange_on: more than 4 gas exchange conditions");
-    if (!slot->flux) OBGC_CUDA(cudaMalloc(&slot->flux, sizeof(double) * (size_t)c->desc.grid.Nx * c->desc.grid.Ny));
+    const size_t cols = (size_t)c->desc.grid.Nx * c->desc.grid.Ny;
+    if (!slot->flux) OBGC_CUDA(cudaMalloc(&slot->flux, sizeof(double) * cols));
+    // the warm start of the pCO2 solve: zero (none yet) whenever the condition is (re)set
+    if (!slot->H) OBGC_CUDA(cudaMalloc(&slot->H, sizeof(double) * cols));
+    OBGC_CUDA(cudaMemset(slot->H, 0, sizeof(double) * cols));
     slot->g = *g;
     slot->target = target;
     slot->dic = sd;
@@ -750,7 +757,7 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
                 const bool co2 = gc.g.gas == OBGC_GAS_CO2;
                 const int rg = launch_gas_exchange<TS>(&gc.g, &grid, at(slot_named(c, OBGC_T)), at(slot_named(c, OBGC_S)),
                                                        co2 ? at(gc.dic) : nullptr, co2 ? at(gc.alk) : nullptr,
-                                                       co2 ? nullptr : at(gc.target), gc.flux, st);
+                                                       co2 ? nullptr : at(gc.target), gc.flux, st, gc.H);
                 if (rg != OBGC_OK) return rg;
             }
             for (SubstepArgs<TS, TC>* x : {&a, &ap}) {
