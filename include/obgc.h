@@ -600,8 +600,9 @@ int obgc_set_sediment(obgc_ctx* ctx, int32_t n_sinking, const int32_t* sinking_n
  * it, then `get` (optional) receives it.  Synchronises the device. */
 int obgc_sediment_storage(obgc_ctx* ctx, const double* set, double* get);
 /* Size and selected field offsets of the ABI structs (which: 0 npd_params, 1 twoband,
- * 2 surface, 3 grid, 4 carbon_options, 5 model_desc, 6 fields) for binding self-checks;
- * no counterpart in the reference. */
+ * 2 surface, 3 grid, 4 carbon_options, 5 model_desc, 6 fields, 7 column_spec, 8 columns_desc,
+ * 9 pisces_params, 10 pisces_phyto, 11 pisces_field, 12 gas_exchange, 13 box_drivers) for binding
+ * self-checks; no counterpart in the reference. */
 int obgc_struct_layout(int32_t which, int64_t* out, int32_t cap);
 
 /* Domain-integrated mass of a conserved group (conserved_tracers, NutrientsPlanktonDetritus/

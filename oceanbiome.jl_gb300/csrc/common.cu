@@ -110,6 +110,8 @@ extern "C" int obgc_struct_layout(int32_t which, int64_t* out, int32_t cap) {
                  out[2] = offsetof(obgc_pisces_field, data); out[3] = 0; return 0;
         case 12: out[0] = sizeof(obgc_gas_exchange); out[1] = offsetof(obgc_gas_exchange, wind_field);
                  out[2] = offsetof(obgc_gas_exchange, o2_solubility); out[3] = offsetof(obgc_gas_exchange, carbon); return 0;
+        case 13: out[0] = sizeof(obgc_box_drivers); out[1] = offsetof(obgc_box_drivers, n_prescribed);
+                 out[2] = offsetof(obgc_box_drivers, prescribed); out[3] = offsetof(obgc_box_drivers, forcing); return 0;
         case 8: out[0] = sizeof(obgc_columns_desc); out[1] = offsetof(obgc_columns_desc, light);
                 out[2] = offsetof(obgc_columns_desc, arena_cells); out[3] = offsetof(obgc_columns_desc, gas); return 0;
     }

@@ -45,6 +45,7 @@ def test_every_declared_symbol_is_exported():
     (10, A.PiscesPhyto, ["exudated_fraction", "base_growth_rate", "silicate_half_saturation_parameter"]),
     (11, A.PiscesField, ["value", "data", None]),
     (12, A.GasExchange, ["wind_field", "o2_solubility", "carbon"]),
+    (13, A.BoxDrivers, ["n_prescribed", "prescribed", "forcing"]),
 ])
 def test_struct_layouts(which, struct, fields):
     lib = A.load()
