@@ -301,9 +301,10 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     // shared-space address of this thread's first tile element
     const unsigned tiles_s = (unsigned)__cvta_generic_to_shared(tiles) + 4u * (unsigned)tid;
 
-    // forcings switched on at this stage's time: bit q of frc_on, and bit t of frc_slots for the
-    // slots they force (one register each, tested per slot with a compile-time shift)
-    uint32_t frc_on = 0u, frc_slots = 0u;
+    // forcings switched on at this stage's time
+    bool frc_on[MAX_FRC];
+#pragma unroll
+    for (int q = 0; q < MAX_FRC; q++) frc_on[q] = false;
     if constexpr (EXT) {
         bool any_frc = false;
 #pragma unroll
@@ -312,10 +313,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             const double t_stage = *a.d_time + a.c_stage * a.dt_d;
 #pragma unroll
             for (int q = 0; q < MAX_FRC; q++)
-                if (a.frc_slot1[q] != 0 && t_stage >= a.frc_t0[q] && t_stage < a.frc_t1[q]) {
-                    frc_on |= 1u << q;
-                    frc_slots |= 1u << (a.frc_slot1[q] - 1);
-                }
+                frc_on[q] = a.frc_slot1[q] != 0 && t_stage >= a.frc_t0[q] && t_stage < a.frc_t1[q];
         }
     }
 
@@ -619,11 +617,9 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                         for (int q = 0; q < MAX_TOP; q++)
                             if (t + 1 == a.top_slot1[q]) Gt -= TC(a.top_flux[q][ic + (int64_t)jc * a.Nx]) * a.inv_dz;
                     }
-                    if (((frc_slots >> t) & 1u) && active) {
 #pragma unroll
-                        for (int q = 0; q < MAX_FRC; q++)
-                            if (((frc_on >> q) & 1u) && t + 1 == a.frc_slot1[q]) Gt += ld<TS, TC>(a.frc[q], idx);
-                    }
+                    for (int q = 0; q < MAX_FRC; q++)
+                        if (frc_on[q] && t + 1 == a.frc_slot1[q] && active) Gt += ld<TS, TC>(a.frc[q], idx);
                 }
                 if (active) {
                     TC Un;
