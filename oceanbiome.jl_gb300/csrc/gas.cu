@@ -24,6 +24,55 @@ __global__ void __launch_bounds__(128) gas_exchange_kernel(obgc_gas_exchange g, 
 }
 
 template <typename T>
+__global__ void __launch_bounds__(128) gas_exchange_multi_kernel(const __grid_constant__ GasMulti m, int Nx, int Ny, int Nz,
+                                                                 int64_t sj, int64_t sk, const T* __restrict__ Tc,
+                                                                 const T* __restrict__ S) {
+    const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= (int64_t)Nx * Ny) return;
+    const int i = (int)(col % Nx), j = (int)(col / Nx);
+    const int64_t o = i + (int64_t)j * sj + (int64_t)(Nz - 1) * sk;
+    const double Tv = (double)Tc[o], Sv = (double)S[o];
+    Co2Column shared;
+    bool prepared = false;
+    for (int q = 0; q < m.n; q++) {
+        const obgc_gas_exchange& g = m.g[q];
+        const double u10 = g.wind_field ? (double)static_cast<const T*>(g.wind_field)[col] : g.wind_speed;
+        const double ca = g.air_field ? (double)static_cast<const T*>(g.air_field)[col] : g.air_concentration;
+        if (g.gas != OBGC_GAS_CO2) {
+            m.flux[q][col] = gas_flux_cell(g, Tv, Sv, 0.0, 0.0, (double)static_cast<const T*>(m.O2[q])[o], u10, ca);
+            continue;
+        }
+        double* Hq = m.H[q] + col;
+        if (!(Hq[0] > 0.0)) Hq[0] = exp(-2.302585092994046 * g.carbon.initial_pH_guess);
+        const double DIC = (double)static_cast<const T*>(m.DIC[q])[o], Alk = (double)static_cast<const T*>(m.Alk[q])[o];
+        if (m.share[q]) {
+            if (!prepared) {
+                co2_column_prepare(g, Tv, Sv, u10, shared);
+                prepared = true;
+            }
+            shared.k_sol = co2_k_sol(g, Tv, shared.sol, u10);
+            m.flux[q][col] = co2_column_flux(g, shared, DIC, Alk, ca, Hq[0]);
+        } else {
+            Co2Column own;
+            co2_column_prepare(g, Tv, Sv, u10, own);
+            m.flux[q][col] = co2_column_flux(g, own, DIC, Alk, ca, Hq[0]);
+        }
+    }
+}
+
+template <typename T>
+int launch_gas_exchange_multi(const GasMulti& m, const obgc_grid* grid, const void* Tc, const void* S, cudaStream_t st) {
+    const int64_t cols = (int64_t)grid->Nx * grid->Ny;
+    gas_exchange_multi_kernel<T><<<(unsigned)((cols + 127) / 128), 128, 0, st>>>(m, grid->Nx, grid->Ny, grid->Nz,
+                                                                              grid->stride_j, grid->stride_k,
+                                                                              (const T*)Tc, (const T*)S);
+    OBGC_LAUNCHED("gas_exchange_multi_kernel");
+    return OBGC_OK;
+}
+template int launch_gas_exchange_multi<float>(const GasMulti&, const obgc_grid*, const void*, const void*, cudaStream_t);
+template int launch_gas_exchange_multi<double>(const GasMulti&, const obgc_grid*, const void*, const void*, cudaStream_t);
+
+template <typename T>
 int launch_gas_exchange(const obgc_gas_exchange* g, const obgc_grid* grid, const void* Tc, const void* S,
                         const void* DIC, const void* Alk, const void* O2, double* flux, cudaStream_t st, double* H) {
     const int64_t cols = (int64_t)grid->Nx * grid->Ny;

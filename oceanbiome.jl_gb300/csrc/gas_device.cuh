@@ -49,14 +49,22 @@ struct Co2Column {
     double conv;       // 1e-3 / rho (mmol/m3 -> mol/kg)
     double k_sol;      // transfer velocity x solubility
     double Tk;
+    double sol;        // solubility K0 rho(T, S, 0) / 1000
 };
 
-__host__ __device__ inline void co2_column_prepare(const obgc_gas_exchange& g, double T, double S, double u10, Co2Column& col) {
+// Transfer velocity x solubility of condition g at wind u10 over water at T (degC), from the
+// solubility the column's constants hold: the same product as gas_flux_cell forms.
+__host__ __device__ inline double co2_k_sol(const obgc_gas_exchange& g, double T, double sol, double u10) {
     const double k660 = g.k660[0] + u10 * (g.k660[1] + u10 * (g.k660[2] + u10 * g.k660[3]));
     const double Sc = g.schmidt[0] + T * (g.schmidt[1] + T * (g.schmidt[2] + T * (g.schmidt[3] + T * g.schmidt[4])));
+    return k660 / sqrt(Sc / 660.0) * sol;
+}
+
+__host__ __device__ inline void co2_column_prepare(const obgc_gas_exchange& g, double T, double S, double u10, Co2Column& col) {
     const double Tk = T + 273.15;
     col.Tk = Tk;
-    col.k_sol = k660 / sqrt(Sc / 660.0) * (weiss_k0(Tk, S, log(Tk), 1.0 / Tk) * seawater_density(g.carbon, T, S, 0.0) / 1000.0);
+    col.sol = weiss_k0(Tk, S, log(Tk), 1.0 / Tk) * seawater_density(g.carbon, T, S, 0.0) / 1000.0;
+    col.k_sol = co2_k_sol(g, T, col.sol, u10);
     col.conv = 1e-3 / seawater_density(g.carbon, T, S, 1.0);   // the pCO2 functor's density at 1 bar
     CarbConsts& c = col.c;
     c.boron = 0.000232 / 10.811 * S / 1.80655;
@@ -81,5 +89,21 @@ __host__ __device__ inline double co2_column_flux(const obgc_gas_exchange& g, co
     const double pCO2 = pco2_from_fco2((CO2 / c.K0) * 1e6, col.Tk, 101325.0);
     return col.k_sol * (pCO2 - air);
 }
+
+// Every gas-exchange condition of a model in one pass over the surface cells.  The CO2 conditions
+// whose carbon-chemistry options equal the first one's (share[q]; the usual case, e.g. one per
+// CarbonateSystem replicate) share that column's T/S constants (the equilibrium constants, the
+// density conversion, the solubility) and differ only in their water's DIC / Alk, wind and air;
+// each condition's Newton solve restarts from its own previous [H+] of the column.
+struct GasMulti {
+    int n;
+    int share[OBGC_MAX_GAS_CONDITIONS];
+    obgc_gas_exchange g[OBGC_MAX_GAS_CONDITIONS];
+    const void* DIC[OBGC_MAX_GAS_CONDITIONS];
+    const void* Alk[OBGC_MAX_GAS_CONDITIONS];
+    const void* O2[OBGC_MAX_GAS_CONDITIONS];
+    double* flux[OBGC_MAX_GAS_CONDITIONS];
+    double* H[OBGC_MAX_GAS_CONDITIONS];
+};
 
 }  // namespace obgc

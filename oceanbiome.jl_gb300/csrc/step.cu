@@ -4,14 +4,14 @@
 #include <cstring>
 #include <mutex>
 #include <vector>
+#include "gas_device.cuh"
 #include "negatives.cuh"
 #include "step_launch.cuh"
 
 namespace obgc {
 
 template <typename T>
-int launch_gas_exchange(const obgc_gas_exchange* g, const obgc_grid* grid, const void* Tc, const void* S,
-                        const void* DIC, const void* Alk, const void* O2, double* flux, cudaStream_t st, double* H);
+int launch_gas_exchange_multi(const GasMulti& m, const obgc_grid* grid, const void* Tc, const void* S, cudaStream_t st);
 bool valid_gas(const obgc_gas_exchange* g);
 
 // ----------------------------------------------------------------------------- registry
@@ -751,14 +751,32 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
     }
     for (int s = 0; s < nsteps; s++) {
         for (int stg = 0; stg < 3; stg++) {
-            for (const auto& gc : c->gas) {
-                if (!gc.on) continue;
-                auto at = [&](int slot) -> const void* { return slot >= 0 ? cur[slot] : nullptr; };
-                const bool co2 = gc.g.gas == OBGC_GAS_CO2;
-                const int rg = launch_gas_exchange<TS>(&gc.g, &grid, at(slot_named(c, OBGC_T)), at(slot_named(c, OBGC_S)),
-                                                       co2 ? at(gc.dic) : nullptr, co2 ? at(gc.alk) : nullptr,
-                                                       co2 ? nullptr : at(gc.target), gc.flux, st, gc.H);
-                if (rg != OBGC_OK) return rg;
+            // every gas-exchange condition in one launch (CO2 conditions with the first one's
+            // carbon-chemistry options share the column's T/S constants)
+            {
+                GasMulti gm;
+                std::memset(&gm, 0, sizeof(gm));
+                const obgc_carbon_options* first = nullptr;
+                for (const auto& gc : c->gas) {
+                    if (!gc.on) continue;
+                    const int q = gm.n++;
+                    gm.g[q] = gc.g;
+                    gm.flux[q] = gc.flux;
+                    gm.H[q] = gc.H;
+                    if (gc.g.gas == OBGC_GAS_CO2) {
+                        gm.DIC[q] = cur[gc.dic];
+                        gm.Alk[q] = cur[gc.alk];
+                        if (!first) first = &gc.g.carbon;
+                        gm.share[q] = std::memcmp(first, &gc.g.carbon, sizeof(obgc_carbon_options)) == 0;
+                    } else {
+                        gm.O2[q] = cur[gc.target];
+                    }
+                }
+                if (gm.n > 0) {
+                    const int rg = launch_gas_exchange_multi<TS>(gm, &grid, cur[slot_named(c, OBGC_T)],
+                                                                 cur[slot_named(c, OBGC_S)], st);
+                    if (rg != OBGC_OK) return rg;
+                }
             }
             for (SubstepArgs<TS, TC>* x : {&a, &ap}) {
                 x->first_stage = stg == 0;
@@ -840,7 +858,7 @@ static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     const bool clock = needs_clock(c);
     const int neg = c->neg.mode == OBGC_NEGATIVES_NONE ? 0 : c->neg_passive.mode != OBGC_NEGATIVES_NONE ? 2 : 1;
     int gases = 0;
-    for (const auto& gc : c->gas) gases += gc.on ? 1 : 0;
+    for (const auto& gc : c->gas) gases = gases || gc.on ? 1 : 0;   // one launch for all conditions
     const bool impl = c->vimplicit && c->kzf;
     const int per_stage = 1 + c->nchunk + gases + (impl ? 1 + neg : 0);
     return (int64_t)nsteps * (3 * per_stage + (clock ? 1 : 0)) + (nsteps % 2 ? c->NT + c->NP : 0) + 1 + neg + (impl ? 1 : 0);
