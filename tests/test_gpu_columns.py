@@ -124,7 +124,8 @@ def test_lobster_columns_with_pulses_match_oracle(precision, eps, floor):
     assert_within_envelope(got, ref, pert, floor)
 
 
-@pytest.mark.parametrize("precision,eps,floor", [("f64", 2.0 ** -53, 1e-12), ("mixed", 2.0 ** -24, 1e-4)])
+@pytest.mark.parametrize("precision,eps,floor", [("f64", 2.0 ** -53, 1e-12), ("mixed", 2.0 ** -24, 1e-4),
+                                                 ("f32", 2.0 ** -24, 1e-4)])
 def test_lobster_columns_with_co2_exchange_match_oracle(precision, eps, floor):
     # examples/column.jl:54-64: the CO2 gas exchange on every column's DIC, each column with its own
     # surface T and S, a wind of 8 m/s and the air's 413 ppm; the alkalinity pulses then drive uptake
