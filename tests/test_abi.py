@@ -79,3 +79,25 @@ def test_no_device_is_reported():
     ctx = C.c_void_p()
     rc = lib.obgc_create(C.byref(d), C.byref(ctx))
     assert rc in (2, 7) and not ctx.value
+
+
+def test_new_entry_points_reject_bad_arguments_without_a_device():
+    # argument checks run before any device work, so they answer on a machine without a GPU
+    lib = A.load()
+    g = A.GasExchange()
+    assert lib.obgc_gas_exchange_defaults(A.GAS_CO2, C.byref(g)) == 0
+    assert lib.obgc_set_gas_exchange_on(None, A.NAME_INDEX["DIC"], C.byref(g), A.NAME_INDEX["DIC"], A.NAME_INDEX["Alk"]) == 1
+    assert lib.obgc_set_forcing(None, A.NAME_INDEX["Alk"], None, 0.0, 1.0) == 1
+    assert lib.obgc_set_vertical_time_discretization(None, A.VERTICALLY_IMPLICIT) == 1
+    p = A.NPDParams()
+    assert lib.obgc_npd_preset(A.PRESET_NPZD, C.byref(p)) == 0
+    d = A.BoxDrivers()
+    d.n_prescribed = A.BOX_MAX_DRIVERS + 1
+    assert lib.obgc_box_run_drivers(C.byref(p), None, 1, C.c_void_p(1), C.byref(d), 0.0, 1.0, 1, 0, None,
+                                    A.PREC_F64, None) == 1
+    d.n_prescribed = 1
+    d.prescribed_names[0] = A.NUM_NAMED                 # not a tracer name
+    d.prescribed[0] = 1
+    assert lib.obgc_box_run_drivers(C.byref(p), None, 1, C.c_void_p(1), C.byref(d), 0.0, 1.0, 1, 0, None,
+                                    A.PREC_F64, None) == 1
+    assert "prescribed" in lib.obgc_last_error_message().decode()
