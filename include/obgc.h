@@ -8,8 +8,7 @@
  * thread-safe: serialise calls on one context externally.
  *
  * Each declaration names the OceanBioME.jl (v0.17.6) interface it replaces, as file:line within
- * that project.  The Julia `ccall` bindings a maintainer would add are written out in
- * INTEGRATION.md.
+ * that project.
  */
 #ifndef OBGC_H
 #define OBGC_H
@@ -627,8 +626,11 @@ int obgc_tracer_budget(obgc_ctx* ctx, int32_t group, double* total, void* stream
  * finished it.  n_fields above OBGC_BUDGET_STATIC_MAX_FIELDS is rejected (OBGC_ERR_INVALID_ARGUMENT).
  *
  * The first call on each device looks up the array's device address on that device; make that
- * first call before any stream capture.  All calls share the one array: calls that overlap on
- * the GPU (different streams or host threads without ordering) race and corrupt each other's sums.
+ * first call before any stream capture.  The address is kept for the life of the process: after
+ * a cudaDeviceReset (or any teardown of the device's primary context) the library's module is
+ * loaded again elsewhere, so do not call this entry point on that device again.  All calls share
+ * the one array: calls that overlap on the GPU (different streams or host threads without
+ * ordering) race and corrupt each other's sums.
  */
 #define OBGC_BUDGET_STATIC_SLOTS 1024
 #define OBGC_BUDGET_STATIC_MAX_FIELDS 8

@@ -115,8 +115,8 @@ int run_static_budget(const obgc_grid* g, int n, const void* const* fields, cons
         b.scale[q] = scale[q];
     }
     int dev = 0, nsm = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    OBGC_CUDA(cudaGetDevice(&dev));
+    OBGC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const int64_t N = (int64_t)g->Nx * g->Ny * g->Nz;
     int64_t want = (N + THREADS - 1) / THREADS;
     int blocks = (int)(want < 4 * nsm ? want : 4 * nsm);

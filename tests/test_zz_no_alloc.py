@@ -57,6 +57,27 @@ def test_static_budget_matches_context_budget_on_two_calls(precision):
     assert got2 != got
 
 
+def test_static_budget_grid_stride_at_the_block_cap():
+    """128 x 128 x 16 cells is more than 4 blocks per SM x 256 threads: every block loops over
+    several cells and the block count sits at its cap, on two calls in a row."""
+    torch = cuda()
+    g = obgc.RectilinearGrid((128, 128, 16), (25000.0, 25000.0, 160.0), dtype="f64")
+    bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem())
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=7)
+    model = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None),
+                                     precision="f64")
+    obgc.set_(model, **obgc.lobster_initial_conditions(g, seed=8))
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    assert g.N > 4 * nsm * 256
+    nitrogen, _ = obgc.conserved_tracers(bgc)
+    for _ in range(2):
+        rc, got = static_budget(model, nitrogen, [1.0] * len(nitrogen))
+        assert rc == 0, A.load().obgc_last_error_message()
+        ref = model.budget("nitrogen")
+        assert abs(got - ref) <= 1e-15 * abs(ref)
+        obgc.time_step(model, 300.0, nsteps=1)
+
+
 def test_static_budget_rejects_too_many_fields():
     torch = cuda()
     g = obgc.RectilinearGrid((8, 8, 4), (1.0, 1.0, 4.0))
