@@ -104,11 +104,23 @@ typedef struct or_model3d {
                                       * tendency the slot takes (CarbonateSystem replicates), 0 none */
     const double* forcing[32];       /* per slot: a source rate [Nz*Ny*Nx] (per second) or NULL,  */
     double forcing_t0[32], forcing_t1[32]; /* added at stage times t0 <= t < t1              */
+    double stage_rounding;           /* conditioning probe, 0 = off: after every stage each state
+                                      * value is multiplied by (1 +/- stage_rounding), the sign
+                                      * drawn from a hash of (value index, stage count, seed): a
+                                      * model of one rounding of that relative size per stored value */
+    uint64_t rounding_seed;
 } or_model3d;
 /* state: [n_tracers][Nz*Ny*Nx]; u, v, w: [Nz*Ny*Nx] or NULL. */
 void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,
                const double* w, double t, double dt, int nsteps, int nthreads);
 void or_par3d(const or_model3d* m, const double* state, double t, double* PAR, int nthreads);
+/* One RK3 stage (0, 1, 2) of the step starting at t: G[n_tracers*N] receives the stage's
+ * tendency, Gm holds the previous stage's (unused by stage 0), sed_Gm[Ny*Nx] the sediment's
+ * previous-stage burial (or NULL without a sediment); the caller swaps G and Gm between stages.
+ * No modifier is applied to the entering state (or_step3d applies it once before its first stage).
+ * The stage-level form lets a domain split into y slabs exchange halo rows between stages. */
+void or_stage3d(const or_model3d* m, double* state, const double* u, const double* v, const double* w,
+                double t, double dt, int stage, double* G, double* Gm, double* sed_Gm, int nthreads);
 
 /* ---- batched uneven columns with vertically implicit diffusion ---- */
 typedef struct or_column {

@@ -22,6 +22,13 @@ static const double RK_G[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
 static const double RK_Z[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
 static const double RK_C[3] = {0.0, 8.0 / 15.0, 2.0 / 3.0};
 
+/* splitmix64 finaliser: the sign source of the conditioning probe (or_model3d.stage_rounding) */
+static uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
 /* ------------------------------------------------------------------ WENO ---------- */
 static double weno5(double v1, double v2, double v3, double v4, double v5) {
     const double eps = 1e-8;
@@ -174,8 +181,12 @@ static void or_negatives3d(const or_model3d* m, double* state, long N, int ng, c
 
 static void implicit_diffusion(int Nz, double dz, const double* kf, double dts, double* x, double* cp, double* dp);
 
-void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,
-               const double* w, double t, double dt, int nsteps, int nthreads) {
+/* nsteps RK3 steps; or, with only_stage in 0..2, that one stage of one step, with the tendency
+ * arrays supplied by the caller (Gx receives the stage's tendency, Gmx holds the previous stage's,
+ * sedx the sediment's previous-stage burial) and no modifier applied to the entering state. */
+static void step3d_impl(const or_model3d* m, double* state, const double* u, const double* v,
+                        const double* w, double t, double dt, int nsteps, int nthreads, int only_stage,
+                        double* Gx, double* Gmx, double* sedx) {
     const obgc_grid* g = &m->grid;
     int Nx = g->Nx, Ny = g->Ny, Nz = g->Nz, nt = m->n_tracers;
     long NN = (long)Nx * Ny, N = NN * Nz;
@@ -183,12 +194,13 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
     int px = g->topology_x == OBGC_PERIODIC, py = g->topology_y == OBGC_PERIODIC;
     int flat_y = g->topology_y == OBGC_FLAT || Ny == 1;
     int flat_x = g->topology_x == OBGC_FLAT;
-    double* G = calloc((size_t)nt * N, sizeof(double));
-    double* Gm = calloc((size_t)nt * N, sizeof(double));
+    const int ext = only_stage >= 0;
+    double* G = ext ? Gx : calloc((size_t)nt * N, sizeof(double));
+    double* Gm = ext ? Gmx : calloc((size_t)nt * N, sizeof(double));
     double* PAR = malloc(sizeof(double) * N);
     double* drift = calloc((size_t)nt * (Nz + 1), sizeof(double));
     int* has_drift = calloc(nt, sizeof(int));
-    double* sed_Gm = calloc((size_t)NN, sizeof(double));
+    double* sed_Gm = ext ? sedx : calloc((size_t)NN, sizeof(double));
     int32_t req[32];
     int nreq = or_npd_required_tracers(&m->npd, req, 32);
     int is_bgc[32] = {0};
@@ -206,9 +218,10 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
     int32_t gn[OR_MAX_GROUPS], gslot[OR_MAX_GROUPS * OR_MAX_GROUP];
     double gfac[OR_MAX_GROUPS * OR_MAX_GROUP];
     const int ng = m->negatives == 1 ? or_conserved_groups(&m->npd, nt, m->names, gn, gslot, gfac) : 0;
-    if (m->negatives) or_negatives3d(m, state, N, ng, gn, gslot, gfac, nthreads);
+    if (m->negatives && !ext) or_negatives3d(m, state, N, ng, gn, gslot, gfac, nthreads);
+    const int st0 = ext ? only_stage : 0, st1 = ext ? only_stage + 1 : 3;
     for (int s = 0; s < nsteps; s++) {
-        for (int st = 0; st < 3; st++) {
+        for (int st = st0; st < st1; st++) {
             double ts = t + RK_C[st] * dt;
             or_par3d(m, state, ts, PAR, nthreads);
 #pragma omp parallel for num_threads(nthreads) schedule(static)
@@ -342,6 +355,14 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
                 if (st == 0) state[x] += dt * g * G[x];
                 else state[x] += dt * (g * G[x] + z * Gm[x]);
             }
+            if (m->stage_rounding > 0.0) {
+                const uint64_t stage_count = (uint64_t)s * 3u + (uint64_t)st;
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+                for (long x = 0; x < (long)nt * N; x++) {
+                    const uint64_t h = mix64((uint64_t)x * 0x9E3779B97F4A7C15ull ^ (stage_count << 40) ^ m->rounding_seed);
+                    state[x] *= 1.0 + ((h >> 63) ? m->stage_rounding : -m->stage_rounding);
+                }
+            }
             /* VerticallyImplicitTimeDiscretization: (I - dt_s d/dz kappa d/dz) U = U* per column and
              * tracer with dt_s = (gamma + zeta) dt, walls at the bottom and top */
             if (m->kappa_z_faces && m->vertical_implicit) {
@@ -359,7 +380,19 @@ void or_step3d(const or_model3d* m, double* state, const double* u, const double
         }
         t += dt;
     }
-    free(G); free(Gm); free(PAR); free(drift); free(has_drift); free(sed_Gm);
+    if (!ext) { free(G); free(Gm); free(sed_Gm); }
+    free(PAR); free(drift); free(has_drift);
+}
+
+void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,
+               const double* w, double t, double dt, int nsteps, int nthreads) {
+    step3d_impl(m, state, u, v, w, t, dt, nsteps, nthreads, -1, NULL, NULL, NULL);
+}
+
+void or_stage3d(const or_model3d* m, double* state, const double* u, const double* v, const double* w,
+                double t, double dt, int stage, double* G, double* Gm, double* sed_Gm, int nthreads) {
+    if (stage < 0 || stage > 2) return;
+    step3d_impl(m, state, u, v, w, t, dt, 1, nthreads, stage, G, Gm, sed_Gm);
 }
 
 /* ------------------------------------------------------------------ negative tracers -- */

@@ -32,7 +32,8 @@ class Model3D(C.Structure):
                 ("sed_receiver", C.c_int32), ("sed_sink_mask", C.c_uint32),
                 ("sed_a", C.c_double), ("sed_b", C.c_double), ("sed_k", C.c_double),
                 ("sed_storage", C.POINTER(C.c_double)), ("tendency_of", C.c_int32 * 32),
-                ("forcing", C.POINTER(C.c_double) * 32), ("forcing_t0", C.c_double * 32), ("forcing_t1", C.c_double * 32)]
+                ("forcing", C.POINTER(C.c_double) * 32), ("forcing_t0", C.c_double * 32), ("forcing_t1", C.c_double * 32),
+                ("stage_rounding", C.c_double), ("rounding_seed", C.c_uint64)]
 
 
 class Pisces3D(C.Structure):
@@ -100,6 +101,7 @@ def lib():
         L.or_box_run_drivers.argtypes = [P(A.NPDParams), P(D), VP, D, D, C.c_int, C.c_int, P(I32), P(P(D)), C.c_int,
                                          P(I32), P(P(D))]
         L.or_step3d.argtypes = [P(Model3D), P(D), VP, VP, VP, D, D, C.c_int, C.c_int]
+        L.or_stage3d.argtypes = [P(Model3D), P(D), VP, VP, VP, D, D, C.c_int, P(D), P(D), VP, C.c_int]
         L.or_par3d.argtypes = [P(Model3D), P(D), D, P(D), C.c_int]
         L.or_columns_run.argtypes = [P(A.NPDParams), P(A.TwoBandParams), C.c_int, P(Column), P(I64),
                                      P(I64), C.c_int, P(I32), P(D), P(D), D, D, C.c_int, C.c_int, D, C.c_int,
@@ -368,6 +370,16 @@ def step3d(m, state, u=None, v=None, w=None, t=0.0, dt=1.0, nsteps=1, threads=No
     """state: float64 array (n_tracers, Nz, Ny, Nx), stepped in place."""
     assert state.dtype == np.float64 and state.flags.c_contiguous
     lib().or_step3d(C.byref(m), _dp(state), _opt(u), _opt(v), _opt(w), t, dt, nsteps, threads or nthreads())
+    return state
+
+
+def stage3d(m, state, G, Gm, u=None, v=None, w=None, t=0.0, dt=1.0, stage=0, sed_Gm=None, threads=None):
+    """One RK3 stage in place (or_stage3d): G receives the stage's tendency, Gm holds the previous
+    stage's; swap them before the next stage."""
+    for a in (state, G, Gm):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    lib().or_stage3d(C.byref(m), _dp(state), _opt(u), _opt(v), _opt(w), t, dt, stage, _dp(G), _dp(Gm), _opt(sed_Gm),
+                     threads or nthreads())
     return state
 
 
