@@ -544,6 +544,20 @@ int obgc_step(obgc_ctx* ctx, double t, double dt, int32_t nsteps, void* stream);
 /* Capture `nsteps` steps into a CUDA graph owned by the context and replay it (same semantics as
  * obgc_step; re-captured when dt, nsteps or bindings change). */
 int obgc_step_graph(obgc_ctx* ctx, double t, double dt, int32_t nsteps, void* stream);
+/* Device-side status of the fused step.  Every obgc_step / obgc_step_graph call clears a per-context
+ * device word, and its kernels set flags in it: OBGC_FLAG_NAN when a substep writes a NaN or an
+ * infinity into the state (the reference lets NaN propagate, src/Utils/negative_tracers.jl:197,266;
+ * Oceananigans' NaNChecker stops a simulation on one), OBGC_FLAG_NOT_CONVERGED when a surface pCO2
+ * solve of the gas exchange ends unconverged (src/Utils/solvers.jl:118 warns).  The word is copied
+ * to pinned host memory behind the call's last kernel.
+ *   obgc_step_status waits for the context's last call and returns OBGC_ERR_NAN (NaN first) or
+ *   OBGC_ERR_NOT_CONVERGED when a flag is set, else OBGC_OK; flags (optional) receives the word.
+ *   obgc_set_status_check(ctx, 1) (the default) makes obgc_step itself wait for its kernels and
+ *   return that status; with 0, obgc_step returns as soon as the work is enqueued.  obgc_step_graph
+ *   never waits: call obgc_step_status after it. */
+enum obgc_step_flags { OBGC_FLAG_NAN = 1, OBGC_FLAG_NOT_CONVERGED = 2 };
+int obgc_step_status(obgc_ctx* ctx, int32_t* flags);
+int obgc_set_status_check(obgc_ctx* ctx, int32_t on);
 /* Device kernel time of the last obgc_step / obgc_step_graph measured with CUDA events on the
  * launching stream (ms); with profiling on, also the summed duration of the fused substep kernel
  * launches (event pairs around each launch).  launches: kernels the call enqueued. */

@@ -51,11 +51,15 @@ __global__ void __launch_bounds__(128) gas_exchange_multi_kernel(const __grid_co
                 prepared = true;
             }
             shared.k_sol = co2_k_sol(g, Tv, shared.sol, u10);
-            m.flux[q][col] = co2_column_flux(g, shared, DIC, Alk, ca, Hq[0]);
+            bool ok = true;
+            m.flux[q][col] = co2_column_flux(g, shared, DIC, Alk, ca, Hq[0], &ok);
+            if (!ok && m.status) atomicOr(m.status, OBGC_FLAG_NOT_CONVERGED);
         } else {
             Co2Column own;
             co2_column_prepare(g, Tv, Sv, u10, own);
-            m.flux[q][col] = co2_column_flux(g, own, DIC, Alk, ca, Hq[0]);
+            bool ok = true;
+            m.flux[q][col] = co2_column_flux(g, own, DIC, Alk, ca, Hq[0], &ok);
+            if (!ok && m.status) atomicOr(m.status, OBGC_FLAG_NOT_CONVERGED);
         }
     }
 }

@@ -77,13 +77,14 @@ __host__ __device__ inline void co2_column_prepare(const obgc_gas_exchange& g, d
 
 // Flux (positive out of the ocean) from the surface DIC and Alk; H: the column's [H+], updated.
 __host__ __device__ inline double co2_column_flux(const obgc_gas_exchange& g, const Co2Column& col, double DIC,
-                                                  double Alk, double air, double& H) {
+                                                  double Alk, double air, double& H, bool* converged = nullptr) {
     CarbConsts c = col.c;
     c.DIC = DIC * col.conv;
     c.Alk = Alk * col.conv;
     obgc_carbon_options o = g.carbon;
     o.output = OBGC_OUT_PCO2;
     const CarbSolve r = solve_H(o, H, c);
+    if (converged) *converged = r.converged;
     H = r.H;
     const double CO2 = c.DIC * (H * H) / (H * H + c.K1 * H + c.K1 * c.K2);
     const double pCO2 = pco2_from_fco2((CO2 / c.K0) * 1e6, col.Tk, 101325.0);
@@ -104,6 +105,7 @@ struct GasMulti {
     const void* O2[OBGC_MAX_GAS_CONDITIONS];
     double* flux[OBGC_MAX_GAS_CONDITIONS];
     double* H[OBGC_MAX_GAS_CONDITIONS];
+    int* status;   // OBGC_FLAG_NOT_CONVERGED is set here when a pCO2 solve ends unconverged (NULL: none)
 };
 
 }  // namespace obgc

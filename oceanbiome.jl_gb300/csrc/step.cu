@@ -39,7 +39,10 @@ bool drift_speed(const obgc_npd_params* p, int name, double* w0);
 void drift_profile(double w0, int open_bottom, int Nz, double* w);
 
 // ----------------------------------------------------------------------------- small kernels
-__global__ void set_time_kernel(double* t, double v) { *t = v; }
+__global__ void set_time_kernel(double* t, double v, int* status) {
+    *t = v;
+    if (status) *status = 0;
+}
 __global__ void advance_time_kernel(double* t, double dt) { *t += dt; }
 
 // Thomas factors of the vertically implicit diffusion for the three RK3 stages (the same in every
@@ -222,6 +225,9 @@ struct obgc_ctx {
     void* sed_storage = nullptr;
     void* sed_G = nullptr;
     double* d_time = nullptr;
+    int* d_status = nullptr;            // OBGC_FLAG_* of the current call (device)
+    int* h_status = nullptr;            // its copy behind the call's last kernel (pinned host)
+    bool status_check = true;           // obgc_step waits and returns the status
     DD* partial = nullptr;
     int n_partial = 0;
     double* d_budget = nullptr;
@@ -251,6 +257,8 @@ static int ctx_free(obgc_ctx* c) {
     }
     if (c->drift) cudaFree(c->drift);
     if (c->d_time) cudaFree(c->d_time);
+    if (c->d_status) cudaFree(c->d_status);
+    if (c->h_status) cudaFreeHost(c->h_status);
     if (c->partial) cudaFree(c->partial);
     if (c->d_budget) cudaFree(c->d_budget);
     for (auto& gc : c->gas) {
@@ -354,6 +362,12 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
     }
     alloc(&c->drift, c->tc * prof.size());
     alloc((void**)&c->d_time, sizeof(double));
+    alloc((void**)&c->d_status, sizeof(int));
+    if (rc == OBGC_OK) {
+        cudaError_t e = cudaHostAlloc((void**)&c->h_status, sizeof(int), cudaHostAllocDefault);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaHostAlloc(status)");
+        else *c->h_status = 0;
+    }
     c->n_partial = 4 * 152;
     alloc((void**)&c->partial, sizeof(DD) * c->n_partial);
     alloc((void**)&c->d_budget, sizeof(double));
@@ -659,6 +673,7 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.surf_value = TC(c->desc.surface.value);
     a.surf_field = (const TS*)c->desc.surface.field;
     a.d_time = c->d_time;
+    a.status = c->d_status;
     a.neg = c->neg;        // the modifier after every substep, fused into the substep's update
     a.kh_dx = g.topology_x == OBGC_FLAT ? TC(0) : TC(c->kappa_h * g.Nx / g.Lx);
     a.kh_dy = g.topology_y == OBGC_FLAT ? TC(0) : TC(c->kappa_h * g.Ny / g.Ly);
@@ -756,6 +771,7 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
             {
                 GasMulti gm;
                 std::memset(&gm, 0, sizeof(gm));
+                gm.status = c->d_status;
                 const obgc_carbon_options* first = nullptr;
                 for (const auto& gc : c->gas) {
                     if (!gc.on) continue;
@@ -877,10 +893,11 @@ extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void*
         }
     }
     OBGC_CUDA(cudaEventRecord(c->ev_begin, st));
-    set_time_kernel<<<1, 1, 0, st>>>(c->d_time, t);
+    set_time_kernel<<<1, 1, 0, st>>>(c->d_time, t, c->d_status);
     OBGC_LAUNCHED("set_time_kernel");
     int rc = dispatch_steps(c, dt, nsteps, st, c->profile);
     if (rc != OBGC_OK) return rc;
+    OBGC_CUDA(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     OBGC_CUDA(cudaEventRecord(c->ev_end, st));
     c->last_launches = launches_per_call(c, nsteps);
     if (c->profile) {
@@ -896,7 +913,7 @@ extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void*
         }
         c->last_substep_ms = sub;
     }
-    return OBGC_OK;
+    return c->status_check ? obgc_step_status(c, nullptr) : OBGC_OK;
 }
 
 extern "C" int obgc_step_graph(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {
@@ -923,12 +940,30 @@ extern "C" int obgc_step_graph(obgc_ctx* c, double t, double dt, int32_t nsteps,
         c->graph_version = c->bind_version;
     }
     OBGC_CUDA(cudaEventRecord(c->ev_begin, st));
-    set_time_kernel<<<1, 1, 0, st>>>(c->d_time, t);
+    set_time_kernel<<<1, 1, 0, st>>>(c->d_time, t, c->d_status);
     OBGC_LAUNCHED("set_time_kernel");
     OBGC_CUDA(cudaGraphLaunch(c->graph, st));
     count_launches(launches_per_call(c, nsteps) - 1);
+    OBGC_CUDA(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     OBGC_CUDA(cudaEventRecord(c->ev_end, st));
     c->last_launches = launches_per_call(c, nsteps);
+    return OBGC_OK;
+}
+
+extern "C" int obgc_step_status(obgc_ctx* c, int32_t* flags) {
+    if (!c || !c->h_status) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_step_status: no context");
+    OBGC_CUDA(cudaEventSynchronize(c->ev_end));
+    const int f = *c->h_status;
+    if (flags) *flags = f;
+    if (f & OBGC_FLAG_NAN) return fail(OBGC_ERR_NAN, "obgc_step: a substep wrote a NaN or an infinity into the state");
+    if (f & OBGC_FLAG_NOT_CONVERGED)
+        return fail(OBGC_ERR_NOT_CONVERGED, "obgc_step: a surface pCO2 solve of the gas exchange did not converge");
+    return OBGC_OK;
+}
+
+extern "C" int obgc_set_status_check(obgc_ctx* c, int32_t on) {
+    if (!c) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_status_check: no context");
+    c->status_check = on != 0;
     return OBGC_OK;
 }
 

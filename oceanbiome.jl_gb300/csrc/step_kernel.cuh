@@ -102,6 +102,7 @@ struct SubstepArgs {
     TC surf_value;            // OBGC_SURFACE_PAR_CONSTANT value
     const TS* surf_field;     // OBGC_SURFACE_PAR_FIELD
     const double* d_time;     // step start time (device), OBGC_SURFACE_PAR_DEFAULT
+    int* status;              // OBGC_FLAG_NAN is set here when a stored value is not finite (NULL: no check)
     double c_stage, dt_d;
     TC dt, gamma, zeta;
     int first_stage, write_G;
@@ -323,6 +324,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
         else PAR0 = a.surf_value;
     }
 
+    bool bad = false;   // a non-finite value was stored by this thread
     for (int item = blockIdx.x; item < a.n_items; item += gridDim.x) {
         const int seg = item % a.nseg;                       // top segment first
         const int tile = item / a.nseg;
@@ -630,19 +632,26 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                         Un = a.dt * (a.gamma * Gt + a.zeta * Gm);
                     }
                     // accumulate in the storage precision (FP64 for the mixed path)
-                    if constexpr (sizeof(TS) == sizeof(TC)) a.out[t][idx] = c[t] + Un;
-                    else a.out[t][idx] = TS(__ldg(a.in[t] + idx)) + TS(Un);
+                    TS Uo;
+                    if constexpr (sizeof(TS) == sizeof(TC)) Uo = c[t] + Un;
+                    else Uo = TS(__ldg(a.in[t] + idx)) + TS(Un);
+                    a.out[t][idx] = Uo;
+                    bad |= !(fabs(Uo) <= TS(INFINITY));
                     if (a.write_G) a.G[t][idx] = Gt;
                 }
             }
             // ScaleNegativeTracers / ZeroNegativeTracers on the values this thread just stored,
             // the update_state! that follows the substep (negative_tracers.jl:136-276)
             if constexpr (EXT) {
-                if (a.neg.mode != OBGC_NEGATIVES_NONE && active)
+                if (a.neg.mode != OBGC_NEGATIVES_NONE && active) {
                     negatives_cell<TS>(a.neg, [&](int q) -> TS& { return a.out[q][idx]; });
+#pragma unroll 1
+                    for (int t = 0; t < NT; t++) bad |= !(fabs(a.out[t][idx]) <= TS(INFINITY));
+                }
             }
         }
     }
+    if (bad && a.status) atomicOr(a.status, OBGC_FLAG_NAN);
 }
 
 }  // namespace obgc

@@ -12,6 +12,7 @@ LIB_PATH = os.path.join(_HERE, "libobgc.so")
 
 # ----------------------------------------------------------------------------- enums
 OBGC_OK = 0
+ERR_NOT_CONVERGED, ERR_NAN = 3, 4
 STATUS_NAMES = {
     0: "OBGC_OK", 1: "OBGC_ERR_INVALID_ARGUMENT", 2: "OBGC_ERR_CUDA", 3: "OBGC_ERR_NOT_CONVERGED",
     4: "OBGC_ERR_NAN", 5: "OBGC_ERR_UNSUPPORTED", 6: "OBGC_ERR_OUT_OF_MEMORY",
@@ -48,6 +49,7 @@ PRESET_LOBSTER, PRESET_NPZD = 0, 1
 SURFACE_DEFAULT, SURFACE_CONSTANT, SURFACE_FIELD = 0, 1, 2
 PERIODIC, BOUNDED, FLAT = 0, 1, 2
 ADVECTION_NONE, ADVECTION_WENO5 = 0, 1
+FLAG_NAN, FLAG_NOT_CONVERGED = 1, 2     # enum obgc_step_flags
 OUT_FCO2, OUT_PCO2, OUT_PH_FREE, OUT_PH_TOTAL, OUT_PH_SWS, OUT_H, OUT_CARBONATE, OUT_OMEGA = range(8)
 DENSITY_EOS80, DENSITY_CONSTANT, DENSITY_TEOS10_POLYNOMIAL = 0, 1, 2
 
@@ -347,6 +349,8 @@ def load():
     _sig(lib, "obgc_step", C.c_int, VP, D, D, I32, VP)
     _sig(lib, "obgc_step_graph", C.c_int, VP, D, D, I32, VP)
     _sig(lib, "obgc_last_step_timing", C.c_int, VP, P(D), P(D), P(I64))
+    _sig(lib, "obgc_step_status", C.c_int, VP, P(I32))
+    _sig(lib, "obgc_set_status_check", C.c_int, VP, I32)
     _sig(lib, "obgc_tracer_budget", C.c_int, VP, I32, P(D), VP)
     _sig(lib, "obgc_tracer_budget_static", C.c_int, P(Grid), I32, I32, P(VP), P(D), P(D), VP)
     _sig(lib, "obgc_set_profiling", C.c_int, VP, I32)
@@ -403,7 +407,7 @@ EXPORTED = [
     "obgc_multiband_coefficients", "obgc_euphotic_depth", "obgc_carbon_default_options",
     "obgc_carbon_chemistry", "obgc_carbon_chemistry_point", "obgc_create", "obgc_destroy",
     "obgc_bind_fields", "obgc_update_state", "obgc_compute_tendencies", "obgc_step",
-    "obgc_step_graph", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run", "obgc_box_run_drivers",
+    "obgc_step_graph", "obgc_step_status", "obgc_set_status_check", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run", "obgc_box_run_drivers",
     "obgc_set_profiling", "obgc_set_tiling", "obgc_struct_layout", "obgc_tracer_budget_static",
     "obgc_columns_create", "obgc_columns_destroy", "obgc_columns_tracers", "obgc_columns_add",
     "obgc_columns_advance", "obgc_columns_run", "obgc_columns_remaining", "obgc_columns_read", "obgc_columns_remove",

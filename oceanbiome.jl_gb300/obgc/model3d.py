@@ -222,6 +222,17 @@ class NonhydrostaticModel:
                                                 out.ctypes.data_as(P)), "obgc_sediment_storage")
         return out
 
+    def step_status(self):
+        """Waits for the last step call and returns (status, OBGC_FLAG_* word) of its device-side
+        checks: a NaN / infinity written into the state, an unconverged surface pCO2 solve."""
+        flags = C.c_int32(0)
+        rc = self._lib.obgc_step_status(self._ctx, C.byref(flags))
+        return rc, flags.value
+
+    def set_status_check(self, on):
+        """Whether obgc_step waits for its kernels and returns their status (default on)."""
+        A.check(self._lib.obgc_set_status_check(self._ctx, int(on)), "obgc_set_status_check")
+
     def set_tiling(self, levels):
         A.check(self._lib.obgc_set_tiling(self._ctx, int(levels)), "obgc_set_tiling")
 
@@ -265,7 +276,8 @@ def compute_tendencies(model):
 def time_step(model, dt, nsteps=1, graph=False):
     """time_step!(model, Δt): RK3 steps through the fused kernels (a CUDA graph with graph=True)."""
     fn = model._lib.obgc_step_graph if graph else model._lib.obgc_step
-    A.check(fn(model._ctx, model.clock.time, float(dt), int(nsteps), model._stream()),
-            "obgc_step_graph" if graph else "obgc_step")
-    model.clock.time += dt * nsteps
-    model.clock.iteration += nsteps
+    rc = fn(model._ctx, model.clock.time, float(dt), int(nsteps), model._stream())
+    if rc in (A.OBGC_OK, A.ERR_NAN, A.ERR_NOT_CONVERGED):   # the steps ran: the clock moves on
+        model.clock.time += dt * nsteps
+        model.clock.iteration += nsteps
+    A.check(rc, "obgc_step_graph" if graph else "obgc_step")

@@ -101,3 +101,10 @@ def test_new_entry_points_reject_bad_arguments_without_a_device():
     assert lib.obgc_box_run_drivers(C.byref(p), None, 1, C.c_void_p(1), C.byref(d), 0.0, 1.0, 1, 0, None,
                                     A.PREC_F64, None) == 1
     assert "prescribed" in lib.obgc_last_error_message().decode()
+
+
+def test_step_status_entry_points_reject_a_null_context():
+    lib = A.load()
+    flags = C.c_int32(-1)
+    assert lib.obgc_step_status(None, C.byref(flags)) == 1
+    assert lib.obgc_set_status_check(None, 1) == 1
