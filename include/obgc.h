@@ -558,6 +558,30 @@ int obgc_step_graph(obgc_ctx* ctx, double t, double dt, int32_t nsteps, void* st
 enum obgc_step_flags { OBGC_FLAG_NAN = 1, OBGC_FLAG_NOT_CONVERGED = 2 };
 int obgc_step_status(obgc_ctx* ctx, int32_t* flags);
 int obgc_set_status_check(obgc_ctx* ctx, int32_t on);
+/* One RK3 stage (0, 1 or 2) of the step that starts at time t (Oceananigans rk3_substep! followed
+ * by update_state!, as inside obgc_step), from the caller's arrays in[] into out[] (one per slot in
+ * the context's order: the model's tracers, then passive tracers; the bound grid's layout and
+ * strides; in[q] != out[q]).  The context keeps the previous stage's tendencies, so the three
+ * stages of a step run in order on one context.  The entering state is taken as it is (obgc_step
+ * runs the negative-tracer modifier once on its entering state; here the caller's state is
+ * already past update_state!).  This is the form a domain split across GPUs needs: a y slab with
+ * three halo rows on each side (a Periodic-y grid of Ny_slab + 6 rows) exchanges its halos between
+ * stages (obgc_halo_pack / obgc_halo_unpack), as Oceananigans' distributed architecture fills
+ * halos before each tendency computation.  Status as obgc_step (the status word is cleared by
+ * stage 0 and collects the step's three stages). */
+int obgc_substep(obgc_ctx* ctx, double t, double dt, int32_t stage, const void* const* in, void* const* out,
+                 void* stream);
+/* Halo rows of a y slab.  `slab` is the slab's grid: Ny = Ny_slab + 2 * halo rows, rows [halo,
+ * Ny - halo) its own.  pack copies the slab's first `halo` own rows (those its southern neighbour
+ * needs) into `south` and its last `halo` own rows into `north`; unpack writes `south` (the
+ * southern neighbour's `north` buffer) into rows [0, halo) and `north` (the northern neighbour's
+ * `south` buffer) into rows [Ny - halo, Ny).  Buffers: dense [n_fields][Nz][halo][Nx] of dtype.
+ * n_fields <= 32.  No counterpart in the reference (Oceananigans' fill_halo_regions! over MPI
+ * plays this part); the exchange of the buffers between ranks is the caller's (NCCL send/recv). */
+int obgc_halo_pack(const obgc_grid* slab, int32_t dtype, int32_t n_fields, const void* const* fields, int32_t halo,
+                   void* south, void* north, void* stream);
+int obgc_halo_unpack(const obgc_grid* slab, int32_t dtype, int32_t n_fields, void* const* fields, int32_t halo,
+                     const void* south, const void* north, void* stream);
 /* Device kernel time of the last obgc_step / obgc_step_graph measured with CUDA events on the
  * launching stream (ms); with profiling on, also the summed duration of the fused substep kernel
  * launches (event pairs around each launch).  launches: kernels the call enqueued. */

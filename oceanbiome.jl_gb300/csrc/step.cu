@@ -713,136 +713,175 @@ static void launch_terms(const obgc_ctx* c, SubstepArgs<TS, TC>& a, int b, int n
         }
 }
 
-// Enqueue nsteps steps on stream st (no synchronisation).  The state ping-pongs between the bound
-// arrays and the context's scratch buffers; after an odd number of substeps the interior is copied
-// back so the bound arrays always hold the result.  Per RK3 stage: the gas-exchange flux of every
-// condition, the main launch (the model's tracers, T and S), then the passive launches (their BGC
-// tendency, if any, is the main launch's DIC / Alk tendency of the same stage).
+// Launch arguments of a context's steps of size dt: the main launch (a) and the passive launches
+// (ap: no drift, no sediment, ZeroNegativeTracers only).
 template <typename TS, typename TC>
-static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nsteps, cudaStream_t st, bool profile) {
-    SubstepArgs<TS, TC> a;
+struct StepPlan {
+    SubstepArgs<TS, TC> a, ap;
+    const FusedEntry* fe = nullptr;
+    const FusedEntry* pe[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool impl = false;        // VerticallyImplicitTimeDiscretization with a vertical diffusivity
+    double inv_dz2 = 0.0;
+    int blocks = 0;
+};
+
+template <typename TS, typename TC>
+static int plan_steps(obgc_ctx* c, const FusedEntry* fe, double dt, StepPlan<TS, TC>& p) {
+    SubstepArgs<TS, TC>& a = p.a;
     fill_args<TS, TC>(c, a);
     a.dt_d = dt;
     a.dt = TC(dt);
     a.bgc_out[0] = (TC*)c->bgc_out[0];
     a.bgc_out[1] = (TC*)c->bgc_out[1];
-    // the passive launches: no drift, no sediment, ZeroNegativeTracers only
-    SubstepArgs<TS, TC> ap = a;
-    ap.drift_mask = 0;
-    ap.sed_recv1 = 0;
-    ap.sed_sink_mask = 0;
-    ap.bgc_out[0] = ap.bgc_out[1] = nullptr;
-    const FusedEntry* pe[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    p.ap = a;
+    p.ap.drift_mask = 0;
+    p.ap.sed_recv1 = 0;
+    p.ap.sed_sink_mask = 0;
+    p.ap.bgc_out[0] = p.ap.bgc_out[1] = nullptr;
+    p.fe = fe;
     for (int q = 0; q < c->nchunk; q++) {
-        pe[c->pchunk[q]] = find_fused(c->prec, V_EXTERNAL, c->pchunk[q]);
-        if (!pe[c->pchunk[q]]) return fail(OBGC_ERR_UNSUPPORTED, "obgc_step: no passive-tracer kernel for this precision");
+        p.pe[c->pchunk[q]] = find_fused(c->prec, V_EXTERNAL, c->pchunk[q]);
+        if (!p.pe[c->pchunk[q]]) return fail(OBGC_ERR_UNSUPPORTED, "obgc_step: no passive-tracer kernel for this precision");
     }
+    // VerticallyImplicitTimeDiscretization: after every stage an implicit solve of every column and
+    // slot, followed by the negative-tracer modifier (which the substep then must not fuse: it acts
+    // on the diffused state)
+    const obgc_grid& gz = c->desc.grid;
+    p.impl = c->vimplicit && c->kzf;
+    p.inv_dz2 = (double)gz.Nz * gz.Nz / (gz.Lz * gz.Lz);
+    if (p.impl) a.neg.mode = OBGC_NEGATIVES_NONE;
+    p.blocks = c->blocks < a.n_items ? c->blocks : a.n_items;
+    return OBGC_OK;
+}
+
+// The Thomas factors of the implicit vertical diffusion for steps of this dt (when it is on).
+template <typename TS, typename TC>
+static int launch_thomas(obgc_ctx* c, const StepPlan<TS, TC>& p, double dt, cudaStream_t st) {
+    if (!p.impl) return OBGC_OK;
+    thomas_factors_kernel<<<1, 32, 0, st>>>(c->kzf, c->desc.grid.Nz, p.inv_dz2, dt, c->thomas);
+    OBGC_LAUNCHED("thomas_factors_kernel");
+    return OBGC_OK;
+}
+
+// RK3 stage `stg` from the slot arrays cur[] into nxt[]: the gas-exchange flux of every condition,
+// the main launch (the model's tracers, T and S), the passive launches (their BGC tendency, if any,
+// is the main launch's DIC / Alk tendency of the same stage), then the implicit vertical solve.
+template <typename TS, typename TC>
+static int enqueue_stage(obgc_ctx* c, StepPlan<TS, TC>& p, int stg, void* const* cur, void* const* nxt, cudaStream_t st,
+                         bool profile, size_t& ev) {
+    SubstepArgs<TS, TC>& a = p.a;
+    SubstepArgs<TS, TC>& ap = p.ap;
+    const int NS = c->NT + c->NP;
+    const obgc_grid& grid = c->desc.grid;
+    // every gas-exchange condition in one launch (CO2 conditions with the first one's
+    // carbon-chemistry options share the column's T/S constants)
+    {
+        GasMulti gm;
+        std::memset(&gm, 0, sizeof(gm));
+        gm.status = c->d_status;
+        const obgc_carbon_options* first = nullptr;
+        for (const auto& gc : c->gas) {
+            if (!gc.on) continue;
+            const int q = gm.n++;
+            gm.g[q] = gc.g;
+            gm.flux[q] = gc.flux;
+            gm.H[q] = gc.H;
+            if (gc.g.gas == OBGC_GAS_CO2) {
+                gm.DIC[q] = cur[gc.dic];
+                gm.Alk[q] = cur[gc.alk];
+                if (!first) first = &gc.g.carbon;
+                gm.share[q] = std::memcmp(first, &gc.g.carbon, sizeof(obgc_carbon_options)) == 0;
+            } else {
+                gm.O2[q] = cur[gc.target];
+            }
+        }
+        if (gm.n > 0) {
+            const int rg = launch_gas_exchange_multi<TS>(gm, &grid, cur[slot_named(c, OBGC_T)], cur[slot_named(c, OBGC_S)], st);
+            if (rg != OBGC_OK) return rg;
+        }
+    }
+    for (SubstepArgs<TS, TC>* x : {&a, &ap}) {
+        x->first_stage = stg == 0;
+        x->write_G = stg < 2;
+        x->gamma = TC(rk3_gamma(stg));
+        x->zeta = TC(rk3_zeta(stg));
+        x->c_stage = rk3_c(stg);
+    }
+    for (int t = 0; t < c->NT; t++) { a.in[t] = (const TS*)cur[t]; a.out[t] = (TS*)nxt[t]; }
+    launch_terms(c, a, 0, c->NT);
+    if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
+    int rc = p.fe->launch(&a, p.blocks, st);
+    if (rc != OBGC_OK) return rc;
+    for (int q = 0, b = c->NT; q < c->nchunk; b += c->pchunk[q++]) {
+        const int n = c->pchunk[q];
+        for (int t = 0; t < MAX_NT; t++) { ap.in[t] = nullptr; ap.out[t] = nullptr; ap.G[t] = nullptr; ap.ext[t] = nullptr; }
+        for (int t = 0; t < n; t++) {
+            ap.in[t] = (const TS*)cur[b + t];
+            ap.out[t] = (TS*)nxt[b + t];
+            ap.G[t] = (TC*)c->G[b + t];
+            const int src = c->psrc[b + t - c->NT];
+            ap.ext[t] = src < 0 ? nullptr : (const TC*)c->bgc_out[src == OBGC_ALK];
+        }
+        ap.n_ext = n;
+        ap.neg = c->neg_passive;
+        if (p.impl) ap.neg.mode = OBGC_NEGATIVES_NONE;
+        if (ap.neg.mode != OBGC_NEGATIVES_NONE) {
+            ap.neg.nt = n;
+            ap.neg.zero_skip = (c->neg_passive.zero_skip >> (b - c->NT)) & ((1u << n) - 1u);
+        }
+        launch_terms(c, ap, b, n);
+        const int pb = c->pblocks[n] < ap.n_items ? c->pblocks[n] : ap.n_items;
+        rc = p.pe[n]->launch(&ap, pb, st);
+        if (rc != OBGC_OK) return rc;
+    }
+    if (p.impl) {
+        const obgc_grid& gz = grid;
+        ImplicitFields<TS> F;
+        for (int t = 0; t < NS; t++) F.f[t] = (TS*)nxt[t];
+        const int64_t nthr = (int64_t)gz.Nx * gz.Ny * NS;
+        implicit_vertical_kernel<TS><<<(unsigned)((nthr + 127) / 128), 128, 0, st>>>(
+            F, NS, gz.Nx, gz.Ny, gz.Nz, gz.stride_j, gz.stride_k, c->kzf, p.inv_dz2, a.dt_d, stg, c->thomas);
+        OBGC_LAUNCHED("implicit_vertical_kernel");
+        if (c->neg.mode != OBGC_NEGATIVES_NONE) {
+            rc = launch_negatives(c->neg, sizeof(TS), const_cast<void**>(nxt), grid, st);
+            if (rc == OBGC_OK && c->neg_passive.mode != OBGC_NEGATIVES_NONE)
+                rc = launch_negatives(c->neg_passive, sizeof(TS), const_cast<void**>(nxt) + c->NT, grid, st);
+            if (rc != OBGC_OK) return rc;
+        }
+    }
+    if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
+    return OBGC_OK;
+}
+
+// Enqueue nsteps steps on stream st (no synchronisation).  The state ping-pongs between the bound
+// arrays and the context's scratch buffers; after an odd number of substeps the interior is copied
+// back so the bound arrays always hold the result.
+template <typename TS, typename TC>
+static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nsteps, cudaStream_t st, bool profile) {
+    StepPlan<TS, TC> p;
+    int rc = plan_steps<TS, TC>(c, fe, dt, p);
+    if (rc != OBGC_OK) return rc;
     const int NS = c->NT + c->NP;
     void* cur[MAX_NT];
     void* nxt[MAX_NT];
     for (int t = 0; t < NS; t++) { cur[t] = c->user[t]; nxt[t] = c->scratch[t]; }
     const bool clock = needs_clock(c);
-    // VerticallyImplicitTimeDiscretization: the Thomas factors of this dt, then after every stage an
-    // implicit solve of every column and slot, followed by the negative-tracer modifier (which the
-    // substep then must not fuse: it acts on the diffused state)
-    const obgc_grid& gz = c->desc.grid;
-    const bool impl = c->vimplicit && c->kzf;
-    const double inv_dz2 = (double)gz.Nz * gz.Nz / (gz.Lz * gz.Lz);
-    if (impl) {
-        a.neg.mode = OBGC_NEGATIVES_NONE;
-        thomas_factors_kernel<<<1, 32, 0, st>>>(c->kzf, gz.Nz, inv_dz2, dt, c->thomas);
-        OBGC_LAUNCHED("thomas_factors_kernel");
-    }
-    int blocks = c->blocks < a.n_items ? c->blocks : a.n_items;
+    rc = launch_thomas<TS, TC>(c, p, dt, st);
+    if (rc != OBGC_OK) return rc;
     size_t ev = 0;
     const obgc_grid& grid = c->desc.grid;
     if (c->neg.mode != OBGC_NEGATIVES_NONE) {
         // the state entering the first stage has been through update_state! (iteration 0); applying
         // the modifier again to a state it already produced changes nothing
-        int rc = launch_negatives(c->neg, sizeof(TS), cur, grid, st);
+        rc = launch_negatives(c->neg, sizeof(TS), cur, grid, st);
         if (rc == OBGC_OK && c->neg_passive.mode != OBGC_NEGATIVES_NONE)
             rc = launch_negatives(c->neg_passive, sizeof(TS), cur + c->NT, grid, st);
         if (rc != OBGC_OK) return rc;
     }
     for (int s = 0; s < nsteps; s++) {
         for (int stg = 0; stg < 3; stg++) {
-            // every gas-exchange condition in one launch (CO2 conditions with the first one's
-            // carbon-chemistry options share the column's T/S constants)
-            {
-                GasMulti gm;
-                std::memset(&gm, 0, sizeof(gm));
-                gm.status = c->d_status;
-                const obgc_carbon_options* first = nullptr;
-                for (const auto& gc : c->gas) {
-                    if (!gc.on) continue;
-                    const int q = gm.n++;
-                    gm.g[q] = gc.g;
-                    gm.flux[q] = gc.flux;
-                    gm.H[q] = gc.H;
-                    if (gc.g.gas == OBGC_GAS_CO2) {
-                        gm.DIC[q] = cur[gc.dic];
-                        gm.Alk[q] = cur[gc.alk];
-                        if (!first) first = &gc.g.carbon;
-                        gm.share[q] = std::memcmp(first, &gc.g.carbon, sizeof(obgc_carbon_options)) == 0;
-                    } else {
-                        gm.O2[q] = cur[gc.target];
-                    }
-                }
-                if (gm.n > 0) {
-                    const int rg = launch_gas_exchange_multi<TS>(gm, &grid, cur[slot_named(c, OBGC_T)],
-                                                                 cur[slot_named(c, OBGC_S)], st);
-                    if (rg != OBGC_OK) return rg;
-                }
-            }
-            for (SubstepArgs<TS, TC>* x : {&a, &ap}) {
-                x->first_stage = stg == 0;
-                x->write_G = stg < 2;
-                x->gamma = TC(rk3_gamma(stg));
-                x->zeta = TC(rk3_zeta(stg));
-                x->c_stage = rk3_c(stg);
-            }
-            for (int t = 0; t < c->NT; t++) { a.in[t] = (const TS*)cur[t]; a.out[t] = (TS*)nxt[t]; }
-            launch_terms(c, a, 0, c->NT);
-            if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
-            int rc = fe->launch(&a, blocks, st);
+            rc = enqueue_stage<TS, TC>(c, p, stg, cur, nxt, st, profile, ev);
             if (rc != OBGC_OK) return rc;
-            for (int q = 0, b = c->NT; q < c->nchunk; b += c->pchunk[q++]) {
-                const int n = c->pchunk[q];
-                for (int t = 0; t < MAX_NT; t++) { ap.in[t] = nullptr; ap.out[t] = nullptr; ap.G[t] = nullptr; ap.ext[t] = nullptr; }
-                for (int t = 0; t < n; t++) {
-                    ap.in[t] = (const TS*)cur[b + t];
-                    ap.out[t] = (TS*)nxt[b + t];
-                    ap.G[t] = (TC*)c->G[b + t];
-                    const int src = c->psrc[b + t - c->NT];
-                    ap.ext[t] = src < 0 ? nullptr : (const TC*)c->bgc_out[src == OBGC_ALK];
-                }
-                ap.n_ext = n;
-                ap.neg = c->neg_passive;
-                if (impl) ap.neg.mode = OBGC_NEGATIVES_NONE;
-                if (ap.neg.mode != OBGC_NEGATIVES_NONE) {
-                    ap.neg.nt = n;
-                    ap.neg.zero_skip = (c->neg_passive.zero_skip >> (b - c->NT)) & ((1u << n) - 1u);
-                }
-                launch_terms(c, ap, b, n);
-                const int pb = c->pblocks[n] < ap.n_items ? c->pblocks[n] : ap.n_items;
-                rc = pe[n]->launch(&ap, pb, st);
-                if (rc != OBGC_OK) return rc;
-            }
-            if (impl) {
-                ImplicitFields<TS> F;
-                for (int t = 0; t < NS; t++) F.f[t] = (TS*)nxt[t];
-                const int64_t nthr = (int64_t)gz.Nx * gz.Ny * NS;
-                implicit_vertical_kernel<TS><<<(unsigned)((nthr + 127) / 128), 128, 0, st>>>(
-                    F, NS, gz.Nx, gz.Ny, gz.Nz, gz.stride_j, gz.stride_k, c->kzf, inv_dz2, dt, stg, c->thomas);
-                OBGC_LAUNCHED("implicit_vertical_kernel");
-                if (c->neg.mode != OBGC_NEGATIVES_NONE) {
-                    rc = launch_negatives(c->neg, sizeof(TS), nxt, grid, st);
-                    if (rc == OBGC_OK && c->neg_passive.mode != OBGC_NEGATIVES_NONE)
-                        rc = launch_negatives(c->neg_passive, sizeof(TS), nxt + c->NT, grid, st);
-                    if (rc != OBGC_OK) return rc;
-                }
-            }
-            if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
             for (int t = 0; t < NS; t++) { void* tmp = cur[t]; cur[t] = nxt[t]; nxt[t] = tmp; }
         }
         if (clock) {
@@ -862,12 +901,51 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
     return OBGC_OK;
 }
 
+// One RK3 stage from caller arrays `in` into caller arrays `out` (the bound grid's layout).
+template <typename TS, typename TC>
+static int enqueue_one_stage(obgc_ctx* c, const FusedEntry* fe, double dt, int stage, const void* const* in,
+                             void* const* out, cudaStream_t st) {
+    StepPlan<TS, TC> p;
+    int rc = plan_steps<TS, TC>(c, fe, dt, p);
+    if (rc != OBGC_OK) return rc;
+    rc = launch_thomas<TS, TC>(c, p, dt, st);
+    if (rc != OBGC_OK) return rc;
+    size_t ev = 0;
+    return enqueue_stage<TS, TC>(c, p, stage, const_cast<void* const*>(in), out, st, false, ev);
+}
+
 static int dispatch_steps(obgc_ctx* c, double dt, int nsteps, cudaStream_t st, bool profile) {
     const FusedEntry* fe = c->V >= 0 ? find_fused(c->prec, c->V, c->NT) : nullptr;
     if (!fe) return fail(OBGC_ERR_UNSUPPORTED, "obgc_step: no fused kernel for this model variant / tracer set");
     if (c->prec == OBGC_PREC_F32) return enqueue_steps<float, float>(c, fe, dt, nsteps, st, profile);
     if (c->prec == OBGC_PREC_F64) return enqueue_steps<double, double>(c, fe, dt, nsteps, st, profile);
     return enqueue_steps<double, float>(c, fe, dt, nsteps, st, profile);
+}
+
+extern "C" int obgc_substep(obgc_ctx* c, double t, double dt, int32_t stage, const void* const* in, void* const* out,
+                            void* stream) {
+    if (!c || !c->bound) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_substep: context not bound");
+    if (stage < 0 || stage > 2 || !(dt > 0) || !in || !out)
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_substep: bad stage, dt or field arrays");
+    const int NS = c->NT + c->NP;
+    for (int q = 0; q < NS; q++)
+        if (!in[q] || !out[q] || in[q] == out[q])
+            return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_substep: every slot needs distinct input and output arrays");
+    const FusedEntry* fe = c->V >= 0 ? find_fused(c->prec, c->V, c->NT) : nullptr;
+    if (!fe) return fail(OBGC_ERR_UNSUPPORTED, "obgc_substep: no fused kernel for this model variant / tracer set");
+    cudaStream_t st = (cudaStream_t)stream;
+    OBGC_CUDA(cudaEventRecord(c->ev_begin, st));
+    // the step's start time; the status word is cleared by the first stage and collects all three
+    set_time_kernel<<<1, 1, 0, st>>>(c->d_time, t, stage == 0 ? c->d_status : nullptr);
+    OBGC_LAUNCHED("set_time_kernel");
+    int rc;
+    if (c->prec == OBGC_PREC_F32) rc = enqueue_one_stage<float, float>(c, fe, dt, stage, in, out, st);
+    else if (c->prec == OBGC_PREC_F64) rc = enqueue_one_stage<double, double>(c, fe, dt, stage, in, out, st);
+    else rc = enqueue_one_stage<double, float>(c, fe, dt, stage, in, out, st);
+    if (rc != OBGC_OK) return rc;
+    OBGC_CUDA(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    OBGC_CUDA(cudaEventRecord(c->ev_end, st));
+    return c->status_check ? obgc_step_status(c, nullptr) : OBGC_OK;
 }
 
 static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {

@@ -351,6 +351,9 @@ def load():
     _sig(lib, "obgc_last_step_timing", C.c_int, VP, P(D), P(D), P(I64))
     _sig(lib, "obgc_step_status", C.c_int, VP, P(I32))
     _sig(lib, "obgc_set_status_check", C.c_int, VP, I32)
+    _sig(lib, "obgc_substep", C.c_int, VP, D, D, I32, P(VP), P(VP), VP)
+    _sig(lib, "obgc_halo_pack", C.c_int, P(Grid), I32, I32, P(VP), I32, VP, VP, VP)
+    _sig(lib, "obgc_halo_unpack", C.c_int, P(Grid), I32, I32, P(VP), I32, VP, VP, VP)
     _sig(lib, "obgc_tracer_budget", C.c_int, VP, I32, P(D), VP)
     _sig(lib, "obgc_tracer_budget_static", C.c_int, P(Grid), I32, I32, P(VP), P(D), P(D), VP)
     _sig(lib, "obgc_set_profiling", C.c_int, VP, I32)
@@ -407,7 +410,7 @@ EXPORTED = [
     "obgc_multiband_coefficients", "obgc_euphotic_depth", "obgc_carbon_default_options",
     "obgc_carbon_chemistry", "obgc_carbon_chemistry_point", "obgc_create", "obgc_destroy",
     "obgc_bind_fields", "obgc_update_state", "obgc_compute_tendencies", "obgc_step",
-    "obgc_step_graph", "obgc_step_status", "obgc_set_status_check", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run", "obgc_box_run_drivers",
+    "obgc_step_graph", "obgc_step_status", "obgc_set_status_check", "obgc_substep", "obgc_halo_pack", "obgc_halo_unpack", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run", "obgc_box_run_drivers",
     "obgc_set_profiling", "obgc_set_tiling", "obgc_struct_layout", "obgc_tracer_budget_static",
     "obgc_columns_create", "obgc_columns_destroy", "obgc_columns_tracers", "obgc_columns_add",
     "obgc_columns_advance", "obgc_columns_run", "obgc_columns_remaining", "obgc_columns_read", "obgc_columns_remove",
