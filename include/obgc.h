@@ -780,7 +780,7 @@ typedef struct obgc_pisces_model obgc_pisces_model;
 typedef struct obgc_pisces_model_desc {
     obgc_pisces_params pisces;
     obgc_grid grid;
-    int32_t precision;           /* OBGC_PREC_F32 or OBGC_PREC_MIXED                          */
+    int32_t precision;           /* OBGC_PREC_F32, OBGC_PREC_MIXED or OBGC_PREC_F64 (plain FP64) */
     int32_t advection;           /* enum obgc_advection                                        */
     int32_t nbands;              /* MultiBand bands: 3 (PISCES reads PAR₁, PAR₂, PAR₃)           */
     int32_t negatives;           /* OBGC_NEGATIVES_NONE or _SCALE (conserved_tracers(::PISCES)) */
@@ -802,7 +802,7 @@ enum obgc_pisces_model_field {
 int obgc_pisces_model_create(const obgc_pisces_model_desc* desc, obgc_pisces_model** out);
 int obgc_pisces_model_destroy(obgc_pisces_model* m);
 /* tracers: OBGC_PIS_NUM device fields with the grid's strides (state precision: FP32 for
- * OBGC_PREC_F32, FP64 for OBGC_PREC_MIXED); u, v as for obgc_bind_fields, or NULL. */
+ * OBGC_PREC_F32, FP64 for OBGC_PREC_MIXED and OBGC_PREC_F64); u, v as for obgc_bind_fields, or NULL. */
 int obgc_pisces_model_bind(obgc_pisces_model* m, void* const* tracers, const void* u, const void* v);
 int obgc_pisces_model_update_state(obgc_pisces_model* m, double t, void* stream);
 int obgc_pisces_model_step(obgc_pisces_model* m, double t, double dt, int32_t nsteps, void* stream);

@@ -170,8 +170,9 @@ int update_state(obgc_pisces_model* m, double t, cudaStream_t st) {
     chl_sum_kernel<TS><<<blocks, 256, 0, st>>>(PChl, DChl, static_cast<TS*>(m->chl), g.Nx, g.Ny, g.Nz, g.stride_j, g.stride_k);
     OBGC_LAUNCHED("chl_sum_kernel");
     void* bands[4] = {m->par[1], m->par[2], m->par[3], nullptr};
-    // light in FP32 arithmetic for both precisions (FP64 fields for the mixed path)
-    int rc = m->ts == 4 ? obgc_multiband_par(m->desc.nbands, m->desc.kw, m->desc.e, m->desc.chi, m->desc.division,
+    // light in FP32 arithmetic for the FP32 and mixed paths (FP64 fields for the mixed path), FP64
+    // for the plain FP64 path
+    int rc = (m->ts == 4 || m->desc.precision == OBGC_PREC_F64) ? obgc_multiband_par(m->desc.nbands, m->desc.kw, m->desc.e, m->desc.chi, m->desc.division,
                                              &m->desc.surface, &g, state_dtype(m), m->chl, bands, m->par[0], t, st)
                         : multiband_par_mixed(m->desc.nbands, m->desc.kw, m->desc.e, m->desc.chi, m->desc.division,
                                               &m->desc.surface, &g, m->chl, bands, m->par[0], t, st);
@@ -353,7 +354,7 @@ int build_profiles(obgc_pisces_model* m) {
 extern "C" int obgc_pisces_model_create(const obgc_pisces_model_desc* d, obgc_pisces_model** out) {
     if (!d || !out) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_pisces_model_create: null argument");
     *out = nullptr;
-    if (!valid_grid(&d->grid) || (d->precision != OBGC_PREC_F32 && d->precision != OBGC_PREC_MIXED) || d->nbands != 3 || (d->negatives != OBGC_NEGATIVES_NONE && d->negatives != OBGC_NEGATIVES_SCALE) ||
+    if (!valid_grid(&d->grid) || (d->precision < OBGC_PREC_F32 || d->precision > OBGC_PREC_MIXED) || d->nbands != 3 || (d->negatives != OBGC_NEGATIVES_NONE && d->negatives != OBGC_NEGATIVES_SCALE) ||
         (d->surface.kind != OBGC_SURFACE_PAR_DEFAULT && d->surface.kind != OBGC_SURFACE_PAR_CONSTANT) || !(d->mean_kappa > 0))
         return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_pisces_model_create: bad descriptor");
     double sum = 0;
@@ -362,7 +363,7 @@ extern "C" int obgc_pisces_model_create(const obgc_pisces_model_desc* d, obgc_pi
     obgc_pisces_model* m = new obgc_pisces_model();
     m->desc = *d;
     m->ts = d->precision == OBGC_PREC_F32 ? 4 : 8;
-    m->tc = 4;
+    m->tc = d->precision == OBGC_PREC_F64 ? 8 : 4;
     const obgc_grid& g = d->grid;
     m->extent = g.stride_k * (int64_t)g.Nz;
     const int64_t xy = (int64_t)g.Nx * g.Ny;
@@ -388,7 +389,9 @@ extern "C" int obgc_pisces_model_create(const obgc_pisces_model_desc* d, obgc_pi
     alloc(&m->wprof, m->ts * 2 * (size_t)(g.Nz + 1));
     if (rc == OBGC_OK && cudaMemset(m->H, 0, sizeof(double) * (size_t)xy * g.Nz) != cudaSuccess)
         rc = fail(OBGC_ERR_CUDA, "cudaMemset(H)");
-    if (rc == OBGC_OK) rc = m->ts == 4 ? build_profiles<float, float>(m) : build_profiles<double, float>(m);
+    if (rc == OBGC_OK)
+        rc = m->ts == 4 ? build_profiles<float, float>(m)
+                        : m->tc == 8 ? build_profiles<double, double>(m) : build_profiles<double, float>(m);
     m->neg = pisces_negatives_spec(d->pisces, d->invalid_fill_value);
     int dev = 0, nsm = 152;
     cudaGetDevice(&dev);
@@ -423,7 +426,8 @@ extern "C" int obgc_pisces_model_step(obgc_pisces_model* m, double t, double dt,
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     m->ev_used = 0;
     m->in_step = true;
-    const int rc = m->ts == 4 ? enqueue<float, float>(m, t, dt, nsteps, st) : enqueue<double, float>(m, t, dt, nsteps, st);
+    const int rc = m->ts == 4 ? enqueue<float, float>(m, t, dt, nsteps, st)
+                   : m->tc == 8 ? enqueue<double, double>(m, t, dt, nsteps, st) : enqueue<double, float>(m, t, dt, nsteps, st);
     m->in_step = false;
     if (rc != OBGC_OK) m->ev_used = 0;
     return rc;

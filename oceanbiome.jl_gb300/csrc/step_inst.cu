@@ -26,7 +26,7 @@ typedef float TC_;
 
 constexpr int V_ = OBGC_INST_V;
 // tracer counts with a kernel: the BGC tracers alone, and followed by the carried T/S.  The
-// external-tendency variant serves the PISCES groups of 9 and 8 of its 26 slots (FP32 and mixed)
+// external-tendency variant serves the PISCES groups of 9 and 8 of its 26 slots (every precision)
 // and the passive tracers of every model (CarbonateSystem replicates included) in launches of 4,
 // 2 and 1 tracers.
 [[maybe_unused]] constexpr int NT_A = V_ == V_EXTERNAL ? 9 : n_bgc(V_);
@@ -46,10 +46,8 @@ struct Registrar {
         register_fused({OBGC_INST_PREC, V_, 2, &launch_fn<2>, &occupancy_fn<2>});
         register_fused({OBGC_INST_PREC, V_, 4, &launch_fn<4>, &occupancy_fn<4>});
 #endif
-#if !(OBGC_INST_V == 5 && OBGC_INST_PREC == 1)   // the PISCES model steps in FP32 and mixed precision
         register_fused({OBGC_INST_PREC, V_, NT_A, &launch_fn<NT_A>, &occupancy_fn<NT_A>});
         if (NT_B != NT_A) register_fused({OBGC_INST_PREC, V_, NT_B, &launch_fn<NT_B>, &occupancy_fn<NT_B>});
-#endif
     }
 };
 Registrar registrar;

@@ -130,7 +130,7 @@ class PiscesModel:
         d = A.PiscesModelDesc()
         d.pisces = bgc.params
         d.grid = grid.c_grid()
-        d.precision = A.PREC_F32 if precision == "f32" else A.PREC_MIXED
+        d.precision = {"f32": A.PREC_F32, "mixed": A.PREC_MIXED, "f64": A.PREC_F64}[precision]
         d.advection = A.ADVECTION_WENO5 if advection else A.ADVECTION_NONE
         d.nbands = len(self.light.kw)
         d.negatives = A.NEGATIVES_SCALE if bgc.scale_negatives else A.NEGATIVES_NONE
