@@ -889,8 +889,10 @@ int obgc_columns_remaining(const obgc_columns* eng, int64_t slot, int32_t* steps
 /* Copy a slot's state to host [n_tracers][Nz] FP64 (synchronises the engine's last stream). */
 int obgc_columns_read(obgc_columns* eng, int64_t slot, double* state);
 int obgc_columns_remove(obgc_columns* eng, int64_t slot);
-/* Time a few candidate (threads, pack cells) shapes on the live columns (state restored
- * afterwards) and keep the fastest; writes the choice to *threads / *pack_cells. */
+/* Autotune the launch shape on the live columns: time `steps` steps of candidate (threads, pack
+ * cells) pairs (the pack size at 256 threads, then the block size at the best pack size, then the
+ * neighbouring pack sizes; each from the same state, which is restored afterwards) and keep the
+ * fastest; writes the choice to *threads / *pack_cells. */
 int obgc_columns_autotune(obgc_columns* eng, int32_t steps, int32_t* threads, int32_t* pack_cells,
                           void* stream);
 

@@ -767,41 +767,71 @@ extern "C" int obgc_columns_remove(obgc_columns* e, int64_t slot) {
     return OBGC_OK;
 }
 
+// Scratch of the autotuner (a copy of the arena's state, two timing events), released on every
+// return path.
+struct TuneScratch {
+    void* saved = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ~TuneScratch() {
+        if (saved) cudaFree(saved);
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+
 extern "C" int obgc_columns_autotune(obgc_columns* e, int32_t steps, int32_t* threads, int32_t* pack_cells, void* stream) {
     if (!e || steps < 1) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_columns_autotune: bad argument");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int rc0 = drain(e);
     if (rc0 != OBGC_OK) return rc0;
     const size_t bytes = e->ts * e->NT * (size_t)e->desc.arena_cells;
-    void* saved = nullptr;
-    OBGC_CUDA(cudaMalloc(&saved, bytes));
-    OBGC_CUDA(cudaMemcpyAsync(saved, e->state, bytes, cudaMemcpyDeviceToDevice, st));
-    const int cand[][2] = {{128, 512}, {256, 512}, {256, 1024}, {512, 1024}, {256, 2048}, {512, 2048}};
-    cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
+    TuneScratch x;
+    OBGC_CUDA(cudaMalloc(&x.saved, bytes));
+    OBGC_CUDA(cudaEventCreate(&x.a));
+    OBGC_CUDA(cudaEventCreate(&x.b));
+    OBGC_CUDA(cudaMemcpyAsync(x.saved, e->state, bytes, cudaMemcpyDeviceToDevice, st));
+    // time `steps` steps of one (threads, pack cap) pair from the saved state (after a warm-up run)
+    auto time_pair = [&](int th, int cap, float* ms) -> int {
+        int rc = advance_with(e, steps, th, cap, st, false);
+        if (rc != OBGC_OK) return rc;
+        OBGC_CUDA(cudaMemcpyAsync(e->state, x.saved, bytes, cudaMemcpyDeviceToDevice, st));
+        OBGC_CUDA(cudaEventRecord(x.a, st));
+        rc = advance_with(e, steps, th, cap, st, false);
+        if (rc != OBGC_OK) return rc;
+        OBGC_CUDA(cudaEventRecord(x.b, st));
+        OBGC_CUDA(cudaEventSynchronize(x.b));
+        OBGC_CUDA(cudaEventElapsedTime(ms, x.a, x.b));
+        OBGC_CUDA(cudaMemcpyAsync(e->state, x.saved, bytes, cudaMemcpyDeviceToDevice, st));
+        return OBGC_OK;
+    };
+    auto usable = [&](int cap) { return cap >= OBGC_COLUMN_MAX_LEVELS && smem_for(e, cap) <= 227 * 1024; };
     float best = 1e30f;
     int bt = e->threads, bc = e->cap;
-    int rc = OBGC_OK;
-    for (const auto& cd : cand) {
-        if (cd[1] < OBGC_COLUMN_MAX_LEVELS || smem_for(e, cd[1]) > 227 * 1024) continue;
-        rc = advance_with(e, steps, cd[0], cd[1], st, false);   // warm
-        if (rc != OBGC_OK) break;
-        cudaEventRecord(a, st);
-        rc = advance_with(e, steps, cd[0], cd[1], st, false);
-        if (rc != OBGC_OK) break;
-        cudaEventRecord(b, st);
-        cudaEventSynchronize(b);
+    auto consider = [&](int th, int cap) -> int {
+        if (!usable(cap)) return OBGC_OK;
         float ms = 0;
-        cudaEventElapsedTime(&ms, a, b);
-        if (ms < best) { best = ms; bt = cd[0]; bc = cd[1]; }
-        OBGC_CUDA(cudaMemcpyAsync(e->state, saved, bytes, cudaMemcpyDeviceToDevice, st));
-    }
-    cudaStreamSynchronize(st);
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    cudaFree(saved);
-    if (rc != OBGC_OK) return rc;
+        const int rc = time_pair(th, cap, &ms);
+        if (rc == OBGC_OK && ms < best) { best = ms; bt = th; bc = cap; }
+        return rc;
+    };
+    // the pack size at 256 threads, then the block size at the best pack size, then the pack sizes
+    // next to the best at that block size
+    const int caps[] = {256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096};
+    const int ths[] = {64, 128, 192, 256, 320, 384, 448, 512};
+    const int ncaps = (int)(sizeof(caps) / sizeof(caps[0]));
+    int rc = OBGC_OK;
+    for (int cap : caps)
+        if ((rc = consider(256, cap)) != OBGC_OK) return rc;
+    const int cap1 = bc;
+    for (int th : ths)
+        if (th != 256 && (rc = consider(th, cap1)) != OBGC_OK) return rc;
+    const int th1 = bt;
+    for (int q = 0; q < ncaps; q++)
+        if (caps[q] == cap1) {
+            if (q > 0 && (rc = consider(th1, caps[q - 1])) != OBGC_OK) return rc;
+            if (q + 1 < ncaps && (rc = consider(th1, caps[q + 1])) != OBGC_OK) return rc;
+        }
+    OBGC_CUDA(cudaStreamSynchronize(st));
     e->threads = bt;
     e->cap = bc;
     if (threads) *threads = bt;
