@@ -330,6 +330,7 @@ def run_gpu(args):
     launches = lib.obgc_kernel_launch_count() - launches0
     ms = ev0.elapsed_time(ev1)
     _, substep_ms, _ = model.last_timing()
+    staging = "tma" if model.staging()[1] else "cp.async"
     model.set_profiling(False)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -399,6 +400,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD if shape == SHAPE else WORKLOAD.replace("256x256x64", "x".join(map(str, shape))),
                        "grid": list(shape), "tracers": N_TRACERS, "dt_s": DT,
                        "precision": prec, "l2": "state (%.0f MB) larger than L2 (129 MB)" % (N_TRACERS * g.N * s / 1e6),
+                       "tile_staging": staging,
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "ms_per_step": e2e_ms, "steps": e2e_steps,

@@ -554,8 +554,10 @@ int obgc_step_graph(obgc_ctx* ctx, double t, double dt, int32_t nsteps, void* st
  *   OBGC_ERR_NOT_CONVERGED when a flag is set, else OBGC_OK; flags (optional) receives the word.
  *   obgc_set_status_check(ctx, 1) (the default) makes obgc_step itself wait for its kernels and
  *   return that status; with 0, obgc_step returns as soon as the work is enqueued.  obgc_step_graph
- *   never waits: call obgc_step_status after it. */
-enum obgc_step_flags { OBGC_FLAG_NAN = 1, OBGC_FLAG_NOT_CONVERGED = 2 };
+ *   never waits: call obgc_step_status after it.
+ * OBGC_FLAG_TIMEOUT (status OBGC_ERR_TIMEOUT) reports a tile copy of the tensor-memory accelerator
+ * that a block stopped waiting for after a bounded number of polls. */
+enum obgc_step_flags { OBGC_FLAG_NAN = 1, OBGC_FLAG_NOT_CONVERGED = 2, OBGC_FLAG_TIMEOUT = 4 };
 int obgc_step_status(obgc_ctx* ctx, int32_t* flags);
 int obgc_set_status_check(obgc_ctx* ctx, int32_t on);
 /* One RK3 stage (0, 1 or 2) of the step that starts at time t (Oceananigans rk3_substep! followed
@@ -587,6 +589,15 @@ int obgc_halo_unpack(const obgc_grid* slab, int32_t dtype, int32_t n_fields, voi
  * launches (event pairs around each launch).  launches: kernels the call enqueued. */
 int obgc_last_step_timing(const obgc_ctx* ctx, double* total_ms, double* substep_ms,
                           int64_t* launches);
+/* How the fused substep stages its tiles.  mode 1 (the default): with the tensor-memory
+ * accelerator when the steps qualify (FP32 state, no passive tracers, no model w, and none of the
+ * optional terms: closure, gas exchange, forcing, fused modifier, sediment, replicates); each step
+ * then runs bound arrays -> two padded context copies -> bound arrays, and the second and third
+ * stages copy every tracer's tile of a level with one tensor copy.  mode 0: per-element cp.async
+ * staging always.  obgc_get_staging reports whether the context has the padded copies and tensor
+ * maps (available) and whether the last obgc_step / obgc_step_graph capture used them. */
+int obgc_set_staging(obgc_ctx* ctx, int32_t mode);
+int obgc_get_staging(const obgc_ctx* ctx, int32_t* available, int32_t* last_used);
 /* Bracket every fused substep launch of obgc_step with CUDA events (off by default). */
 int obgc_set_profiling(obgc_ctx* ctx, int32_t on);
 /* Vertical segment length (levels) of the fused kernel's work items (default: chosen per grid, 8 when the grid has enough tiles to fill the GPU, down to 2). */

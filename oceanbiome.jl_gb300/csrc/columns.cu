@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(512, 1) column_kernel(const __grid_constant__ 
     constexpr int SP = slot_of_P(V);
     constexpr int WA = V == V_NPZD ? 1 : 4, WB = V == V_NPZD ? 4 : 5;
     constexpr int SALK = V == V_NPZD ? -1 : 8, SDIC = V == V_NPZD ? -1 : 7;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const ColPack pk = a.packs[blockIdx.x];
     const int ncol = pk.count, cells = pk.cells, cap = a.cap;
     const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;

@@ -241,6 +241,9 @@ int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t 
     a.flat_x = g.topology_x == OBGC_FLAT || !m->desc.advection;
     a.flat_y = g.topology_y == OBGC_FLAT || !m->desc.advection;
     a.sj = g.stride_j; a.sk = g.stride_k;
+    a.osj = g.stride_j; a.osk = g.stride_k;
+    a.vsj = g.stride_j; a.vsk = g.stride_k;
+    a.gsj = g.stride_j; a.gsk = g.stride_k;
     a.dx = TC(g.Lx / g.Nx); a.dy = TC(g.Ly / g.Ny); a.dz = TC(g.Lz / g.Nz); a.Lz = TC(g.Lz);
     a.inv_dx = TC(g.Nx / g.Lx); a.inv_dy = TC(g.Ny / g.Ly); a.inv_dz = TC(g.Nz / g.Lz);
     a.TZ = g.Nz < 8 ? g.Nz : 8;

@@ -1,5 +1,7 @@
 // step.cu — the 3-D model context: fused RK3 stepping (mode (ii)), the plugin hooks of mode (i)
 // (update_state / compute_tendencies), CUDA-graph replay, and the FP64 compensated tracer budget.
+#include <cudaTypedefs.h>
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -231,6 +233,16 @@ struct obgc_ctx {
     DD* partial = nullptr;
     int n_partial = 0;
     double* d_budget = nullptr;
+    // tensor-memory-accelerator staging (FP32 state, no passive tracers): two padded copies of every
+    // slot (x halo TMA_HX, y halo HALO cells, rows of pad_sj values), the tensor maps of both sets
+    // (device), the staging choice (1: TMA when a launch qualifies, 0: cp.async) and what the last
+    // obgc_step used
+    void* pad[2][MAX_NT] = {};
+    CUtensorMap* d_tmaps = nullptr;
+    int64_t pad_sj = 0, pad_sk = 0;
+    bool tma_ready = false;
+    int staging = 0;
+    bool last_used_tma = false;
     int TZ = 0;                         // levels per work item; 0: chosen per grid (fill_args)
     int blocks = 0;
     bool bound = false;
@@ -258,6 +270,10 @@ static int ctx_free(obgc_ctx* c) {
     if (c->drift) cudaFree(c->drift);
     if (c->d_time) cudaFree(c->d_time);
     if (c->d_status) cudaFree(c->d_status);
+    for (int q = 0; q < 2; q++)
+        for (int t = 0; t < MAX_NT; t++)
+            if (c->pad[q][t]) cudaFree(c->pad[q][t]);
+    if (c->d_tmaps) cudaFree(c->d_tmaps);
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->partial) cudaFree(c->partial);
     if (c->d_budget) cudaFree(c->d_budget);
@@ -276,6 +292,45 @@ static int ctx_free(obgc_ctx* c) {
     if (c->ev_end) cudaEventDestroy(c->ev_end);
     for (auto e : c->prof_events) cudaEventDestroy(e);
     delete c;
+    return OBGC_OK;
+}
+
+// The padded slot copies and their tensor maps (3-D: the padded row, the padded rows, the levels;
+// box TMA_TILE_W x TILE_H x 1 in FP32).  Without the driver's encoder the context keeps cp.async
+// staging (obgc_get_staging reports it).
+static int setup_tma(obgc_ctx* c) {
+    const obgc_grid& g = c->desc.grid;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return OBGC_OK;
+    }
+    auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    const size_t bytes = sizeof(float) * (size_t)c->pad_sk * g.Nz;
+    std::vector<CUtensorMap> maps(2 * MAX_NT);
+    std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
+    for (int s = 0; s < 2; s++)
+        for (int t = 0; t < c->NT; t++) {
+            cudaError_t e = cudaMalloc(&c->pad[s][t], bytes);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(padded slot)");
+            e = cudaMemset(c->pad[s][t], 0, bytes);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(padded slot)");
+            const cuuint64_t dims[3] = {(cuuint64_t)c->pad_sj, (cuuint64_t)(g.Ny + 2 * HALO), (cuuint64_t)g.Nz};
+            const cuuint64_t strides[2] = {(cuuint64_t)c->pad_sj * sizeof(float), (cuuint64_t)c->pad_sk * sizeof(float)};
+            const cuuint32_t box[3] = {(cuuint32_t)TMA_TILE_W, (cuuint32_t)TILE_H, 1};
+            const cuuint32_t es[3] = {1, 1, 1};
+            const CUresult r = encode(&maps[(size_t)s * MAX_NT + t], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, c->pad[s][t], dims,
+                                      strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return fail(OBGC_ERR_CUDA, "cuTensorMapEncodeTiled(padded slot) failed: " + std::to_string((int)r));
+        }
+    cudaError_t e = cudaMalloc(&c->d_tmaps, sizeof(CUtensorMap) * maps.size());
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(tensor maps)");
+    e = cudaMemcpy(c->d_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(tensor maps)");
+    c->tma_ready = true;
     return OBGC_OK;
 }
 
@@ -345,9 +400,17 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
         cudaError_t e = cudaMalloc(p, bytes);
         if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc");
     };
+    // FP32 without passive tracers can stage tiles with the tensor-memory accelerator: the tendency
+    // arrays then use the padded layout
+    const bool tma_capable = c->prec == OBGC_PREC_F32 && c->NP == 0;
+    if (tma_capable) {
+        c->pad_sj = ((int64_t)g.Nx + 2 * TMA_HX + 3) / 4 * 4;
+        c->pad_sk = c->pad_sj * (g.Ny + 2 * HALO);
+    }
+    const int64_t g_extent = std::max<int64_t>(c->extent, c->pad_sk * g.Nz);
     for (int t = 0; t < c->NT + c->NP; t++) {
         alloc(&c->scratch[t], c->ts * c->extent);
-        alloc(&c->G[t], c->tc * c->extent);
+        alloc(&c->G[t], c->tc * g_extent);
     }
     for (int q = 0; q < 2; q++)
         if (need_out[q]) alloc(&c->bgc_out[q], c->tc * c->extent);
@@ -383,6 +446,7 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
     }
     if (rc == OBGC_OK && (cudaEventCreate(&c->ev_begin) != cudaSuccess || cudaEventCreate(&c->ev_end) != cudaSuccess))
         rc = fail(OBGC_ERR_CUDA, "cudaEventCreate");
+    if (rc == OBGC_OK && tma_capable) rc = setup_tma(c);
     // persistent grid size
     if (rc == OBGC_OK) {
         const FusedEntry* fe = c->V >= 0 ? find_fused(c->prec, c->V, c->NT) : nullptr;
@@ -645,6 +709,12 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.flat_x = g.topology_x == OBGC_FLAT || !c->desc.advection;
     a.flat_y = g.topology_y == OBGC_FLAT || !c->desc.advection;
     a.sj = g.stride_j; a.sk = g.stride_k;
+    a.osj = g.stride_j; a.osk = g.stride_k;
+    a.vsj = g.stride_j; a.vsk = g.stride_k;
+    a.gsj = g.stride_j; a.gsk = g.stride_k;
+    a.out_halo = 0;
+    a.tma_layout = 0;
+    a.tmap = nullptr;
     a.dx = TC(g.Lx / g.Nx); a.dy = TC(g.Ly / g.Ny); a.dz = TC(g.Lz / g.Nz); a.Lz = TC(g.Lz);
     a.inv_dx = TC(g.Nx / g.Lx); a.inv_dy = TC(g.Ny / g.Ly); a.inv_dz = TC(g.Nz / g.Lz);
     if (c->TZ > 0) {
@@ -853,6 +923,62 @@ static int enqueue_stage(obgc_ctx* c, StepPlan<TS, TC>& p, int stg, void* const*
     return OBGC_OK;
 }
 
+// Whether the steps can stage tiles with the tensor-memory accelerator: FP32, the lean kernel (no
+// closure, surface flux, forcing, fused modifier, sediment or replicate outputs), no passive
+// tracers, no model w and no implicit vertical solve.
+template <typename TS, typename TC>
+static bool tma_eligible(obgc_ctx* c, const StepPlan<TS, TC>& p) {
+    if (sizeof(TS) != 4 || sizeof(TC) != 4 || !c->tma_ready || c->staging != 1 || c->NP != 0 || p.impl || p.a.w) return false;
+    SubstepArgs<TS, TC> x = p.a;
+    launch_terms(c, x, 0, c->NT);
+    return !substep_needs_ext(x);
+}
+
+// Steps with TMA-staged tiles.  Every step runs bound arrays -> padded set 0 -> padded set 1 ->
+// bound arrays: the first stage stages its tiles from the caller's arrays by cp.async; it and the
+// second stage write the padded sets together with their periodic halo images, so that the second
+// and third stages stage whole tiles with one tensor copy per tracer and level.
+template <typename TS, typename TC>
+static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int nsteps, cudaStream_t st, bool profile) {
+    SubstepArgs<TS, TC>& a = p.a;
+    const obgc_grid& g = c->desc.grid;
+    const int64_t org = TMA_HX + (int64_t)HALO * c->pad_sj;   // the padded arrays' first interior cell
+    launch_terms(c, a, 0, c->NT);
+    a.gsj = c->pad_sj;
+    a.gsk = c->pad_sk;
+    a.tma_layout = 1;
+    const bool clock = needs_clock(c);
+    size_t ev = 0;
+    for (int s = 0; s < nsteps; s++) {
+        for (int stg = 0; stg < 3; stg++) {
+            a.first_stage = stg == 0;
+            a.write_G = stg < 2;
+            a.gamma = TC(rk3_gamma(stg));
+            a.zeta = TC(rk3_zeta(stg));
+            a.c_stage = rk3_c(stg);
+            for (int t = 0; t < c->NT; t++) {
+                a.in[t] = stg == 0 ? (const TS*)c->user[t] : (const TS*)c->pad[stg - 1][t] + org;
+                a.out[t] = stg == 2 ? (TS*)c->user[t] : (TS*)c->pad[stg][t] + org;
+            }
+            a.sj = stg == 0 ? g.stride_j : c->pad_sj;
+            a.sk = stg == 0 ? g.stride_k : c->pad_sk;
+            a.osj = stg == 2 ? g.stride_j : c->pad_sj;
+            a.osk = stg == 2 ? g.stride_k : c->pad_sk;
+            a.out_halo = stg < 2;
+            a.tmap = stg == 0 ? nullptr : c->d_tmaps + (size_t)(stg - 1) * MAX_NT;
+            if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
+            const int rc = p.fe->launch(&a, p.blocks, st);
+            if (rc != OBGC_OK) return rc;
+            if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
+        }
+        if (clock) {
+            advance_time_kernel<<<1, 1, 0, st>>>(c->d_time, dt);
+            OBGC_LAUNCHED("advance_time_kernel");
+        }
+    }
+    return OBGC_OK;
+}
+
 // Enqueue nsteps steps on stream st (no synchronisation).  The state ping-pongs between the bound
 // arrays and the context's scratch buffers; after an odd number of substeps the interior is copied
 // back so the bound arrays always hold the result.
@@ -861,6 +987,8 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
     StepPlan<TS, TC> p;
     int rc = plan_steps<TS, TC>(c, fe, dt, p);
     if (rc != OBGC_OK) return rc;
+    c->last_used_tma = tma_eligible<TS, TC>(c, p);
+    if (c->last_used_tma) return enqueue_steps_tma<TS, TC>(c, p, dt, nsteps, st, profile);
     const int NS = c->NT + c->NP;
     void* cur[MAX_NT];
     void* nxt[MAX_NT];
@@ -948,6 +1076,19 @@ extern "C" int obgc_substep(obgc_ctx* c, double t, double dt, int32_t stage, con
     return c->status_check ? obgc_step_status(c, nullptr) : OBGC_OK;
 }
 
+extern "C" int obgc_set_staging(obgc_ctx* c, int32_t mode) {
+    if (!c || mode < 0 || mode > 1) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_staging: bad argument");
+    c->staging = mode;
+    return OBGC_OK;
+}
+
+extern "C" int obgc_get_staging(const obgc_ctx* c, int32_t* available, int32_t* last_used) {
+    if (!c) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_get_staging: no context");
+    if (available) *available = c->tma_ready ? 1 : 0;
+    if (last_used) *last_used = c->last_used_tma ? 1 : 0;
+    return OBGC_OK;
+}
+
 static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     const bool clock = needs_clock(c);
     const int neg = c->neg.mode == OBGC_NEGATIVES_NONE ? 0 : c->neg_passive.mode != OBGC_NEGATIVES_NONE ? 2 : 1;
@@ -955,7 +1096,7 @@ static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     for (const auto& gc : c->gas) gases = gases || gc.on ? 1 : 0;   // one launch for all conditions
     const bool impl = c->vimplicit && c->kzf;
     const int per_stage = 1 + c->nchunk + gases + (impl ? 1 + neg : 0);
-    return (int64_t)nsteps * (3 * per_stage + (clock ? 1 : 0)) + (nsteps % 2 ? c->NT + c->NP : 0) + 1 + neg + (impl ? 1 : 0);
+    return (int64_t)nsteps * (3 * per_stage + (clock ? 1 : 0)) + (nsteps % 2 && !c->last_used_tma ? c->NT + c->NP : 0) + 1 + neg + (impl ? 1 : 0);
 }
 
 extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {
@@ -1036,6 +1177,8 @@ extern "C" int obgc_step_status(obgc_ctx* c, int32_t* flags) {
     if (f & OBGC_FLAG_NAN) return fail(OBGC_ERR_NAN, "obgc_step: a substep wrote a NaN or an infinity into the state");
     if (f & OBGC_FLAG_NOT_CONVERGED)
         return fail(OBGC_ERR_NOT_CONVERGED, "obgc_step: a surface pCO2 solve of the gas exchange did not converge");
+    if (f & OBGC_FLAG_TIMEOUT)
+        return fail(OBGC_ERR_TIMEOUT, "obgc_step: a block stopped waiting for its tile copies (tensor-memory accelerator)");
     return OBGC_OK;
 }
 

@@ -15,6 +15,7 @@
 // row/column are computed by one warp per tracer, rotating the warp with the tracer index so the
 // extra work is spread evenly.  Blocks loop over work items (persistent grid).
 #pragma once
+#include <cuda.h>
 #include "light_device.cuh"
 #include "negatives.cuh"
 #include "npd_device.cuh"
@@ -53,7 +54,18 @@ template <typename TS, typename TC>
 struct SubstepArgs {
     int Nx, Ny, Nz;
     int periodic_x, periodic_y, flat_x, flat_y;
-    int64_t sj, sk;
+    int64_t sj, sk;           // layout of the input arrays in[] (and of w)
+    int64_t vsj, vsk;         // layout of u and v
+    int64_t osj, osk;         // layout of the output arrays out[]
+    int64_t gsj, gsk;         // layout of the tendency arrays G[] (and ext, bgc_out, frc)
+    // out[] are padded arrays (x halo of TMA_HX, y halo of HALO cells): the update also writes each
+    // value into the halo cells that hold its periodic image, so the next stage can stage whole
+    // tiles of it with the tensor-memory accelerator
+    int out_halo;
+    int tma_layout;           // launch an instantiation of the TMA-staged steps (the layouts above may differ)
+    // tensor maps of in[] (3-D, padded layout, box TMA_TILE_W x TILE_H x 1) in global memory, or
+    // NULL: the tiles are then staged by per-element cp.async
+    const CUtensorMap* tmap;
     TC dx, dy, dz, Lz, inv_dx, inv_dy, inv_dz;
     int TZ, nseg, ntx, nty, n_items;
     const TS* in[MAX_NT];
@@ -180,17 +192,59 @@ __device__ __forceinline__ TC face_velocity(const TS* __restrict__ vel, int64_t 
     return ld<TS, TC>(vel, base + (int64_t)f * s);
 }
 
-template <typename TC, int NT>
-constexpr size_t substep_smem_bytes() {
-    // fx, fy face fluxes, the carried vertical flux and its divergence, and every tracer's tile
-    return sizeof(TC) * NT * (STEP_BY * (STEP_BX + 1) + (STEP_BY + 1) * STEP_BX + 2 * STEP_BX * STEP_BY +
-                              (STEP_BY + 6) * (STEP_BX + 6));
+constexpr int HALO = 3;
+// A tile holds TILE_H rows of the cells x = i0 - 3 .. i0 + 34 that the stencils of a 32 x 8 tile
+// read (38 values).  With TMA staging a row holds x = i0 - 4 .. i0 + 35 (40 values), so that the
+// tensor copy's box starts at x = i0 - 4, a multiple of 4 FP32 values (16 bytes), and x = i0 - 3 sits
+// in column 1.
+constexpr int TILE_H = STEP_BY + 2 * HALO;
+constexpr int TILE_CELLS = (STEP_BX + 2 * HALO) * TILE_H;   // the cells a tile stages
+constexpr int TILE_LOADS = (TILE_CELLS + STEP_BX * STEP_BY - 1) / (STEP_BX * STEP_BY);
+constexpr int TMA_TILE_W = STEP_BX + 8;
+constexpr int TMA_HX = 4;                                   // x halo of the padded arrays
+template <bool SPLIT>
+__host__ __device__ constexpr int tile_w() { return SPLIT ? TMA_TILE_W : STEP_BX + 2 * HALO; }
+template <bool SPLIT>
+__host__ __device__ constexpr int tile_x0() { return SPLIT ? 1 : 0; }
+// shared-memory elements per tracer tile: in the TMA-staged instantiations rounded up to 128 bytes
+// (the alignment of a tensor copy's destination)
+template <typename TC, bool SPLIT>
+__host__ __device__ constexpr int tile_elems() {
+    return SPLIT ? ((TMA_TILE_W * TILE_H * (int)sizeof(TC) + 127) / 128) * 128 / (int)sizeof(TC) : TILE_CELLS;
 }
 
-constexpr int HALO = 3;
-constexpr int TILE_W = STEP_BX + 2 * HALO;
-constexpr int TILE_H = STEP_BY + 2 * HALO;
-constexpr int TILE_LOADS = (TILE_W * TILE_H + STEP_BX * STEP_BY - 1) / (STEP_BX * STEP_BY);
+template <typename TC, int NT, bool SPLIT = false>
+constexpr size_t substep_smem_bytes() {
+    // every tracer's tile (first: 128-byte aligned), the fx, fy face fluxes, and the carried
+    // vertical flux and its divergence
+    return sizeof(TC) * NT * (tile_elems<TC, SPLIT>() + STEP_BY * (STEP_BX + 1) + (STEP_BY + 1) * STEP_BX + 2 * STEP_BX * STEP_BY);
+}
+
+// ---- tensor-memory-accelerator staging: one mbarrier per block, armed by thread 0 with the bytes
+// of every tracer's tile of a level, completed by the tile copies
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arm(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return done != 0;
+}
+// Box (TMA_TILE_W x TILE_H x 1) of a padded array at padded coordinates (x, y, z) into shared memory.
+__device__ __forceinline__ void tma_tile(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar)) : "memory");
+}
+// A wait on the staging mbarrier gives up after this many polls (each poll may suspend the thread
+// for a while): the block then goes on with whatever the tile holds and reports OBGC_FLAG_TIMEOUT.
+constexpr unsigned TMA_MAX_POLLS = 1u << 22;
 
 // Face flux from six tile values s[0], s[st], ..., s[5 st] = c[f-3 .. f+2] of a line of N cells,
 // with the Bounded-wall order reduction of face_flux.
@@ -264,20 +318,31 @@ __host__ __device__ inline bool substep_needs_ext(const SubstepArgs<TS, TC>& a) 
     return any;
 }
 
-template <int V, int NT, typename TS, typename TC, bool EXT>
+// MODE 0: every array in the input layout, tiles staged by cp.async.  MODE 1 and 2 are the
+// instantiations of the TMA-staged steps: input, output and tendency arrays in their own layouts
+// (a.sj/sk, osj/osk, gsj/gsk; u and v in vsj/vsk), 40-wide tile rows, and periodic halo images
+// written when a.out_halo is set; MODE 1 stages its tiles by cp.async (the step's first stage, from
+// the caller's arrays), MODE 2 by tensor copies through a.tmap.
+template <int V, int NT, typename TS, typename TC, bool EXT, int MODE = 0>
 __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <= 12 ? 3 : NT <= 16 ? 2 : 1)
     substep_kernel(const __grid_constant__ SubstepArgs<TS, TC> a) {
+    constexpr bool SPLIT = MODE != 0;
+    constexpr bool TMA = MODE == 2;
+    constexpr int TILE_W = tile_w<SPLIT>();
+    constexpr int TILE_X0 = tile_x0<SPLIT>();
     constexpr int NB = n_bgc(V);
     constexpr int SP = slot_of_P(V);
     constexpr int NTH = STEP_BX * STEP_BY;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TC (*fx)[STEP_BY][STEP_BX + 1] = reinterpret_cast<TC (*)[STEP_BY][STEP_BX + 1]>(smem_raw);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int TILE_SZ = tile_elems<TC, SPLIT>();
+    TC* tiles = reinterpret_cast<TC*>(smem_raw);     // NT tiles of TILE_H rows of TILE_W
+    unsigned char* after_tiles = smem_raw + sizeof(TC) * NT * TILE_SZ;
+    TC (*fx)[STEP_BY][STEP_BX + 1] = reinterpret_cast<TC (*)[STEP_BY][STEP_BX + 1]>(after_tiles);
     TC (*fy)[STEP_BY + 1][STEP_BX] =
-        reinterpret_cast<TC (*)[STEP_BY + 1][STEP_BX]>(smem_raw + sizeof(TC) * NT * STEP_BY * (STEP_BX + 1));
-    TC* fzu = reinterpret_cast<TC*>(smem_raw + sizeof(TC) * NT * (STEP_BY * (STEP_BX + 1) + (STEP_BY + 1) * STEP_BX));
+        reinterpret_cast<TC (*)[STEP_BY + 1][STEP_BX]>(after_tiles + sizeof(TC) * NT * STEP_BY * (STEP_BX + 1));
+    TC* fzu = reinterpret_cast<TC*>(after_tiles + sizeof(TC) * NT * (STEP_BY * (STEP_BX + 1) + (STEP_BY + 1) * STEP_BX));
     TC* vdv = fzu + NT * NTH;
-    TC* tiles = vdv + NT * NTH;     // NT tiles of TILE_H x TILE_W (tile + 3-cell halo)
-    constexpr int TILE_SZ = TILE_H * TILE_W;
+    __shared__ uint64_t stage_bar;   // TMA staging (MODE 2)
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = tx + STEP_BX * ty;
@@ -299,8 +364,30 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     const bool hdiff = EXT && (a.kh_dx != TC(0) || a.kh_dy != TC(0));
     // previous-stage tendencies staged in shared memory (the generic-drift buffer, when unused)
     const bool gm_smem = !any_generic && !a.first_stage;
-    // shared-space address of this thread's first tile element
-    const unsigned tiles_s = (unsigned)__cvta_generic_to_shared(tiles) + 4u * (unsigned)tid;
+    // shared-space address of the tiles
+    const unsigned tiles_s = smem_u32(tiles);
+    unsigned tma_phase = 0;
+    bool tma_timeout = false;
+    if constexpr (TMA) {
+        // a tensor copy's destination must be 128-byte aligned: never issue one to a tile that is not
+        // (the block then does no work and reports OBGC_FLAG_TIMEOUT)
+        if ((tiles_s & 127u) != 0u) {
+            if (tid == 0 && a.status) atomicOr(a.status, OBGC_FLAG_TIMEOUT);
+            return;
+        }
+        if (tid == 0) mbar_init(&stage_bar, 1);
+        __syncthreads();
+    }
+    (void)tma_phase;
+    constexpr unsigned TILE_BYTES = (unsigned)(sizeof(TC) * TMA_TILE_W * TILE_H);
+    // thread 0 arms the barrier and copies every tracer's tile of level kk of the work item at
+    // (i0, j0): padded coordinates x = i0 (x = i0 - 4 of the grid), y = j0 (y = j0 - 3)
+    auto tma_issue = [&](int i0_, int j0_, int kk) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arm(&stage_bar, TILE_BYTES * NT);
+#pragma unroll 1
+        for (int t = 0; t < NT; t++) tma_tile(tiles + t * TILE_SZ, a.tmap + t, i0_, j0_, kk, &stage_bar);
+    };
 
     // forcings switched on at this stage's time
     bool frc_on[MAX_FRC];
@@ -348,12 +435,18 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
         // and tracer of the work item)
         int64_t toff[TILE_LOADS];
 #pragma unroll
-        for (int q = 0; q < TILE_LOADS; q++) {
-            const int e = min(tid + q * NTH, TILE_H * TILE_W - 1);
-            const int r = e / TILE_W, c = e - r * TILE_W;
+        for (int q = 0; q < (TMA ? 0 : TILE_LOADS); q++) {
+            const int e = min(tid + q * NTH, TILE_CELLS - 1);
+            const int r = e / (STEP_BX + 2 * HALO), c = e - r * (STEP_BX + 2 * HALO);
             toff[q] = wrap_or_clamp(i0 - HALO + c, a.Nx, periodic_x) +
                       (int64_t)wrap_or_clamp(j0 - HALO + r, a.Ny, periodic_y) * a.sj;
         }
+        // shared-memory element of staged cell q (dense rows, or 40-wide rows with x = i0 - 3 in
+        // column 1 in the TMA-staged instantiations)
+        auto soff = [&](int q) -> int {
+            const int e = tid + q * NTH;
+            return SPLIT ? e + (TILE_W - (STEP_BX + 2 * HALO)) * (e / (STEP_BX + 2 * HALO)) + TILE_X0 : e;
+        };
 
         // chlorophyll integral of the cells above the segment
         TC Sr = TC(0), Sb = TC(0);
@@ -390,32 +483,50 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 
 #pragma unroll 1
         for (int k = k_top; k >= k_bot; --k) {
-            const int64_t idx = col + (int64_t)k * a.sk;
+            const int64_t idx = col + (int64_t)k * a.sk;                                      // in[]
+            const int64_t gidx = SPLIT ? ic + (int64_t)jc * a.gsj + (int64_t)k * a.gsk : idx;   // G[], EXT fields
             const int64_t kofs = (int64_t)k * a.sk;
             // stage every tracer's tile and halo for this level: all loads in flight together (FP32:
             // asynchronous copies, no registers), and, from the second stage on, the cell's previous
             // tendencies into the generic-drift buffer when no tracer uses it
+            if constexpr (TMA) {
+                // the tiles of this level: issued here at the item's first level, otherwise during
+                // the previous level's update
+                if (tid == 0 && k == k_top) tma_issue(i0, j0, k);
+#pragma unroll 1
+                for (int t = 0; t < NT; t++)
+                    if (gm_smem) cp_async_elem<TC>(vdv + t * NTH + tid, a.G[t] + gidx);
+                if (gm_smem) cp_async_wait_all();
+                unsigned polls = 0;
+                if (!tma_timeout)
+                    while (!mbar_try_wait(&stage_bar, tma_phase & 1u))
+                        if (++polls >= TMA_MAX_POLLS) { tma_timeout = true; break; }
+                tma_phase++;
+            } else {
 #pragma unroll
-            for (int t = 0; t < NT; t++) {
-                const TS* __restrict__ base = a.in[t] + kofs;
-                TC* tl = tiles + t * TILE_SZ;
+                for (int t = 0; t < NT; t++) {
+                    const TS* __restrict__ base = a.in[t] + kofs;
+                    TC* tl = tiles + t * TILE_SZ;
 #pragma unroll
-                for (int q = 0; q < TILE_LOADS; q++)
-                    if (q < TILE_LOADS - 1 || tid + q * NTH < TILE_SZ) {
-                        if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4)
-                            cp_async4_at(tiles_s + 4u * (unsigned)(t * TILE_SZ + q * NTH), base + toff[q]);
-                        else tl[tid + q * NTH] = ld<TS, TC>(base, toff[q]);
-                    }
-                if (gm_smem) cp_async_elem<TC>(vdv + t * NTH + tid, a.G[t] + idx);
+                    for (int q = 0; q < TILE_LOADS; q++)
+                        if (q < TILE_LOADS - 1 || tid + q * NTH < TILE_CELLS) {
+                            if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4)
+                                cp_async4_at(tiles_s + 4u * (unsigned)(t * TILE_SZ + soff(q)), base + toff[q]);
+                            else tl[soff(q)] = ld<TS, TC>(base, toff[q]);
+                        }
+                    if (gm_smem) cp_async_elem<TC>(vdv + t * NTH + tid, a.G[t] + gidx);
+                }
+                if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) cp_async_wait_all();
+                else if (gm_smem) cp_async_wait_all();
             }
-            if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) cp_async_wait_all();
-            else if (gm_smem) cp_async_wait_all();
-            const int64_t rowb = (int64_t)jc * a.sj + kofs;
-            const int64_t cb = ic + kofs;
+            const int64_t vsj = SPLIT ? a.vsj : a.sj;
+            const int64_t vk = (int64_t)k * (SPLIT ? a.vsk : a.sk);
+            const int64_t rowb = (int64_t)jc * vsj + vk;
+            const int64_t cb = ic + vk;
             const bool xok = !a.flat_x && i <= a.Nx && j < a.Ny;
             const bool yok = !a.flat_y && i < a.Nx && j <= a.Ny;
             const TC Ux = xok ? face_velocity<TS, TC>(a.u, rowb, 1, a.Nx, periodic_x, i) : TC(0);
-            const TC Uy = yok ? face_velocity<TS, TC>(a.v, cb, a.sj, a.Ny, periodic_y, j) : TC(0);
+            const TC Uy = yok ? face_velocity<TS, TC>(a.v, cb, vsj, a.Ny, periodic_y, j) : TC(0);
             const bool full5 = (periodic_x || min(i, a.Nx - i) >= 3) && (periodic_y || min(j, a.Ny - j) >= 3);
             __syncthreads();
 
@@ -425,8 +536,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 #pragma unroll 1
             for (int t = 0; t < (row_faces ? NT : 0); t++) {
                 const TC* tl = tiles + t * TILE_SZ;
-                const TC* xs = tl + (ty + HALO) * TILE_W + tx;   // c[i-3 .. i+2] along x
-                const TC* ys = tl + ty * TILE_W + tx + HALO;     // c[j-3 .. j+2] along y
+                const TC* xs = tl + (ty + HALO) * TILE_W + TILE_X0 + tx;   // c[i-3 .. i+2] along x
+                const TC* ys = tl + ty * TILE_W + TILE_X0 + tx + HALO;     // c[j-3 .. j+2] along y
                 TC Fx, Fy;
 #ifdef __CUDA_ARCH__
                 if constexpr (sizeof(TC) == 4) {
@@ -465,8 +576,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 #pragma unroll 1
                 for (int t = 0; t < NT; t++) {
                     const TC* tl = tiles + t * TILE_SZ;
-                    if (xok) fx[t][ty][tx] += tile_diff_flux<TC>(tl + (ty + HALO) * TILE_W + tx, 1, periodic_x, i, a.Nx, a.kh_dx);
-                    if (yok) fy[t][ty][tx] += tile_diff_flux<TC>(tl + ty * TILE_W + tx + HALO, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
+                    if (xok) fx[t][ty][tx] += tile_diff_flux<TC>(tl + (ty + HALO) * TILE_W + TILE_X0 + tx, 1, periodic_x, i, a.Nx, a.kh_dx);
+                    if (yok) fy[t][ty][tx] += tile_diff_flux<TC>(tl + ty * TILE_W + TILE_X0 + tx + HALO, TILE_W, periodic_y, j, a.Ny, a.kh_dy);
                 }
             }
             // the tile's east (8 per tracer) and north (32 per tracer) edge faces, spread over
@@ -480,20 +591,20 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     const int jr = j0 + r, f = i0 + STEP_BX;
                     TC Fe = TC(0);
                     if (!a.flat_x && jr < a.Ny && f <= a.Nx) {
-                        const int64_t rb = (int64_t)jr * a.sj + kofs;
-                        Fe = tile_face_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx,
+                        const int64_t rb = (int64_t)jr * vsj + vk;
+                        Fe = tile_face_flux<TC>(tl + (r + HALO) * TILE_W + TILE_X0 + STEP_BX, 1, periodic_x, f, a.Nx,
                                                 face_velocity<TS, TC>(a.u, rb, 1, a.Nx, periodic_x, f));
-                        if (hdiff) Fe += tile_diff_flux<TC>(tl + (r + HALO) * TILE_W + STEP_BX, 1, periodic_x, f, a.Nx, a.kh_dx);
+                        if (hdiff) Fe += tile_diff_flux<TC>(tl + (r + HALO) * TILE_W + TILE_X0 + STEP_BX, 1, periodic_x, f, a.Nx, a.kh_dx);
                     }
                     fx[t][r][STEP_BX] = Fe;
                 } else {
                     const int cc = r - STEP_BY, ix = i0 + cc, f = j0 + STEP_BY;
                     TC Fe = TC(0);
                     if (!a.flat_y && ix < a.Nx && f <= a.Ny) {
-                        const int64_t cb2 = ix + kofs;
-                        Fe = tile_face_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny,
-                                                face_velocity<TS, TC>(a.v, cb2, a.sj, a.Ny, periodic_y, f));
-                        if (hdiff) Fe += tile_diff_flux<TC>(tl + STEP_BY * TILE_W + cc + HALO, TILE_W, periodic_y, f, a.Ny, a.kh_dy);
+                        const int64_t cb2 = ix + vk;
+                        Fe = tile_face_flux<TC>(tl + STEP_BY * TILE_W + TILE_X0 + cc + HALO, TILE_W, periodic_y, f, a.Ny,
+                                                face_velocity<TS, TC>(a.v, cb2, vsj, a.Ny, periodic_y, f));
+                        if (hdiff) Fe += tile_diff_flux<TC>(tl + STEP_BY * TILE_W + TILE_X0 + cc + HALO, TILE_W, periodic_y, f, a.Ny, a.kh_dy);
                     }
                     fy[t][STEP_BY][cc] = Fe;
                 }
@@ -502,8 +613,11 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             // before the barrier that lets the next level's staging overwrite the tiles
             TC c[NT];
 #pragma unroll
-            for (int t = 0; t < NT; t++) c[t] = tiles[t * TILE_SZ + (ty + HALO) * TILE_W + tx + HALO];
+            for (int t = 0; t < NT; t++) c[t] = tiles[t * TILE_SZ + (ty + HALO) * TILE_W + TILE_X0 + tx + HALO];
             __syncthreads();
+            // the tiles are free again: the next level's copies fly during this level's update
+            if constexpr (TMA)
+                if (tid == 0 && k > k_bot) tma_issue(i0, j0, k - 1);
             if (!row_cells) continue;   // no cell on this row: nothing below reads its registers
 
             // window tracers: flux through the face below this cell, divergence, and slide the
@@ -592,11 +706,19 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 for (int s = 0; s < NB; s++) vals[slot_name(V, s)] = c[s];
                 npd_tendencies<V, TC>(a.bgc, vals, PAR, g);
                 if constexpr (EXT) {
-                    if (active && a.bgc_out[0]) a.bgc_out[0][idx] = g[OBGC_DIC];
-                    if (active && a.bgc_out[1]) a.bgc_out[1][idx] = g[OBGC_ALK];
+                    if (active && a.bgc_out[0]) a.bgc_out[0][gidx] = g[OBGC_DIC];
+                    if (active && a.bgc_out[1]) a.bgc_out[1][gidx] = g[OBGC_ALK];
                 }
             }
 
+            const int64_t oidx = SPLIT ? ic + (int64_t)jc * a.osj + (int64_t)k * a.osk : idx;   // out[]
+            // the periodic images of this cell in a padded output's halo: x = i -/+ Nx for the first
+            // and last TMA_HX columns, y = j -/+ Ny for the first and last HALO rows (none: 0)
+            int img_x = 0, img_y = 0;
+            if (SPLIT && a.out_halo) {
+                if (periodic_x) img_x = i < TMA_HX ? a.Nx : (i >= a.Nx - TMA_HX ? -a.Nx : 0);
+                if (periodic_y) img_y = j < HALO ? a.Ny * (int)a.osj : (j >= a.Ny - HALO ? -a.Ny * (int)a.osj : 0);
+            }
 #pragma unroll
             for (int t = 0; t < NT; t++) {
                 TC adv = TC(0);
@@ -607,7 +729,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 if (t == WB) adv += vdB;
                 TC Gb = TC(0);
                 if constexpr (V == V_EXTERNAL) {
-                    if (t < a.n_ext && a.ext[t] != nullptr) Gb = a.ext[t][idx];
+                    if (t < a.n_ext && a.ext[t] != nullptr) Gb = a.ext[t][gidx];
                 } else {
                     if (t < NB) Gb = g[slot_name(V, t)];
                 }
@@ -621,37 +743,42 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     }
 #pragma unroll
                     for (int q = 0; q < MAX_FRC; q++)
-                        if (frc_on[q] && t + 1 == a.frc_slot1[q] && active) Gt += ld<TS, TC>(a.frc[q], idx);
+                        if (frc_on[q] && t + 1 == a.frc_slot1[q] && active) Gt += ld<TS, TC>(a.frc[q], gidx);
                 }
                 if (active) {
                     TC Un;
                     if (a.first_stage) {
                         Un = a.dt * a.gamma * Gt;
                     } else {
-                        const TC Gm = gm_smem ? vdv[t * NTH + tid] : a.G[t][idx];
+                        const TC Gm = gm_smem ? vdv[t * NTH + tid] : a.G[t][gidx];
                         Un = a.dt * (a.gamma * Gt + a.zeta * Gm);
                     }
                     // accumulate in the storage precision (FP64 for the mixed path)
                     TS Uo;
                     if constexpr (sizeof(TS) == sizeof(TC)) Uo = c[t] + Un;
                     else Uo = TS(__ldg(a.in[t] + idx)) + TS(Un);
-                    a.out[t][idx] = Uo;
+                    a.out[t][oidx] = Uo;
                     bad |= !(fabs(Uo) <= TS(INFINITY));
-                    if (a.write_G) a.G[t][idx] = Gt;
+                    if (SPLIT) {
+                        if (img_x) a.out[t][oidx + img_x] = Uo;
+                        if (img_y) a.out[t][oidx + img_y] = Uo;
+                    }
+                    if (a.write_G) a.G[t][gidx] = Gt;
                 }
             }
             // ScaleNegativeTracers / ZeroNegativeTracers on the values this thread just stored,
             // the update_state! that follows the substep (negative_tracers.jl:136-276)
             if constexpr (EXT) {
                 if (a.neg.mode != OBGC_NEGATIVES_NONE && active) {
-                    negatives_cell<TS>(a.neg, [&](int q) -> TS& { return a.out[q][idx]; });
+                    negatives_cell<TS>(a.neg, [&](int q) -> TS& { return a.out[q][oidx]; });
 #pragma unroll 1
-                    for (int t = 0; t < NT; t++) bad |= !(fabs(a.out[t][idx]) <= TS(INFINITY));
+                    for (int t = 0; t < NT; t++) bad |= !(fabs(a.out[t][oidx]) <= TS(INFINITY));
                 }
             }
         }
     }
     if (bad && a.status) atomicOr(a.status, OBGC_FLAG_NAN);
+    if (tma_timeout && a.status) atomicOr(a.status, OBGC_FLAG_TIMEOUT);
 }
 
 }  // namespace obgc

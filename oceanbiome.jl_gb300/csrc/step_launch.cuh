@@ -6,36 +6,57 @@
 
 namespace obgc {
 
-template <int V, int NT, typename TS, typename TC, bool EXT>
+template <int V, int NT, typename TS, typename TC, bool EXT, int MODE = 0>
 int ensure_configured() {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(substep_kernel<V, NT, TS, TC, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)substep_smem_bytes<TC, NT>());
+        cudaError_t e = cudaFuncSetAttribute(substep_kernel<V, NT, TS, TC, EXT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)substep_smem_bytes<TC, NT, MODE != 0>());
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(substep_kernel)");
         configured = true;
     }
     return OBGC_OK;
 }
 
-// The lean instantiation unless the launch uses an optional term (substep_needs_ext).
+// The lean instantiation unless the launch uses an optional term (substep_needs_ext); for the
+// TMA-staged steps (FP32, lean) MODE 1 (cp.async staging from the caller's arrays) or MODE 2
+// (tensor copies from a padded set).
 template <int V, int NT, typename TS, typename TC>
 int launch_one(const SubstepArgs<TS, TC>& a, int blocks, cudaStream_t st) {
+    const dim3 block(STEP_BX, STEP_BY);
     if (substep_needs_ext(a)) {
+        if (a.tma_layout) return fail(OBGC_ERR_UNSUPPORTED, "substep: TMA staging needs the lean kernel");
         const int rc = ensure_configured<V, NT, TS, TC, true>();
         if (rc != OBGC_OK) return rc;
-        substep_kernel<V, NT, TS, TC, true><<<blocks, dim3(STEP_BX, STEP_BY), substep_smem_bytes<TC, NT>(), st>>>(a);
+        substep_kernel<V, NT, TS, TC, true><<<blocks, block, substep_smem_bytes<TC, NT>(), st>>>(a);
     } else {
-        const int rc = ensure_configured<V, NT, TS, TC, false>();
-        if (rc != OBGC_OK) return rc;
-        substep_kernel<V, NT, TS, TC, false><<<blocks, dim3(STEP_BX, STEP_BY), substep_smem_bytes<TC, NT>(), st>>>(a);
+        bool done = false;
+        if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) {
+            if (a.tma_layout && a.tmap) {
+                const int rc = ensure_configured<V, NT, TS, TC, false, 2>();
+                if (rc != OBGC_OK) return rc;
+                substep_kernel<V, NT, TS, TC, false, 2><<<blocks, block, substep_smem_bytes<TC, NT, true>(), st>>>(a);
+                done = true;
+            } else if (a.tma_layout) {
+                const int rc = ensure_configured<V, NT, TS, TC, false, 1>();
+                if (rc != OBGC_OK) return rc;
+                substep_kernel<V, NT, TS, TC, false, 1><<<blocks, block, substep_smem_bytes<TC, NT, true>(), st>>>(a);
+                done = true;
+            }
+        }
+        if (!done) {
+            if (a.tma_layout) return fail(OBGC_ERR_UNSUPPORTED, "substep: TMA staging needs FP32 state");
+            const int rc = ensure_configured<V, NT, TS, TC, false>();
+            if (rc != OBGC_OK) return rc;
+            substep_kernel<V, NT, TS, TC, false><<<blocks, block, substep_smem_bytes<TC, NT>(), st>>>(a);
+        }
     }
     OBGC_LAUNCHED("substep_kernel");
     return OBGC_OK;
 }
 
-// Blocks per SM (both instantiations share the launch bounds and shared memory; the larger one's
-// figure is the one the persistent grid is sized by).
+// Blocks per SM (the instantiations share the launch bounds; the smallest figure among them is the
+// one the persistent grid is sized by).
 template <int V, int NT, typename TS, typename TC>
 int occupancy_one(int* blocks_per_sm) {
     int rc = ensure_configured<V, NT, TS, TC, true>();
@@ -47,8 +68,22 @@ int occupancy_one(int* blocks_per_sm) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, substep_kernel<V, NT, TS, TC, true>,
                                                       STEP_BX * STEP_BY, substep_smem_bytes<TC, NT>());
-    if (*blocks_per_sm > lean) *blocks_per_sm = lean;
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (*blocks_per_sm > lean) *blocks_per_sm = lean;
+    if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) {
+        rc = ensure_configured<V, NT, TS, TC, false, 1>();
+        if (rc == OBGC_OK) rc = ensure_configured<V, NT, TS, TC, false, 2>();
+        if (rc != OBGC_OK) return rc;
+        int m1 = 0, m2 = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m1, substep_kernel<V, NT, TS, TC, false, 1>,
+                                                          STEP_BX * STEP_BY, substep_smem_bytes<TC, NT, true>());
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m2, substep_kernel<V, NT, TS, TC, false, 2>,
+                                                              STEP_BX * STEP_BY, substep_smem_bytes<TC, NT, true>());
+        if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        if (*blocks_per_sm > m1) *blocks_per_sm = m1;
+        if (*blocks_per_sm > m2) *blocks_per_sm = m2;
+    }
     return OBGC_OK;
 }
 

@@ -49,7 +49,7 @@ PRESET_LOBSTER, PRESET_NPZD = 0, 1
 SURFACE_DEFAULT, SURFACE_CONSTANT, SURFACE_FIELD = 0, 1, 2
 PERIODIC, BOUNDED, FLAT = 0, 1, 2
 ADVECTION_NONE, ADVECTION_WENO5 = 0, 1
-FLAG_NAN, FLAG_NOT_CONVERGED = 1, 2     # enum obgc_step_flags
+FLAG_NAN, FLAG_NOT_CONVERGED, FLAG_TIMEOUT = 1, 2, 4     # enum obgc_step_flags
 OUT_FCO2, OUT_PCO2, OUT_PH_FREE, OUT_PH_TOTAL, OUT_PH_SWS, OUT_H, OUT_CARBONATE, OUT_OMEGA = range(8)
 DENSITY_EOS80, DENSITY_CONSTANT, DENSITY_TEOS10_POLYNOMIAL = 0, 1, 2
 
@@ -352,6 +352,8 @@ def load():
     _sig(lib, "obgc_step_status", C.c_int, VP, P(I32))
     _sig(lib, "obgc_set_status_check", C.c_int, VP, I32)
     _sig(lib, "obgc_substep", C.c_int, VP, D, D, I32, P(VP), P(VP), VP)
+    _sig(lib, "obgc_set_staging", C.c_int, VP, I32)
+    _sig(lib, "obgc_get_staging", C.c_int, VP, P(I32), P(I32))
     _sig(lib, "obgc_halo_pack", C.c_int, P(Grid), I32, I32, P(VP), I32, VP, VP, VP)
     _sig(lib, "obgc_halo_unpack", C.c_int, P(Grid), I32, I32, P(VP), I32, VP, VP, VP)
     _sig(lib, "obgc_tracer_budget", C.c_int, VP, I32, P(D), VP)
@@ -410,7 +412,8 @@ EXPORTED = [
     "obgc_multiband_coefficients", "obgc_euphotic_depth", "obgc_carbon_default_options",
     "obgc_carbon_chemistry", "obgc_carbon_chemistry_point", "obgc_create", "obgc_destroy",
     "obgc_bind_fields", "obgc_update_state", "obgc_compute_tendencies", "obgc_step",
-    "obgc_step_graph", "obgc_step_status", "obgc_set_status_check", "obgc_substep", "obgc_halo_pack", "obgc_halo_unpack", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run", "obgc_box_run_drivers",
+    "obgc_step_graph", "obgc_step_status", "obgc_set_status_check", "obgc_substep", "obgc_halo_pack", "obgc_halo_unpack",
+    "obgc_set_staging", "obgc_get_staging", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run", "obgc_box_run_drivers",
     "obgc_set_profiling", "obgc_set_tiling", "obgc_struct_layout", "obgc_tracer_budget_static",
     "obgc_columns_create", "obgc_columns_destroy", "obgc_columns_tracers", "obgc_columns_add",
     "obgc_columns_advance", "obgc_columns_run", "obgc_columns_remaining", "obgc_columns_read", "obgc_columns_remove",

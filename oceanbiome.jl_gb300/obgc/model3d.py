@@ -233,6 +233,16 @@ class NonhydrostaticModel:
         """Whether obgc_step waits for its kernels and returns their status (default on)."""
         A.check(self._lib.obgc_set_status_check(self._ctx, int(on)), "obgc_set_status_check")
 
+    def set_staging(self, mode):
+        """1: TMA-staged tiles when the steps qualify (default); 0: per-element cp.async staging."""
+        A.check(self._lib.obgc_set_staging(self._ctx, int(mode)), "obgc_set_staging")
+
+    def staging(self):
+        """(available, last_used) of the TMA staging."""
+        av, used = C.c_int32(0), C.c_int32(0)
+        A.check(self._lib.obgc_get_staging(self._ctx, C.byref(av), C.byref(used)), "obgc_get_staging")
+        return bool(av.value), bool(used.value)
+
     def set_tiling(self, levels):
         A.check(self._lib.obgc_set_tiling(self._ctx, int(levels)), "obgc_set_tiling")
 
