@@ -647,6 +647,41 @@ int obgc_set_sediment(obgc_ctx* ctx, int32_t n_sinking, const int32_t* sinking_n
 /* The sediment storage of every column (Ny x Nx dense, FP64 on the host): `set` (optional) replaces
  * it, then `get` (optional) receives it.  Synchronises the device. */
 int obgc_sediment_storage(obgc_ctx* ctx, const double* set, double* get);
+
+/* sediment = SimpleMultiGSediment(grid; ...) (src/Models/Sediments/simple_multi_G.jl:15-430; the
+ * nitrogen-only form, sinking_carbon = nothing): a single-layer sediment per column with slow, fast
+ * and refractory organic nitrogen (Ns, Nf, Nr, mmol N/m2), fed by the sinking fluxes of the named
+ * tracers through the bottom face and returning its remineralisation to the bottom cell's NH4 and
+ * NO3 and drawing O2 (Soetaert et al. 2000 fractions: ammonia oxidation, denitrification, anoxic
+ * remineralisation, solid deposition).  It is coupled as BiogeochemicalSediment does
+ * (src/Sediments/update_state.jl:6-17, tracer_coupling.jl, tracked_fields.jl): after every RK3 stage
+ * of the water, the bottom-cell NO3, NH4, O2 and the sinking fluxes are tracked from the new state,
+ * the sediment takes a full RK3 step (timesteppers.jl:48-73) of the stage's length ((gamma + zeta)
+ * dt), its first stage from the tendency cached at the end of its previous step, and the coupled
+ * tendencies (sediment_tendency / dz) enter the bottom cells of the next water stage.  The model
+ * needs NO3, NH4 and O2 (LOBSTER with Oxygen).  n_sinking = 0 removes it. */
+typedef struct obgc_multig_params {
+    double fast_decay_rate;          /* 2 / day                                              */
+    double slow_decay_rate;          /* 0.2 / day                                            */
+    double fast_redfield;            /* 0.1509 (the carbon form's)                           */
+    double slow_redfield;            /* 0.13                                                 */
+    double fast_fraction;            /* 0.74                                                 */
+    double slow_fraction;            /* 0.26                                                 */
+    double refactory_fraction;       /* 0.1                                                  */
+    double sedimentation_rate;       /* cm/year; <= 0: 982 |z_bottom|^-1.548 of the grid      */
+    double anoxia_half_saturation;   /* 1 mmol/m3                                            */
+    double sinking_redfield;         /* 6.56: C:N of the sinking nitrogen                     */
+    double nitrate_oxidation[6];     /* A..F of the ammonia oxidation fraction's fit          */
+    double denitrification[6];
+    double anoxic[6];
+} obgc_multig_params;
+/* The reference's SimpleMultiGSediment keyword defaults (sedimentation_rate left <= 0: from the grid). */
+int obgc_multig_default_params(obgc_multig_params* p);
+int obgc_set_multig_sediment(obgc_ctx* ctx, const obgc_multig_params* p, int32_t n_sinking, const int32_t* sinking_names);
+/* The sediment's fields [3][Ny][Nx] (Ns, Nf, Nr; FP64 on the host): `set` (optional) replaces them
+ * (and restarts its clock: the next step computes its first tendency afresh), then `get` (optional)
+ * receives them.  Synchronises the device. */
+int obgc_multig_sediment_state(obgc_ctx* ctx, const double* set, double* get);
 /* Size and selected field offsets of the ABI structs (which: 0 npd_params, 1 twoband,
  * 2 surface, 3 grid, 4 carbon_options, 5 model_desc, 6 fields, 7 column_spec, 8 columns_desc,
  * 9 pisces_params, 10 pisces_phyto, 11 pisces_field, 12 gas_exchange, 13 box_drivers) for binding

@@ -7,6 +7,7 @@
 #include <mutex>
 #include <vector>
 #include "gas_device.cuh"
+#include "multig_device.cuh"
 #include "negatives.cuh"
 #include "step_launch.cuh"
 
@@ -46,6 +47,68 @@ __global__ void set_time_kernel(double* t, double v, int* status) {
     if (status) *status = 0;
 }
 __global__ void advance_time_kernel(double* t, double dt) { *t += dt; }
+
+// SimpleMultiGSediment, one thread per column after every RK3 stage of the water (and once before a
+// call's first stage with dt = 0): track the bottom cells of the new state, step the sediment fields
+// a full RK3 step of dt (the first stage from the tendency cached at the end of the previous step;
+// afresh on the first step), cache the final tendency, and write the coupled bottom-cell tendencies
+// for the next water stage.
+template <typename TS>
+struct MultiGArgs {
+    MultiG m;
+    int Nx, Ny;
+    int64_t sj;                 // the bottom level (k = 0) of the state arrays: i + j sj
+    int n_sink;
+    const TS* sink[4];          // sinking tracers
+    double w0[4];               // their drift velocity at the bottom face (negative: downward)
+    const TS* no3;
+    const TS* nh4;
+    const TS* o2;
+    double* state;              // [4][Ny Nx]: Ns, Nf, Nr, started (0 / 1)
+    double* gcache;             // [3][Ny Nx]: the fields' tendency at the end of the last step
+    double* flux;               // [3][Ny Nx]: coupled tendencies of NO3, NH4, O2 (mmol/m2/s)
+    double dt;                  // step length (0: the coupled tendencies only)
+};
+
+template <typename TS>
+__global__ void __launch_bounds__(128) multig_kernel(const __grid_constant__ MultiGArgs<TS> a) {
+    const int64_t NN = (int64_t)a.Nx * a.Ny;
+    const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= NN) return;
+    const int i = (int)(col % a.Nx), j = (int)(col / a.Nx);
+    const int64_t o = i + (int64_t)j * a.sj;
+    // sinking_flux (tracked_fields.jl:55-70): minus the advective flux through the bottom face,
+    // whose face value next to the wall is the bottom cell's
+    double dep = 0.0;
+    for (int q = 0; q < a.n_sink; q++) dep -= a.w0[q] * (double)a.sink[q][o];
+    double* S = a.state;
+    double s0 = S[col], s1 = S[NN + col], s2 = S[2 * NN + col];
+    if (a.dt > 0.0) {
+        const double g[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0}, z[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
+        double G0[3], G1[3];
+        if (S[3 * NN + col] == 0.0) {
+            multig_fields_tendency(a.m, s0, s1, dep, G0);
+            S[3 * NN + col] = 1.0;
+        } else {
+            for (int q = 0; q < 3; q++) G0[q] = a.gcache[q * NN + col];
+        }
+        double x[3] = {s0, s1, s2};
+        for (int q = 0; q < 3; q++) x[q] += a.dt * g[0] * G0[q];
+        multig_fields_tendency(a.m, x[0], x[1], dep, G1);
+        for (int q = 0; q < 3; q++) x[q] += a.dt * (g[1] * G1[q] + z[1] * G0[q]);
+        multig_fields_tendency(a.m, x[0], x[1], dep, G0);
+        for (int q = 0; q < 3; q++) x[q] += a.dt * (g[2] * G0[q] + z[2] * G1[q]);
+        multig_fields_tendency(a.m, x[0], x[1], dep, G1);
+        for (int q = 0; q < 3; q++) a.gcache[q * NN + col] = G1[q];
+        s0 = x[0]; s1 = x[1]; s2 = x[2];
+        S[col] = s0; S[NN + col] = s1; S[2 * NN + col] = s2;
+    }
+    double F0, F1, F2;
+    multig_coupling(a.m, s0, s1, (double)a.no3[o], (double)a.nh4[o], (double)a.o2[o], &F0, &F1, &F2);
+    a.flux[col] = F0;
+    a.flux[NN + col] = F1;
+    a.flux[2 * NN + col] = F2;
+}
 
 // Thomas factors of the vertically implicit diffusion for the three RK3 stages (the same in every
 // column): out[(2 st) Nz + k] = c'_k and out[(2 st + 1) Nz + k] = 1 / pivot_k of
@@ -226,6 +289,16 @@ struct obgc_ctx {
     double sed_a = 0, sed_b = 0, sed_k = 0;
     void* sed_storage = nullptr;
     void* sed_G = nullptr;
+    // SimpleMultiGSediment (none when mg_on is false)
+    bool mg_on = false;
+    MultiG mg;
+    int mg_nsink = 0;
+    int mg_sink[4] = {-1, -1, -1, -1};
+    double mg_w0[4] = {0, 0, 0, 0};
+    int mg_no3 = -1, mg_nh4 = -1, mg_o2 = -1;
+    double* mg_state = nullptr;        // [4][Ny Nx]
+    double* mg_gcache = nullptr;       // [3][Ny Nx]
+    double* mg_flux = nullptr;         // [3][Ny Nx]
     double* d_time = nullptr;
     int* d_status = nullptr;            // OBGC_FLAG_* of the current call (device)
     int* h_status = nullptr;            // its copy behind the call's last kernel (pinned host)
@@ -288,6 +361,9 @@ static int ctx_free(obgc_ctx* c) {
     if (c->thomas) cudaFree(c->thomas);
     if (c->sed_storage) cudaFree(c->sed_storage);
     if (c->sed_G) cudaFree(c->sed_G);
+    if (c->mg_state) cudaFree(c->mg_state);
+    if (c->mg_gcache) cudaFree(c->mg_gcache);
+    if (c->mg_flux) cudaFree(c->mg_flux);
     if (c->ev_begin) cudaEventDestroy(c->ev_begin);
     if (c->ev_end) cudaEventDestroy(c->ev_end);
     for (auto e : c->prof_events) cudaEventDestroy(e);
@@ -621,6 +697,7 @@ extern "C" int obgc_set_sediment(obgc_ctx* c, int32_t n_sinking, const int32_t* 
         c->bind_version++;
         return OBGC_OK;
     }
+    c->mg_on = false;        // one sediment model at a time
     // the sediment couples to the main launch's slots (passive tracers neither sink nor receive)
     uint32_t mask = 0;
     for (int q = 0; q < n_sinking; q++) {
@@ -641,6 +718,89 @@ extern "C" int obgc_set_sediment(obgc_ctx* c, int32_t n_sinking, const int32_t* 
     c->sed_mask = mask;
     c->sed_a = a; c->sed_b = b; c->sed_k = k;
     c->bind_version++;
+    return OBGC_OK;
+}
+
+extern "C" int obgc_multig_default_params(obgc_multig_params* p) {
+    if (!p) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_multig_default_params: null argument");
+    std::memset(p, 0, sizeof(*p));
+    // SimpleMultiGSediment keyword defaults (simple_multi_G.jl:101-120)
+    p->fast_decay_rate = 2.0 / 86400.0;
+    p->slow_decay_rate = 0.2 / 86400.0;
+    p->fast_redfield = 0.1509;
+    p->slow_redfield = 0.13;
+    p->fast_fraction = 0.74;
+    p->slow_fraction = 0.26;
+    p->refactory_fraction = 0.1;
+    p->sedimentation_rate = 0.0;          // from the grid at obgc_set_multig_sediment
+    p->anoxia_half_saturation = 1.0;
+    p->sinking_redfield = 6.56;
+    const double nox[6] = {-1.9785, 0.2261, -0.0615, -0.0289, -0.36109, -0.0232};
+    const double den[6] = {-3.0790, 1.7509, 0.0593, -0.1923, 0.0604, 0.0662};
+    const double anx[6] = {-3.9476, 2.6269, -0.2426, -1.3349, 0.1826, -0.0143};
+    std::memcpy(p->nitrate_oxidation, nox, sizeof(nox));
+    std::memcpy(p->denitrification, den, sizeof(den));
+    std::memcpy(p->anoxic, anx, sizeof(anx));
+    return OBGC_OK;
+}
+
+extern "C" int obgc_set_multig_sediment(obgc_ctx* c, const obgc_multig_params* p, int32_t n_sinking,
+                                        const int32_t* sinking_names) {
+    if (!c || n_sinking < 0 || n_sinking > 4 || (n_sinking > 0 && (!sinking_names || !p)))
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_multig_sediment: bad argument");
+    if (n_sinking == 0) {
+        c->mg_on = false;
+        c->bind_version++;
+        return OBGC_OK;
+    }
+    const obgc_grid& g = c->desc.grid;
+    const int no3 = slot_named(c, OBGC_NO3), nh4 = slot_named(c, OBGC_NH4), o2 = slot_named(c, OBGC_O2);
+    if (no3 < 0 || nh4 < 0 || o2 < 0 || no3 >= c->NT || nh4 >= c->NT || o2 >= c->NT)
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_multig_sediment: the model needs NO3, NH4 and O2 (LOBSTER with Oxygen)");
+    obgc_multig_params q = *p;
+    if (!(q.sedimentation_rate > 0)) {
+        // 982 |znode(1, 1, 1)|^-1.548 cm/year: the depth of the bottom cell's centre
+        const double zb = -g.Lz + 0.5 * g.Lz / g.Nz;
+        q.sedimentation_rate = 982.0 * std::pow(std::fabs(zb), -1.548);
+    }
+    for (int s = 0; s < n_sinking; s++) {
+        const int t = slot_named(c, sinking_names[s]);
+        double w0 = 0.0;
+        if (t < 0 || t >= c->NT || !drift_speed(&c->desc.npd, sinking_names[s], &w0))
+            return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_set_multig_sediment: a sinking tracer is not a sinking tracer of the model");
+        std::vector<double> prof((size_t)g.Nz + 1);
+        drift_profile(w0, c->desc.npd.open_bottom, g.Nz, prof.data());
+        c->mg_sink[s] = t;
+        c->mg_w0[s] = c->desc.advection ? prof[0] : 0.0;
+    }
+    const size_t cols = (size_t)g.Nx * g.Ny;
+    if (!c->mg_state) {
+        OBGC_CUDA(cudaMalloc(&c->mg_state, sizeof(double) * 4 * cols));
+        OBGC_CUDA(cudaMemset(c->mg_state, 0, sizeof(double) * 4 * cols));
+        OBGC_CUDA(cudaMalloc(&c->mg_gcache, sizeof(double) * 3 * cols));
+        OBGC_CUDA(cudaMemset(c->mg_gcache, 0, sizeof(double) * 3 * cols));
+        OBGC_CUDA(cudaMalloc(&c->mg_flux, sizeof(double) * 3 * cols));
+        OBGC_CUDA(cudaMemset(c->mg_flux, 0, sizeof(double) * 3 * cols));
+    }
+    c->mg = make_multig(q);
+    c->mg_nsink = n_sinking;
+    c->mg_no3 = no3; c->mg_nh4 = nh4; c->mg_o2 = o2;
+    c->mg_on = true;
+    c->sed_recv = -1;        // one sediment model at a time
+    c->sed_mask = 0;
+    c->bind_version++;
+    return OBGC_OK;
+}
+
+extern "C" int obgc_multig_sediment_state(obgc_ctx* c, const double* set, double* get) {
+    if (!c || !c->mg_state) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_multig_sediment_state: no SimpleMultiG sediment");
+    const size_t cols = (size_t)c->desc.grid.Nx * c->desc.grid.Ny;
+    OBGC_CUDA(cudaDeviceSynchronize());
+    if (set) {
+        OBGC_CUDA(cudaMemcpy(c->mg_state, set, sizeof(double) * 3 * cols, cudaMemcpyHostToDevice));
+        OBGC_CUDA(cudaMemset(c->mg_state + 3 * cols, 0, sizeof(double) * cols));   // the clock restarts
+    }
+    if (get) OBGC_CUDA(cudaMemcpy(get, c->mg_state, sizeof(double) * 3 * cols, cudaMemcpyDeviceToHost));
     return OBGC_OK;
 }
 
@@ -753,6 +913,14 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.sed_a = TC(c->sed_a); a.sed_b = TC(c->sed_b); a.sed_k = TC(c->sed_k);
     a.sed_storage = (TS*)c->sed_storage;
     a.sed_G = (TC*)c->sed_G;
+    if (c->mg_on) {
+        const int64_t cols = (int64_t)g.Nx * g.Ny;
+        const int slots[3] = {c->mg_no3, c->mg_nh4, c->mg_o2};
+        for (int q = 0; q < 3; q++) {
+            a.bot_slot1[q] = slots[q] + 1;
+            a.bot_flux[q] = c->mg_flux + q * cols;
+        }
+    }
 }
 
 // Whether the device clock (d_time) must advance with the steps: the default surface PAR and the
@@ -783,6 +951,31 @@ static void launch_terms(const obgc_ctx* c, SubstepArgs<TS, TC>& a, int b, int n
         }
 }
 
+// The SimpleMultiG sediment's per-column kernel on the state in `cur` (dt = 0: the coupled
+// tendencies only).
+template <typename TS>
+static int launch_multig(obgc_ctx* c, void* const* cur, double dt, cudaStream_t st) {
+    if (!c->mg_on) return OBGC_OK;
+    const obgc_grid& g = c->desc.grid;
+    MultiGArgs<TS> a;
+    std::memset(&a, 0, sizeof(a));
+    a.m = c->mg;
+    a.Nx = g.Nx; a.Ny = g.Ny; a.sj = g.stride_j;
+    a.n_sink = c->mg_nsink;
+    for (int q = 0; q < c->mg_nsink; q++) { a.sink[q] = (const TS*)cur[c->mg_sink[q]]; a.w0[q] = c->mg_w0[q]; }
+    a.no3 = (const TS*)cur[c->mg_no3];
+    a.nh4 = (const TS*)cur[c->mg_nh4];
+    a.o2 = (const TS*)cur[c->mg_o2];
+    a.state = c->mg_state;
+    a.gcache = c->mg_gcache;
+    a.flux = c->mg_flux;
+    a.dt = dt;
+    const int64_t cols = (int64_t)g.Nx * g.Ny;
+    multig_kernel<TS><<<(unsigned)((cols + 127) / 128), 128, 0, st>>>(a);
+    OBGC_LAUNCHED("multig_kernel");
+    return OBGC_OK;
+}
+
 // Launch arguments of a context's steps of size dt: the main launch (a) and the passive launches
 // (ap: no drift, no sediment, ZeroNegativeTracers only).
 template <typename TS, typename TC>
@@ -806,6 +999,7 @@ static int plan_steps(obgc_ctx* c, const FusedEntry* fe, double dt, StepPlan<TS,
     p.ap = a;
     p.ap.drift_mask = 0;
     p.ap.sed_recv1 = 0;
+    for (int q = 0; q < 3; q++) { p.ap.bot_slot1[q] = 0; p.ap.bot_flux[q] = nullptr; }
     p.ap.sed_sink_mask = 0;
     p.ap.bgc_out[0] = p.ap.bgc_out[1] = nullptr;
     p.fe = fe;
@@ -1006,11 +1200,17 @@ static int enqueue_steps(obgc_ctx* c, const FusedEntry* fe, double dt, int nstep
             rc = launch_negatives(c->neg_passive, sizeof(TS), cur + c->NT, grid, st);
         if (rc != OBGC_OK) return rc;
     }
+    // the sediment's coupled tendencies of the entering state
+    rc = launch_multig<TS>(c, cur, 0.0, st);
+    if (rc != OBGC_OK) return rc;
     for (int s = 0; s < nsteps; s++) {
         for (int stg = 0; stg < 3; stg++) {
             rc = enqueue_stage<TS, TC>(c, p, stg, cur, nxt, st, profile, ev);
             if (rc != OBGC_OK) return rc;
             for (int t = 0; t < NS; t++) { void* tmp = cur[t]; cur[t] = nxt[t]; nxt[t] = tmp; }
+            // update_state! after the substep: the sediment tracks the new state and steps the stage
+            rc = launch_multig<TS>(c, cur, (rk3_gamma(stg) + rk3_zeta(stg)) * dt, st);
+            if (rc != OBGC_OK) return rc;
         }
         if (clock) {
             advance_time_kernel<<<1, 1, 0, st>>>(c->d_time, dt);
@@ -1055,6 +1255,7 @@ extern "C" int obgc_substep(obgc_ctx* c, double t, double dt, int32_t stage, con
     if (!c || !c->bound) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_substep: context not bound");
     if (stage < 0 || stage > 2 || !(dt > 0) || !in || !out)
         return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_substep: bad stage, dt or field arrays");
+    if (c->mg_on) return fail(OBGC_ERR_UNSUPPORTED, "obgc_substep: the SimpleMultiG sediment steps with obgc_step only");
     const int NS = c->NT + c->NP;
     for (int q = 0; q < NS; q++)
         if (!in[q] || !out[q] || in[q] == out[q])
@@ -1095,8 +1296,8 @@ static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     int gases = 0;
     for (const auto& gc : c->gas) gases = gases || gc.on ? 1 : 0;   // one launch for all conditions
     const bool impl = c->vimplicit && c->kzf;
-    const int per_stage = 1 + c->nchunk + gases + (impl ? 1 + neg : 0);
-    return (int64_t)nsteps * (3 * per_stage + (clock ? 1 : 0)) + (nsteps % 2 && !c->last_used_tma ? c->NT + c->NP : 0) + 1 + neg + (impl ? 1 : 0);
+    const int per_stage = 1 + c->nchunk + gases + (impl ? 1 + neg : 0) + (c->mg_on ? 1 : 0);
+    return (c->mg_on ? 1 : 0) + (int64_t)nsteps * (3 * per_stage + (clock ? 1 : 0)) + (nsteps % 2 && !c->last_used_tma ? c->NT + c->NP : 0) + 1 + neg + (impl ? 1 : 0);
 }
 
 extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {

@@ -100,6 +100,10 @@ struct SubstepArgs {
     // burial in sed_G), the rest returns to slot sed_recv1 - 1 in the bottom cell (0: no sediment)
     int sed_recv1;
     uint32_t sed_sink_mask;
+    // SimpleMultiGSediment: slot bot_slot1[q] - 1 gains bot_flux[q][i + j Nx] / dz in its bottom cell
+    // (the sediment's coupled tendency of NO3, NH4, O2; none when 0)
+    int bot_slot1[3];
+    const double* bot_flux[3];
     TC sed_a, sed_b, sed_k;
     TS* sed_storage;
     TC* sed_G;
@@ -313,6 +317,7 @@ template <typename TS, typename TC>
 __host__ __device__ inline bool substep_needs_ext(const SubstepArgs<TS, TC>& a) {
     bool any = a.kh_dx != TC(0) || a.kh_dy != TC(0) || a.kzz != nullptr || a.neg.mode != OBGC_NEGATIVES_NONE ||
                a.sed_recv1 != 0 || a.bgc_out[0] != nullptr || a.bgc_out[1] != nullptr;
+    for (int q = 0; q < 3; q++) any = any || a.bot_slot1[q] != 0;
     for (int q = 0; q < MAX_TOP; q++) any = any || a.top_slot1[q] != 0;
     for (int q = 0; q < MAX_FRC; q++) any = any || a.frc_slot1[q] != 0;
     return any;
@@ -736,6 +741,11 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 TC Gt = Gb - adv;
                 if constexpr (EXT) {
                     if (t + 1 == a.sed_recv1) Gt += sed_remin;   // zero above the bottom cell
+                    if (k == 0) {
+#pragma unroll
+                        for (int q = 0; q < 3; q++)
+                            if (t + 1 == a.bot_slot1[q]) Gt += TC(a.bot_flux[q][ic + (int64_t)jc * a.Nx]) * a.inv_dz;
+                    }
                     if (k == a.Nz - 1) {
 #pragma unroll
                         for (int q = 0; q < MAX_TOP; q++)

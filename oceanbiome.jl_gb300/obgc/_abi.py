@@ -128,6 +128,15 @@ class GasExchange(C.Structure):
                 ("air_field", C.c_void_p), ("o2_solubility", C.c_double * 6), ("carbon", CarbonOptions)]
 
 
+class MultiGParams(C.Structure):
+    """obgc_multig_params (SimpleMultiGSediment, nitrogen-only form)."""
+    _fields_ = [("fast_decay_rate", C.c_double), ("slow_decay_rate", C.c_double), ("fast_redfield", C.c_double),
+                ("slow_redfield", C.c_double), ("fast_fraction", C.c_double), ("slow_fraction", C.c_double),
+                ("refactory_fraction", C.c_double), ("sedimentation_rate", C.c_double),
+                ("anoxia_half_saturation", C.c_double), ("sinking_redfield", C.c_double),
+                ("nitrate_oxidation", C.c_double * 6), ("denitrification", C.c_double * 6), ("anoxic", C.c_double * 6)]
+
+
 class ModelDesc(C.Structure):
     _fields_ = [("npd", NPDParams), ("light", TwoBandParams), ("surface", Surface),
                 ("grid", Grid), ("precision", C.c_int32), ("advection", C.c_int32),
@@ -352,6 +361,9 @@ def load():
     _sig(lib, "obgc_step_status", C.c_int, VP, P(I32))
     _sig(lib, "obgc_set_status_check", C.c_int, VP, I32)
     _sig(lib, "obgc_substep", C.c_int, VP, D, D, I32, P(VP), P(VP), VP)
+    _sig(lib, "obgc_multig_default_params", C.c_int, P(MultiGParams))
+    _sig(lib, "obgc_set_multig_sediment", C.c_int, VP, P(MultiGParams), I32, P(I32))
+    _sig(lib, "obgc_multig_sediment_state", C.c_int, VP, P(D), P(D))
     _sig(lib, "obgc_set_staging", C.c_int, VP, I32)
     _sig(lib, "obgc_get_staging", C.c_int, VP, P(I32), P(I32))
     _sig(lib, "obgc_halo_pack", C.c_int, P(Grid), I32, I32, P(VP), I32, VP, VP, VP)
@@ -413,6 +425,7 @@ EXPORTED = [
     "obgc_carbon_chemistry", "obgc_carbon_chemistry_point", "obgc_create", "obgc_destroy",
     "obgc_bind_fields", "obgc_update_state", "obgc_compute_tendencies", "obgc_step",
     "obgc_step_graph", "obgc_step_status", "obgc_set_status_check", "obgc_substep", "obgc_halo_pack", "obgc_halo_unpack",
+    "obgc_multig_default_params", "obgc_set_multig_sediment", "obgc_multig_sediment_state",
     "obgc_set_staging", "obgc_get_staging", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run", "obgc_box_run_drivers",
     "obgc_set_profiling", "obgc_set_tiling", "obgc_struct_layout", "obgc_tracer_budget_static",
     "obgc_columns_create", "obgc_columns_destroy", "obgc_columns_tracers", "obgc_columns_add",

@@ -151,12 +151,18 @@ class NonhydrostaticModel:
         sed = getattr(bgc, "sediment", None)
         self.sediment = sed
         if sed is not None:
-            from .sediments import InstantRemineralisationSediment
-            if not isinstance(sed, InstantRemineralisationSediment):
+            from .sediments import InstantRemineralisationSediment, SimpleMultiGSediment
+            if isinstance(sed, SimpleMultiGSediment):
+                names = (C.c_int32 * len(sed.sinking_nitrogen))(*[self.code(n) for n in sed.sinking_nitrogen])
+                A.check(lib.obgc_set_multig_sediment(ctx, C.byref(sed.params), len(sed.sinking_nitrogen), names),
+                        "obgc_set_multig_sediment")
+            elif isinstance(sed, InstantRemineralisationSediment):
+                names = (C.c_int32 * len(sed.sinking_tracers))(*[self.code(n) for n in sed.sinking_tracers])
+                A.check(lib.obgc_set_sediment(ctx, len(sed.sinking_tracers), names,
+                                              self.code(sed.remineralisation_reciever), sed.a, sed.b, sed.k),
+                        "obgc_set_sediment")
+            else:
                 raise NotImplementedError(f"sediment model {type(sed).__name__} in the fused step")
-            names = (C.c_int32 * len(sed.sinking_tracers))(*[self.code(n) for n in sed.sinking_tracers])
-            A.check(lib.obgc_set_sediment(ctx, len(sed.sinking_tracers), names, self.code(sed.remineralisation_reciever),
-                                          sed.a, sed.b, sed.k), "obgc_set_sediment")
         self.closure = closure
         if closure is not None:
             if closure.horizontal and callable(closure.kappa):
@@ -210,6 +216,17 @@ class NonhydrostaticModel:
 
     def set_profiling(self, on):
         A.check(self._lib.obgc_set_profiling(self._ctx, int(on)), "obgc_set_profiling")
+
+    def sediment_fields(self, set=None):
+        """SimpleMultiG: the sediment's (Ns, Nf, Nr) as FP64 numpy (3, Ny, Nx); `set` replaces them first."""
+        import numpy as np
+        g = self.grid
+        out = np.empty((3, g.Ny, g.Nx), dtype=np.float64)
+        src = None if set is None else np.ascontiguousarray(np.broadcast_to(set, (3, g.Ny, g.Nx)), dtype=np.float64)
+        P = C.POINTER(C.c_double)
+        A.check(self._lib.obgc_multig_sediment_state(self._ctx, None if src is None else src.ctypes.data_as(P),
+                                                     out.ctypes.data_as(P)), "obgc_multig_sediment_state")
+        return out
 
     def sediment_storage(self, set=None):
         """The sediment's storage field (Ny, Nx) as FP64 numpy; `set` replaces it first."""

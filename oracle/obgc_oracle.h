@@ -74,6 +74,19 @@ void or_box_run(const obgc_npd_params* p, double* v, const double* PAR_stages, d
 
 /* ---- 3-D fused model: WENO5 + drift + BGC + TwoBand light + RK3 ---- */
 #define OR_MAX_GAS 4
+/* SimpleMultiGSediment, nitrogen-only form (src/Models/Sediments/simple_multi_G.jl:15-430) coupled
+ * as BiogeochemicalSediment (src/Sediments/): after every water RK3 stage the bottom cells are
+ * tracked, the fields take a full RK3 step of the stage's length (first stage from the tendency
+ * cached at the end of the previous step), and the coupled tendencies enter the next stage. */
+typedef struct or_multig {
+    obgc_multig_params p;        /* sedimentation_rate resolved (> 0)                          */
+    int32_t n_sinking;
+    int32_t sinking_slot[4];
+    int32_t no3, nh4, o2;        /* slots of the coupled tracers                                */
+    double* state;               /* [4][Ny*Nx]: Ns, Nf, Nr, started                              */
+    double* gcache;              /* [3][Ny*Nx]: the fields' tendency at the end of the last step */
+} or_multig;
+
 typedef struct or_model3d {
     obgc_npd_params npd;
     obgc_twoband_params light;
@@ -109,6 +122,7 @@ typedef struct or_model3d {
                                       * drawn from a hash of (value index, stage count, seed): a
                                       * model of one rounding of that relative size per stored value */
     uint64_t rounding_seed;
+    const or_multig* multig;         /* SimpleMultiG sediment, or NULL                              */
 } or_model3d;
 /* state: [n_tracers][Nz*Ny*Nx]; u, v, w: [Nz*Ny*Nx] or NULL. */
 void or_step3d(const or_model3d* m, double* state, const double* u, const double* v,

@@ -14,6 +14,7 @@
  *  - ScaleNegativeTracers (src/Utils/negative_tracers.jl:250-276).
  */
 #include <math.h>
+#include <float.h>
 #include <stdlib.h>
 #include <string.h>
 #include "obgc_oracle.h"
@@ -181,6 +182,85 @@ static void or_negatives3d(const or_model3d* m, double* state, long N, int ng, c
 
 static void implicit_diffusion(int Nz, double dz, const double* kf, double dts, double* x, double* cp, double* dp);
 
+/* ------------------------------------------------------------------ SimpleMultiG ---------- */
+/* simple_multi_G.jl:163-189: the fields' tendencies from the deposited nitrogen flux */
+static void or_mg_tendency(const obgc_multig_params* p, double Ns, double Nf, double flux, double G[3]) {
+    G[0] = (1 - p->refactory_fraction) * p->slow_fraction * flux - p->slow_decay_rate * Ns;
+    G[1] = (1 - p->refactory_fraction) * p->fast_fraction * flux - p->fast_decay_rate * Nf;
+    G[2] = p->refactory_fraction * flux;
+}
+
+/* ifelse(isfinite(p), p, zero(Nr)) (simple_multi_G.jl:379,395,410).  A log of a negative argument
+ * throws in Julia on the CPU and gives NaN on the GPU; here it is NaN, so the fraction is zero. */
+static double or_mg_fraction(double p) { return isfinite(p) ? p : 0.0; }
+
+/* simple_multi_G.jl:193-247 (NH4, NO3, O2 of the nitrogen-only form) with the fractions of
+ * :352-426; F = (NO3, NH4, O2) in mmol / m2 / s */
+static void or_mg_coupling(const obgc_multig_params* p, double Ns, double Nf, double NO3, double NH4, double O2,
+                           double F[3]) {
+    const double day = 86400.0, R = p->sinking_redfield, ls = p->slow_decay_rate, lf = p->fast_decay_rate;
+    const double Nr = ls * Ns + lf * Nf;
+    const double Cr = Nr * R;
+    const double k = (ls * (Ns * R) + lf * (Nf * R)) / (Ns * R + Nf * R + DBL_TRUE_MIN);   /* reactivity */
+    const double kO2 = p->anoxia_half_saturation;
+    const double* A = p->nitrate_oxidation;
+    const double pn = or_mg_fraction(exp(A[0] + A[1] * log(Cr * day) * log(O2) + A[2] * pow(log(Cr * day), 2) +
+                                         A[3] * log(k * day) * log(NH4) + A[4] * log(Cr * day) +
+                                         A[5] * log(Cr * day) * log(NH4)) / (Nr * day) * O2 / (kO2 + O2));
+    const double* B = p->denitrification;
+    const double pd = or_mg_fraction(exp(B[0] + B[1] * log(Cr * day) + B[2] * pow(log(NO3), 2) +
+                                         B[3] * pow(log(Cr * day), 2) + B[4] * pow(log(k * day), 2) +
+                                         B[5] * log(O2) * log(k)) / (Cr * day) * O2 / (kO2 + O2));
+    const double* Cc = p->anoxic;
+    const double pa = or_mg_fraction(exp(Cc[0] + Cc[1] * log(Cr * day) + Cc[2] * pow(log(Cr * day), 2) +
+                                         Cc[3] * log(k * day) + Cc[4] * log(O2) * log(k) +
+                                         Cc[5] * pow(log(NO3), 2)) / (Cr * day));
+    const double ps = 0.223 * pow(p->sedimentation_rate, 0.336);
+    F[1] = (1 - pn) * Nr + 0.8 * pd * Cr;
+    F[0] = pn * Nr - 0.8 * pd * Cr;
+    F[2] = -(1 - pa * ps - pd) * O2 / (kO2 + O2) * Cr - 2 * pn * Nr;
+}
+
+/* update_biogeochemical_state!(model, sediment) (src/Sediments/update_state.jl:6-17): track the
+ * bottom cells of `state` (tracked_fields.jl), take a full RK3 step of length dt (none for dt = 0;
+ * timesteppers.jl:48-73, the first stage from the tendency cached by the previous step's
+ * update_state!, computed afresh on the first step), then the coupled tendencies F[3][NN]
+ * (tracer_coupling.jl) for the next water stage. */
+static void or_mg_update(const or_model3d* m, const double* state, const double* drift, double dt, double* F) {
+    const or_multig* g = m->multig;
+    const int Nx = m->grid.Nx, Ny = m->grid.Ny, Nz = m->grid.Nz;
+    const long NN = (long)Nx * Ny, N = NN * Nz;
+    for (long col = 0; col < NN; col++) {
+        double dep = 0.0;   /* sinking_flux: minus the advective flux through the bottom face */
+        for (int s = 0; s < g->n_sinking; s++) {
+            const int q = g->sinking_slot[s];
+            dep -= drift[(long)q * (Nz + 1)] * state[(long)q * N + col];
+        }
+        double* S = g->state;
+        double x[3] = {S[col], S[NN + col], S[2 * NN + col]};
+        if (dt > 0.0) {
+            double G0[3], G1[3], G2[3];
+            if (S[3 * NN + col] == 0.0) {
+                or_mg_tendency(&g->p, x[0], x[1], dep, G0);
+                S[3 * NN + col] = 1.0;
+            } else {
+                for (int q = 0; q < 3; q++) G0[q] = g->gcache[q * NN + col];
+            }
+            for (int q = 0; q < 3; q++) x[q] += dt * RK_G[0] * G0[q];
+            or_mg_tendency(&g->p, x[0], x[1], dep, G1);
+            for (int q = 0; q < 3; q++) x[q] += dt * (RK_G[1] * G1[q] + RK_Z[1] * G0[q]);
+            or_mg_tendency(&g->p, x[0], x[1], dep, G2);
+            for (int q = 0; q < 3; q++) x[q] += dt * (RK_G[2] * G2[q] + RK_Z[2] * G1[q]);
+            or_mg_tendency(&g->p, x[0], x[1], dep, G0);
+            for (int q = 0; q < 3; q++) { g->gcache[q * NN + col] = G0[q]; S[q * NN + col] = x[q]; }
+        }
+        double f[3];
+        or_mg_coupling(&g->p, x[0], x[1], state[(long)g->no3 * N + col], state[(long)g->nh4 * N + col],
+                       state[(long)g->o2 * N + col], f);
+        for (int q = 0; q < 3; q++) F[q * NN + col] = f[q];
+    }
+}
+
 /* nsteps RK3 steps; or, with only_stage in 0..2, that one stage of one step, with the tendency
  * arrays supplied by the caller (Gx receives the stage's tendency, Gmx holds the previous stage's,
  * sedx the sediment's previous-stage burial) and no modifier applied to the entering state. */
@@ -219,6 +299,9 @@ static void step3d_impl(const or_model3d* m, double* state, const double* u, con
     double gfac[OR_MAX_GROUPS * OR_MAX_GROUP];
     const int ng = m->negatives == 1 ? or_conserved_groups(&m->npd, nt, m->names, gn, gslot, gfac) : 0;
     if (m->negatives && !ext) or_negatives3d(m, state, N, ng, gn, gslot, gfac, nthreads);
+    /* the SimpleMultiG sediment's coupled tendencies of the entering state (full steps only) */
+    double* mgF = (m->multig && !ext) ? calloc((size_t)3 * NN, sizeof(double)) : NULL;
+    if (mgF) or_mg_update(m, state, drift, 0.0, mgF);
     const int st0 = ext ? only_stage : 0, st1 = ext ? only_stage + 1 : 3;
     for (int s = 0; s < nsteps; s++) {
         for (int st = st0; st < st1; st++) {
@@ -327,6 +410,12 @@ static void step3d_impl(const or_model3d* m, double* state, const double* u, con
                     G[(long)target * N + c] -= F / dz;
                 }
             }
+            /* SimpleMultiG: the coupled tendencies enter the bottom cells (tracer_coupling.jl) */
+            if (mgF) {
+                const int slots[3] = {m->multig->no3, m->multig->nh4, m->multig->o2};
+                for (long col = 0; col < NN; col++)
+                    for (int q = 0; q < 3; q++) G[(long)slots[q] * N + col] += mgF[q * NN + col] / dz;
+            }
             /* InstantRemineralisationSediment (instant_remineralisation.jl:96-120; tracer_coupling.jl,
              * tracked_fields.jl): the sinking fluxes through the bottom face deposit F, a fraction
              * e = a + b (F/(k+F))^2 is buried, the rest returns to the receiver's bottom cell */
@@ -376,11 +465,14 @@ static void step3d_impl(const or_model3d* m, double* state, const double* u, con
                 }
             }
             if (m->negatives) or_negatives3d(m, state, N, ng, gn, gslot, gfac, nthreads);
+            /* update_state!: the sediment tracks the new state and steps the stage's length */
+            if (mgF) or_mg_update(m, state, drift, (g + z) * dt, mgF);
             double* tmp = G; G = Gm; Gm = tmp;
         }
         t += dt;
     }
     if (!ext) { free(G); free(Gm); free(sed_Gm); }
+    free(mgF);
     free(PAR); free(drift); free(has_drift);
 }
 

@@ -33,7 +33,13 @@ class Model3D(C.Structure):
                 ("sed_a", C.c_double), ("sed_b", C.c_double), ("sed_k", C.c_double),
                 ("sed_storage", C.POINTER(C.c_double)), ("tendency_of", C.c_int32 * 32),
                 ("forcing", C.POINTER(C.c_double) * 32), ("forcing_t0", C.c_double * 32), ("forcing_t1", C.c_double * 32),
-                ("stage_rounding", C.c_double), ("rounding_seed", C.c_uint64)]
+                ("stage_rounding", C.c_double), ("rounding_seed", C.c_uint64), ("multig", C.c_void_p)]
+
+
+class MultiG(C.Structure):
+    _fields_ = [("p", A.MultiGParams), ("n_sinking", C.c_int32), ("sinking_slot", C.c_int32 * 4),
+                ("no3", C.c_int32), ("nh4", C.c_int32), ("o2", C.c_int32),
+                ("state", C.POINTER(C.c_double)), ("gcache", C.POINTER(C.c_double))]
 
 
 class Pisces3D(C.Structure):
@@ -364,6 +370,30 @@ def model3d(p, grid, names, light=None, surface_kind=A.SURFACE_DEFAULT, surface_
     for q, nm in enumerate(names):
         m.names[q] = -1 if nm is None else (A.NAME_INDEX[nm] if isinstance(nm, str) else nm)
     return m
+
+
+def attach_multig(m, params, names, sinking, grid, state=None):
+    """Give model `m` a SimpleMultiG sediment: params (A.MultiGParams; sedimentation_rate <= 0 is
+    resolved from the grid's bottom cell), tracer names of the model's slots, the sinking tracers.
+    Returns the sediment's field array [4][Ny*Nx] (Ns, Nf, Nr, started), updated in place by step3d."""
+    mg = MultiG()
+    C.memmove(C.byref(mg.p), C.byref(params), C.sizeof(A.MultiGParams))
+    if not (mg.p.sedimentation_rate > 0):
+        zb = -grid.Lz + 0.5 * grid.Lz / grid.Nz
+        mg.p.sedimentation_rate = 982.0 * abs(zb) ** -1.548
+    idx = {n: q for q, n in enumerate(names)}
+    mg.n_sinking = len(sinking)
+    for q, n in enumerate(sinking):
+        mg.sinking_slot[q] = idx[n]
+    mg.no3, mg.nh4, mg.o2 = idx["NO3"], idx["NH4"], idx["O2"]
+    NN = grid.Nx * grid.Ny
+    st = np.zeros(4 * NN) if state is None else np.ascontiguousarray(state, dtype=np.float64)
+    gc = np.zeros(3 * NN)
+    mg.state = st.ctypes.data_as(C.POINTER(C.c_double))
+    mg.gcache = gc.ctypes.data_as(C.POINTER(C.c_double))
+    m._mg_keep = (mg, st, gc)
+    m.multig = C.cast(C.pointer(mg), C.c_void_p)
+    return st
 
 
 def step3d(m, state, u=None, v=None, w=None, t=0.0, dt=1.0, nsteps=1, threads=None):
