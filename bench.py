@@ -304,6 +304,8 @@ def run_gpu(args):
                                      precision=prec)
     if args.tz:
         model.set_tiling(args.tz)
+    if args.staging != "default":
+        model.set_staging(1 if args.staging == "tma" else 0)
     obgc.set_(model, **obgc.lobster_initial_conditions(g, seed=11 + rank))
     assert len(model.tracer_names) == N_TRACERS
 
@@ -347,6 +349,8 @@ def run_gpu(args):
                                        precision=prec)
     if args.tz:
         member2.set_tiling(args.tz)
+    if args.staging != "default":
+        member2.set_staging(1 if args.staging == "tma" else 0)
     obgc.set_(member2, **obgc.lobster_initial_conditions(g, seed=23 + rank))
     obgc.time_step(member2, DT, nsteps=1, graph=True)          # warm-up: builds its graph
     members = []
@@ -1217,6 +1221,8 @@ def main():
     ap.add_argument("--impl", default="obgc", choices=["obgc", "reference"])
     ap.add_argument("--precision", default="f32", choices=["f32", "mixed", "f64"])
     ap.add_argument("--tz", type=int, default=0)
+    ap.add_argument("--staging", default="default", choices=["default", "tma", "cp.async"],
+                    help="tile staging of the fused substep (default: the library's choice)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--shape", type=int, nargs=3, default=None,
                     help="grid size for profiling a smaller case of the same kernel (default 256 256 64)")

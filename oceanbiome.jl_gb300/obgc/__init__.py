@@ -22,7 +22,7 @@ from .model3d import (Clock, ExplicitTimeDiscretization, HorizontalScalarDiffusi
                       ScalarDiffusivity, VerticallyImplicitTimeDiscretization, VerticalScalarDiffusivity,
                       compute_tendencies, set_, time_step, update_biogeochemical_state)
 from .negatives import ScaleNegativeTracers, ZeroNegativeTracers
-from .sediments import InstantRemineralisationSediment
+from .sediments import InstantRemineralisationSediment, SimpleMultiGSediment
 from .distributed import SlabDecomposition, SlabModel
 from .models import (LOBSTER, NPZD, CarbonateSystem, Detritus, NitrateAmmonia, NitrateAmmoniaIron, Nutrient,
                      NutrientsPlanktonDetritus, Oxygen, PhytoZoo, TwoParticleAndDissolved, VariableRedfieldDetritus,

@@ -127,9 +127,10 @@ class NutrientsPlanktonDetritus:
                  invalid_fill_value=float("nan"), particles=None, modifiers=None, _base="LOBSTER"):
         if particles is not None:
             raise NotImplementedError("particles are outside this engine's path")
-        from .sediments import InstantRemineralisationSediment
-        if sediment is not None and not isinstance(sediment, InstantRemineralisationSediment):
-            raise NotImplementedError(f"sediment model {type(sediment).__name__}: only InstantRemineralisationSediment")
+        from .sediments import InstantRemineralisationSediment, SimpleMultiGSediment
+        if sediment is not None and not isinstance(sediment, (InstantRemineralisationSediment, SimpleMultiGSediment)):
+            raise NotImplementedError(f"sediment model {type(sediment).__name__}: InstantRemineralisationSediment or "
+                                      "SimpleMultiGSediment")
         self.sediment = sediment
         p = preset(_base)
         if nutrients is not None:
