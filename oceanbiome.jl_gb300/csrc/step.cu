@@ -314,7 +314,7 @@ struct obgc_ctx {
     CUtensorMap* d_tmaps = nullptr;
     int64_t pad_sj = 0, pad_sk = 0;
     bool tma_ready = false;
-    int staging = 0;
+    int staging = 1;
     bool last_used_tma = false;
     int TZ = 0;                         // levels per work item; 0: chosen per grid (fill_args)
     int blocks = 0;

@@ -116,6 +116,9 @@ def test_pisces_scale_negatives_match_oracle():
         assert got[A.PISCES_INDEX[name]].min() >= 0, name
     errs = tracer_errors(got, ref)
     assert errs.pop("CaCO3") < 1e-5      # 3.4e-6: FP32 light and tendencies on a 1e-10 start
+    # the two tracers made negative: ScaleNegativeTracers leaves cells near zero where the FP32
+    # tendencies' rounding is large against the value (3.8e-6 for DOC)
+    assert max(errs.pop("DOC"), errs.pop("NH4")) < 1e-5
     assert max(errs.values()) < 1e-6, sorted(errs.items(), key=lambda kv: -kv[1])[:6]
 
 
