@@ -311,7 +311,9 @@ struct obgc_ctx {
     // (device), the staging choice (1: TMA when a launch qualifies, 0: cp.async) and what the last
     // obgc_step used
     void* pad[2][MAX_NT] = {};
-    CUtensorMap* d_tmaps = nullptr;
+    CUtensorMap* d_tmaps = nullptr;     // [2][MAX_NT]: the padded sets; [2 MAX_NT + t]: the bound arrays
+    void* tma_encode = nullptr;         // the driver's cuTensorMapEncodeTiled
+    bool umaps_ok = false;              // the bound arrays have tensor maps (16-byte aligned layout)
     int64_t pad_sj = 0, pad_sk = 0;
     bool tma_ready = false;
     int staging = 1;
@@ -385,7 +387,8 @@ static int setup_tma(obgc_ctx* c) {
     }
     auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     const size_t bytes = sizeof(float) * (size_t)c->pad_sk * g.Nz;
-    std::vector<CUtensorMap> maps(2 * MAX_NT);
+    c->tma_encode = fn;
+    std::vector<CUtensorMap> maps(3 * MAX_NT);
     std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
     for (int s = 0; s < 2; s++)
         for (int t = 0; t < c->NT; t++) {
@@ -567,6 +570,34 @@ extern "C" int obgc_bind_fields(obgc_ctx* c, const obgc_fields* f) {
     c->fields = *f;
     c->bound = true;
     c->bind_version++;
+    // tensor maps of the bound arrays (the TMA-staged steps' first stage), when their layout allows
+    // them: 16-byte aligned origins and row / level strides
+    c->umaps_ok = false;
+    if (c->tma_ready && c->tma_encode) {
+        const obgc_grid& g = c->desc.grid;
+        bool ok = (g.stride_j * 4) % 16 == 0 && (g.stride_k * 4) % 16 == 0;
+        for (int t = 0; t < c->NT && ok; t++) ok = reinterpret_cast<uintptr_t>(c->user[t]) % 16 == 0;
+        if (ok) {
+            auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(c->tma_encode);
+            std::vector<CUtensorMap> maps(MAX_NT);
+            std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
+            for (int t = 0; t < c->NT && ok; t++) {
+                const cuuint64_t dims[3] = {(cuuint64_t)g.Nx, (cuuint64_t)g.Ny, (cuuint64_t)g.Nz};
+                const cuuint64_t strides[2] = {(cuuint64_t)g.stride_j * sizeof(float), (cuuint64_t)g.stride_k * sizeof(float)};
+                const cuuint32_t box[3] = {(cuuint32_t)TMA_TILE_W, (cuuint32_t)TILE_H, 1};
+                const cuuint32_t es[3] = {1, 1, 1};
+                ok = encode(&maps[t], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, c->user[t], dims, strides, box, es,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+            }
+            if (ok) {
+                const cudaError_t e = cudaMemcpy(c->d_tmaps + 2 * MAX_NT, maps.data(), sizeof(CUtensorMap) * MAX_NT,
+                                                 cudaMemcpyHostToDevice);
+                if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(tensor maps of the bound arrays)");
+                c->umaps_ok = true;
+            }
+        }
+    }
     return OBGC_OK;
 }
 
@@ -875,6 +906,7 @@ static void fill_args(obgc_ctx* c, SubstepArgs<TS, TC>& a) {
     a.out_halo = 0;
     a.tma_layout = 0;
     a.tmap = nullptr;
+    a.tma_x0 = a.tma_y0 = 0;
     a.dx = TC(g.Lx / g.Nx); a.dy = TC(g.Ly / g.Ny); a.dz = TC(g.Lz / g.Nz); a.Lz = TC(g.Lz);
     a.inv_dx = TC(g.Nx / g.Lx); a.inv_dy = TC(g.Ny / g.Ly); a.inv_dz = TC(g.Nz / g.Lz);
     if (c->TZ > 0) {
@@ -1140,7 +1172,6 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
     launch_terms(c, a, 0, c->NT);
     a.gsj = c->pad_sj;
     a.gsk = c->pad_sk;
-    a.tma_layout = 1;
     const bool clock = needs_clock(c);
     size_t ev = 0;
     for (int s = 0; s < nsteps; s++) {
@@ -1159,7 +1190,11 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
             a.osj = stg == 2 ? g.stride_j : c->pad_sj;
             a.osk = stg == 2 ? g.stride_k : c->pad_sk;
             a.out_halo = stg < 2;
-            a.tmap = stg == 0 ? nullptr : c->d_tmaps + (size_t)(stg - 1) * MAX_NT;
+            a.tma_layout = stg == 0 ? 1 : 2;
+            // the first stage copies the bound arrays' wrap-free tiles when they have tensor maps
+            a.tmap = stg == 0 ? (c->umaps_ok ? c->d_tmaps + 2 * MAX_NT : nullptr) : c->d_tmaps + (size_t)(stg - 1) * MAX_NT;
+            a.tma_x0 = stg == 0 ? -TMA_HX : 0;
+            a.tma_y0 = stg == 0 ? -HALO : 0;
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
             const int rc = p.fe->launch(&a, p.blocks, st);
             if (rc != OBGC_OK) return rc;

@@ -62,10 +62,13 @@ struct SubstepArgs {
     // value into the halo cells that hold its periodic image, so the next stage can stage whole
     // tiles of it with the tensor-memory accelerator
     int out_halo;
-    int tma_layout;           // launch an instantiation of the TMA-staged steps (the layouts above may differ)
-    // tensor maps of in[] (3-D, padded layout, box TMA_TILE_W x TILE_H x 1) in global memory, or
-    // NULL: the tiles are then staged by per-element cp.async
+    int tma_layout;           // the TMA-staged steps: 1 their first stage, 2 their later stages (0: neither)
+    // tensor maps of in[] (3-D, box TMA_TILE_W x TILE_H x 1) in global memory, or NULL: the tiles are
+    // then staged by per-element cp.async.  A tile at (i0, j0, k) is the box at (i0 + tma_x0,
+    // j0 + tma_y0, k): (0, 0) for the padded sets, (-4, -3) for the caller's arrays, whose tiles
+    // on a periodic edge (that would need the wrap) are staged by cp.async
     const CUtensorMap* tmap;
+    int tma_x0, tma_y0;
     TC dx, dy, dz, Lz, inv_dx, inv_dy, inv_dz;
     int TZ, nseg, ntx, nty, n_items;
     const TS* in[MAX_NT];
@@ -326,8 +329,9 @@ __host__ __device__ inline bool substep_needs_ext(const SubstepArgs<TS, TC>& a) 
 // MODE 0: every array in the input layout, tiles staged by cp.async.  MODE 1 and 2 are the
 // instantiations of the TMA-staged steps: input, output and tendency arrays in their own layouts
 // (a.sj/sk, osj/osk, gsj/gsk; u and v in vsj/vsk), 40-wide tile rows, and periodic halo images
-// written when a.out_halo is set; MODE 1 stages its tiles by cp.async (the step's first stage, from
-// the caller's arrays), MODE 2 by tensor copies through a.tmap.
+// written when a.out_halo is set.  MODE 2 (the later stages, from the padded sets) stages every tile
+// by tensor copies through a.tmap; MODE 1 (the first stage, from the caller's arrays) does so for the
+// tiles that need no periodic wrap when a.tmap is set, and stages the rest by cp.async.
 template <int V, int NT, typename TS, typename TC, bool EXT, int MODE = 0>
 __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <= 12 ? 3 : NT <= 16 ? 2 : 1)
     substep_kernel(const __grid_constant__ SubstepArgs<TS, TC> a) {
@@ -373,7 +377,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     const unsigned tiles_s = smem_u32(tiles);
     unsigned tma_phase = 0;
     bool tma_timeout = false;
-    if constexpr (TMA) {
+    const bool may_tma = TMA || (MODE == 1 && a.tmap != nullptr);
+    if (may_tma) {
         // a tensor copy's destination must be 128-byte aligned: never issue one to a tile that is not
         // (the block then does no work and reports OBGC_FLAG_TIMEOUT)
         if ((tiles_s & 127u) != 0u) {
@@ -386,12 +391,13 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     (void)tma_phase;
     constexpr unsigned TILE_BYTES = (unsigned)(sizeof(TC) * TMA_TILE_W * TILE_H);
     // thread 0 arms the barrier and copies every tracer's tile of level kk of the work item at
-    // (i0, j0): padded coordinates x = i0 (x = i0 - 4 of the grid), y = j0 (y = j0 - 3)
+    // (i0, j0): the box whose first cell is x = i0 - 4, y = j0 - 3 of the grid
     auto tma_issue = [&](int i0_, int j0_, int kk) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arm(&stage_bar, TILE_BYTES * NT);
 #pragma unroll 1
-        for (int t = 0; t < NT; t++) tma_tile(tiles + t * TILE_SZ, a.tmap + t, i0_, j0_, kk, &stage_bar);
+        for (int t = 0; t < NT; t++)
+            tma_tile(tiles + t * TILE_SZ, a.tmap + t, i0_ + a.tma_x0, j0_ + a.tma_y0, kk, &stage_bar);
     };
 
     // forcings switched on at this stage's time
@@ -438,6 +444,11 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 
         // horizontal offsets of the tile elements this thread stages (the same for every level
         // and tracer of the work item)
+        // tensor copies for this item: always in MODE 2; in MODE 1 where the tile needs no periodic wrap
+        // (a Bounded direction's out-of-range cells are filled with zeros, which only the unused
+        // stencil cells beyond a wall read)
+        const bool item_tma = TMA || (may_tma && (!periodic_x || (i0 >= TMA_HX && i0 + TMA_TILE_W - TMA_HX <= a.Nx)) &&
+                                      (!periodic_y || (j0 >= HALO && j0 + STEP_BY + HALO <= a.Ny)));
         int64_t toff[TILE_LOADS];
 #pragma unroll
         for (int q = 0; q < (TMA ? 0 : TILE_LOADS); q++) {
@@ -494,7 +505,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             // stage every tracer's tile and halo for this level: all loads in flight together (FP32:
             // asynchronous copies, no registers), and, from the second stage on, the cell's previous
             // tendencies into the generic-drift buffer when no tracer uses it
-            if constexpr (TMA) {
+            if (item_tma) {
                 // the tiles of this level: issued here at the item's first level, otherwise during
                 // the previous level's update
                 if (tid == 0 && k == k_top) tma_issue(i0, j0, k);
@@ -621,8 +632,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             for (int t = 0; t < NT; t++) c[t] = tiles[t * TILE_SZ + (ty + HALO) * TILE_W + TILE_X0 + tx + HALO];
             __syncthreads();
             // the tiles are free again: the next level's copies fly during this level's update
-            if constexpr (TMA)
-                if (tid == 0 && k > k_bot) tma_issue(i0, j0, k - 1);
+            if (item_tma && tid == 0 && k > k_bot) tma_issue(i0, j0, k - 1);
             if (!row_cells) continue;   // no cell on this row: nothing below reads its registers
 
             // window tracers: flux through the face below this cell, divergence, and slide the

@@ -32,7 +32,7 @@ int launch_one(const SubstepArgs<TS, TC>& a, int blocks, cudaStream_t st) {
     } else {
         bool done = false;
         if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) {
-            if (a.tma_layout && a.tmap) {
+            if (a.tma_layout == 2) {
                 const int rc = ensure_configured<V, NT, TS, TC, false, 2>();
                 if (rc != OBGC_OK) return rc;
                 substep_kernel<V, NT, TS, TC, false, 2><<<blocks, block, substep_smem_bytes<TC, NT, true>(), st>>>(a);
