@@ -308,6 +308,13 @@ def run_gpu(args):
         model.set_staging(1 if args.staging == "tma" else 0)
     obgc.set_(model, **obgc.lobster_initial_conditions(g, seed=11 + rank))
     assert len(model.tracer_names) == N_TRACERS
+    # the launch shape: the library's autotuner on this state (restored afterwards), outside the
+    # timed region, unless the command line fixes the shape
+    tuning = {"levels_per_item": args.tz or "rule", "staging": args.staging, "autotuned": False}
+    if not args.tz and args.staging == "default" and not args.no_autotune:
+        tz, sg, tms = model.autotune(DT, steps=3)
+        tuning = {"levels_per_item": tz, "staging": "tma" if sg else "cp.async", "autotuned": True,
+                  "autotune_ms_per_step": tms}
 
     def barrier():
         torch.cuda.synchronize()
@@ -347,10 +354,10 @@ def run_gpu(args):
     names = model.tracer_names
     member2 = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None),
                                        precision=prec)
-    if args.tz:
-        member2.set_tiling(args.tz)
-    if args.staging != "default":
-        member2.set_staging(1 if args.staging == "tma" else 0)
+    if args.tz or tuning["autotuned"]:
+        member2.set_tiling(tuning["levels_per_item"])
+    if args.staging != "default" or tuning["autotuned"]:
+        member2.set_staging(1 if tuning["staging"] == "tma" else 0)
     obgc.set_(member2, **obgc.lobster_initial_conditions(g, seed=23 + rank))
     obgc.time_step(member2, DT, nsteps=1, graph=True)          # warm-up: builds its graph
     members = []
@@ -405,7 +412,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD if shape == SHAPE else WORKLOAD.replace("256x256x64", "x".join(map(str, shape))),
                        "grid": list(shape), "tracers": N_TRACERS, "dt_s": DT,
                        "precision": prec, "l2": "state (%.0f MB) larger than L2 (129 MB)" % (N_TRACERS * g.N * s / 1e6),
-                       "tile_staging": staging,
+                       "tile_staging": staging, "launch_shape": tuning,
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "ms_per_step": e2e_ms, "steps": e2e_steps,
@@ -1227,6 +1234,7 @@ def main():
     ap.add_argument("--staging", default="default", choices=["default", "tma", "cp.async"],
                     help="tile staging of the fused substep (default: the library's choice)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="lobster3d: keep the library's default launch shape")
     ap.add_argument("--shape", type=int, nargs=3, default=None,
                     help="grid size for profiling a smaller case of the same kernel (default 256 256 64)")
     args = ap.parse_args()

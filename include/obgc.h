@@ -602,6 +602,16 @@ int obgc_get_staging(const obgc_ctx* ctx, int32_t* available, int32_t* last_used
 int obgc_set_profiling(obgc_ctx* ctx, int32_t on);
 /* Vertical segment length (levels) of the fused kernel's work items (default: chosen per grid, 8 when the grid has enough tiles to fill the GPU, down to 2). */
 int obgc_set_tiling(obgc_ctx* ctx, int32_t levels_per_item);
+/* Autotune the fused step's launch shape on the bound state: for each candidate vertical segment
+ * length (2 .. 32 levels, capped at Nz) and tile staging (tensor copies where available, and
+ * cp.async), one warm-up step and `steps` timed steps of obgc_step(t, dt) from the saved state.
+ * Keeps the fastest (obgc_set_tiling / obgc_set_staging) and returns it with its ms per step (any
+ * output may be NULL).  The bound tracers, the sediment storages and the gas exchange's [H+] are
+ * restored before it returns, so the caller's state is unchanged; synchronizes the stream.
+ * The reference's functors (src/OceanBioME.jl:157-159) run inside Oceananigans' tendency kernels,
+ * launched with a fixed workgroup shape and no tuner. */
+int obgc_autotune_step(obgc_ctx* ctx, double t, double dt, int32_t steps, int32_t* levels_per_item,
+                       int32_t* staging, double* ms_per_step, void* stream);
 /* Air-sea gas exchange as the top boundary condition of the fused step (obgc_step, obgc_step_graph):
  * FieldBoundaryConditions(top = CarbonDioxideGasExchangeBoundaryCondition()) on DIC (g->gas CO2;
  * the model carries DIC, Alk, T and S) or OxygenGasExchangeBoundaryCondition() on O2 (the model

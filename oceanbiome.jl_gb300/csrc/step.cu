@@ -1424,6 +1424,107 @@ extern "C" int obgc_set_status_check(obgc_ctx* c, int32_t on) {
     return OBGC_OK;
 }
 
+// Device copies of everything an obgc_step call carries into the next one (the bound tracers, the
+// sediment storages and the gas exchange's warm-start [H+]), taken before the autotuner's trial
+// steps and written back after them; freed on every return path.
+struct StepSnapshot {
+    struct Piece {
+        void* live;
+        void* copy;
+        size_t bytes;
+    };
+    std::vector<Piece> pieces;
+    ~StepSnapshot() {
+        for (auto& p : pieces) cudaFree(p.copy);
+    }
+    int add(void* live, size_t bytes) {
+        if (!live || !bytes) return OBGC_OK;
+        Piece p{live, nullptr, bytes};
+        OBGC_CUDA(cudaMalloc(&p.copy, bytes));
+        pieces.push_back(p);
+        return OBGC_OK;
+    }
+    int save(cudaStream_t st) {
+        for (auto& p : pieces) OBGC_CUDA(cudaMemcpyAsync(p.copy, p.live, p.bytes, cudaMemcpyDeviceToDevice, st));
+        return OBGC_OK;
+    }
+    int restore(cudaStream_t st) {
+        for (auto& p : pieces) OBGC_CUDA(cudaMemcpyAsync(p.live, p.copy, p.bytes, cudaMemcpyDeviceToDevice, st));
+        return OBGC_OK;
+    }
+};
+
+extern "C" int obgc_autotune_step(obgc_ctx* c, double t, double dt, int32_t steps, int32_t* levels_per_item,
+                                  int32_t* staging, double* ms_per_step, void* stream) {
+    if (!c || !c->bound) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_autotune_step: context not bound");
+    if (steps < 1 || !(dt > 0)) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_autotune_step: bad dt / steps");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const obgc_grid& g = c->desc.grid;
+    const int64_t cols = (int64_t)g.Nx * g.Ny;
+    // the span of a bound field the kernels touch: its last cell is (Nx-1, Ny-1, Nz-1)
+    const int64_t span = (int64_t)g.stride_k * (g.Nz - 1) + (int64_t)g.stride_j * (g.Ny - 1) + g.Nx;
+    StepSnapshot snap;
+    for (int t = 0; t < c->NT + c->NP; t++) {
+        const int rc = snap.add(c->user[t], c->ts * span);
+        if (rc != OBGC_OK) return rc;
+    }
+    int rc = snap.add(c->sed_storage, c->ts * cols);
+    if (rc == OBGC_OK) rc = snap.add(c->mg_state, sizeof(double) * 4 * cols);
+    for (const auto& gc : c->gas)
+        if (rc == OBGC_OK && gc.on) rc = snap.add(gc.H, sizeof(double) * cols);
+    if (rc == OBGC_OK) rc = snap.save(st);
+    if (rc != OBGC_OK) return rc;
+
+    const int TZ0 = c->TZ, staging0 = c->staging;
+    const bool profile0 = c->profile, check0 = c->status_check;
+    c->profile = false;
+    c->status_check = true;
+    // the candidates: levels per work item, each with both tile stagings where the tensor copies exist
+    std::vector<int> tzs;
+    for (int tz : {2, 3, 4, 6, 8, 10, 12, 16, 24, 32}) {
+        const int v = std::min(tz, g.Nz);
+        if (std::find(tzs.begin(), tzs.end(), v) == tzs.end()) tzs.push_back(v);
+    }
+    double best = 1e300;
+    int best_tz = TZ0, best_staging = staging0;
+    for (int tz : tzs) {
+        for (int sg = c->tma_ready ? 1 : 0; sg >= 0 && rc == OBGC_OK; sg--) {
+            c->TZ = tz;
+            c->staging = sg;
+            // one warm-up step, then the timed steps; each candidate from the saved state
+            rc = obgc_step(c, t, dt, 1, stream);
+            if (rc == OBGC_OK) rc = snap.restore(st);
+            if (rc != OBGC_OK) break;
+            rc = obgc_step(c, t, dt, steps, stream);
+            if (rc != OBGC_OK) break;
+            float ms = 0;
+            const cudaError_t e = cudaEventElapsedTime(&ms, c->ev_begin, c->ev_end);
+            if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventElapsedTime"); break; }
+            if (ms < best) { best = ms; best_tz = tz; best_staging = sg; }
+            rc = snap.restore(st);
+        }
+        if (rc != OBGC_OK) break;
+    }
+    const int rc_restore = snap.restore(st);
+    const cudaError_t e_sync = cudaStreamSynchronize(st);
+    c->profile = profile0;
+    c->status_check = check0;
+    c->graph_version = ~0ull;
+    if (rc != OBGC_OK) {
+        c->TZ = TZ0;
+        c->staging = staging0;
+        return rc;
+    }
+    if (rc_restore != OBGC_OK) return rc_restore;
+    if (e_sync != cudaSuccess) return cuda_fail(e_sync, "cudaStreamSynchronize");
+    c->TZ = best_tz;
+    c->staging = best_staging;
+    if (levels_per_item) *levels_per_item = best_tz;
+    if (staging) *staging = best_staging;
+    if (ms_per_step) *ms_per_step = best / steps;
+    return OBGC_OK;
+}
+
 extern "C" int obgc_last_step_timing(const obgc_ctx* c, double* total_ms, double* substep_ms, int64_t* launches) {
     if (!c) return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_last_step_timing: null context");
     if (!c->profile) {

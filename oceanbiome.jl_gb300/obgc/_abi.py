@@ -372,6 +372,7 @@ def load():
     _sig(lib, "obgc_tracer_budget_static", C.c_int, P(Grid), I32, I32, P(VP), P(D), P(D), VP)
     _sig(lib, "obgc_set_profiling", C.c_int, VP, I32)
     _sig(lib, "obgc_set_tiling", C.c_int, VP, I32)
+    _sig(lib, "obgc_autotune_step", C.c_int, VP, D, D, I32, P(I32), P(I32), P(D), VP)
     _sig(lib, "obgc_box_run", C.c_int, P(NPDParams), VP, I64, VP, VP, D, D, D, I32, I32, VP, I32, VP)
     _sig(lib, "obgc_box_run_drivers", C.c_int, P(NPDParams), VP, I64, VP, P(BoxDrivers), D, D, I32, I32, VP, I32, VP)
     _sig(lib, "obgc_npd_conserved_tracers", C.c_int, P(NPDParams), I32, P(I32), P(D), I32)
@@ -427,7 +428,7 @@ EXPORTED = [
     "obgc_step_graph", "obgc_step_status", "obgc_set_status_check", "obgc_substep", "obgc_halo_pack", "obgc_halo_unpack",
     "obgc_multig_default_params", "obgc_set_multig_sediment", "obgc_multig_sediment_state",
     "obgc_set_staging", "obgc_get_staging", "obgc_last_step_timing", "obgc_tracer_budget", "obgc_box_run", "obgc_box_run_drivers",
-    "obgc_set_profiling", "obgc_set_tiling", "obgc_struct_layout", "obgc_tracer_budget_static",
+    "obgc_set_profiling", "obgc_set_tiling", "obgc_autotune_step", "obgc_struct_layout", "obgc_tracer_budget_static",
     "obgc_columns_create", "obgc_columns_destroy", "obgc_columns_tracers", "obgc_columns_add",
     "obgc_columns_advance", "obgc_columns_run", "obgc_columns_remaining", "obgc_columns_read", "obgc_columns_remove",
     "obgc_columns_autotune", "obgc_npd_conserved_tracers", "obgc_scale_negatives", "obgc_zero_negatives",

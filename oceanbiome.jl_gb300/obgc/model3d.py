@@ -263,6 +263,14 @@ class NonhydrostaticModel:
     def set_tiling(self, levels):
         A.check(self._lib.obgc_set_tiling(self._ctx, int(levels)), "obgc_set_tiling")
 
+    def autotune(self, dt, steps=3):
+        """Time the fused step's candidate segment lengths and tile stagings on the current state
+        (restored afterwards) and keep the fastest: returns (levels per item, staging, ms per step)."""
+        tz, sg, ms = C.c_int32(0), C.c_int32(0), C.c_double(0)
+        A.check(self._lib.obgc_autotune_step(self._ctx, self.clock.time, float(dt), int(steps), C.byref(tz), C.byref(sg),
+                                             C.byref(ms), self._stream()), "obgc_autotune_step")
+        return tz.value, sg.value, ms.value
+
     def last_timing(self):
         tot, sub, n = C.c_double(0), C.c_double(0), C.c_int64(0)
         A.check(self._lib.obgc_last_step_timing(self._ctx, C.byref(tot), C.byref(sub), C.byref(n)), "obgc_last_step_timing")
