@@ -599,8 +599,70 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             // the tile's east (8 per tracer) and north (32 per tracer) edge faces, spread over
             // every thread of the block
             constexpr int NEDGE = STEP_BY + STEP_BX;
+            bool edges_done = false;
+#ifdef __CUDA_ARCH__
+            if constexpr (sizeof(TC) == 4) {
+                // FP32 without horizontal diffusion: the 40 edge faces of a tracer as 20 pairs, each one
+                // packed WENO5 (east face r with north face r for r < 8, then the remaining north faces
+                // two by two), so one pass over the block covers up to 12 tracers; a pair with a face
+                // next to a wall takes the scalar reconstruction of each face
+                if (!hdiff) {
+                    constexpr int NPAIR = NEDGE / 2;
+                    // face q of a pair: its stencil (6 values c[f-3 .. f+2], stride st), face index f of
+                    // a line of N cells, periodicity, and its normal velocity (0 where it has no flux)
+                    auto edge_face = [&](int t, int e, const TC*& s, int& st, int& f, int& N, bool& per, TC& U) {
+                        const TC* tl = tiles + t * TILE_SZ;
+                        if (e < STEP_BY) {
+                            const int jr = j0 + e;
+                            f = i0 + STEP_BX; N = a.Nx; per = periodic_x; st = 1;
+                            s = tl + (e + HALO) * TILE_W + TILE_X0 + STEP_BX;
+                            U = (!a.flat_x && jr < a.Ny && f <= a.Nx)
+                                    ? face_velocity<TS, TC>(a.u, (int64_t)jr * vsj + vk, 1, a.Nx, periodic_x, f) : TC(0);
+                        } else {
+                            const int cc = e - STEP_BY, ix = i0 + cc;
+                            f = j0 + STEP_BY; N = a.Ny; per = periodic_y; st = TILE_W;
+                            s = tl + STEP_BY * TILE_W + TILE_X0 + cc + HALO;
+                            U = (!a.flat_y && ix < a.Nx && f <= a.Ny)
+                                    ? face_velocity<TS, TC>(a.v, ix + vk, vsj, a.Ny, periodic_y, f) : TC(0);
+                        }
+                    };
+                    auto store_face = [&](int t, int e, TC F) {
+                        if (e < STEP_BY) fx[t][e][STEP_BX] = F;
+                        else fy[t][STEP_BY][e - STEP_BY] = F;
+                    };
 #pragma unroll 1
-            for (int e = tid; e < NT * NEDGE; e += NTH) {
+                    for (int p = tid; p < NT * NPAIR; p += NTH) {
+                        const int t = p / NPAIR, r = p - t * NPAIR;
+                        const int eA = r < STEP_BY ? r : STEP_BY + 2 * r - STEP_BY;      // 0..7, then north 8, 10, ..
+                        const int eB = r < STEP_BY ? STEP_BY + r : eA + 1;               // north 0..7, then 9, 11, ..
+                        const TC *sA, *sB;
+                        int stA, stB, fA, fB, NA, NB;
+                        bool perA, perB;
+                        TC UA, UB;
+                        edge_face(t, eA, sA, stA, fA, NA, perA, UA);
+                        edge_face(t, eB, sB, stB, fB, NB, perB, UB);
+                        if ((perA || min(fA, NA - fA) >= 3) && (perB || min(fB, NB - fB) >= 3)) {
+                            const bool pa = UA > TC(0), pb = UB > TC(0);
+                            const f32x2 w = weno5_x2(pk2(pa ? sA[0] : sA[5 * stA], pb ? sB[0] : sB[5 * stB]),
+                                                     pk2(pa ? sA[stA] : sA[4 * stA], pb ? sB[stB] : sB[4 * stB]),
+                                                     pk2(pa ? sA[2 * stA] : sA[3 * stA], pb ? sB[2 * stB] : sB[3 * stB]),
+                                                     pk2(pa ? sA[3 * stA] : sA[2 * stA], pb ? sB[3 * stB] : sB[2 * stB]),
+                                                     pk2(pa ? sA[4 * stA] : sA[stA], pb ? sB[4 * stB] : sB[stB]));
+                            float ra, rb;
+                            up2(w, ra, rb);
+                            store_face(t, eA, UA == TC(0) ? TC(0) : UA * ra);
+                            store_face(t, eB, UB == TC(0) ? TC(0) : UB * rb);
+                        } else {
+                            store_face(t, eA, tile_face_flux<TC>(sA, stA, perA, fA, NA, UA));
+                            store_face(t, eB, tile_face_flux<TC>(sB, stB, perB, fB, NB, UB));
+                        }
+                    }
+                    edges_done = true;
+                }
+            }
+#endif
+#pragma unroll 1
+            for (int e = edges_done ? NT * NEDGE : tid; e < NT * NEDGE; e += NTH) {
                 const int t = e / NEDGE, r = e - t * NEDGE;
                 const TC* tl = tiles + t * TILE_SZ;
                 if (r < STEP_BY) {
