@@ -319,6 +319,12 @@ struct obgc_ctx {
     int staging = 1;
     bool last_used_tma = false;
     int TZ = 0;                         // levels per work item; 0: chosen per grid (fill_args)
+    // the chlorophyll sums above each segment (par_prefix_kernel), room for par_prefix_segs segments
+    // below the first (enough for any segment length of two levels or more), and whether the last
+    // dispatch launched the pre-pass
+    void* par_prefix = nullptr;
+    int par_prefix_segs = 0;
+    bool prefix_on = false;
     int blocks = 0;
     bool bound = false;
     // graph replay
@@ -343,6 +349,7 @@ static int ctx_free(obgc_ctx* c) {
         if (c->G[t]) cudaFree(c->G[t]);
     }
     if (c->drift) cudaFree(c->drift);
+    if (c->par_prefix) cudaFree(c->par_prefix);
     if (c->d_time) cudaFree(c->d_time);
     if (c->d_status) cudaFree(c->d_status);
     for (int q = 0; q < 2; q++)
@@ -503,6 +510,8 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
         }
     }
     alloc(&c->drift, c->tc * prof.size());
+    c->par_prefix_segs = (g.Nz + 1) / 2 - 1;
+    if (c->par_prefix_segs > 0) alloc(&c->par_prefix, c->tc * 2 * (size_t)c->par_prefix_segs * g.Nx * g.Ny);
     alloc((void**)&c->d_time, sizeof(double));
     alloc((void**)&c->d_status, sizeof(int));
     if (rc == OBGC_OK) {
@@ -964,6 +973,23 @@ static bool needs_clock(const obgc_ctx* c) {
 }
 
 // The surface-flux and forcing slots of the launch over slots [b, b + n).
+// The TwoBand chlorophyll sums above every segment of the stage's input, for the substep launch that
+// follows (segments of two levels or more, a model with the in-kernel PAR); otherwise the work items
+// sum them themselves.
+template <typename TS, typename TC>
+static int launch_par_prefix(obgc_ctx* c, SubstepArgs<TS, TC>& a, cudaStream_t st) {
+    a.par_prefix = nullptr;
+    c->prefix_on = false;
+    if (!c->par_prefix || c->V == V_EXTERNAL || a.nseg < 2 || a.nseg - 1 > c->par_prefix_segs) return OBGC_OK;
+    const int64_t cols = (int64_t)a.Nx * a.Ny;
+    par_prefix_kernel<TS, TC><<<(unsigned)((cols + 255) / 256), 256, 0, st>>>(
+        a.in[slot_of_P(c->V)], a.sj, a.sk, a.Nx, a.Ny, a.Nz, a.TZ, a.nseg, a.light, (TC*)c->par_prefix);
+    OBGC_LAUNCHED("par_prefix_kernel");
+    a.par_prefix = (const TC*)c->par_prefix;
+    c->prefix_on = true;
+    return OBGC_OK;
+}
+
 template <typename TS, typename TC>
 static void launch_terms(const obgc_ctx* c, SubstepArgs<TS, TC>& a, int b, int n) {
     int nt = 0, nf = 0;
@@ -1105,8 +1131,10 @@ static int enqueue_stage(obgc_ctx* c, StepPlan<TS, TC>& p, int stg, void* const*
     }
     for (int t = 0; t < c->NT; t++) { a.in[t] = (const TS*)cur[t]; a.out[t] = (TS*)nxt[t]; }
     launch_terms(c, a, 0, c->NT);
+    int rc = launch_par_prefix(c, a, st);
+    if (rc != OBGC_OK) return rc;
     if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
-    int rc = p.fe->launch(&a, p.blocks, st);
+    rc = p.fe->launch(&a, p.blocks, st);
     if (rc != OBGC_OK) return rc;
     for (int q = 0, b = c->NT; q < c->nchunk; b += c->pchunk[q++]) {
         const int n = c->pchunk[q];
@@ -1195,8 +1223,10 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
             a.tmap = stg == 0 ? (c->umaps_ok ? c->d_tmaps + 2 * MAX_NT : nullptr) : c->d_tmaps + (size_t)(stg - 1) * MAX_NT;
             a.tma_x0 = stg == 0 ? -TMA_HX : 0;
             a.tma_y0 = stg == 0 ? -HALO : 0;
+            int rc = launch_par_prefix(c, a, st);
+            if (rc != OBGC_OK) return rc;
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
-            const int rc = p.fe->launch(&a, p.blocks, st);
+            rc = p.fe->launch(&a, p.blocks, st);
             if (rc != OBGC_OK) return rc;
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
         }
@@ -1331,7 +1361,7 @@ static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     int gases = 0;
     for (const auto& gc : c->gas) gases = gases || gc.on ? 1 : 0;   // one launch for all conditions
     const bool impl = c->vimplicit && c->kzf;
-    const int per_stage = 1 + c->nchunk + gases + (impl ? 1 + neg : 0) + (c->mg_on ? 1 : 0);
+    const int per_stage = 1 + c->nchunk + gases + (impl ? 1 + neg : 0) + (c->mg_on ? 1 : 0) + (c->prefix_on ? 1 : 0);
     return (c->mg_on ? 1 : 0) + (int64_t)nsteps * (3 * per_stage + (clock ? 1 : 0)) + (nsteps % 2 && !c->last_used_tma ? c->NT + c->NP : 0) + 1 + neg + (impl ? 1 : 0);
 }
 

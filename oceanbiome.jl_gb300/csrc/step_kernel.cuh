@@ -117,6 +117,10 @@ struct SubstepArgs {
     uint32_t drift_mask;
     NPDParamsT<TC> bgc;
     TwoBandT<TC> light;
+    // the chlorophyll sums of TwoBand PAR above each segment: par_prefix[(2 (s - 1) + b) Nx Ny + i + j Nx]
+    // for segment s >= 1 and band b (red 0, blue 1), written by par_prefix_kernel before the launch;
+    // NULL: each work item sums the cells above its segment itself
+    const TC* par_prefix;
     int surf_kind;
     TC surf_value;            // OBGC_SURFACE_PAR_CONSTANT value
     const TS* surf_field;     // OBGC_SURFACE_PAR_FIELD
@@ -464,15 +468,23 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             return SPLIT ? e + (TILE_W - (STEP_BX + 2 * HALO)) * (e / (STEP_BX + 2 * HALO)) + TILE_X0 : e;
         };
 
-        // chlorophyll integral of the cells above the segment
+        // chlorophyll integral of the cells above the segment: from the pre-pass, or summed here
         TC Sr = TC(0), Sb = TC(0);
         if constexpr (V != V_EXTERNAL) {
+            if (a.par_prefix != nullptr) {
+                if (seg > 0) {
+                    const int64_t cols = (int64_t)a.Nx * a.Ny, c2 = ic + (int64_t)jc * a.Nx;
+                    Sr = a.par_prefix[(int64_t)(2 * seg - 2) * cols + c2];
+                    Sb = a.par_prefix[(int64_t)(2 * seg - 1) * cols + c2];
+                }
+            } else {
 #pragma unroll 1
-            for (int k = a.Nz - 1; k > k_top; --k) {
-                TC fr, fb;
-                twoband_terms(a.light, ld<TS, TC>(a.in[SP], col + (int64_t)k * a.sk), fr, fb);
-                Sr += fr;
-                Sb += fb;
+                for (int k = a.Nz - 1; k > k_top; --k) {
+                    TC fr, fb;
+                    twoband_terms(a.light, ld<TS, TC>(a.in[SP], col + (int64_t)k * a.sk), fr, fb);
+                    Sr += fr;
+                    Sb += fb;
+                }
             }
         }
 
@@ -861,6 +873,44 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     }
     if (bad && a.status) atomicOr(a.status, OBGC_FLAG_NAN);
     if (tma_timeout && a.status) atomicOr(a.status, OBGC_FLAG_TIMEOUT);
+}
+
+// The chlorophyll sums of TwoBand PAR above the top of every segment of TZ levels but the first,
+// for the substep launch that follows (its par_prefix).  One thread per column sums the cells from
+// the surface down in the order the substep kernel's own loop does (the same terms and additions,
+// so the sums are bit for bit the ones a work item would form), eight loads in flight at a time.
+// Each work item of the substep then reads two values instead of summing up to Nz - TZ levels: the
+// lower segments' items otherwise repeated the upper segments' logarithms and powers.
+template <typename TS, typename TC>
+__global__ void __launch_bounds__(256) par_prefix_kernel(const TS* __restrict__ P, int64_t sj, int64_t sk, int Nx, int Ny,
+                                                         int Nz, int TZ, int nseg, TwoBandT<TC> L, TC* __restrict__ out) {
+    const int64_t cols = (int64_t)Nx * Ny;
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    const int i = (int)(c % Nx), j = (int)(c / Nx);
+    const TS* p = P + i + (int64_t)j * sj;
+    TC Sr = TC(0), Sb = TC(0);
+    int k = Nz - 1;
+    for (int s = 1; s < nseg; s++) {
+        const int kend = Nz - 1 - s * TZ;   // the top level of segment s, the first one not summed
+        while (k > kend) {
+            const int n = min(8, k - kend);
+            TC v[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) v[q] = q < n ? ld<TS, TC>(p, (int64_t)(k - q) * sk) : TC(0);
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+                if (q < n) {
+                    TC fr, fb;
+                    twoband_terms(L, v[q], fr, fb);
+                    Sr += fr;
+                    Sb += fb;
+                }
+            k -= n;
+        }
+        out[(int64_t)(2 * s - 2) * cols + c] = Sr;
+        out[(int64_t)(2 * s - 1) * cols + c] = Sb;
+    }
 }
 
 }  // namespace obgc
