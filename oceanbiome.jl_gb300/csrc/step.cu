@@ -1188,10 +1188,11 @@ static bool tma_eligible(obgc_ctx* c, const StepPlan<TS, TC>& p) {
     return !substep_needs_ext(x);
 }
 
-// Steps with TMA-staged tiles.  Every step runs bound arrays -> padded set 0 -> padded set 1 ->
-// bound arrays: the first stage stages its tiles from the caller's arrays by cp.async; it and the
-// second stage write the padded sets together with their periodic halo images, so that the second
-// and third stages stage whole tiles with one tensor copy per tracer and level.
+// Steps with TMA-staged tiles.  The 3 nsteps stages of the call run bound arrays -> padded set 0 ->
+// padded set 1 -> padded set 0 -> ... -> bound arrays: only the call's first stage reads the caller's
+// arrays (MODE 1: tensor copies of the wrap-free tiles, cp.async for the others) and only its last
+// stage writes them; every other stage writes a padded set together with its periodic halo images,
+// so that the next stage stages whole tiles with one tensor copy per tracer and level (MODE 2).
 template <typename TS, typename TC>
 static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int nsteps, cudaStream_t st, bool profile) {
     SubstepArgs<TS, TC>& a = p.a;
@@ -1202,27 +1203,29 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
     a.gsk = c->pad_sk;
     const bool clock = needs_clock(c);
     size_t ev = 0;
+    const int last = 3 * nsteps - 1;
     for (int s = 0; s < nsteps; s++) {
         for (int stg = 0; stg < 3; stg++) {
+            const int q = 3 * s + stg;          // the stage's place in the call
             a.first_stage = stg == 0;
             a.write_G = stg < 2;
             a.gamma = TC(rk3_gamma(stg));
             a.zeta = TC(rk3_zeta(stg));
             a.c_stage = rk3_c(stg);
             for (int t = 0; t < c->NT; t++) {
-                a.in[t] = stg == 0 ? (const TS*)c->user[t] : (const TS*)c->pad[stg - 1][t] + org;
-                a.out[t] = stg == 2 ? (TS*)c->user[t] : (TS*)c->pad[stg][t] + org;
+                a.in[t] = q == 0 ? (const TS*)c->user[t] : (const TS*)c->pad[(q - 1) % 2][t] + org;
+                a.out[t] = q == last ? (TS*)c->user[t] : (TS*)c->pad[q % 2][t] + org;
             }
-            a.sj = stg == 0 ? g.stride_j : c->pad_sj;
-            a.sk = stg == 0 ? g.stride_k : c->pad_sk;
-            a.osj = stg == 2 ? g.stride_j : c->pad_sj;
-            a.osk = stg == 2 ? g.stride_k : c->pad_sk;
-            a.out_halo = stg < 2;
-            a.tma_layout = stg == 0 ? 1 : 2;
-            // the first stage copies the bound arrays' wrap-free tiles when they have tensor maps
-            a.tmap = stg == 0 ? (c->umaps_ok ? c->d_tmaps + 2 * MAX_NT : nullptr) : c->d_tmaps + (size_t)(stg - 1) * MAX_NT;
-            a.tma_x0 = stg == 0 ? -TMA_HX : 0;
-            a.tma_y0 = stg == 0 ? -HALO : 0;
+            a.sj = q == 0 ? g.stride_j : c->pad_sj;
+            a.sk = q == 0 ? g.stride_k : c->pad_sk;
+            a.osj = q == last ? g.stride_j : c->pad_sj;
+            a.osk = q == last ? g.stride_k : c->pad_sk;
+            a.out_halo = q != last;
+            a.tma_layout = q == 0 ? 1 : 2;
+            // the call's first stage copies the bound arrays' wrap-free tiles when they have tensor maps
+            a.tmap = q == 0 ? (c->umaps_ok ? c->d_tmaps + 2 * MAX_NT : nullptr) : c->d_tmaps + (size_t)((q - 1) % 2) * MAX_NT;
+            a.tma_x0 = q == 0 ? -TMA_HX : 0;
+            a.tma_y0 = q == 0 ? -HALO : 0;
             int rc = launch_par_prefix(c, a, st);
             if (rc != OBGC_OK) return rc;
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
