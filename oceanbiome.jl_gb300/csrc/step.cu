@@ -982,7 +982,7 @@ static int launch_par_prefix(obgc_ctx* c, SubstepArgs<TS, TC>& a, cudaStream_t s
     c->prefix_on = false;
     if (!c->par_prefix || c->V == V_EXTERNAL || a.nseg < 2 || a.nseg - 1 > c->par_prefix_segs) return OBGC_OK;
     const int64_t cols = (int64_t)a.Nx * a.Ny;
-    par_prefix_kernel<TS, TC><<<(unsigned)((cols + 255) / 256), 256, 0, st>>>(
+    par_prefix_kernel<TS, TC><<<(unsigned)((cols + PP_COLS - 1) / PP_COLS), 256, 0, st>>>(
         a.in[slot_of_P(c->V)], a.sj, a.sk, a.Nx, a.Ny, a.Nz, a.TZ, a.nseg, a.light, (TC*)c->par_prefix);
     OBGC_LAUNCHED("par_prefix_kernel");
     a.par_prefix = (const TC*)c->par_prefix;

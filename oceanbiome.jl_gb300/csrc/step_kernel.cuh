@@ -427,6 +427,9 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     }
 
     bool bad = false;   // a non-finite value was stored by this thread
+    // FP32: NaN-or-infinity detector on the FMA pipe, fma(U, 0, acc) (0 for a finite U, NaN otherwise),
+    // in place of a compare and a predicate OR per stored value on the busier ALU pipe
+    TS nanacc = TS(0);
     for (int item = blockIdx.x; item < a.n_items; item += gridDim.x) {
         const int seg = item % a.nseg;                       // top segment first
         const int tile = item / a.nseg;
@@ -852,7 +855,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     if constexpr (sizeof(TS) == sizeof(TC)) Uo = c[t] + Un;
                     else Uo = TS(__ldg(a.in[t] + idx)) + TS(Un);
                     a.out[t][oidx] = Uo;
-                    bad |= !(fabs(Uo) <= TS(INFINITY));
+                    if constexpr (sizeof(TS) == 4) nanacc = fmaf(Uo, 0.f, nanacc);
+                    else bad |= !(fabs(Uo) <= TS(INFINITY));
                     if (SPLIT) {
                         if (img_x) a.out[t][oidx + img_x] = Uo;
                         if (img_y) a.out[t][oidx + img_y] = Uo;
@@ -871,45 +875,55 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             }
         }
     }
+    bad |= !(nanacc == TS(0));
     if (bad && a.status) atomicOr(a.status, OBGC_FLAG_NAN);
     if (tma_timeout && a.status) atomicOr(a.status, OBGC_FLAG_TIMEOUT);
 }
 
 // The chlorophyll sums of TwoBand PAR above the top of every segment of TZ levels but the first,
-// for the substep launch that follows (its par_prefix).  One thread per column sums the cells from
-// the surface down in the order the substep kernel's own loop does (the same terms and additions,
-// so the sums are bit for bit the ones a work item would form), eight loads in flight at a time.
-// Each work item of the substep then reads two values instead of summing up to Nz - TZ levels: the
-// lower segments' items otherwise repeated the upper segments' logarithms and powers.
+// for the substep launch that follows (its par_prefix).  A block takes PP_COLS columns: its eight
+// warps evaluate the terms of PP_CHUNK levels at a time into shared memory (all loads and powers of
+// a chunk in parallel), then the first warp adds them up per column from the surface down, in the
+// order the substep kernel's own loop does (the same terms and additions, so the sums are bit for
+// bit the ones a work item would form), and writes the sum at each segment's top.  Each work item of
+// the substep then reads two values instead of summing up to Nz - TZ levels.
+constexpr int PP_COLS = 32;
+constexpr int PP_CHUNK = 64;
 template <typename TS, typename TC>
 __global__ void __launch_bounds__(256) par_prefix_kernel(const TS* __restrict__ P, int64_t sj, int64_t sk, int Nx, int Ny,
                                                          int Nz, int TZ, int nseg, TwoBandT<TC> L, TC* __restrict__ out) {
+    __shared__ TC fr_s[PP_CHUNK][PP_COLS], fb_s[PP_CHUNK][PP_COLS];
     const int64_t cols = (int64_t)Nx * Ny;
-    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (c >= cols) return;
-    const int i = (int)(c % Nx), j = (int)(c / Nx);
-    const TS* p = P + i + (int64_t)j * sj;
+    const int col = threadIdx.x % PP_COLS, lane = threadIdx.x / PP_COLS;   // lane: 0 .. 7
+    const int64_t c = (int64_t)blockIdx.x * PP_COLS + col;
+    const bool live = c < cols;
+    const TS* p = P + (live ? (c % Nx) + (c / Nx) * sj : 0);
+    const int nlev = (nseg - 1) * TZ;   // the levels above the last segment's top, from the surface
     TC Sr = TC(0), Sb = TC(0);
-    int k = Nz - 1;
-    for (int s = 1; s < nseg; s++) {
-        const int kend = Nz - 1 - s * TZ;   // the top level of segment s, the first one not summed
-        while (k > kend) {
-            const int n = min(8, k - kend);
-            TC v[8];
-#pragma unroll
-            for (int q = 0; q < 8; q++) v[q] = q < n ? ld<TS, TC>(p, (int64_t)(k - q) * sk) : TC(0);
-#pragma unroll
-            for (int q = 0; q < 8; q++)
-                if (q < n) {
-                    TC fr, fb;
-                    twoband_terms(L, v[q], fr, fb);
-                    Sr += fr;
-                    Sb += fb;
-                }
-            k -= n;
+    int s = 1;                          // the next segment whose sum is due
+    for (int c0 = 0; c0 < nlev; c0 += PP_CHUNK) {
+        const int n = min(PP_CHUNK, nlev - c0);
+        for (int q = lane; q < n; q += 256 / PP_COLS) {
+            TC fr = TC(0), fb = TC(0);
+            if (live) twoband_terms(L, ld<TS, TC>(p, (int64_t)(Nz - 1 - (c0 + q)) * sk), fr, fb);
+            fr_s[q][col] = fr;
+            fb_s[q][col] = fb;
         }
-        out[(int64_t)(2 * s - 2) * cols + c] = Sr;
-        out[(int64_t)(2 * s - 1) * cols + c] = Sb;
+        __syncthreads();
+        if (lane == 0) {
+            for (int q = 0; q < n; q++) {
+                Sr += fr_s[q][col];
+                Sb += fb_s[q][col];
+                if (c0 + q + 1 == s * TZ) {   // the levels above segment s are summed
+                    if (live) {
+                        out[(int64_t)(2 * s - 2) * cols + c] = Sr;
+                        out[(int64_t)(2 * s - 1) * cols + c] = Sb;
+                    }
+                    s++;
+                }
+            }
+        }
+        __syncthreads();
     }
 }
 

@@ -39,7 +39,6 @@ __device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
-__device__ __forceinline__ f32x2 abs2(f32x2 a) { return a & 0x7fffffff7fffffffull; }
 __device__ __forceinline__ f32x2 splat2(float x) { return pk2(x, x); }
 __device__ __forceinline__ f32x2 rcp2(f32x2 a) {
     float lo, hi;
@@ -69,7 +68,9 @@ __device__ __forceinline__ f32x2 weno5_x2(f32x2 v1, f32x2 v2, f32x2 v3, f32x2 v4
     a = fma2(m2, d4, d5);
     b = fma2(m4, d4, d5);
     const f32x2 b2 = fma2(mul2(k1312, a), a, mul2(mul2(k14, b), b));
-    const f32x2 tau = abs2(sub2(b0, b2));
+    // tau = |b0 - b2| enters only through r_k^2: its sign changes no weight, so no abs (two ALU
+    // instructions a pair)
+    const f32x2 tau = sub2(b0, b2);
     const f32x2 r0 = mul2(tau, rcp2(add2(b0, eps)));
     const f32x2 r1 = mul2(tau, rcp2(add2(b1, eps)));
     const f32x2 r2 = mul2(tau, rcp2(add2(b2, eps)));

@@ -34,11 +34,12 @@ def raw_step(model, graph=False):
     return fn(model._ctx, model.clock.time, 300.0, 2, model._stream())
 
 
-@pytest.mark.parametrize("precision", ["f32", "mixed", "f64"])
-def test_nan_in_the_state_is_reported(precision):
+@pytest.mark.parametrize("precision,bad", [("f32", math.nan), ("mixed", math.nan), ("f64", math.nan),
+                                          ("f32", math.inf), ("f64", -math.inf)])
+def test_nan_in_the_state_is_reported(precision, bad):
     model, init = lobster(precision)
     p = model.tracers["P"].cpu().numpy().copy()
-    p[3, 4, 5] = math.nan
+    p[3, 4, 5] = bad
     obgc.set_(model, P=p)
     with pytest.raises(A.ObgcError) as e:
         obgc.time_step(model, 300.0, nsteps=2)
