@@ -325,6 +325,10 @@ struct obgc_ctx {
     void* par_prefix = nullptr;
     int par_prefix_segs = 0;
     bool prefix_on = false;
+    // the window slots' vertical face fluxes of the TMA-staged stages (sink_flux_kernel), and
+    // whether the last dispatch launched that pre-pass
+    void* fz_pre = nullptr;
+    bool sinkpre_on = false;
     int blocks = 0;
     bool bound = false;
     // graph replay
@@ -350,6 +354,7 @@ static int ctx_free(obgc_ctx* c) {
     }
     if (c->drift) cudaFree(c->drift);
     if (c->par_prefix) cudaFree(c->par_prefix);
+    if (c->fz_pre) cudaFree(c->fz_pre);
     if (c->d_time) cudaFree(c->d_time);
     if (c->d_status) cudaFree(c->d_status);
     for (int q = 0; q < 2; q++)
@@ -414,6 +419,11 @@ static int setup_tma(obgc_ctx* c) {
         }
     cudaError_t e = cudaMalloc(&c->d_tmaps, sizeof(CUtensorMap) * maps.size());
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(tensor maps)");
+    // the sinking tracers' face fluxes of the TMA-staged stages
+    if (c->drift_mask & ((1u << window_a(c->V)) | (1u << window_b(c->V)))) {
+        e = cudaMalloc(&c->fz_pre, sizeof(float) * 2 * (size_t)(g.Nz + 1) * g.Nx * g.Ny);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(sinking fluxes)");
+    }
     e = cudaMemcpy(c->d_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(tensor maps)");
     c->tma_ready = true;
@@ -990,6 +1000,25 @@ static int launch_par_prefix(obgc_ctx* c, SubstepArgs<TS, TC>& a, cudaStream_t s
     return OBGC_OK;
 }
 
+// The window slots' vertical face fluxes of the stage's input, for the TMA-staged substep launch that
+// follows (when the model has sinking tracers in the window slots).
+template <typename TS, typename TC>
+static int launch_sink_flux(obgc_ctx* c, SubstepArgs<TS, TC>& a, cudaStream_t st) {
+    a.fz_pre = nullptr;
+    c->sinkpre_on = false;
+    const int wa = window_a(c->V), wb = window_b(c->V);
+    if (!(a.drift_mask & ((1u << wa) | (1u << wb)))) return OBGC_OK;
+    if (!c->fz_pre) return fail(OBGC_ERR_UNSUPPORTED, "obgc_step: no buffer for the sinking fluxes");
+    const int64_t cols = (int64_t)a.Nx * a.Ny;
+    const dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((a.Nz + 1 + 7) / 8));
+    sink_flux_kernel<TS, TC><<<grid, 256, 0, st>>>(a.in[wa], a.in[wb], a.sj, a.sk, a.Nx, a.Ny, a.Nz, a.drift, wa, wb,
+                                                   (TC*)c->fz_pre);
+    OBGC_LAUNCHED("sink_flux_kernel");
+    a.fz_pre = (const TC*)c->fz_pre;
+    c->sinkpre_on = true;
+    return OBGC_OK;
+}
+
 template <typename TS, typename TC>
 static void launch_terms(const obgc_ctx* c, SubstepArgs<TS, TC>& a, int b, int n) {
     int nt = 0, nf = 0;
@@ -1227,6 +1256,7 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
             a.tma_x0 = q == 0 ? -TMA_HX : 0;
             a.tma_y0 = q == 0 ? -HALO : 0;
             int rc = launch_par_prefix(c, a, st);
+            if (rc == OBGC_OK) rc = launch_sink_flux(c, a, st);
             if (rc != OBGC_OK) return rc;
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
             rc = p.fe->launch(&a, p.blocks, st);
@@ -1364,7 +1394,8 @@ static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     int gases = 0;
     for (const auto& gc : c->gas) gases = gases || gc.on ? 1 : 0;   // one launch for all conditions
     const bool impl = c->vimplicit && c->kzf;
-    const int per_stage = 1 + c->nchunk + gases + (impl ? 1 + neg : 0) + (c->mg_on ? 1 : 0) + (c->prefix_on ? 1 : 0);
+    const int per_stage = 1 + c->nchunk + gases + (impl ? 1 + neg : 0) + (c->mg_on ? 1 : 0) + (c->prefix_on ? 1 : 0) +
+                          (c->last_used_tma && c->sinkpre_on ? 1 : 0);
     return (c->mg_on ? 1 : 0) + (int64_t)nsteps * (3 * per_stage + (clock ? 1 : 0)) + (nsteps % 2 && !c->last_used_tma ? c->NT + c->NP : 0) + 1 + neg + (impl ? 1 : 0);
 }
 

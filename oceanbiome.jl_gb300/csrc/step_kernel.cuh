@@ -121,6 +121,10 @@ struct SubstepArgs {
     // for segment s >= 1 and band b (red 0, blue 1), written by par_prefix_kernel before the launch;
     // NULL: each work item sums the cells above its segment itself
     const TC* par_prefix;
+    // the TMA-staged instantiations (MODE 1, 2): the vertical face fluxes of the two window slots,
+    // written by sink_flux_kernel before the launch: fz_pre[(q (Nz + 1) + f) Nx Ny + i + j Nx] for
+    // face f of window q (0: window_a, 1: window_b)
+    const TC* fz_pre;
     int surf_kind;
     TC surf_value;            // OBGC_SURFACE_PAR_CONSTANT value
     const TS* surf_field;     // OBGC_SURFACE_PAR_FIELD
@@ -230,6 +234,11 @@ constexpr size_t substep_smem_bytes() {
     // vertical flux and its divergence
     return sizeof(TC) * NT * (tile_elems<TC, SPLIT>() + STEP_BY * (STEP_BX + 1) + (STEP_BY + 1) * STEP_BX + 2 * STEP_BX * STEP_BY);
 }
+
+// The two slots whose vertical stencil the kernel keeps in register windows (LOBSTER: sPOM, bPOM;
+// NPZD: P, D; PISCES' middle launch: POC, GOC).
+__host__ __device__ constexpr int window_a(int V) { return V == V_NPZD ? 1 : V == V_EXTERNAL ? 1 : 4; }
+__host__ __device__ constexpr int window_b(int V) { return V == V_NPZD ? 4 : V == V_EXTERNAL ? 2 : 5; }
 
 // ---- tensor-memory-accelerator staging: one mbarrier per block, armed by thread 0 with the bytes
 // of every tracer's tile of a level, completed by the tile copies
@@ -365,9 +374,14 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     // vertically advected tracer, and every tracer when a model w is given, takes the generic path.
     // PISCES (V_EXTERNAL, launched on tracers 0-8, 9-17 and 18-25): POC and GOC are slots 1 and 2
     // of the second launch; the other four sinking tracers take the generic path.
-    constexpr int WA = V == V_NPZD ? 1 : V == V_EXTERNAL ? 1 : 4, WB = V == V_NPZD ? 4 : V == V_EXTERNAL ? 2 : 5;
-    const bool winA = a.w == nullptr && ((a.drift_mask >> WA) & 1u);
-    const bool winB = a.w == nullptr && ((a.drift_mask >> WB) & 1u);
+    constexpr int WA = window_a(V), WB = window_b(V);
+    // MODE 1 and 2 read the window slots' face fluxes from sink_flux_kernel instead (no window
+    // registers: they were 12 % of a launch)
+    constexpr bool PREFZ = MODE != 0;
+    const bool winA = !PREFZ && a.w == nullptr && ((a.drift_mask >> WA) & 1u);
+    const bool winB = !PREFZ && a.w == nullptr && ((a.drift_mask >> WB) & 1u);
+    const bool preA = PREFZ && ((a.drift_mask >> WA) & 1u);
+    const bool preB = PREFZ && ((a.drift_mask >> WB) & 1u);
     // tracers whose vertical advection takes the generic path, and those whose vertical face flux
     // does (the generic advection set, plus every tracer under explicit vertical diffusion)
     const uint32_t adv_mask = a.w != nullptr ? 0xffffffffu : (a.drift_mask & ~((1u << WA) | (1u << WB)));
@@ -511,6 +525,9 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
         }
         if (winA) FzA = window_face_flux(wA[1], wA[2], wA[3], wA[4], wA[5], wA[6], k_top + 1, a.Nz, a.drift[WA * (a.Nz + 1) + k_top + 1]);
         if (winB) FzB = window_face_flux(wB[1], wB[2], wB[3], wB[4], wB[5], wB[6], k_top + 1, a.Nz, a.drift[WB * (a.Nz + 1) + k_top + 1]);
+        const int64_t fz_cols = (int64_t)a.Nx * a.Ny, fz_c = ic + (int64_t)jc * a.Nx;
+        if (preA) FzA = a.fz_pre[(int64_t)(k_top + 1) * fz_cols + fz_c];
+        if (preB) FzB = a.fz_pre[(int64_t)(a.Nz + 1 + k_top + 1) * fz_cols + fz_c];
 
 #pragma unroll 1
         for (int k = k_top; k >= k_bot; --k) {
@@ -747,6 +764,16 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 vdB = (FzB - F) * a.inv_dz;
                 FzB = F;
             }
+            if (preA) {
+                const TC F = a.fz_pre[(int64_t)k * fz_cols + fz_c];
+                vdA = (FzA - F) * a.inv_dz;
+                FzA = F;
+            }
+            if (preB) {
+                const TC F = a.fz_pre[(int64_t)(a.Nz + 1 + k) * fz_cols + fz_c];
+                vdB = (FzB - F) * a.inv_dz;
+                FzB = F;
+            }
             // the sediment: deposition through the bottom face, its burial and the remineralised rest
             TC sed_remin = TC(0);
             if constexpr (EXT) {
@@ -880,6 +907,54 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     if (tma_timeout && a.status) atomicOr(a.status, OBGC_FLAG_TIMEOUT);
 }
 
+// The vertical face fluxes of the two window slots (the sinking tracers) at every face of every
+// column, for the TMA-staged substep launch that follows (its fz_pre).  A block takes 32 columns and
+// 8 faces; each thread loads c[f-3 .. f+2] of both slots (levels clamped to the grid, as the
+// substep's windows are) and forms the two fluxes exactly as the windows do: one packed WENO5 where
+// both drift speeds are non-zero at an interior face, window_face_flux otherwise (the same
+// arithmetic per element, so the fluxes are bit for bit the windows').
+template <typename TS, typename TC>
+__global__ void __launch_bounds__(256) sink_flux_kernel(const TS* __restrict__ cA, const TS* __restrict__ cB, int64_t sj,
+                                                        int64_t sk, int Nx, int Ny, int Nz, const TC* __restrict__ drift,
+                                                        int WA, int WB, TC* __restrict__ out) {
+    const int64_t cols = (int64_t)Nx * Ny;
+    const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x % 32;
+    const int f = blockIdx.y * 8 + threadIdx.x / 32;
+    if (c >= cols || f > Nz) return;
+    const int64_t col = (c % Nx) + (c / Nx) * sj;
+    TC wA[6], wB[6];
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+        const int64_t kk = min(max(f - 3 + m, 0), Nz - 1);
+        wA[m] = ld<TS, TC>(cA, col + kk * sk);
+        wB[m] = ld<TS, TC>(cB, col + kk * sk);
+    }
+    const TC UA = drift[WA * (Nz + 1) + f], UB = drift[WB * (Nz + 1) + f];
+    TC FA, FB;
+    bool done = false;
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(TC) == 4) {
+        if (UA != TC(0) && UB != TC(0) && min(f, Nz - f) >= 3) {
+            const bool pa = UA > TC(0), pb = UB > TC(0);
+            const f32x2 r = weno5_x2(pk2(pa ? wA[0] : wA[5], pb ? wB[0] : wB[5]), pk2(pa ? wA[1] : wA[4], pb ? wB[1] : wB[4]),
+                                     pk2(pa ? wA[2] : wA[3], pb ? wB[2] : wB[3]), pk2(pa ? wA[3] : wA[2], pb ? wB[3] : wB[2]),
+                                     pk2(pa ? wA[4] : wA[1], pb ? wB[4] : wB[1]));
+            float ra, rb;
+            up2(r, ra, rb);
+            FA = UA * ra;
+            FB = UB * rb;
+            done = true;
+        }
+    }
+#endif
+    if (!done) {
+        FA = window_face_flux(wA[0], wA[1], wA[2], wA[3], wA[4], wA[5], f, Nz, UA);
+        FB = window_face_flux(wB[0], wB[1], wB[2], wB[3], wB[4], wB[5], f, Nz, UB);
+    }
+    out[(int64_t)f * cols + c] = FA;
+    out[(int64_t)(Nz + 1 + f) * cols + c] = FB;
+}
+
 // The chlorophyll sums of TwoBand PAR above the top of every segment of TZ levels but the first,
 // for the substep launch that follows (its par_prefix).  A block takes PP_COLS columns: its eight
 // warps evaluate the terms of PP_CHUNK levels at a time into shared memory (all loads and powers of
@@ -903,11 +978,23 @@ __global__ void __launch_bounds__(256) par_prefix_kernel(const TS* __restrict__ 
     int s = 1;                          // the next segment whose sum is due
     for (int c0 = 0; c0 < nlev; c0 += PP_CHUNK) {
         const int n = min(PP_CHUNK, nlev - c0);
-        for (int q = lane; q < n; q += 256 / PP_COLS) {
-            TC fr = TC(0), fb = TC(0);
-            if (live) twoband_terms(L, ld<TS, TC>(p, (int64_t)(Nz - 1 - (c0 + q)) * sk), fr, fb);
-            fr_s[q][col] = fr;
-            fb_s[q][col] = fb;
+        // this thread's levels of the chunk: every load in flight first, then the terms
+        constexpr int PER = PP_CHUNK / (256 / PP_COLS);
+        TC v[PER];
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int q = lane + u * (256 / PP_COLS);
+            v[u] = live && q < n ? ld<TS, TC>(p, (int64_t)(Nz - 1 - (c0 + q)) * sk) : TC(0);
+        }
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int q = lane + u * (256 / PP_COLS);
+            if (q < n) {
+                TC fr = TC(0), fb = TC(0);
+                if (live) twoband_terms(L, v[u], fr, fb);
+                fr_s[q][col] = fr;
+                fb_s[q][col] = fb;
+            }
         }
         __syncthreads();
         if (lane == 0) {

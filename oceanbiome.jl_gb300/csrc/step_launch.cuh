@@ -31,6 +31,8 @@ int launch_one(const SubstepArgs<TS, TC>& a, int blocks, cudaStream_t st) {
         substep_kernel<V, NT, TS, TC, true><<<blocks, block, substep_smem_bytes<TC, NT>(), st>>>(a);
     } else {
         bool done = false;
+        if (a.tma_layout && (a.drift_mask & ((1u << window_a(V)) | (1u << window_b(V)))) && !a.fz_pre)
+            return fail(OBGC_ERR_UNSUPPORTED, "substep: TMA staging needs the sinking fluxes of sink_flux_kernel");
         if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) {
             if (a.tma_layout == 2) {
                 const int rc = ensure_configured<V, NT, TS, TC, false, 2>();
