@@ -1010,7 +1010,7 @@ static int launch_sink_flux(obgc_ctx* c, SubstepArgs<TS, TC>& a, cudaStream_t st
     if (!(a.drift_mask & ((1u << wa) | (1u << wb)))) return OBGC_OK;
     if (!c->fz_pre) return fail(OBGC_ERR_UNSUPPORTED, "obgc_step: no buffer for the sinking fluxes");
     const int64_t cols = (int64_t)a.Nx * a.Ny;
-    const dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((a.Nz + 1 + 7) / 8));
+    const dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((a.Nz + 1 + 8 * SF_FACES - 1) / (8 * SF_FACES)));
     sink_flux_kernel<TS, TC><<<grid, 256, 0, st>>>(a.in[wa], a.in[wb], a.sj, a.sk, a.Nx, a.Ny, a.Nz, a.drift, wa, wb,
                                                    (TC*)c->fz_pre);
     OBGC_LAUNCHED("sink_flux_kernel");

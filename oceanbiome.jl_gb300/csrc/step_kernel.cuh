@@ -908,51 +908,60 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 }
 
 // The vertical face fluxes of the two window slots (the sinking tracers) at every face of every
-// column, for the TMA-staged substep launch that follows (its fz_pre).  A block takes 32 columns and
-// 8 faces; each thread loads c[f-3 .. f+2] of both slots (levels clamped to the grid, as the
-// substep's windows are) and forms the two fluxes exactly as the windows do: one packed WENO5 where
-// both drift speeds are non-zero at an interior face, window_face_flux otherwise (the same
-// arithmetic per element, so the fluxes are bit for bit the windows').
+// column, for the TMA-staged substep launch that follows (its fz_pre).  A block takes 32 columns;
+// each of its warps takes SF_FACES consecutive faces, loading the SF_FACES + 5 levels their stencils
+// span once (clamped to the grid, as the substep's windows are).  A face's two fluxes are formed
+// exactly as the windows form them: one packed WENO5 where both drift speeds are non-zero at an
+// interior face, window_face_flux otherwise (the same arithmetic per element, so the fluxes are bit
+// for bit the windows').
+constexpr int SF_FACES = 8;
 template <typename TS, typename TC>
 __global__ void __launch_bounds__(256) sink_flux_kernel(const TS* __restrict__ cA, const TS* __restrict__ cB, int64_t sj,
                                                         int64_t sk, int Nx, int Ny, int Nz, const TC* __restrict__ drift,
                                                         int WA, int WB, TC* __restrict__ out) {
     const int64_t cols = (int64_t)Nx * Ny;
     const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x % 32;
-    const int f = blockIdx.y * 8 + threadIdx.x / 32;
-    if (c >= cols || f > Nz) return;
+    const int f0 = (blockIdx.y * 8 + threadIdx.x / 32) * SF_FACES;   // this thread's first face
+    if (c >= cols || f0 > Nz) return;
     const int64_t col = (c % Nx) + (c / Nx) * sj;
-    TC wA[6], wB[6];
+    TC wA[SF_FACES + 5], wB[SF_FACES + 5];   // c[f0 - 3 .. f0 + SF_FACES + 1]
 #pragma unroll
-    for (int m = 0; m < 6; m++) {
-        const int64_t kk = min(max(f - 3 + m, 0), Nz - 1);
+    for (int m = 0; m < SF_FACES + 5; m++) {
+        const int64_t kk = min(max(f0 - 3 + m, 0), Nz - 1);
         wA[m] = ld<TS, TC>(cA, col + kk * sk);
         wB[m] = ld<TS, TC>(cB, col + kk * sk);
     }
-    const TC UA = drift[WA * (Nz + 1) + f], UB = drift[WB * (Nz + 1) + f];
-    TC FA, FB;
-    bool done = false;
+#pragma unroll
+    for (int q = 0; q < SF_FACES; q++) {
+        const int f = f0 + q;
+        if (f > Nz) break;
+        const TC UA = drift[WA * (Nz + 1) + f], UB = drift[WB * (Nz + 1) + f];
+        TC FA, FB;
+        bool done = false;
 #ifdef __CUDA_ARCH__
-    if constexpr (sizeof(TC) == 4) {
-        if (UA != TC(0) && UB != TC(0) && min(f, Nz - f) >= 3) {
-            const bool pa = UA > TC(0), pb = UB > TC(0);
-            const f32x2 r = weno5_x2(pk2(pa ? wA[0] : wA[5], pb ? wB[0] : wB[5]), pk2(pa ? wA[1] : wA[4], pb ? wB[1] : wB[4]),
-                                     pk2(pa ? wA[2] : wA[3], pb ? wB[2] : wB[3]), pk2(pa ? wA[3] : wA[2], pb ? wB[3] : wB[2]),
-                                     pk2(pa ? wA[4] : wA[1], pb ? wB[4] : wB[1]));
-            float ra, rb;
-            up2(r, ra, rb);
-            FA = UA * ra;
-            FB = UB * rb;
-            done = true;
+        if constexpr (sizeof(TC) == 4) {
+            if (UA != TC(0) && UB != TC(0) && min(f, Nz - f) >= 3) {
+                const bool pa = UA > TC(0), pb = UB > TC(0);
+                const f32x2 r = weno5_x2(pk2(pa ? wA[q] : wA[q + 5], pb ? wB[q] : wB[q + 5]),
+                                         pk2(pa ? wA[q + 1] : wA[q + 4], pb ? wB[q + 1] : wB[q + 4]),
+                                         pk2(pa ? wA[q + 2] : wA[q + 3], pb ? wB[q + 2] : wB[q + 3]),
+                                         pk2(pa ? wA[q + 3] : wA[q + 2], pb ? wB[q + 3] : wB[q + 2]),
+                                         pk2(pa ? wA[q + 4] : wA[q + 1], pb ? wB[q + 4] : wB[q + 1]));
+                float ra, rb;
+                up2(r, ra, rb);
+                FA = UA * ra;
+                FB = UB * rb;
+                done = true;
+            }
         }
-    }
 #endif
-    if (!done) {
-        FA = window_face_flux(wA[0], wA[1], wA[2], wA[3], wA[4], wA[5], f, Nz, UA);
-        FB = window_face_flux(wB[0], wB[1], wB[2], wB[3], wB[4], wB[5], f, Nz, UB);
+        if (!done) {
+            FA = window_face_flux(wA[q], wA[q + 1], wA[q + 2], wA[q + 3], wA[q + 4], wA[q + 5], f, Nz, UA);
+            FB = window_face_flux(wB[q], wB[q + 1], wB[q + 2], wB[q + 3], wB[q + 4], wB[q + 5], f, Nz, UB);
+        }
+        out[(int64_t)f * cols + c] = FA;
+        out[(int64_t)(Nz + 1 + f) * cols + c] = FB;
     }
-    out[(int64_t)f * cols + c] = FA;
-    out[(int64_t)(Nz + 1 + f) * cols + c] = FB;
 }
 
 // The chlorophyll sums of TwoBand PAR above the top of every segment of TZ levels but the first,
