@@ -1,9 +1,11 @@
-"""The fused substep with TMA-staged tiles: every step runs bound arrays -> padded copy 0 -> padded
-copy 1 -> bound arrays, the second and third stages copying each tracer's tile of a level with one
-tensor copy, the first stage doing the same for the tiles of the bound arrays that need no periodic
-wrap.  The arithmetic per cell is the same as with cp.async staging, so the two agree bit for
-bit, on grids whose sizes are not multiples of the 32 x 8 tile (tiles hang over the padded arrays'
-edges) and with walls as well as periodic directions; and both agree with the oracle."""
+"""The fused substep with TMA-staged tiles: a call's stages run bound arrays -> padded copy 0 ->
+padded copy 1 -> padded copy 0 ... -> bound arrays, every stage but the first copying each tracer's
+tile of a level with one tensor copy, the first doing the same for the tiles of the bound arrays
+that need no periodic wrap (when their layout allows tensor maps) and staging the others by
+per-element cp.async.  The arithmetic per cell is the same as with cp.async staging, so the two agree bit
+for bit, on grids whose sizes are not multiples of the 32 x 8 tile (tiles hang over the padded
+arrays' edges), with walls as well as periodic directions, and with a row pitch that allows no
+tensor map of the bound arrays; and both agree with the oracle."""
 import numpy as np
 import pytest
 
@@ -36,6 +38,7 @@ def run(shape, topology, staging, nsteps=3, graph=False, seed=2):
     ((32, 19, 10), ("Periodic", "Bounded", "Bounded")),
     ((96, 32, 8), ("Periodic", "Periodic", "Bounded")),     # wrap-free tiles: the first stage's tensor copies
     ((100, 28, 6), ("Bounded", "Periodic", "Bounded")),
+    ((37, 20, 8), ("Periodic", "Periodic", "Bounded")),     # 148-byte rows: the first stage by cp.async
 ])
 def test_tma_staging_equals_cp_async_staging(shape, topology):
     _, _, _, m1, _, tma = run(shape, topology, staging=1)
