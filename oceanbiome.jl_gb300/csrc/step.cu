@@ -174,6 +174,35 @@ __global__ void copy_interior_kernel(const TS* __restrict__ src, TS* __restrict_
     dst[idx] = src[idx];
 }
 
+// The caller's arrays copied into a padded set (x halo TMA_HX, y halo HALO, rows of pad_sj values)
+// with the periodic images in the halos, so that the first TMA-staged stage of a call copies every
+// tile with tensor copies.  One thread per padded cell and level, every slot; halo cells of a
+// Bounded direction and the row tails past Nx + 2 TMA_HX are left as they are (no stencil reads
+// them).
+struct PadCopyArgs {
+    const float* src[MAX_NT];
+    float* dst[MAX_NT];           // the padded arrays' first cell (x = -TMA_HX, y = -HALO)
+    int nt;
+};
+__global__ void pad_copy_kernel(PadCopyArgs p, int Nx, int Ny, int Nz, int64_t sj, int64_t sk, int64_t psj, int64_t psk,
+                                int periodic_x, int periodic_y) {
+    const int PW = Nx + 2 * TMA_HX, PH = Ny + 2 * HALO;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (int64_t)PW * PH * Nz) return;
+    const int px = (int)(c % PW), py = (int)((c / PW) % PH), k = (int)(c / ((int64_t)PW * PH));
+    int x = px - TMA_HX, y = py - HALO;
+    if (x < 0 || x >= Nx) {
+        if (!periodic_x) return;
+        x = x < 0 ? x + Nx : x - Nx;
+    }
+    if (y < 0 || y >= Ny) {
+        if (!periodic_y) return;
+        y = y < 0 ? y + Ny : y - Ny;
+    }
+    const int64_t s = x + (int64_t)y * sj + (int64_t)k * sk, d = px + (int64_t)py * psj + (int64_t)k * psk;
+    for (int t = 0; t < p.nt; t++) p.dst[t][d] = __ldg(p.src[t] + s);
+}
+
 // Neumaier-compensated FP64 accumulation (sum, compensation).
 struct DD {
     double s, c;
@@ -319,6 +348,8 @@ struct obgc_ctx {
     int staging = 1;
     bool last_used_tma = false;
     int TZ = 0;                         // levels per work item; 0: chosen per grid (fill_args)
+    bool pad_first = true;              // a call's first TMA-staged stage from a padded copy of the caller's arrays
+    bool copied_first = false;          // the last TMA-staged dispatch launched that copy
     // the chlorophyll sums above each segment (par_prefix_kernel), room for par_prefix_segs segments
     // below the first (enough for any segment length of two levels or more), and whether the last
     // dispatch launched the pre-pass
@@ -1233,6 +1264,31 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
     const bool clock = needs_clock(c);
     size_t ev = 0;
     const int last = 3 * nsteps - 1;
+    // when no tile needs the periodic wrap, the call's first stage copies every tile from the
+    // caller's arrays with tensor copies: the MODE 2 kernel, which compiles no per-element staging
+    // (with any wrapping tile the first stage is one MODE 1 launch: splitting it into a MODE 2 launch
+    // for the other tiles and a MODE 1 launch for the wrapping ones, in turn or on two streams, was
+    // slower)
+    bool none_wrap = c->umaps_ok;
+    for (int tj = 0; tj < a.nty && none_wrap; tj++)
+        for (int ti = 0; ti < a.ntx && none_wrap; ti++) none_wrap = !tile_wraps(a, ti * STEP_BX, tj * STEP_BY);
+    // otherwise the caller's arrays are first copied into padded set 1 with their periodic images
+    // (pad_copy_kernel), and the first stage too runs the MODE 2 kernel from that set
+    const bool copy_first = !none_wrap && c->pad_first;
+    c->copied_first = copy_first;
+    if (copy_first) {
+        PadCopyArgs pc;
+        std::memset(&pc, 0, sizeof(pc));
+        pc.nt = c->NT;
+        for (int t = 0; t < c->NT; t++) {
+            pc.src[t] = (const float*)c->user[t];
+            pc.dst[t] = (float*)c->pad[1][t];
+        }
+        const int64_t n = (int64_t)(g.Nx + 2 * TMA_HX) * (g.Ny + 2 * HALO) * g.Nz;
+        pad_copy_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pc, g.Nx, g.Ny, g.Nz, g.stride_j, g.stride_k, c->pad_sj,
+                                                                     c->pad_sk, a.periodic_x, a.periodic_y);
+        OBGC_LAUNCHED("pad_copy_kernel");
+    }
     for (int s = 0; s < nsteps; s++) {
         for (int stg = 0; stg < 3; stg++) {
             const int q = 3 * s + stg;          // the stage's place in the call
@@ -1241,20 +1297,22 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
             a.gamma = TC(rk3_gamma(stg));
             a.zeta = TC(rk3_zeta(stg));
             a.c_stage = rk3_c(stg);
+            const bool from_user = q == 0 && !copy_first;   // this stage reads the caller's arrays
+            const int pin = q == 0 ? 1 : (q - 1) % 2;       // else the padded set it reads
             for (int t = 0; t < c->NT; t++) {
-                a.in[t] = q == 0 ? (const TS*)c->user[t] : (const TS*)c->pad[(q - 1) % 2][t] + org;
+                a.in[t] = from_user ? (const TS*)c->user[t] : (const TS*)c->pad[pin][t] + org;
                 a.out[t] = q == last ? (TS*)c->user[t] : (TS*)c->pad[q % 2][t] + org;
             }
-            a.sj = q == 0 ? g.stride_j : c->pad_sj;
-            a.sk = q == 0 ? g.stride_k : c->pad_sk;
+            a.sj = from_user ? g.stride_j : c->pad_sj;
+            a.sk = from_user ? g.stride_k : c->pad_sk;
             a.osj = q == last ? g.stride_j : c->pad_sj;
             a.osk = q == last ? g.stride_k : c->pad_sk;
             a.out_halo = q != last;
-            a.tma_layout = q == 0 ? 1 : 2;
-            // the call's first stage copies the bound arrays' wrap-free tiles when they have tensor maps
-            a.tmap = q == 0 ? (c->umaps_ok ? c->d_tmaps + 2 * MAX_NT : nullptr) : c->d_tmaps + (size_t)((q - 1) % 2) * MAX_NT;
-            a.tma_x0 = q == 0 ? -TMA_HX : 0;
-            a.tma_y0 = q == 0 ? -HALO : 0;
+            a.tma_layout = from_user && !none_wrap ? 1 : 2;
+            // the caller's arrays: tensor copies of the wrap-free tiles when they have tensor maps
+            a.tmap = from_user ? (c->umaps_ok ? c->d_tmaps + 2 * MAX_NT : nullptr) : c->d_tmaps + (size_t)pin * MAX_NT;
+            a.tma_x0 = from_user ? -TMA_HX : 0;
+            a.tma_y0 = from_user ? -HALO : 0;
             int rc = launch_par_prefix(c, a, st);
             if (rc == OBGC_OK) rc = launch_sink_flux(c, a, st);
             if (rc != OBGC_OK) return rc;
@@ -1396,7 +1454,8 @@ static int64_t launches_per_call(const obgc_ctx* c, int nsteps) {
     const bool impl = c->vimplicit && c->kzf;
     const int per_stage = 1 + c->nchunk + gases + (impl ? 1 + neg : 0) + (c->mg_on ? 1 : 0) + (c->prefix_on ? 1 : 0) +
                           (c->last_used_tma && c->sinkpre_on ? 1 : 0);
-    return (c->mg_on ? 1 : 0) + (int64_t)nsteps * (3 * per_stage + (clock ? 1 : 0)) + (nsteps % 2 && !c->last_used_tma ? c->NT + c->NP : 0) + 1 + neg + (impl ? 1 : 0);
+    return (c->mg_on ? 1 : 0) + (int64_t)nsteps * (3 * per_stage + (clock ? 1 : 0)) + (c->last_used_tma && c->copied_first ? 1 : 0) +
+           (nsteps % 2 && !c->last_used_tma ? c->NT + c->NP : 0) + 1 + neg + (impl ? 1 : 0);
 }
 
 extern "C" int obgc_step(obgc_ctx* c, double t, double dt, int32_t nsteps, void* stream) {

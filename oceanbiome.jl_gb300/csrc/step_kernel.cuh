@@ -217,6 +217,14 @@ constexpr int TILE_CELLS = (STEP_BX + 2 * HALO) * TILE_H;   // the cells a tile 
 constexpr int TILE_LOADS = (TILE_CELLS + STEP_BX * STEP_BY - 1) / (STEP_BX * STEP_BY);
 constexpr int TMA_TILE_W = STEP_BX + 8;
 constexpr int TMA_HX = 4;                                   // x halo of the padded arrays
+
+// Whether the tile at (i0, j0) needs the periodic wrap: its staged halo leaves the grid in a
+// periodic direction.
+template <typename TS, typename TC>
+__host__ __device__ inline bool tile_wraps(const SubstepArgs<TS, TC>& a, int i0, int j0) {
+    return (a.periodic_x && (i0 < TMA_HX || i0 + TMA_TILE_W - TMA_HX > a.Nx)) ||
+           (a.periodic_y && (j0 < HALO || j0 + STEP_BY + HALO > a.Ny));
+}
 template <bool SPLIT>
 __host__ __device__ constexpr int tile_w() { return SPLIT ? TMA_TILE_W : STEP_BX + 2 * HALO; }
 template <bool SPLIT>
@@ -468,8 +476,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
         // tensor copies for this item: always in MODE 2; in MODE 1 where the tile needs no periodic wrap
         // (a Bounded direction's out-of-range cells are filled with zeros, which only the unused
         // stencil cells beyond a wall read)
-        const bool item_tma = TMA || (may_tma && (!periodic_x || (i0 >= TMA_HX && i0 + TMA_TILE_W - TMA_HX <= a.Nx)) &&
-                                      (!periodic_y || (j0 >= HALO && j0 + STEP_BY + HALO <= a.Ny)));
+        const bool item_tma = TMA || (may_tma && !tile_wraps(a, i0, j0));
         int64_t toff[TILE_LOADS];
 #pragma unroll
         for (int q = 0; q < (TMA ? 0 : TILE_LOADS); q++) {

@@ -39,6 +39,7 @@ def run(shape, topology, staging, nsteps=3, graph=False, seed=2):
     ((96, 32, 8), ("Periodic", "Periodic", "Bounded")),     # wrap-free tiles: the first stage's tensor copies
     ((100, 28, 6), ("Bounded", "Periodic", "Bounded")),
     ((37, 20, 8), ("Periodic", "Periodic", "Bounded")),     # 148-byte rows: the first stage by cp.async
+    ((64, 32, 8), ("Bounded", "Bounded", "Bounded")),       # no tile wraps: the first stage by tensor copies alone
 ])
 def test_tma_staging_equals_cp_async_staging(shape, topology):
     _, _, _, m1, _, tma = run(shape, topology, staging=1)
@@ -78,3 +79,18 @@ def test_configurations_outside_the_lean_kernel_keep_cp_async():
     mixed = obgc.NonhydrostaticModel(g64, biogeochemistry=obgc.LOBSTER(g64, carbonate_system=obgc.CarbonateSystem()),
                                      tracers=("T", "S"), velocities=(u64, v64, None), precision="mixed")
     assert mixed.staging() == (False, False)     # the padded copies exist for FP32 state only
+
+
+def test_first_stage_with_wrapping_and_plain_tiles_in_a_graph():
+    # 96 x 32 periodic: some tiles wrap and some do not (a call's first stage copies the plain ones
+    # from the caller's arrays by tensor copies and stages the others per element); captured into a
+    # CUDA graph it gives the same state as eager calls
+    shape, topo = (96, 32, 8), ("Periodic", "Periodic", "Bounded")
+    _, _, _, me, _, eager = run(shape, topo, staging=1, nsteps=2)
+    _, _, _, mg, _, graph = run(shape, topo, staging=1, nsteps=2, graph=True)
+    assert mg.staging() == (True, True)
+    assert np.array_equal(graph, eager)
+    # one step per call, as an ensemble host drives it
+    _, _, _, m1, _, one = run(shape, topo, staging=1, nsteps=1)
+    _, _, _, m0, _, ref = run(shape, topo, staging=0, nsteps=1)
+    assert np.array_equal(one, ref)
