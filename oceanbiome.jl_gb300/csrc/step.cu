@@ -348,8 +348,7 @@ struct obgc_ctx {
     int staging = 1;
     bool last_used_tma = false;
     int TZ = 0;                         // levels per work item; 0: chosen per grid (fill_args)
-    bool pad_first = true;              // a call's first TMA-staged stage from a padded copy of the caller's arrays
-    bool copied_first = false;          // the last TMA-staged dispatch launched that copy
+    bool copied_first = false;          // the last TMA-staged dispatch copied the caller's arrays into a padded set
     // the chlorophyll sums above each segment (par_prefix_kernel), room for par_prefix_segs segments
     // below the first (enough for any segment length of two levels or more), and whether the last
     // dispatch launched the pre-pass
@@ -1248,11 +1247,12 @@ static bool tma_eligible(obgc_ctx* c, const StepPlan<TS, TC>& p) {
     return !substep_needs_ext(x);
 }
 
-// Steps with TMA-staged tiles.  The 3 nsteps stages of the call run bound arrays -> padded set 0 ->
-// padded set 1 -> padded set 0 -> ... -> bound arrays: only the call's first stage reads the caller's
-// arrays (MODE 1: tensor copies of the wrap-free tiles, cp.async for the others) and only its last
-// stage writes them; every other stage writes a padded set together with its periodic halo images,
-// so that the next stage stages whole tiles with one tensor copy per tracer and level (MODE 2).
+// Steps with TMA-staged tiles (the MODE 2 kernel: one tensor copy per tracer and level).  The caller's
+// arrays are first copied into padded set 1 with their periodic images (pad_copy_kernel), then the
+// 3 nsteps stages of the call run padded set 1 -> padded set 0 -> padded set 1 -> ... -> bound
+// arrays: every stage but the last writes a padded set together with its periodic halo images, and
+// only the last writes the caller's arrays.  When no tile needs the periodic wrap (and the caller's
+// arrays have tensor maps) there is no copy: the first stage copies its tiles from them directly.
 template <typename TS, typename TC>
 static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int nsteps, cudaStream_t st, bool profile) {
     SubstepArgs<TS, TC>& a = p.a;
@@ -1264,17 +1264,10 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
     const bool clock = needs_clock(c);
     size_t ev = 0;
     const int last = 3 * nsteps - 1;
-    // when no tile needs the periodic wrap, the call's first stage copies every tile from the
-    // caller's arrays with tensor copies: the MODE 2 kernel, which compiles no per-element staging
-    // (with any wrapping tile the first stage is one MODE 1 launch: splitting it into a MODE 2 launch
-    // for the other tiles and a MODE 1 launch for the wrapping ones, in turn or on two streams, was
-    // slower)
     bool none_wrap = c->umaps_ok;
     for (int tj = 0; tj < a.nty && none_wrap; tj++)
         for (int ti = 0; ti < a.ntx && none_wrap; ti++) none_wrap = !tile_wraps(a, ti * STEP_BX, tj * STEP_BY);
-    // otherwise the caller's arrays are first copied into padded set 1 with their periodic images
-    // (pad_copy_kernel), and the first stage too runs the MODE 2 kernel from that set
-    const bool copy_first = !none_wrap && c->pad_first;
+    const bool copy_first = !none_wrap;
     c->copied_first = copy_first;
     if (copy_first) {
         PadCopyArgs pc;
@@ -1308,9 +1301,8 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
             a.osj = q == last ? g.stride_j : c->pad_sj;
             a.osk = q == last ? g.stride_k : c->pad_sk;
             a.out_halo = q != last;
-            a.tma_layout = from_user && !none_wrap ? 1 : 2;
-            // the caller's arrays: tensor copies of the wrap-free tiles when they have tensor maps
-            a.tmap = from_user ? (c->umaps_ok ? c->d_tmaps + 2 * MAX_NT : nullptr) : c->d_tmaps + (size_t)pin * MAX_NT;
+            a.tma_layout = 2;
+            a.tmap = from_user ? c->d_tmaps + 2 * MAX_NT : c->d_tmaps + (size_t)pin * MAX_NT;
             a.tma_x0 = from_user ? -TMA_HX : 0;
             a.tma_y0 = from_user ? -HALO : 0;
             int rc = launch_par_prefix(c, a, st);

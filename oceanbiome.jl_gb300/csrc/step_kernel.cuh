@@ -62,7 +62,7 @@ struct SubstepArgs {
     // value into the halo cells that hold its periodic image, so the next stage can stage whole
     // tiles of it with the tensor-memory accelerator
     int out_halo;
-    int tma_layout;           // the TMA-staged steps: 1 their first stage, 2 their later stages (0: neither)
+    int tma_layout;           // non-zero: a stage of the TMA-staged steps (the MODE 2 instantiation)
     // tensor maps of in[] (3-D, box TMA_TILE_W x TILE_H x 1) in global memory, or NULL: the tiles are
     // then staged by per-element cp.async.  A tile at (i0, j0, k) is the box at (i0 + tma_x0,
     // j0 + tma_y0, k): (0, 0) for the padded sets, (-4, -3) for the caller's arrays, whose tiles
@@ -121,7 +121,7 @@ struct SubstepArgs {
     // for segment s >= 1 and band b (red 0, blue 1), written by par_prefix_kernel before the launch;
     // NULL: each work item sums the cells above its segment itself
     const TC* par_prefix;
-    // the TMA-staged instantiations (MODE 1, 2): the vertical face fluxes of the two window slots,
+    // the TMA-staged instantiation (MODE 2): the vertical face fluxes of the two window slots,
     // written by sink_flux_kernel before the launch: fz_pre[(q (Nz + 1) + f) Nx Ny + i + j Nx] for
     // face f of window q (0: window_a, 1: window_b)
     const TC* fz_pre;
@@ -347,12 +347,11 @@ __host__ __device__ inline bool substep_needs_ext(const SubstepArgs<TS, TC>& a) 
     return any;
 }
 
-// MODE 0: every array in the input layout, tiles staged by cp.async.  MODE 1 and 2 are the
-// instantiations of the TMA-staged steps: input, output and tendency arrays in their own layouts
-// (a.sj/sk, osj/osk, gsj/gsk; u and v in vsj/vsk), 40-wide tile rows, and periodic halo images
-// written when a.out_halo is set.  MODE 2 (the later stages, from the padded sets) stages every tile
-// by tensor copies through a.tmap; MODE 1 (the first stage, from the caller's arrays) does so for the
-// tiles that need no periodic wrap when a.tmap is set, and stages the rest by cp.async.
+// MODE 0: every array in the input layout, tiles staged by cp.async.  MODE 2: the TMA-staged steps'
+// instantiation: input, output and tendency arrays in their own layouts (a.sj/sk, osj/osk, gsj/gsk;
+// u and v in vsj/vsk), 40-wide tile rows, every tile copied by tensor copies through a.tmap (from a
+// padded set, or from the caller's arrays when none of their tiles needs the periodic wrap), and
+// periodic halo images written when a.out_halo is set.
 template <int V, int NT, typename TS, typename TC, bool EXT, int MODE = 0>
 __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <= 12 ? 3 : NT <= 16 ? 2 : 1)
     substep_kernel(const __grid_constant__ SubstepArgs<TS, TC> a) {
@@ -383,7 +382,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     // PISCES (V_EXTERNAL, launched on tracers 0-8, 9-17 and 18-25): POC and GOC are slots 1 and 2
     // of the second launch; the other four sinking tracers take the generic path.
     constexpr int WA = window_a(V), WB = window_b(V);
-    // MODE 1 and 2 read the window slots' face fluxes from sink_flux_kernel instead (no window
+    // MODE 2 reads the window slots' face fluxes from sink_flux_kernel instead (no window
     // registers: they were 12 % of a launch)
     constexpr bool PREFZ = MODE != 0;
     const bool winA = !PREFZ && a.w == nullptr && ((a.drift_mask >> WA) & 1u);
@@ -403,8 +402,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     const unsigned tiles_s = smem_u32(tiles);
     unsigned tma_phase = 0;
     bool tma_timeout = false;
-    const bool may_tma = TMA || (MODE == 1 && a.tmap != nullptr);
-    if (may_tma) {
+    if (TMA) {
         // a tensor copy's destination must be 128-byte aligned: never issue one to a tile that is not
         // (the block then does no work and reports OBGC_FLAG_TIMEOUT)
         if ((tiles_s & 127u) != 0u) {
@@ -473,10 +471,9 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 
         // horizontal offsets of the tile elements this thread stages (the same for every level
         // and tracer of the work item)
-        // tensor copies for this item: always in MODE 2; in MODE 1 where the tile needs no periodic wrap
-        // (a Bounded direction's out-of-range cells are filled with zeros, which only the unused
-        // stencil cells beyond a wall read)
-        const bool item_tma = TMA || (may_tma && !tile_wraps(a, i0, j0));
+        // tensor copies in MODE 2 (a Bounded direction's out-of-range cells are filled with zeros,
+        // which only the unused stencil cells beyond a wall read)
+        constexpr bool item_tma = TMA;
         int64_t toff[TILE_LOADS];
 #pragma unroll
         for (int q = 0; q < (TMA ? 0 : TILE_LOADS); q++) {

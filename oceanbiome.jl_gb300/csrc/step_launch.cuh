@@ -19,8 +19,7 @@ int ensure_configured() {
 }
 
 // The lean instantiation unless the launch uses an optional term (substep_needs_ext); for the
-// TMA-staged steps (FP32, lean) MODE 1 (cp.async staging from the caller's arrays) or MODE 2
-// (tensor copies from a padded set).
+// TMA-staged steps (FP32, lean) MODE 2 (tensor copies).
 template <int V, int NT, typename TS, typename TC>
 int launch_one(const SubstepArgs<TS, TC>& a, int blocks, cudaStream_t st) {
     const dim3 block(STEP_BX, STEP_BY);
@@ -34,15 +33,10 @@ int launch_one(const SubstepArgs<TS, TC>& a, int blocks, cudaStream_t st) {
         if (a.tma_layout && (a.drift_mask & ((1u << window_a(V)) | (1u << window_b(V)))) && !a.fz_pre)
             return fail(OBGC_ERR_UNSUPPORTED, "substep: TMA staging needs the sinking fluxes of sink_flux_kernel");
         if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) {
-            if (a.tma_layout == 2) {
+            if (a.tma_layout) {
                 const int rc = ensure_configured<V, NT, TS, TC, false, 2>();
                 if (rc != OBGC_OK) return rc;
                 substep_kernel<V, NT, TS, TC, false, 2><<<blocks, block, substep_smem_bytes<TC, NT, true>(), st>>>(a);
-                done = true;
-            } else if (a.tma_layout) {
-                const int rc = ensure_configured<V, NT, TS, TC, false, 1>();
-                if (rc != OBGC_OK) return rc;
-                substep_kernel<V, NT, TS, TC, false, 1><<<blocks, block, substep_smem_bytes<TC, NT, true>(), st>>>(a);
                 done = true;
             }
         }
@@ -73,17 +67,12 @@ int occupancy_one(int* blocks_per_sm) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     if (*blocks_per_sm > lean) *blocks_per_sm = lean;
     if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) {
-        rc = ensure_configured<V, NT, TS, TC, false, 1>();
-        if (rc == OBGC_OK) rc = ensure_configured<V, NT, TS, TC, false, 2>();
+        rc = ensure_configured<V, NT, TS, TC, false, 2>();
         if (rc != OBGC_OK) return rc;
-        int m1 = 0, m2 = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m1, substep_kernel<V, NT, TS, TC, false, 1>,
+        int m2 = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m2, substep_kernel<V, NT, TS, TC, false, 2>,
                                                           STEP_BX * STEP_BY, substep_smem_bytes<TC, NT, true>());
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m2, substep_kernel<V, NT, TS, TC, false, 2>,
-                                                              STEP_BX * STEP_BY, substep_smem_bytes<TC, NT, true>());
         if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-        if (*blocks_per_sm > m1) *blocks_per_sm = m1;
         if (*blocks_per_sm > m2) *blocks_per_sm = m2;
     }
     return OBGC_OK;

@@ -1,11 +1,12 @@
-"""The fused substep with TMA-staged tiles: a call's stages run bound arrays -> padded copy 0 ->
-padded copy 1 -> padded copy 0 ... -> bound arrays, every stage but the first copying each tracer's
-tile of a level with one tensor copy, the first doing the same for the tiles of the bound arrays
-that need no periodic wrap (when their layout allows tensor maps) and staging the others by
-per-element cp.async.  The arithmetic per cell is the same as with cp.async staging, so the two agree bit
-for bit, on grids whose sizes are not multiples of the 32 x 8 tile (tiles hang over the padded
-arrays' edges), with walls as well as periodic directions, and with a row pitch that allows no
-tensor map of the bound arrays; and both agree with the oracle."""
+"""The fused substep with TMA-staged tiles (the MODE 2 kernel, every tile of a level copied with
+one tensor copy per tracer): a call copies the bound arrays into padded copy 1 with their periodic
+images (pad_copy_kernel), then its stages run padded copy 1 -> padded copy 0 -> padded copy 1 ...
+-> bound arrays; when no tile needs the periodic wrap and the bound arrays' layout allows tensor maps,
+the first stage copies its tiles from the bound arrays directly.  The arithmetic per cell is the
+same as with cp.async staging, so the two agree bit for bit, on grids whose sizes are not multiples
+of the 32 x 8 tile (tiles hang over the padded arrays' edges), with walls as well as periodic
+directions, and with a row pitch that allows no tensor map of the bound arrays; and both agree with
+the oracle."""
 import numpy as np
 import pytest
 
@@ -36,10 +37,10 @@ def run(shape, topology, staging, nsteps=3, graph=False, seed=2):
     ((64, 16, 9), ("Periodic", "Periodic", "Bounded")),
     ((36, 24, 8), ("Bounded", "Periodic", "Bounded")),
     ((32, 19, 10), ("Periodic", "Bounded", "Bounded")),
-    ((96, 32, 8), ("Periodic", "Periodic", "Bounded")),     # wrap-free tiles: the first stage's tensor copies
+    ((96, 32, 8), ("Periodic", "Periodic", "Bounded")),     # wrapping and wrap-free tiles
     ((100, 28, 6), ("Bounded", "Periodic", "Bounded")),
-    ((37, 20, 8), ("Periodic", "Periodic", "Bounded")),     # 148-byte rows: the first stage by cp.async
-    ((64, 32, 8), ("Bounded", "Bounded", "Bounded")),       # no tile wraps: the first stage by tensor copies alone
+    ((37, 20, 8), ("Periodic", "Periodic", "Bounded")),     # 148-byte rows: no tensor map of the bound arrays
+    ((64, 32, 8), ("Bounded", "Bounded", "Bounded")),       # no tile wraps: no copy, the bound arrays' tensor maps
 ])
 def test_tma_staging_equals_cp_async_staging(shape, topology):
     _, _, _, m1, _, tma = run(shape, topology, staging=1)
@@ -81,10 +82,9 @@ def test_configurations_outside_the_lean_kernel_keep_cp_async():
     assert mixed.staging() == (False, False)     # the padded copies exist for FP32 state only
 
 
-def test_first_stage_with_wrapping_and_plain_tiles_in_a_graph():
-    # 96 x 32 periodic: some tiles wrap and some do not (a call's first stage copies the plain ones
-    # from the caller's arrays by tensor copies and stages the others per element); captured into a
-    # CUDA graph it gives the same state as eager calls
+def test_padded_copy_and_stages_in_a_graph():
+    # 96 x 32 periodic (some tiles wrap, some do not): the copy into the padded set and the stages,
+    # captured into a CUDA graph, give the same state as eager calls
     shape, topo = (96, 32, 8), ("Periodic", "Periodic", "Bounded")
     _, _, _, me, _, eager = run(shape, topo, staging=1, nsteps=2)
     _, _, _, mg, _, graph = run(shape, topo, staging=1, nsteps=2, graph=True)
