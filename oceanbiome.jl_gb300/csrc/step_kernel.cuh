@@ -545,10 +545,11 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                 // the tiles of this level: issued here at the item's first level, otherwise during
                 // the previous level's update
                 if (tid == 0 && k == k_top) tma_issue(i0, j0, k);
+                // the previous tendencies into this thread's own slots: waited for just before the
+                // update reads them, so the loads fly during the face loop
 #pragma unroll 1
                 for (int t = 0; t < NT; t++)
                     if (gm_smem) cp_async_elem<TC>(vdv + t * NTH + tid, a.G[t] + gidx);
-                if (gm_smem) cp_async_wait_all();
                 unsigned polls = 0;
                 if (!tma_timeout)
                     while (!mbar_try_wait(&stage_bar, tma_phase & 1u))
@@ -731,6 +732,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             __syncthreads();
             // the tiles are free again: the next level's copies fly during this level's update
             if (item_tma && tid == 0 && k > k_bot) tma_issue(i0, j0, k - 1);
+            if (TMA && gm_smem) cp_async_wait_all();   // this thread's previous tendencies (every thread)
             if (!row_cells) continue;   // no cell on this row: nothing below reads its registers
 
             // window tracers: flux through the face below this cell, divergence, and slide the
