@@ -920,7 +920,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 // exactly as the windows form them: one packed WENO5 where both drift speeds are non-zero at an
 // interior face, window_face_flux otherwise (the same arithmetic per element, so the fluxes are bit
 // for bit the windows').
-constexpr int SF_FACES = 8;
+constexpr int SF_FACES = 4;   // faces a thread: four ran faster than eight or sixteen
 template <typename TS, typename TC>
 __global__ void __launch_bounds__(256) sink_flux_kernel(const TS* __restrict__ cA, const TS* __restrict__ cB, int64_t sj,
                                                         int64_t sk, int Nx, int Ny, int Nz, const TC* __restrict__ drift,
