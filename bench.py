@@ -403,9 +403,9 @@ def run_gpu(args):
     achieved = bytes_per_launch / (substep_avg_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
     # DRAM bytes per cell of one substep launch, FP32: dram__bytes_read.sum + dram__bytes_write.sum of
-    # the ncu capture of an RK3 stage-2 launch (TMA-staged) at 256x256x32 (373.3 MB / 2,097,152
+    # the ncu capture of an RK3 stage-2 launch (TMA-staged) at 256x256x32 (372.9 MB / 2,097,152
     # cells), scaled by the cells of this grid
-    traffic = 178.0 * g.N if prec == "f32" else None
+    traffic = 177.8 * g.N if prec == "f32" else None
 
     # the other precisions of the same workload (spec: mixed vs FP64), and the error
     # statement of the timed precision after 1000 steps against the FP64 oracle
