@@ -1238,10 +1238,14 @@ static int enqueue_stage(obgc_ctx* c, StepPlan<TS, TC>& p, int stg, void* const*
 
 // Whether the steps can stage tiles with the tensor-memory accelerator: FP32, the lean kernel (no
 // closure, surface flux, forcing, fused modifier, sediment or replicate outputs), no passive
-// tracers, no model w and no implicit vertical solve.
+// tracers, no model w, no implicit vertical solve, and at least 8 cells in a periodic x and 6 in a
+// periodic y.
 template <typename TS, typename TC>
 static bool tma_eligible(obgc_ctx* c, const StepPlan<TS, TC>& p) {
     if (sizeof(TS) != 4 || sizeof(TC) != 4 || !c->tma_ready || c->staging != 1 || c->NP != 0 || p.impl || p.a.w) return false;
+    // a cell writes one periodic image per direction into the padded halos: a periodic direction needs
+    // at least two halos' width of cells (8 in x, 6 in y)
+    if ((p.a.periodic_x && p.a.Nx < 2 * TMA_HX) || (p.a.periodic_y && p.a.Ny < 2 * HALO)) return false;
     SubstepArgs<TS, TC> x = p.a;
     launch_terms(c, x, 0, c->NT);
     return !substep_needs_ext(x);
@@ -1596,7 +1600,7 @@ extern "C" int obgc_autotune_step(obgc_ctx* c, double t, double dt, int32_t step
     c->status_check = true;
     // the candidates: levels per work item, each with both tile stagings where the tensor copies exist
     std::vector<int> tzs;
-    for (int tz : {2, 3, 4, 6, 8, 10, 12, 16, 24, 32}) {
+    for (int tz : {2, 3, 4, 5, 6, 7, 8, 9, 10, 12, 16, 24, 32}) {
         const int v = std::min(tz, g.Nz);
         if (std::find(tzs.begin(), tzs.end(), v) == tzs.end()) tzs.push_back(v);
     }

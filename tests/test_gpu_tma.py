@@ -65,6 +65,17 @@ def test_tma_staging_matches_oracle_and_graph_replay():
     assert np.array_equal(gg, got)
 
 
+@pytest.mark.parametrize("shape", [(6, 16, 8), (32, 5, 8)])
+def test_periodic_grids_narrower_than_two_halos_keep_cp_async(shape):
+    # one periodic image per cell and side fills the padded halos only when a periodic direction has
+    # at least 8 (x) or 6 (y) cells: narrower grids stay on cp.async staging, and agree with it
+    topo = ("Periodic", "Periodic", "Bounded")
+    _, _, _, m1, _, got = run(shape, topo, staging=1)
+    assert m1.staging() == (True, False)
+    _, _, _, m0, _, ref = run(shape, topo, staging=0)
+    assert np.array_equal(got, ref)
+
+
 def test_configurations_outside_the_lean_kernel_keep_cp_async():
     torch = cuda()
     g = obgc.RectilinearGrid((32, 16, 8), (6250.0, 3125.0, 62.5), dtype="f32")
