@@ -11,7 +11,7 @@ from gpuhelp import cuda, rel_err
 
 pytestmark = pytest.mark.gpu
 
-CANDIDATES = {2, 3, 4, 6, 8, 10, 12, 16, 24, 32}
+CANDIDATES = {2, 3, 4, 5, 6, 7, 8, 9, 10, 12, 16, 24, 32}
 
 
 def lobster(precision, shape, seed=3, gas=False):
