@@ -105,3 +105,32 @@ def test_padded_copy_and_stages_in_a_graph():
     _, _, _, m1, _, one = run(shape, topo, staging=1, nsteps=1)
     _, _, _, m0, _, ref = run(shape, topo, staging=0, nsteps=1)
     assert np.array_equal(one, ref)
+
+
+def test_ensemble_members_through_host_copies_equal_eager_steps():
+    # two members stepped in turn from CUDA graphs, each step's state copied in from pinned host
+    # memory and back (the bench's end-to-end pipeline), equal one member stepped eagerly
+    torch = cuda()
+    shape, topo = (96, 32, 8), ("Periodic", "Periodic", "Bounded")
+    _, _, _, _, _, ref = run(shape, topo, staging=1, nsteps=3)
+    L = (shape[0] * 195.3125, shape[1] * 195.3125, shape[2] * 7.8125)
+    g = obgc.RectilinearGrid(shape, L, topo, dtype="f32")
+    bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem())
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=2, dtype=torch.float32)
+    members = []
+    for q in range(2):
+        m = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None), precision="f32")
+        obgc.set_(m, **obgc.lobster_initial_conditions(g, seed=3))
+        host = {n: m.tracers[n].cpu().pin_memory() for n in m.tracer_names}
+        members.append((m, host))
+    for _ in range(3):
+        for m, host in members:
+            for n in m.tracer_names:
+                m.tracers[n].copy_(host[n], non_blocking=True)
+            obgc.time_step(m, 300.0, nsteps=1, graph=True)
+            for n in m.tracer_names:
+                host[n].copy_(m.tracers[n], non_blocking=True)
+    torch.cuda.synchronize()
+    for m, host in members:
+        got = np.stack([host[n].double().numpy() for n in m.tracer_names])
+        assert np.array_equal(got, ref)
