@@ -864,6 +864,15 @@ int obgc_pisces_model_destroy(obgc_pisces_model* m);
 int obgc_pisces_model_bind(obgc_pisces_model* m, void* const* tracers, const void* u, const void* v);
 int obgc_pisces_model_update_state(obgc_pisces_model* m, double t, void* stream);
 int obgc_pisces_model_step(obgc_pisces_model* m, double t, double dt, int32_t nsteps, void* stream);
+/* One RK3 stage (0, 1, 2) of the step that starts at t, from the 26 tracer arrays `in` into `out`
+ * (distinct arrays in the model's grid layout): update_state! on `in`, the functor, the fused
+ * substeps; the previous stage's tendencies stay in the model.  finish != 0 applies the
+ * negative-tracer modifier to `out` afterwards, as obgc_pisces_model_step does after its last
+ * substep.  For a custom stage loop that fills halos between stages (the y-slab split: one
+ * NonhydrostaticModel(grid; biogeochemistry = PISCES(...)) per rank of Oceananigans' Distributed
+ * architecture, whose fill_halo_regions! runs before each tendency computation). */
+int obgc_pisces_model_substep(obgc_pisces_model* m, double t, double dt, int32_t stage, const void* const* in,
+                              void* const* out, int32_t finish, void* stream);
 /* Device pointer of an auxiliary field the model keeps (state precision). */
 int obgc_pisces_model_field(obgc_pisces_model* m, int32_t which, void** ptr);
 /* Host FP64 copy of an auxiliary field: (Nx, Ny) dense, or [Nz][Ny][Nx] dense for centre fields. */

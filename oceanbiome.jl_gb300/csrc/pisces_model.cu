@@ -219,21 +219,29 @@ void aux_fields(const obgc_pisces_model* m, obgc_pisces_field* a) {
     a[OBGC_PAUX_PAR3] = {OBGC_PF_XYZ, 0, 0.0, m->par[3]};
 }
 
+// The fused substep launches of one RK3 stage: the 26 tracers advect independently once their BGC
+// tendencies are in hand, in launches on tracers 0-8, 9-17 (POC and GOC, slots 1 and 2 of the group,
+// keep their register windows) and 18-25, each holding a third of the shared-memory tiles and running
+// three blocks per SM.
+constexpr int NGROUP = 3;
+constexpr int G_FIRST[NGROUP] = {0, 9, 18}, G_SIZE[NGROUP] = {9, 9, 8};
+
 template <typename TS, typename TC>
-int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t st) {
-    // the 26 tracers advect independently once their BGC tendencies are in hand: launches on tracers
-    // 0-8, 9-17 (POC and GOC, slots 1 and 2 of the group, keep their register windows) and 18-25
-    // hold a third of the shared-memory tiles each and run three blocks per SM
-    constexpr int NGROUP = 3;
-    const int g_first[NGROUP] = {0, 9, 18}, g_size[NGROUP] = {9, 9, 8};
-    const FusedEntry* fes[NGROUP];
-    for (int q = 0; q < NGROUP; q++) {
-        fes[q] = find_fused(m->desc.precision, V_EXTERNAL, g_size[q]);
-        if (!fes[q]) return fail(OBGC_ERR_UNSUPPORTED, "obgc_pisces_model_step: no fused PISCES kernel for this precision");
-    }
-    const FusedEntry* fe = fes[0];
-    const obgc_grid& g = m->desc.grid;
+struct PiscesPlan {
     SubstepArgs<TS, TC> a;
+    const FusedEntry* fes[NGROUP];
+    int blocks = 0;
+    obgc_pisces_field aux[OBGC_PAUX_NUM];
+};
+
+template <typename TS, typename TC>
+int plan_pisces(obgc_pisces_model* m, double dt, PiscesPlan<TS, TC>& p) {
+    for (int q = 0; q < NGROUP; q++) {
+        p.fes[q] = find_fused(m->desc.precision, V_EXTERNAL, G_SIZE[q]);
+        if (!p.fes[q]) return fail(OBGC_ERR_UNSUPPORTED, "obgc_pisces_model_step: no fused PISCES kernel for this precision");
+    }
+    const obgc_grid& g = m->desc.grid;
+    SubstepArgs<TS, TC>& a = p.a;
     std::memset(&a, 0, sizeof(a));
     a.Nx = g.Nx; a.Ny = g.Ny; a.Nz = g.Nz;
     a.periodic_x = g.topology_x == OBGC_PERIODIC;
@@ -257,53 +265,69 @@ int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t 
     a.dt_d = dt;
     a.dt = TC(dt);
     int occ = 1;
-    int rc = fe->occupancy(&occ);
+    const int rc = p.fes[0]->occupancy(&occ);
     if (rc != OBGC_OK) return rc;
-    const int blocks = std::min(a.n_items, m->blocks * (occ > 0 ? occ : 1));
+    p.blocks = std::min(a.n_items, m->blocks * (occ > 0 ? occ : 1));
+    aux_fields(m, p.aux);
+    return OBGC_OK;
+}
+
+// One RK3 stage at time ts from the tracers in cur into nxt: update_state! on cur (the negative-tracer
+// modifier, light, euphotic depth, mixed-layer PAR, calcite saturation), the functor, then the
+// substep launches.  The previous stage's tendencies live in the model (m->G).
+template <typename TS, typename TC>
+int pisces_stage(obgc_pisces_model* m, PiscesPlan<TS, TC>& p, int stg, double ts, void* const* cur, void* const* nxt,
+                 cudaStream_t st) {
+    const obgc_grid& g = m->desc.grid;
+    SubstepArgs<TS, TC>& a = p.a;
+    // update_state! reads the current state: point the model at it for this stage
+    void* user_saved[PNT];
+    std::memcpy(user_saved, m->user, sizeof(user_saved));
+    std::memcpy(m->user, cur, sizeof(user_saved));
+    int rc = update_state_any(m, ts, st);
+    std::memcpy(m->user, user_saved, sizeof(user_saved));
+    if (rc == OBGC_OK) rc = prof_mark(m, st);
+    if (rc == OBGC_OK) rc = launch_pisces<TS, TC>(&m->desc.pisces, &g, cur, p.aux, m->Gb, ts, st);
+    if (rc == OBGC_OK) rc = prof_mark(m, st);
+    if (rc != OBGC_OK) return rc;
+    const uint32_t mask = m->desc.advection ? m->drift_mask : 0u;
+    a.first_stage = stg == 0;
+    a.write_G = stg < 2;
+    a.gamma = TC(rk3_gamma(stg));
+    a.zeta = TC(rk3_zeta(stg));
+    a.c_stage = rk3_c(stg);
+    for (int q = 0; q < NGROUP && rc == OBGC_OK; q++) {
+        const int g0 = G_FIRST[q], gn = G_SIZE[q];
+        for (int t = 0; t < gn; t++) {
+            a.in[t] = static_cast<const TS*>(cur[g0 + t]);
+            a.out[t] = static_cast<TS*>(nxt[g0 + t]);
+            a.G[t] = static_cast<TC*>(m->G[g0 + t]);
+            a.ext[t] = g0 + t < OBGC_PIS_NUM_BGC ? static_cast<const TC*>(m->Gb[g0 + t]) : nullptr;
+        }
+        a.n_ext = std::max(0, std::min(gn, OBGC_PIS_NUM_BGC - g0));
+        a.drift = static_cast<const TC*>(m->drift) + (size_t)g0 * (g.Nz + 1);
+        a.drift_mask = (mask >> g0) & ((1u << gn) - 1u);
+        rc = p.fes[q]->launch(&a, p.blocks, st);
+    }
+    if (rc == OBGC_OK) rc = prof_mark(m, st);
+    return rc;
+}
+
+template <typename TS, typename TC>
+int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t st) {
+    PiscesPlan<TS, TC> p;
+    int rc = plan_pisces<TS, TC>(m, dt, p);
+    if (rc != OBGC_OK) return rc;
+    const obgc_grid& g = m->desc.grid;
     void* cur[PNT];
     void* nxt[PNT];
     for (int q = 0; q < PNT; q++) { cur[q] = m->user[q]; nxt[q] = m->scratch[q]; }
-    obgc_pisces_field aux[OBGC_PAUX_NUM];
-    aux_fields(m, aux);
-    void* user_saved[PNT];
-    std::memcpy(user_saved, m->user, sizeof(user_saved));
-    for (int s = 0; s < nsteps; s++) {
-        for (int stg = 0; stg < 3; stg++) {
-            const double ts = t + s * dt + rk3_c(stg) * dt;
-            // update_state! reads the current state: point the model at it for this stage
-            std::memcpy(m->user, cur, sizeof(cur));
-            rc = update_state_any(m, ts, st);
-            if (rc == OBGC_OK) rc = prof_mark(m, st);
-            if (rc != OBGC_OK) break;
-            rc = launch_pisces<TS, TC>(&m->desc.pisces, &g, cur, aux, m->Gb, ts, st);
-            if (rc == OBGC_OK) rc = prof_mark(m, st);
-            if (rc != OBGC_OK) break;
-            const uint32_t mask = m->desc.advection ? m->drift_mask : 0u;
-            a.first_stage = stg == 0;
-            a.write_G = stg < 2;
-            a.gamma = TC(rk3_gamma(stg));
-            a.zeta = TC(rk3_zeta(stg));
-            a.c_stage = rk3_c(stg);
-            for (int q = 0; q < NGROUP && rc == OBGC_OK; q++) {
-                const int g0 = g_first[q], gn = g_size[q];
-                for (int t = 0; t < gn; t++) {
-                    a.in[t] = static_cast<const TS*>(cur[g0 + t]);
-                    a.out[t] = static_cast<TS*>(nxt[g0 + t]);
-                    a.G[t] = static_cast<TC*>(m->G[g0 + t]);
-                    a.ext[t] = g0 + t < OBGC_PIS_NUM_BGC ? static_cast<const TC*>(m->Gb[g0 + t]) : nullptr;
-                }
-                a.n_ext = std::max(0, std::min(gn, OBGC_PIS_NUM_BGC - g0));
-                a.drift = static_cast<const TC*>(m->drift) + (size_t)g0 * (g.Nz + 1);
-                a.drift_mask = (mask >> g0) & ((1u << gn) - 1u);
-                rc = fes[q]->launch(&a, blocks, st);
-            }
-            if (rc == OBGC_OK) rc = prof_mark(m, st);
-            if (rc != OBGC_OK) break;
+    for (int s = 0; s < nsteps && rc == OBGC_OK; s++) {
+        for (int stg = 0; stg < 3 && rc == OBGC_OK; stg++) {
+            rc = pisces_stage<TS, TC>(m, p, stg, t + s * dt + rk3_c(stg) * dt, cur, nxt, st);
             for (int q = 0; q < PNT; q++) { void* tmp = cur[q]; cur[q] = nxt[q]; nxt[q] = tmp; }
         }
-        if (rc != OBGC_OK) break;
     }
-    std::memcpy(m->user, user_saved, sizeof(user_saved));
     if (rc != OBGC_OK) return rc;
     if (m->desc.negatives == OBGC_NEGATIVES_SCALE) {
         rc = launch_negatives(m->neg, m->ts, cur, g, st);   // update_state! after the last substep
@@ -318,6 +342,19 @@ int enqueue(obgc_pisces_model* m, double t, double dt, int nsteps, cudaStream_t 
         OBGC_LAUNCHED("copy_fields_kernel");
     }
     return OBGC_OK;
+}
+
+// One stage from caller arrays `in` into `out` (the model's grid layout), and with `finish` the
+// modifier that ends a call.
+template <typename TS, typename TC>
+int enqueue_one(obgc_pisces_model* m, double t, double dt, int stage, void* const* in, void* const* out, bool finish,
+                cudaStream_t st) {
+    PiscesPlan<TS, TC> p;
+    int rc = plan_pisces<TS, TC>(m, dt, p);
+    if (rc == OBGC_OK) rc = pisces_stage<TS, TC>(m, p, stage, t + rk3_c(stage) * dt, in, out, st);
+    if (rc == OBGC_OK && finish && m->desc.negatives == OBGC_NEGATIVES_SCALE)
+        rc = launch_negatives(m->neg, m->ts, const_cast<void**>(out), m->desc.grid, st);
+    return rc;
 }
 
 template <typename TS, typename TC>
@@ -431,6 +468,25 @@ extern "C" int obgc_pisces_model_step(obgc_pisces_model* m, double t, double dt,
     m->in_step = true;
     const int rc = m->ts == 4 ? enqueue<float, float>(m, t, dt, nsteps, st)
                    : m->tc == 8 ? enqueue<double, double>(m, t, dt, nsteps, st) : enqueue<double, float>(m, t, dt, nsteps, st);
+    m->in_step = false;
+    if (rc != OBGC_OK) m->ev_used = 0;
+    return rc;
+}
+
+extern "C" int obgc_pisces_model_substep(obgc_pisces_model* m, double t, double dt, int32_t stage, const void* const* in,
+                                         void* const* out, int32_t finish, void* stream) {
+    if (!m || !m->bound || stage < 0 || stage > 2 || !(dt > 0) || !in || !out)
+        return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_pisces_model_substep: bad argument");
+    for (int q = 0; q < PNT; q++)
+        if (!in[q] || !out[q] || in[q] == out[q])
+            return fail(OBGC_ERR_INVALID_ARGUMENT, "obgc_pisces_model_substep: every tracer needs distinct input and output arrays");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    void* const* vin = const_cast<void* const*>(in);
+    m->ev_used = 0;
+    m->in_step = true;
+    const int rc = m->ts == 4 ? enqueue_one<float, float>(m, t, dt, stage, vin, out, finish != 0, st)
+                   : m->tc == 8 ? enqueue_one<double, double>(m, t, dt, stage, vin, out, finish != 0, st)
+                                : enqueue_one<double, float>(m, t, dt, stage, vin, out, finish != 0, st);
     m->in_step = false;
     if (rc != OBGC_OK) m->ev_used = 0;
     return rc;

@@ -398,6 +398,7 @@ def load():
     _sig(lib, "obgc_pisces_model_bind", C.c_int, VP, P(VP), VP, VP)
     _sig(lib, "obgc_pisces_model_update_state", C.c_int, VP, D, VP)
     _sig(lib, "obgc_pisces_model_step", C.c_int, VP, D, D, I32, VP)
+    _sig(lib, "obgc_pisces_model_substep", C.c_int, VP, D, D, I32, P(VP), P(VP), I32, VP)
     _sig(lib, "obgc_pisces_model_field", C.c_int, VP, I32, P(VP))
     _sig(lib, "obgc_pisces_model_read_field", C.c_int, VP, I32, P(D))
     _sig(lib, "obgc_pisces_model_set_profiling", C.c_int, VP, I32)
@@ -436,6 +437,6 @@ EXPORTED = [
     "obgc_service_get_stats", "obgc_service_reset_stats", "obgc_service_engine",
     "obgc_pisces_default_params", "obgc_pisces_eval_point", "obgc_pisces_tendencies", "obgc_mixed_layer_mean",
     "obgc_pisces_calcite_saturation", "obgc_pisces_model_create", "obgc_pisces_model_destroy", "obgc_pisces_model_bind",
-    "obgc_pisces_model_update_state", "obgc_pisces_model_step", "obgc_pisces_model_field",
+    "obgc_pisces_model_update_state", "obgc_pisces_model_step", "obgc_pisces_model_substep", "obgc_pisces_model_field",
     "obgc_pisces_model_read_field", "obgc_pisces_model_set_profiling", "obgc_pisces_model_last_timing",
 ]

@@ -167,3 +167,91 @@ class SlabModel:
         import torch
         src = self.cur if self.cur is not None else self.fields
         return torch.stack([f[:, self.decomposition.own(), :] for f in src])
+
+
+class PiscesSlabModel:
+    """One rank's slab of a PISCES 3-D model split in y (configuration 4): a PiscesModel on the slab
+    grid, a second set of state arrays for the stage ping-pong and the halo buffers; the stage loop
+    is SlabModel's.  Light, the euphotic depth, the mixed-layer means and the calcite saturation are
+    column-local, so the halo rows of the 26 tracers are the only exchange."""
+
+    def __init__(self, decomposition, velocities, initial, precision="f32", exchange=None, **model_kw):
+        import torch
+        from .pisces import PiscesModel
+        self.decomposition = d = decomposition
+        u, v = velocities[:2]
+        self.model = PiscesModel(d.slab_grid, velocities=(d.scatter(u), d.scatter(v)), precision=precision, **model_kw)
+        self.model.set_(**{k: d.scatter(np.broadcast_to(np.asarray(x, dtype=np.float64), d.grid.shape))
+                           for k, x in initial.items()})
+        m = self.model
+        self.names = list(A.PISCES_TRACERS)
+        self.fields = [m.tracers[n] for n in self.names]
+        self.other = [torch.empty_like(f) for f in self.fields]
+        shape = d.buffer_shape(len(self.names))
+        dev = self.fields[0].device
+        self.send = [torch.empty(shape, dtype=m.dtype, device=dev) for _ in range(2)]
+        self.recv = [torch.empty(shape, dtype=m.dtype, device=dev) for _ in range(2)]
+        self.exchange = exchange or (lambda ss, sn, rs, rn: d.exchange(ss, sn, rs, rn))
+        self._lib = A.load()
+        self._cgrid = d.slab_grid.c_grid()
+        self._dtype = A.F32 if m.dtype == torch.float32 else A.F64
+        self.cur = self.nxt = None
+        self._last_stage = False
+
+    def _ptrs(self, fields):
+        return (C.c_void_p * len(fields))(*[f.data_ptr() for f in fields])
+
+    @staticmethod
+    def _stream():
+        import torch
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream) if torch.cuda.is_available() else None
+
+    def pack(self, fields):
+        A.check(self._lib.obgc_halo_pack(C.byref(self._cgrid), self._dtype, len(fields), self._ptrs(fields),
+                                         self.decomposition.halo, self.send[0].data_ptr(), self.send[1].data_ptr(),
+                                         self._stream()), "obgc_halo_pack")
+
+    def unpack(self, fields):
+        A.check(self._lib.obgc_halo_unpack(C.byref(self._cgrid), self._dtype, len(fields), self._ptrs(fields),
+                                           self.decomposition.halo, self.recv[0].data_ptr(), self.recv[1].data_ptr(),
+                                           self._stream()), "obgc_halo_unpack")
+
+    def pack_halos(self):
+        if self.cur is None:
+            self.cur, self.nxt = self.fields, self.other
+        self.pack(self.cur)
+
+    def exchange_halos(self):
+        self.exchange(self.send[0], self.send[1], self.recv[0], self.recv[1])
+
+    def run_stage(self, stage, dt, finish=False):
+        """finish: this is the call's last stage (obgc_pisces_model_step applies the negative-tracer
+        modifier after it)."""
+        m = self.model
+        self.unpack(self.cur)
+        A.check(self._lib.obgc_pisces_model_substep(m._h, float(m.time), float(dt), int(stage), self._ptrs(self.cur),
+                                                    self._ptrs(self.nxt), int(bool(finish)), self._stream()),
+                "obgc_pisces_model_substep")
+        self.cur, self.nxt = self.nxt, self.cur
+        if stage == 2:
+            m.time += dt
+
+    def sync_fields(self):
+        if self.cur is not None and self.cur is not self.fields:
+            for a, b in zip(self.fields, self.cur):
+                a.copy_(b)
+        self.cur = None
+
+    def time_step(self, dt, nsteps=1):
+        for s in range(nsteps):
+            for stage in range(3):
+                self.pack_halos()
+                self.exchange_halos()
+                self.run_stage(stage, dt, finish=(s == nsteps - 1 and stage == 2))
+        self.sync_fields()
+
+    def own_state(self):
+        """(26, Nz, Ny_own, Nx) of the slab's own rows."""
+        import torch
+        src = self.cur if self.cur is not None else self.fields
+        return torch.stack([f[:, self.decomposition.own(), :] for f in src])

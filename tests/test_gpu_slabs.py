@@ -91,3 +91,45 @@ def test_slabs_in_lockstep_equal_the_single_domain_step(precision, world):
              t=0.0, dt=dt, nsteps=nsteps)
     tol = {"f64": 1e-11, "mixed": 1e-5, "f32": 5e-5}[precision]
     assert max(rel_err(got[q], ref[q]) for q in range(got.shape[0])) < tol
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed", "f32"])
+def test_pisces_slabs_in_lockstep_equal_the_single_domain_step(precision):
+    # configuration 4's model split in two y slabs: the same cells through the same kernels
+    torch = cuda()
+    g = obgc.RectilinearGrid((16, 12, 10), (16000.0, 12000.0, 500.0), dtype="f32" if precision == "f32" else "f64")
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=4)
+    init = obgc.pisces_initial_conditions(g, seed=6)
+    dt, nsteps = 600.0, 2
+    kw = dict(mixed_layer_depth=-60.0, surface_PAR=100.0)
+    whole = obgc.PiscesModel(g, velocities=(u, v), precision=precision, **kw)
+    whole.set_(**init)
+    whole.time_step(dt, nsteps=nsteps)
+    ref = whole.state_array().double().cpu().numpy()
+    slabs = [obgc.PiscesSlabModel(obgc.SlabDecomposition(g, r, 2), (u, v), init, precision=precision, **kw)
+             for r in range(2)]
+    for s in range(nsteps):
+        for stage in range(3):
+            for sl in slabs:
+                sl.pack_halos()
+            for sl in slabs:
+                d = sl.decomposition
+                sl.recv[0].copy_(slabs[d.south].send[1])
+                sl.recv[1].copy_(slabs[d.north].send[0])
+            for sl in slabs:
+                sl.run_stage(stage, dt, finish=(s == nsteps - 1 and stage == 2))
+    for sl in slabs:
+        sl.sync_fields()
+    got = torch.cat([sl.own_state() for sl in slabs], dim=2).double().cpu().numpy()
+    assert np.array_equal(got, ref), max(rel_err(got[q], ref[q]) for q in range(got.shape[0]))
+
+
+def test_pisces_stage_rejects_shared_arrays():
+    torch = cuda()
+    g = obgc.RectilinearGrid((8, 6, 6), (8000.0, 6000.0, 300.0), dtype="f64")
+    m = obgc.PiscesModel(g, precision="f64")
+    lib = A.load()
+    f = [m.tracers[n] for n in A.PISCES_TRACERS]
+    ptrs = (C.c_void_p * 26)(*[x.data_ptr() for x in f])
+    assert lib.obgc_pisces_model_substep(m._h, 0.0, 600.0, 0, ptrs, ptrs, 0, None) == 1   # OBGC_ERR_INVALID_ARGUMENT
+    assert lib.obgc_pisces_model_substep(m._h, 0.0, 600.0, 3, ptrs, ptrs, 0, None) == 1   # OBGC_ERR_INVALID_ARGUMENT
