@@ -213,6 +213,10 @@ typedef struct or_pisces3d {
 /* state [26][N]; u, v [N] or NULL. */
 void or_pisces_step3d(const or_pisces3d* m, double* state, const double* u, const double* v, double t, double dt,
                       int nsteps, int nthreads);
+/* One RK3 stage of the step that starts at t (G receives the stage's tendency, Gm holds the previous
+ * stage's; start: the negative-tracer modifier first, as or_pisces_step3d applies it on entry). */
+void or_pisces_stage3d(const or_pisces3d* m, double* state, const double* u, const double* v, double t, double dt,
+                       int stage, double* G, const double* Gm, int start, int nthreads);
 /* The auxiliary fields of the last update (for tests): PAR bands and total [4][N], zeu and mixed-layer
  * PAR [2][Nx*Ny], Omega [N]. */
 void or_pisces_update_state3d(const or_pisces3d* m, const double* state, double t, double* par4, double* xy2,

@@ -738,98 +738,136 @@ static void pisces_negatives(const or_pisces3d* m, double* state, long N, int nt
     for (long c = 0; c < N; c++) or_scale_cell(state + c, N, ng, gn, gslot, gfac, m->invalid_fill_value);
 }
 
-void or_pisces_step3d(const or_pisces3d* m, double* state, const double* u, const double* v, double t, double dt,
-                      int nsteps, int nthreads) {
+/* The work buffers of a PISCES stage and the sinking speeds at the faces (POC at a constant speed,
+ * GOC with DepthDependantSinkingSpeed evaluated at construction, euphotic depth 0), built as
+ * setup_velocity_fields does. */
+typedef struct {
+    double *par4, *xy2, *omega, *wpoc, *wgoc, *zc;
+} pisces_work;
+
+static void pisces_work_init(const or_pisces3d* m, pisces_work* w) {
+    const obgc_grid* g = &m->grid;
+    const int Nz = g->Nz;
+    const long NN = (long)g->Nx * g->Ny, N = NN * Nz;
+    const double dz = g->Lz / Nz;
+    w->par4 = malloc(sizeof(double) * 4 * N);
+    w->xy2 = malloc(sizeof(double) * 2 * NN);
+    w->omega = malloc(sizeof(double) * N);
+    w->wpoc = malloc(sizeof(double) * (Nz + 1));
+    w->wgoc = malloc(sizeof(double) * (Nz + 1));
+    w->zc = malloc(sizeof(double) * (Nz + 1));
+    for (int k = 0; k <= Nz; k++) w->zc[k] = -g->Lz + (k + 0.5) * dz;
+    for (int f = 0; f <= Nz; f++)
+        w->wpoc[f] = f < Nz ? -m->p.poc_sinking_speed * (m->p.open_bottom ? 1.0 : 1 - exp((double)(-f) / 2)) : 0.0;
+    or_pisces_goc_speed(&m->p, Nz, w->zc, m->mixed_layer_depth, 0.0, w->wgoc);
+}
+
+static void pisces_work_free(pisces_work* w) {
+    free(w->par4); free(w->xy2); free(w->omega); free(w->wpoc); free(w->wgoc); free(w->zc);
+}
+
+/* One RK3 stage st of the step that starts at t: update_state!, every tendency into G, the update
+ * with the previous stage's Gm, then the negative-tracer modifier. */
+static void pisces_stage(const or_pisces3d* m, double* state, const double* u, const double* v, double t, double dt,
+                         int st, double* G, const double* Gm, pisces_work* w, int nthreads) {
     const obgc_grid* g = &m->grid;
     const int Nx = g->Nx, Ny = g->Ny, Nz = g->Nz, nt = OBGC_PIS_NUM;
     const long NN = (long)Nx * Ny, N = NN * Nz;
     const double dx = g->Lx / Nx, dy = g->Ly / Ny, dz = g->Lz / Nz;
     const int px = g->topology_x == OBGC_PERIODIC, py = g->topology_y == OBGC_PERIODIC;
     const int flat_x = g->topology_x == OBGC_FLAT || !m->advection, flat_y = g->topology_y == OBGC_FLAT || Ny == 1 || !m->advection;
-    double* G = calloc((size_t)nt * N, sizeof(double));
-    double* Gm = calloc((size_t)nt * N, sizeof(double));
-    double* par4 = malloc(sizeof(double) * 4 * N);
-    double* xy2 = malloc(sizeof(double) * 2 * NN);
-    double* omega = malloc(sizeof(double) * N);
-    /* sinking velocities at the faces, built once as setup_velocity_fields does: POC at a constant
-     * speed, GOC with DepthDependantSinkingSpeed evaluated at construction (euphotic depth 0) */
-    double* wpoc = malloc(sizeof(double) * (Nz + 1));
-    double* wgoc = malloc(sizeof(double) * (Nz + 1));
-    double* zc = malloc(sizeof(double) * (Nz + 1));
-    for (int k = 0; k <= Nz; k++) zc[k] = -g->Lz + (k + 0.5) * dz;
-    for (int f = 0; f <= Nz; f++) wpoc[f] = f < Nz ? -m->p.poc_sinking_speed * (m->p.open_bottom ? 1.0 : 1 - exp((double)(-f) / 2)) : 0.0;
-    or_pisces_goc_speed(&m->p, Nz, zc, m->mixed_layer_depth, 0.0, wgoc);
+    double *par4 = w->par4, *xy2 = w->xy2, *omega = w->omega, *wpoc = w->wpoc, *wgoc = w->wgoc, *zc = w->zc;
+    const double ts = t + RK_C[st] * dt;
+    or_pisces_update_state3d(m, state, ts, par4, xy2, omega, nthreads);
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+    for (long c = 0; c < N; c++) {
+        const int i = (int)(c % Nx), j = (int)((c / Nx) % Ny), k = (int)(c / NN);
+        const long col = (long)j * Nx + i;
+        double vals[OBGC_PIS_NUM], aux[OBGC_PAUX_NUM], Gb[OBGC_PIS_NUM_BGC];
+        for (int q = 0; q < nt; q++) vals[q] = state[(long)q * N + c];
+        aux[OBGC_PAUX_ZMXL] = m->mixed_layer_depth;
+        aux[OBGC_PAUX_ZEU] = xy2[col];
+        aux[OBGC_PAUX_SICLIM] = m->p.silicate_climatology;
+        aux[OBGC_PAUX_OMEGA] = omega[c];
+        aux[OBGC_PAUX_KAPPA] = m->mean_kappa;
+        aux[OBGC_PAUX_MLPAR] = xy2[NN + col];
+        aux[OBGC_PAUX_WPOC] = 0.5 * (wpoc[k] + wpoc[k + 1]);
+        aux[OBGC_PAUX_WGOC] = 0.5 * (wgoc[k] + wgoc[k + 1]);
+        aux[OBGC_PAUX_PAR] = par4[c];
+        aux[OBGC_PAUX_PAR1] = par4[N + c];
+        aux[OBGC_PAUX_PAR2] = par4[2 * N + c];
+        aux[OBGC_PAUX_PAR3] = par4[3 * N + c];
+        or_pisces_tendencies(&m->p, vals, aux, zc[k], ts, Gb);
+        for (int q = 0; q < nt; q++) {
+            double tend = q < OBGC_PIS_NUM_BGC ? Gb[q] : 0.0;
+            const double* cq = state + (long)q * N;
+            double adv = 0.0;
+            if (!flat_x && u) {
+                const double* line = cq + (long)k * NN + (long)j * Nx;
+                int f0 = i, f1 = i + 1;
+                double U0 = (px || (f0 > 0 && f0 < Nx)) ? u[(long)k * NN + (long)j * Nx + (f0 % Nx)] : 0.0;
+                double U1 = (px || (f1 > 0 && f1 < Nx)) ? u[(long)k * NN + (long)j * Nx + (f1 % Nx)] : 0.0;
+                double F0 = U0 != 0.0 ? U0 * face_value(line, 1, Nx, px, f0, U0) : 0.0;
+                double F1 = U1 != 0.0 ? U1 * face_value(line, 1, Nx, px, f1, U1) : 0.0;
+                adv += (F1 - F0) / dx;
+            }
+            if (!flat_y && v) {
+                const double* line = cq + (long)k * NN + i;
+                int f0 = j, f1 = j + 1;
+                double V0 = (py || (f0 > 0 && f0 < Ny)) ? v[(long)k * NN + (long)(f0 % Ny) * Nx + i] : 0.0;
+                double V1 = (py || (f1 > 0 && f1 < Ny)) ? v[(long)k * NN + (long)(f1 % Ny) * Nx + i] : 0.0;
+                double F0 = V0 != 0.0 ? V0 * face_value(line, Nx, Ny, py, f0, V0) : 0.0;
+                double F1 = V1 != 0.0 ? V1 * face_value(line, Nx, Ny, py, f1, V1) : 0.0;
+                adv += (F1 - F0) / dy;
+            }
+            /* biogeochemical_drift_velocity (two_size_class.jl:100-107) */
+            const double* wd = NULL;
+            if (m->advection && (q == OBGC_PIS_POC || q == OBGC_PIS_SFE)) wd = wpoc;
+            if (m->advection && (q == OBGC_PIS_GOC || q == OBGC_PIS_BFE || q == OBGC_PIS_PSI || q == OBGC_PIS_CACO3)) wd = wgoc;
+            if (wd) {
+                const double* zline = cq + (long)j * Nx + i;
+                double W0 = wd[k], W1 = wd[k + 1];
+                double F0 = W0 != 0.0 ? W0 * face_value(zline, NN, Nz, 0, k, W0) : 0.0;
+                double F1 = W1 != 0.0 ? W1 * face_value(zline, NN, Nz, 0, k + 1, W1) : 0.0;
+                adv += (F1 - F0) / dz;
+            }
+            G[(long)q * N + c] = tend - adv;
+        }
+    }
+    const double gg = RK_G[st], z = RK_Z[st];
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+    for (long x = 0; x < (long)nt * N; x++) {
+        if (st == 0) state[x] += dt * gg * G[x];
+        else state[x] += dt * (gg * G[x] + z * Gm[x]);
+    }
+    pisces_negatives(m, state, N, nthreads);
+}
+
+void or_pisces_step3d(const or_pisces3d* m, double* state, const double* u, const double* v, double t, double dt,
+                      int nsteps, int nthreads) {
+    const long N = (long)m->grid.Nx * m->grid.Ny * m->grid.Nz;
+    double* G = calloc((size_t)OBGC_PIS_NUM * N, sizeof(double));
+    double* Gm = calloc((size_t)OBGC_PIS_NUM * N, sizeof(double));
+    pisces_work w;
+    pisces_work_init(m, &w);
     pisces_negatives(m, state, N, nthreads);
     for (int s = 0; s < nsteps; s++) {
         for (int st = 0; st < 3; st++) {
-            const double ts = t + RK_C[st] * dt;
-            or_pisces_update_state3d(m, state, ts, par4, xy2, omega, nthreads);
-#pragma omp parallel for num_threads(nthreads) schedule(static)
-            for (long c = 0; c < N; c++) {
-                const int i = (int)(c % Nx), j = (int)((c / Nx) % Ny), k = (int)(c / NN);
-                const long col = (long)j * Nx + i;
-                double vals[OBGC_PIS_NUM], aux[OBGC_PAUX_NUM], Gb[OBGC_PIS_NUM_BGC];
-                for (int q = 0; q < nt; q++) vals[q] = state[(long)q * N + c];
-                aux[OBGC_PAUX_ZMXL] = m->mixed_layer_depth;
-                aux[OBGC_PAUX_ZEU] = xy2[col];
-                aux[OBGC_PAUX_SICLIM] = m->p.silicate_climatology;
-                aux[OBGC_PAUX_OMEGA] = omega[c];
-                aux[OBGC_PAUX_KAPPA] = m->mean_kappa;
-                aux[OBGC_PAUX_MLPAR] = xy2[NN + col];
-                aux[OBGC_PAUX_WPOC] = 0.5 * (wpoc[k] + wpoc[k + 1]);
-                aux[OBGC_PAUX_WGOC] = 0.5 * (wgoc[k] + wgoc[k + 1]);
-                aux[OBGC_PAUX_PAR] = par4[c];
-                aux[OBGC_PAUX_PAR1] = par4[N + c];
-                aux[OBGC_PAUX_PAR2] = par4[2 * N + c];
-                aux[OBGC_PAUX_PAR3] = par4[3 * N + c];
-                or_pisces_tendencies(&m->p, vals, aux, zc[k], ts, Gb);
-                for (int q = 0; q < nt; q++) {
-                    double tend = q < OBGC_PIS_NUM_BGC ? Gb[q] : 0.0;
-                    const double* cq = state + (long)q * N;
-                    double adv = 0.0;
-                    if (!flat_x && u) {
-                        const double* line = cq + (long)k * NN + (long)j * Nx;
-                        int f0 = i, f1 = i + 1;
-                        double U0 = (px || (f0 > 0 && f0 < Nx)) ? u[(long)k * NN + (long)j * Nx + (f0 % Nx)] : 0.0;
-                        double U1 = (px || (f1 > 0 && f1 < Nx)) ? u[(long)k * NN + (long)j * Nx + (f1 % Nx)] : 0.0;
-                        double F0 = U0 != 0.0 ? U0 * face_value(line, 1, Nx, px, f0, U0) : 0.0;
-                        double F1 = U1 != 0.0 ? U1 * face_value(line, 1, Nx, px, f1, U1) : 0.0;
-                        adv += (F1 - F0) / dx;
-                    }
-                    if (!flat_y && v) {
-                        const double* line = cq + (long)k * NN + i;
-                        int f0 = j, f1 = j + 1;
-                        double V0 = (py || (f0 > 0 && f0 < Ny)) ? v[(long)k * NN + (long)(f0 % Ny) * Nx + i] : 0.0;
-                        double V1 = (py || (f1 > 0 && f1 < Ny)) ? v[(long)k * NN + (long)(f1 % Ny) * Nx + i] : 0.0;
-                        double F0 = V0 != 0.0 ? V0 * face_value(line, Nx, Ny, py, f0, V0) : 0.0;
-                        double F1 = V1 != 0.0 ? V1 * face_value(line, Nx, Ny, py, f1, V1) : 0.0;
-                        adv += (F1 - F0) / dy;
-                    }
-                    /* biogeochemical_drift_velocity (two_size_class.jl:100-107) */
-                    const double* wd = NULL;
-                    if (m->advection && (q == OBGC_PIS_POC || q == OBGC_PIS_SFE)) wd = wpoc;
-                    if (m->advection && (q == OBGC_PIS_GOC || q == OBGC_PIS_BFE || q == OBGC_PIS_PSI || q == OBGC_PIS_CACO3)) wd = wgoc;
-                    if (wd) {
-                        const double* zline = cq + (long)j * Nx + i;
-                        double W0 = wd[k], W1 = wd[k + 1];
-                        double F0 = W0 != 0.0 ? W0 * face_value(zline, NN, Nz, 0, k, W0) : 0.0;
-                        double F1 = W1 != 0.0 ? W1 * face_value(zline, NN, Nz, 0, k + 1, W1) : 0.0;
-                        adv += (F1 - F0) / dz;
-                    }
-                    G[(long)q * N + c] = tend - adv;
-                }
-            }
-            const double gg = RK_G[st], z = RK_Z[st];
-#pragma omp parallel for num_threads(nthreads) schedule(static)
-            for (long x = 0; x < (long)nt * N; x++) {
-                if (st == 0) state[x] += dt * gg * G[x];
-                else state[x] += dt * (gg * G[x] + z * Gm[x]);
-            }
-            pisces_negatives(m, state, N, nthreads);
+            pisces_stage(m, state, u, v, t, dt, st, G, Gm, &w, nthreads);
             double* tmp = G; G = Gm; Gm = tmp;
         }
         t += dt;
     }
-    free(G); free(Gm); free(par4); free(xy2); free(omega); free(wpoc); free(wgoc); free(zc);
+    free(G); free(Gm);
+    pisces_work_free(&w);
+}
+
+void or_pisces_stage3d(const or_pisces3d* m, double* state, const double* u, const double* v, double t, double dt,
+                       int stage, double* G, const double* Gm, int start, int nthreads) {
+    pisces_work w;
+    pisces_work_init(m, &w);
+    if (start) pisces_negatives(m, state, (long)m->grid.Nx * m->grid.Ny * m->grid.Nz, nthreads);
+    pisces_stage(m, state, u, v, t, dt, stage, G, Gm, &w, nthreads);
+    pisces_work_free(&w);
 }
 

@@ -133,6 +133,7 @@ def lib():
         L.or_gas_exchange_flux.argtypes = [P(A.GasExchange), D, D, D, D, D, D, D]
         L.or_gas_exchange_flux.restype = D
         L.or_pisces_step3d.argtypes = [P(Pisces3D), P(D), VP, VP, D, D, C.c_int, C.c_int]
+        L.or_pisces_stage3d.argtypes = [P(Pisces3D), P(D), VP, VP, D, D, C.c_int, P(D), P(D), C.c_int, C.c_int]
         L.or_pisces_update_state3d.argtypes = [P(Pisces3D), P(D), D, P(D), P(D), P(D), C.c_int]
         L.or_conserved_groups.argtypes = [P(A.NPDParams), C.c_int, P(I32), P(I32), P(I32), P(D)]
         L.or_scale_cell.argtypes = [P(D), C.c_long, C.c_int, P(I32), P(I32), P(D), D]
@@ -532,6 +533,17 @@ def pisces_step3d(m, state, u=None, v=None, t=0.0, dt=1.0, nsteps=1, threads=Non
     """state: float64 (26, Nz, Ny, Nx), stepped in place."""
     assert state.dtype == np.float64 and state.flags.c_contiguous
     lib().or_pisces_step3d(C.byref(m), _dp(state), _opt(u), _opt(v), t, dt, nsteps, threads or nthreads())
+    return state
+
+
+def pisces_stage3d(m, state, G, Gm, u=None, v=None, t=0.0, dt=1.0, stage=0, start=False, threads=None):
+    """One RK3 stage in place (or_pisces_stage3d): G receives the stage's tendency, Gm holds the
+    previous stage's; swap them before the next stage.  start: the modifier first, as
+    pisces_step3d applies it on entry."""
+    for a in (state, G, Gm):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    lib().or_pisces_stage3d(C.byref(m), _dp(state), _opt(u), _opt(v), t, dt, stage, _dp(G), _dp(Gm), int(bool(start)),
+                            threads or nthreads())
     return state
 
 

@@ -107,3 +107,69 @@ def test_single_rank_exchange_wraps_onto_itself():
     d.exchange(torch.from_numpy(ss), torch.from_numpy(sn), rs, rn)
     unpack_rows(st, d, rs.numpy(), rn.numpy())
     assert np.array_equal(st, np.stack([d.scatter(field[0])]))
+
+
+PISCES_SHAPE, PISCES_STEPS, PISCES_DT = (16, 12, 10), 2, 600.0
+
+
+def pisces_case(grid_shape=PISCES_SHAPE):
+    import obgc
+    g = obgc.RectilinearGrid(grid_shape, (16000.0, 12000.0, 500.0), ("Periodic", "Periodic", "Bounded"))
+    bgc = obgc.PISCES(g)
+    light = obgc.MultiBandPhotosyntheticallyActiveRadiation(grid=g, surface_PAR=100.0)
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=4, device="cpu", dtype=torch.float64)
+    init = obgc.pisces_initial_conditions(g, seed=6)
+    from obgc import _abi as A
+    state0 = np.ascontiguousarray(np.stack([np.broadcast_to(init[n], g.shape) for n in A.PISCES_ASCII]).astype(np.float64))
+    return g, bgc, light, u.numpy(), v.numpy(), state0
+
+
+def pisces_oracle_model(bgc, grid, light):
+    import oracle as O
+    from obgc import _abi as A
+    return O.pisces3d(bgc.params, grid.c_grid(), light, -60.0, surface_kind=A.SURFACE_CONSTANT, surface_value=100.0)
+
+
+def pisces_rank_main(rank, world, port, out_path):
+    import oracle as O
+    import obgc
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        g, bgc, light, u, v, state0 = pisces_case()
+        d = obgc.SlabDecomposition(g, rank, world)
+        m = pisces_oracle_model(bgc, d.slab_grid, light)
+        st = np.ascontiguousarray(np.stack([d.scatter(state0[q]) for q in range(state0.shape[0])]))
+        us = np.ascontiguousarray(d.scatter(u).ravel())
+        vs = np.ascontiguousarray(d.scatter(v).ravel())
+        G, Gm = np.zeros_like(st), np.zeros_like(st)
+        rs = torch.empty(d.buffer_shape(st.shape[0]), dtype=torch.float64)
+        rn = torch.empty_like(rs)
+        for n in range(PISCES_STEPS):
+            for stage in range(3):
+                ss, sn = pack_rows(st, d)
+                d.exchange(torch.from_numpy(ss), torch.from_numpy(sn), rs, rn)
+                unpack_rows(st, d, rs.numpy(), rn.numpy())
+                O.pisces_stage3d(m, st, G, Gm, u=us, v=vs, t=n * PISCES_DT, dt=PISCES_DT, stage=stage,
+                                 start=(n == 0 and stage == 0), threads=1)
+                G, Gm = Gm, G
+        own = torch.from_numpy(np.ascontiguousarray(st[:, :, d.own(), :]))
+        parts = [torch.empty_like(own) for _ in range(world)] if rank == 0 else None
+        dist.gather(own, parts, dst=0)
+        if rank == 0:
+            slabbed = torch.cat(parts, dim=2).numpy()
+            ref = state0.copy()
+            O.pisces_step3d(pisces_oracle_model(bgc, g, light), ref, u=u.ravel().copy(), v=v.ravel().copy(), t=0.0,
+                            dt=PISCES_DT, nsteps=PISCES_STEPS, threads=1)
+            np.savez(out_path, slabbed=slabbed, ref=ref)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_pisces_slabbed_oracle_with_exchanged_halos_equals_single_domain():
+    # configuration 4's model: two gloo ranks, each stepping its slab with the oracle's PISCES stage
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "result.npz")
+        mp.start_processes(pisces_rank_main, args=(2, free_port(), out), nprocs=2, start_method="spawn")
+        r = np.load(out)
+        assert r["slabbed"].shape == r["ref"].shape
+        assert np.array_equal(r["slabbed"], r["ref"])
