@@ -23,7 +23,7 @@ from .model3d import (Clock, ExplicitTimeDiscretization, HorizontalScalarDiffusi
                       compute_tendencies, set_, time_step, update_biogeochemical_state)
 from .negatives import ScaleNegativeTracers, ZeroNegativeTracers
 from .sediments import InstantRemineralisationSediment, SimpleMultiGSediment
-from .distributed import PiscesSlabModel, SlabDecomposition, SlabModel
+from .distributed import PiscesSlabModel, SlabDecomposition, SlabModel, gather_runs, shard_runs
 from .models import (LOBSTER, NPZD, CarbonateSystem, Detritus, NitrateAmmonia, NitrateAmmoniaIron, Nutrient,
                      NutrientsPlanktonDetritus, Oxygen, PhytoZoo, TwoParticleAndDissolved, VariableRedfieldDetritus,
                      biogeochemical_drift_velocity, conserved_tracers, eval_point, preset,

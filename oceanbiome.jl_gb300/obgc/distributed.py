@@ -255,3 +255,35 @@ class PiscesSlabModel:
         import torch
         src = self.cur if self.cur is not None else self.fields
         return torch.stack([f[:, self.decomposition.own(), :] for f in src])
+
+
+def shard_runs(costs, world):
+    """Independent runs (columns, service requests, box models) shared out over `world` ranks: the
+    largest cost first, each to the least-loaded rank so far (ties to the lower rank), so that the
+    ranks' work is balanced and the assignment is the same on every rank.  costs: one number per run
+    (e.g. levels x steps).  Returns, per rank, the sorted indices of its runs."""
+    order = sorted(range(len(costs)), key=lambda q: (-float(costs[q]), q))
+    load = [0.0] * world
+    out = [[] for _ in range(world)]
+    for q in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        out[r].append(q)
+        load[r] += float(costs[q])
+    return [sorted(x) for x in out]
+
+
+def gather_runs(local_results, shards, group=None):
+    """Rank 0 receives every rank's results (a list in the order of that rank's shard) and returns
+    them in the runs' global order; other ranks return None.  One rank: the results as they are."""
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size(group) == 1:
+        return list(local_results)
+    parts = [None] * dist.get_world_size(group) if dist.get_rank(group) == 0 else None
+    dist.gather_object(list(local_results), parts, dst=0, group=group)
+    if parts is None:
+        return None
+    out = [None] * sum(len(s) for s in shards)
+    for shard, res in zip(shards, parts):
+        for q, x in zip(shard, res):
+            out[q] = x
+    return out
