@@ -590,13 +590,17 @@ int obgc_halo_unpack(const obgc_grid* slab, int32_t dtype, int32_t n_fields, voi
 int obgc_last_step_timing(const obgc_ctx* ctx, double* total_ms, double* substep_ms,
                           int64_t* launches);
 /* How the fused substep stages its tiles.  mode 1 (the default): with the tensor-memory
- * accelerator when the steps qualify (FP32 state, no passive tracers, no model w, and none of the
- * optional terms: closure, gas exchange, forcing, fused modifier, sediment, replicates); a call
- * then copies the bound arrays into a padded context copy with their periodic images, runs its
- * stages through two padded copies and writes the bound arrays in its last stage, every stage
- * copying each tracer's tile of a level with one tensor copy (no copy when no tile needs the
- * periodic wrap: the first stage reads the bound arrays through tensor maps).  mode 0: per-element
- * cp.async staging always.  obgc_get_staging reports whether the context has the padded copies and tensor
+ * accelerator when the steps qualify (FP32 arithmetic: OBGC_PREC_F32 or OBGC_PREC_MIXED; no
+ * passive tracers, no model w, and none of the optional terms: closure, gas exchange, forcing,
+ * fused modifier, sediment, replicates); a call then copies the bound arrays into a padded context
+ * copy with their periodic images, runs its stages through two padded copies and writes the bound
+ * arrays in its last stage, every stage copying each tracer's tile of a level with one tensor copy
+ * (no copy when no tile needs the periodic wrap: the first stage reads the bound arrays through
+ * tensor maps).  OBGC_PREC_MIXED: the padded copies hold the FP64 state rounded to FP32 (the copy
+ * rounds it, every stage but the last writes the next one) and every stage updates the FP64 bound
+ * arrays in place; a model with a sinking tracer outside the two flux pre-pass slots, or with
+ * segments whose chlorophyll sums the pre-pass does not form (obgc_set_tiling(1)), keeps cp.async.
+ * mode 0: per-element cp.async staging always.  obgc_get_staging reports whether the context has the padded copies and tensor
  * maps (available) and whether the last obgc_step / obgc_step_graph capture used them. */
 int obgc_set_staging(obgc_ctx* ctx, int32_t mode);
 int obgc_get_staging(const obgc_ctx* ctx, int32_t* available, int32_t* last_used);

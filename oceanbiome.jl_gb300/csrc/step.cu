@@ -179,12 +179,15 @@ __global__ void copy_interior_kernel(const TS* __restrict__ src, TS* __restrict_
 // tile with tensor copies.  One thread per padded cell and level, every slot; halo cells of a
 // Bounded direction and the row tails past Nx + 2 TMA_HX are left as they are (no stencil reads
 // them).
+template <typename TS>
 struct PadCopyArgs {
-    const float* src[MAX_NT];
+    const TS* src[MAX_NT];
     float* dst[MAX_NT];           // the padded arrays' first cell (x = -TMA_HX, y = -HALO)
     int nt;
 };
-__global__ void pad_copy_kernel(PadCopyArgs p, int Nx, int Ny, int Nz, int64_t sj, int64_t sk, int64_t psj, int64_t psk,
+// FP64 state (the mixed path) is rounded to FP32 on the way, as the cp.async staging rounds it
+template <typename TS>
+__global__ void pad_copy_kernel(PadCopyArgs<TS> p, int Nx, int Ny, int Nz, int64_t sj, int64_t sk, int64_t psj, int64_t psk,
                                 int periodic_x, int periodic_y) {
     const int PW = Nx + 2 * TMA_HX, PH = Ny + 2 * HALO;
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -200,7 +203,7 @@ __global__ void pad_copy_kernel(PadCopyArgs p, int Nx, int Ny, int Nz, int64_t s
         y = y < 0 ? y + Ny : y - Ny;
     }
     const int64_t s = x + (int64_t)y * sj + (int64_t)k * sk, d = px + (int64_t)py * psj + (int64_t)k * psk;
-    for (int t = 0; t < p.nt; t++) p.dst[t][d] = __ldg(p.src[t] + s);
+    for (int t = 0; t < p.nt; t++) p.dst[t][d] = float(__ldg(p.src[t] + s));
 }
 
 // Neumaier-compensated FP64 accumulation (sum, compensation).
@@ -526,9 +529,9 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
         cudaError_t e = cudaMalloc(p, bytes);
         if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc");
     };
-    // FP32 without passive tracers can stage tiles with the tensor-memory accelerator: the tendency
-    // arrays then use the padded layout
-    const bool tma_capable = c->prec == OBGC_PREC_F32 && c->NP == 0;
+    // FP32 and mixed without passive tracers can stage tiles with the tensor-memory accelerator (from
+    // FP32 padded copies of the state): the tendency arrays then use the padded layout
+    const bool tma_capable = (c->prec == OBGC_PREC_F32 || c->prec == OBGC_PREC_MIXED) && c->NP == 0;
     if (tma_capable) {
         c->pad_sj = ((int64_t)g.Nx + 2 * TMA_HX + 3) / 4 * 4;
         c->pad_sk = c->pad_sj * (g.Ny + 2 * HALO);
@@ -622,7 +625,7 @@ extern "C" int obgc_bind_fields(obgc_ctx* c, const obgc_fields* f) {
     // tensor maps of the bound arrays (the TMA-staged steps' first stage), when their layout allows
     // them: 16-byte aligned origins and row / level strides
     c->umaps_ok = false;
-    if (c->tma_ready && c->tma_encode) {
+    if (c->tma_ready && c->tma_encode && c->prec == OBGC_PREC_F32) {
         const obgc_grid& g = c->desc.grid;
         bool ok = (g.stride_j * 4) % 16 == 0 && (g.stride_k * 4) % 16 == 0;
         for (int t = 0; t < c->NT && ok; t++) ok = reinterpret_cast<uintptr_t>(c->user[t]) % 16 == 0;
@@ -1236,13 +1239,20 @@ static int enqueue_stage(obgc_ctx* c, StepPlan<TS, TC>& p, int stg, void* const*
     return OBGC_OK;
 }
 
-// Whether the steps can stage tiles with the tensor-memory accelerator: FP32, the lean kernel (no
-// closure, surface flux, forcing, fused modifier, sediment or replicate outputs), no passive
-// tracers, no model w, no implicit vertical solve, and at least 8 cells in a periodic x and 6 in a
-// periodic y.
+// Whether the steps can stage tiles with the tensor-memory accelerator: FP32 arithmetic (FP32 or
+// mixed), the lean kernel (no closure, surface flux, forcing, fused modifier, sediment or replicate
+// outputs), no passive tracers, no model w, no implicit vertical solve, and at least 8 cells in a
+// periodic x and 6 in a periodic y.  The mixed path updates its FP64 state in place, so its stages
+// must read no other cell of it: no sinking tracer outside the two flux pre-pass slots, and the
+// chlorophyll sums from the pre-pass (or a single segment per column).
 template <typename TS, typename TC>
 static bool tma_eligible(obgc_ctx* c, const StepPlan<TS, TC>& p) {
-    if (sizeof(TS) != 4 || sizeof(TC) != 4 || !c->tma_ready || c->staging != 1 || c->NP != 0 || p.impl || p.a.w) return false;
+    if (sizeof(TC) != 4 || !c->tma_ready || c->staging != 1 || c->NP != 0 || p.impl || p.a.w) return false;
+    if (sizeof(TS) != sizeof(TC)) {
+        const uint32_t slots = (1u << window_a(c->V)) | (1u << window_b(c->V));
+        if ((p.a.drift_mask & ~slots) != 0u) return false;
+        if (p.a.nseg > 1 && (!c->par_prefix || c->V == V_EXTERNAL || p.a.nseg - 1 > c->par_prefix_segs)) return false;
+    }
     // a cell writes one periodic image per direction into the padded halos: a periodic direction needs
     // at least two halos' width of cells (8 in x, 6 in y)
     if ((p.a.periodic_x && p.a.Nx < 2 * TMA_HX) || (p.a.periodic_y && p.a.Ny < 2 * HALO)) return false;
@@ -1257,6 +1267,8 @@ static bool tma_eligible(obgc_ctx* c, const StepPlan<TS, TC>& p) {
 // arrays: every stage but the last writes a padded set together with its periodic halo images, and
 // only the last writes the caller's arrays.  When no tile needs the periodic wrap (and the caller's
 // arrays have tensor maps) there is no copy: the first stage copies its tiles from them directly.
+// Mixed precision: the FP64 bound arrays are updated in place by every stage, and the padded sets
+// hold their FP32 rounding (the copy rounds them, each stage but the last writes the next set).
 template <typename TS, typename TC>
 static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int nsteps, cudaStream_t st, bool profile) {
     SubstepArgs<TS, TC>& a = p.a;
@@ -1268,21 +1280,22 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
     const bool clock = needs_clock(c);
     size_t ev = 0;
     const int last = 3 * nsteps - 1;
-    bool none_wrap = c->umaps_ok;
+    constexpr bool mixed = sizeof(TS) != sizeof(TC);
+    bool none_wrap = !mixed && c->umaps_ok;
     for (int tj = 0; tj < a.nty && none_wrap; tj++)
         for (int ti = 0; ti < a.ntx && none_wrap; ti++) none_wrap = !tile_wraps(a, ti * STEP_BX, tj * STEP_BY);
     const bool copy_first = !none_wrap;
     c->copied_first = copy_first;
     if (copy_first) {
-        PadCopyArgs pc;
+        PadCopyArgs<TS> pc;
         std::memset(&pc, 0, sizeof(pc));
         pc.nt = c->NT;
         for (int t = 0; t < c->NT; t++) {
-            pc.src[t] = (const float*)c->user[t];
+            pc.src[t] = (const TS*)c->user[t];
             pc.dst[t] = (float*)c->pad[1][t];
         }
         const int64_t n = (int64_t)(g.Nx + 2 * TMA_HX) * (g.Ny + 2 * HALO) * g.Nz;
-        pad_copy_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pc, g.Nx, g.Ny, g.Nz, g.stride_j, g.stride_k, c->pad_sj,
+        pad_copy_kernel<TS><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pc, g.Nx, g.Ny, g.Nz, g.stride_j, g.stride_k, c->pad_sj,
                                                                      c->pad_sk, a.periodic_x, a.periodic_y);
         OBGC_LAUNCHED("pad_copy_kernel");
     }
@@ -1296,14 +1309,26 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
             a.c_stage = rk3_c(stg);
             const bool from_user = q == 0 && !copy_first;   // this stage reads the caller's arrays
             const int pin = q == 0 ? 1 : (q - 1) % 2;       // else the padded set it reads
-            for (int t = 0; t < c->NT; t++) {
-                a.in[t] = from_user ? (const TS*)c->user[t] : (const TS*)c->pad[pin][t] + org;
-                a.out[t] = q == last ? (TS*)c->user[t] : (TS*)c->pad[q % 2][t] + org;
+            if constexpr (mixed) {
+                for (int t = 0; t < c->NT; t++) {
+                    a.in[t] = (const TS*)c->user[t];
+                    a.out[t] = (TS*)c->user[t];
+                    a.pout[t] = q == last ? nullptr : (TC*)c->pad[q % 2][t] + org;
+                }
+                a.sj = a.osj = g.stride_j;
+                a.sk = a.osk = g.stride_k;
+                a.psj = c->pad_sj;
+                a.psk = c->pad_sk;
+            } else {
+                for (int t = 0; t < c->NT; t++) {
+                    a.in[t] = from_user ? (const TS*)c->user[t] : (const TS*)c->pad[pin][t] + org;
+                    a.out[t] = q == last ? (TS*)c->user[t] : (TS*)c->pad[q % 2][t] + org;
+                }
+                a.sj = from_user ? g.stride_j : c->pad_sj;
+                a.sk = from_user ? g.stride_k : c->pad_sk;
+                a.osj = q == last ? g.stride_j : c->pad_sj;
+                a.osk = q == last ? g.stride_k : c->pad_sk;
             }
-            a.sj = from_user ? g.stride_j : c->pad_sj;
-            a.sk = from_user ? g.stride_k : c->pad_sk;
-            a.osj = q == last ? g.stride_j : c->pad_sj;
-            a.osk = q == last ? g.stride_k : c->pad_sk;
             a.out_halo = q != last;
             a.tma_layout = 2;
             a.tmap = from_user ? c->d_tmaps + 2 * MAX_NT : c->d_tmaps + (size_t)pin * MAX_NT;

@@ -58,6 +58,11 @@ struct SubstepArgs {
     int64_t vsj, vsk;         // layout of u and v
     int64_t osj, osk;         // layout of the output arrays out[]
     int64_t gsj, gsk;         // layout of the tendency arrays G[] (and ext, bgc_out, frc)
+    // TMA-staged stages of the mixed path (FP64 state in out[], updated in place): pout[t] is the
+    // padded FP32 copy of the stage's new state, with its periodic images in the halos when out_halo,
+    // from which the next stage copies its tiles (NULL: none, the call's last stage); layout psj, psk
+    TC* pout[MAX_NT];
+    int64_t psj, psk;
     // out[] are padded arrays (x halo of TMA_HX, y halo of HALO cells): the update also writes each
     // value into the halo cells that hold its periodic image, so the next stage can stage whole
     // tiles of it with the tensor-memory accelerator
@@ -351,12 +356,16 @@ __host__ __device__ inline bool substep_needs_ext(const SubstepArgs<TS, TC>& a) 
 // instantiation: input, output and tendency arrays in their own layouts (a.sj/sk, osj/osk, gsj/gsk;
 // u and v in vsj/vsk), 40-wide tile rows, every tile copied by tensor copies through a.tmap (from a
 // padded set, or from the caller's arrays when none of their tiles needs the periodic wrap), and
-// periodic halo images written when a.out_halo is set.
+// periodic halo images written when a.out_halo is set (mixed precision: out[] is the FP64 state,
+// updated in place, and the FP32 padded copy pout[] takes the images).
 template <int V, int NT, typename TS, typename TC, bool EXT, int MODE = 0>
 __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <= 12 ? 3 : NT <= 16 ? 2 : 1)
     substep_kernel(const __grid_constant__ SubstepArgs<TS, TC> a) {
     constexpr bool SPLIT = MODE != 0;
     constexpr bool TMA = MODE == 2;
+    // mixed precision with TMA-staged tiles: the FP64 state is updated in place (a thread reads and
+    // writes only its own cells of it) and the tiles come from the FP32 padded copies (pout)
+    constexpr bool MIX2 = TMA && sizeof(TS) != sizeof(TC);
     constexpr int TILE_W = tile_w<SPLIT>();
     constexpr int TILE_X0 = tile_x0<SPLIT>();
     constexpr int NB = n_bgc(V);
@@ -842,7 +851,8 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             int img_x = 0, img_y = 0;
             if (SPLIT && a.out_halo) {
                 if (periodic_x) img_x = i < TMA_HX ? a.Nx : (i >= a.Nx - TMA_HX ? -a.Nx : 0);
-                if (periodic_y) img_y = j < HALO ? a.Ny * (int)a.osj : (j >= a.Ny - HALO ? -a.Ny * (int)a.osj : 0);
+                const int ysj = (int)(MIX2 ? a.psj : a.osj);
+                if (periodic_y) img_y = j < HALO ? a.Ny * ysj : (j >= a.Ny - HALO ? -a.Ny * ysj : 0);
             }
 #pragma unroll
             for (int t = 0; t < NT; t++) {
@@ -886,11 +896,20 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     // accumulate in the storage precision (FP64 for the mixed path)
                     TS Uo;
                     if constexpr (sizeof(TS) == sizeof(TC)) Uo = c[t] + Un;
+                    else if constexpr (MIX2) Uo = a.in[t][idx] + TS(Un);   // in place: a plain load
                     else Uo = TS(__ldg(a.in[t] + idx)) + TS(Un);
                     a.out[t][oidx] = Uo;
                     if constexpr (sizeof(TS) == 4) nanacc = fmaf(Uo, 0.f, nanacc);
                     else bad |= !(fabs(Uo) <= TS(INFINITY));
-                    if (SPLIT) {
+                    if constexpr (MIX2) {
+                        if (a.pout[t]) {
+                            const int64_t pidx = ic + (int64_t)jc * a.psj + (int64_t)k * a.psk;
+                            const TC Up = TC(Uo);   // the rounding the cp.async staging applies
+                            a.pout[t][pidx] = Up;
+                            if (img_x) a.pout[t][pidx + img_x] = Up;
+                            if (img_y) a.pout[t][pidx + img_y] = Up;
+                        }
+                    } else if (SPLIT) {
                         if (img_x) a.out[t][oidx + img_x] = Uo;
                         if (img_y) a.out[t][oidx + img_y] = Uo;
                     }

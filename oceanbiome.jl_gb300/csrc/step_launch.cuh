@@ -32,7 +32,7 @@ int launch_one(const SubstepArgs<TS, TC>& a, int blocks, cudaStream_t st) {
         bool done = false;
         if (a.tma_layout && (a.drift_mask & ((1u << window_a(V)) | (1u << window_b(V)))) && !a.fz_pre)
             return fail(OBGC_ERR_UNSUPPORTED, "substep: TMA staging needs the sinking fluxes of sink_flux_kernel");
-        if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) {
+        if constexpr (sizeof(TC) == 4) {   // FP32 and mixed
             if (a.tma_layout) {
                 const int rc = ensure_configured<V, NT, TS, TC, false, 2>();
                 if (rc != OBGC_OK) return rc;
@@ -41,7 +41,7 @@ int launch_one(const SubstepArgs<TS, TC>& a, int blocks, cudaStream_t st) {
             }
         }
         if (!done) {
-            if (a.tma_layout) return fail(OBGC_ERR_UNSUPPORTED, "substep: TMA staging needs FP32 state");
+            if (a.tma_layout) return fail(OBGC_ERR_UNSUPPORTED, "substep: TMA staging needs FP32 arithmetic");
             const int rc = ensure_configured<V, NT, TS, TC, false>();
             if (rc != OBGC_OK) return rc;
             substep_kernel<V, NT, TS, TC, false><<<blocks, block, substep_smem_bytes<TC, NT>(), st>>>(a);
@@ -66,7 +66,7 @@ int occupancy_one(int* blocks_per_sm) {
                                                       STEP_BX * STEP_BY, substep_smem_bytes<TC, NT>());
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     if (*blocks_per_sm > lean) *blocks_per_sm = lean;
-    if constexpr (sizeof(TS) == 4 && sizeof(TC) == 4) {
+    if constexpr (sizeof(TC) == 4) {
         rc = ensure_configured<V, NT, TS, TC, false, 2>();
         if (rc != OBGC_OK) return rc;
         int m2 = 0;

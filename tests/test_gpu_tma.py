@@ -6,7 +6,9 @@ the first stage copies its tiles from the bound arrays directly.  The arithmetic
 same as with cp.async staging, so the two agree bit for bit, on grids whose sizes are not multiples
 of the 32 x 8 tile (tiles hang over the padded arrays' edges), with walls as well as periodic
 directions, and with a row pitch that allows no tensor map of the bound arrays; and both agree with
-the oracle."""
+the oracle.  The mixed path (FP64 state, FP32 arithmetic) stages its tiles the same way from FP32
+padded copies (the copy rounds the state, each stage but the last writes the next copy) and
+updates its FP64 state in place; it equals its own cp.async staging bit for bit too."""
 import numpy as np
 import pytest
 
@@ -17,14 +19,17 @@ from gpuhelp import cuda, rel_err
 pytestmark = pytest.mark.gpu
 
 
-def run(shape, topology, staging, nsteps=3, graph=False, seed=2):
+def run(shape, topology, staging, nsteps=3, graph=False, seed=2, precision="f32", tiling=None):
     torch = cuda()
     L = (shape[0] * 195.3125, shape[1] * 195.3125, shape[2] * 7.8125)
-    g = obgc.RectilinearGrid(shape, L, topology, dtype="f32")
+    f32 = precision == "f32"
+    g = obgc.RectilinearGrid(shape, L, topology, dtype="f32" if f32 else "f64")
     bgc = obgc.LOBSTER(g, carbonate_system=obgc.CarbonateSystem())
-    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=seed, dtype=torch.float32)
-    m = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None), precision="f32")
+    u, v, _ = obgc.random_streamfunction_velocity(g, rms=0.1, seed=seed, dtype=torch.float32 if f32 else torch.float64)
+    m = obgc.NonhydrostaticModel(g, biogeochemistry=bgc, tracers=("T", "S"), velocities=(u, v, None), precision=precision)
     m.set_staging(staging)
+    if tiling is not None:
+        m.set_tiling(tiling)
     obgc.set_(m, **obgc.lobster_initial_conditions(g, seed=seed + 1))
     s0 = m.state_array().double().cpu().numpy()
     obgc.time_step(m, 300.0, nsteps=nsteps, graph=graph)
@@ -88,9 +93,11 @@ def test_configurations_outside_the_lean_kernel_keep_cp_async():
     assert m.staging() == (True, False)          # the fused modifier needs the extended kernel
     g64 = obgc.RectilinearGrid((32, 16, 8), (6250.0, 3125.0, 62.5))
     u64, v64, _ = obgc.random_streamfunction_velocity(g64, rms=0.1, seed=1)
-    mixed = obgc.NonhydrostaticModel(g64, biogeochemistry=obgc.LOBSTER(g64, carbonate_system=obgc.CarbonateSystem()),
-                                     tracers=("T", "S"), velocities=(u64, v64, None), precision="mixed")
-    assert mixed.staging() == (False, False)     # the padded copies exist for FP32 state only
+    for prec in ("mixed", "f64"):
+        mx = obgc.NonhydrostaticModel(g64, biogeochemistry=obgc.LOBSTER(g64, carbonate_system=obgc.CarbonateSystem()),
+                                      tracers=("T", "S"), velocities=(u64, v64, None), precision=prec)
+        # the padded FP32 copies exist for FP32 arithmetic only
+        assert mx.staging() == ((True, False) if prec == "mixed" else (False, False))
 
 
 def test_padded_copy_and_stages_in_a_graph():
@@ -134,3 +141,53 @@ def test_ensemble_members_through_host_copies_equal_eager_steps():
     for m, host in members:
         got = np.stack([host[n].double().numpy() for n in m.tracer_names])
         assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("shape,topology", [
+    ((40, 20, 12), ("Periodic", "Periodic", "Bounded")),
+    ((96, 32, 8), ("Periodic", "Periodic", "Bounded")),
+    ((36, 24, 8), ("Bounded", "Periodic", "Bounded")),
+    ((64, 32, 8), ("Bounded", "Bounded", "Bounded")),       # no tile wraps: still the rounding copy
+])
+def test_mixed_tma_staging_equals_cp_async_staging(shape, topology):
+    _, _, _, m1, _, tma = run(shape, topology, staging=1, precision="mixed")
+    assert m1.staging() == (True, True)
+    _, _, _, m0, _, ref = run(shape, topology, staging=0, precision="mixed")
+    assert m0.staging() == (True, False)
+    assert np.array_equal(tma, ref), max(rel_err(tma[q], ref[q]) for q in range(tma.shape[0]))
+    assert m1.step_status() == (0, 0)
+
+
+def test_mixed_tma_staging_matches_oracle_graph_and_one_step_calls():
+    shape, topo = (48, 24, 16), ("Periodic", "Periodic", "Bounded")
+    g, bgc, (u, v), m, s0, got = run(shape, topo, staging=1, nsteps=4, precision="mixed")
+    mo = O.model3d(bgc.params, g.c_grid(), m.tracer_names)
+    ref = np.ascontiguousarray(s0.copy())
+    O.step3d(mo, ref, u=u.double().cpu().numpy().ravel().copy(), v=v.double().cpu().numpy().ravel().copy(),
+             t=0.0, dt=300.0, nsteps=4)
+    assert max(rel_err(got[q], ref[q]) for q in range(got.shape[0])) < 1e-5
+    _, _, _, mg, _, gg = run(shape, topo, staging=1, nsteps=4, graph=True, precision="mixed")
+    assert mg.staging() == (True, True)
+    assert np.array_equal(gg, got)
+    # four one-step calls (each with its rounding copy) equal one four-step call
+    torch = cuda()
+    L = (shape[0] * 195.3125, shape[1] * 195.3125, shape[2] * 7.8125)
+    g2 = obgc.RectilinearGrid(shape, L, topo, dtype="f64")
+    u2, v2, _ = obgc.random_streamfunction_velocity(g2, rms=0.1, seed=2, dtype=torch.float64)
+    m2 = obgc.NonhydrostaticModel(g2, biogeochemistry=obgc.LOBSTER(g2, carbonate_system=obgc.CarbonateSystem()),
+                                  tracers=("T", "S"), velocities=(u2, v2, None), precision="mixed")
+    m2.set_staging(1)
+    obgc.set_(m2, **obgc.lobster_initial_conditions(g2, seed=3))
+    for _ in range(4):
+        obgc.time_step(m2, 300.0, nsteps=1)
+    assert np.array_equal(m2.state_array().double().cpu().numpy(), got)
+
+
+def test_mixed_stages_that_would_read_other_cells_keep_cp_async():
+    # one-level segments sum the chlorophyll above each segment in the work items, from other cells of
+    # the state that the in-place FP64 update may already have overwritten: cp.async staging
+    shape, topo = (40, 20, 12), ("Periodic", "Periodic", "Bounded")
+    _, _, _, m1, _, got = run(shape, topo, staging=1, precision="mixed", tiling=1)
+    assert m1.staging() == (True, False)
+    _, _, _, _, _, ref = run(shape, topo, staging=1, precision="mixed", tiling=4)
+    assert np.array_equal(got, ref)
