@@ -142,6 +142,9 @@ struct SubstepArgs {
 
 template <typename TS, typename TC>
 __device__ __forceinline__ TC ld(const TS* p, int64_t i) { return TC(__ldg(p + i)); }
+// The exponent field of an FP64 value in place (bits 20-30 of its high word): 0x7ff00000 for a NaN
+// or an infinity.
+__device__ __forceinline__ unsigned d_exponent_bits(double x) { return (unsigned)__double2hiint(x) & 0x7ff00000u; }
 
 // Asynchronous global -> shared copy of one 4- or 8-byte element (cp.async, sm_80+): no register
 // staging; completed by cp_async_wait_all() before the barrier that publishes the shared data.
@@ -155,6 +158,9 @@ __device__ __forceinline__ void cp_async_elem(E* smem, const E* gmem) {
 // The same with the shared-space address given directly (constant offsets fold into the instruction).
 __device__ __forceinline__ void cp_async4_at(unsigned smem_addr, const void* gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void prefetch_l2(const void* gmem) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(gmem));
 }
 __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
@@ -459,6 +465,9 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     // FP32: NaN-or-infinity detector on the FMA pipe, fma(U, 0, acc) (0 for a finite U, NaN otherwise),
     // in place of a compare and a predicate OR per stored value on the busier ALU pipe
     TS nanacc = TS(0);
+    // FP64: the largest exponent field stored, on the integer pipe (all ones: a NaN or an infinity)
+    // in place of an FP64 compare per value on GB300's narrow FP64 pipe
+    unsigned expmax = 0u;
     for (int item = blockIdx.x; item < a.n_items; item += gridDim.x) {
         const int seg = item % a.nseg;                       // top segment first
         const int tile = item / a.nseg;
@@ -559,6 +568,11 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
 #pragma unroll 1
                 for (int t = 0; t < NT; t++)
                     if (gm_smem) cp_async_elem<TC>(vdv + t * NTH + tid, a.G[t] + gidx);
+                // mixed: this cell's FP64 values, read again by the update, into L2 meanwhile
+                if constexpr (MIX2) {
+#pragma unroll 1
+                    for (int t = 0; t < NT; t++) prefetch_l2(a.in[t] + idx);
+                }
                 unsigned polls = 0;
                 if (!tma_timeout)
                     while (!mbar_try_wait(&stage_bar, tma_phase & 1u))
@@ -900,7 +914,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
                     else Uo = TS(__ldg(a.in[t] + idx)) + TS(Un);
                     a.out[t][oidx] = Uo;
                     if constexpr (sizeof(TS) == 4) nanacc = fmaf(Uo, 0.f, nanacc);
-                    else bad |= !(fabs(Uo) <= TS(INFINITY));
+                    else expmax = max(expmax, d_exponent_bits(Uo));
                     if constexpr (MIX2) {
                         if (a.pout[t]) {
                             const int64_t pidx = ic + (int64_t)jc * a.psj + (int64_t)k * a.psk;
@@ -927,7 +941,7 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
             }
         }
     }
-    bad |= !(nanacc == TS(0));
+    bad |= !(nanacc == TS(0)) || expmax == 0x7ff00000u;
     if (bad && a.status) atomicOr(a.status, OBGC_FLAG_NAN);
     if (tma_timeout && a.status) atomicOr(a.status, OBGC_FLAG_TIMEOUT);
 }
