@@ -61,7 +61,7 @@ CARBON_FLOP_PER_CELL = 1671.0
 OMEGA_FLOP_PER_CELL = 1529.0
 
 
-def e2e_members_ms(members, nsteps, stream, lanes=2):
+def e2e_members_ms(members, nsteps, stream, lanes=2, trials=1, info=None):
     """End-to-end steps of an ensemble through the public API, the way a host drives several model
     members on one GPU: member k % M takes step k, which copies that member's fields in from pinned
     host memory (copy-in streams), steps it on the launching stream and reads its result back
@@ -71,7 +71,10 @@ def e2e_members_ms(members, nsteps, stream, lanes=2):
     round of copies both ways comes first: on GB300 the first copies from freshly pinned buffers ran
     at about 90 GB/s, later ones at about 205 GB/s host to device and 189 GB/s back (156 GB/s each
     way when both directions run at once).  members: [(step, dev fields, pinned host fields)].  Returns ms per step (CUDA events on the launching stream, which joins every copy
-    stream before the end event)."""
+    stream before the end event): the median of `trials` timed runs of nsteps steps.  info (a dict,
+    optional) receives every trial's ms per step and the host link's rates in the untimed round
+    (GB/s, each direction alone), since the pipeline is bound by that link when the machine's other
+    work loads it."""
     import torch
     M = len(members)
     ins = [torch.cuda.Stream() for _ in range(lanes)]
@@ -79,10 +82,32 @@ def e2e_members_ms(members, nsteps, stream, lanes=2):
     copied = [[torch.cuda.Event() for _ in range(lanes)] for _ in range(M)]
     stepped = [torch.cuda.Event() for _ in range(M)]
     read = [[torch.cuda.Event() for _ in range(lanes)] for _ in range(M)]
-    for _, dev, host in members:                       # untimed: both directions once
-        for n in dev:
-            dev[n].copy_(host[n], non_blocking=True)
-            host[n].copy_(dev[n], non_blocking=True)
+    # untimed: both directions once, each direction timed alone
+    c0, c1, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    nbytes = sum(h.numel() * h.element_size() for _, _, host in members for h in host.values())
+    torch.cuda.synchronize()
+    c0.record(stream)
+    with torch.cuda.stream(stream):
+        for _, dev, host in members:
+            for n in dev:
+                dev[n].copy_(host[n], non_blocking=True)
+        c1.record(stream)
+        for _, dev, host in members:
+            for n in dev:
+                host[n].copy_(dev[n], non_blocking=True)
+        c2.record(stream)
+    torch.cuda.synchronize()
+    if info is not None:
+        info["host_link_gbs"] = {"h2d": nbytes / c0.elapsed_time(c1) / 1e6, "d2h": nbytes / c1.elapsed_time(c2) / 1e6}
+    runs = sorted(_e2e_trial(members, nsteps, stream, ins, outs, copied, stepped, read) for _ in range(trials))
+    if info is not None:
+        info["trials_ms_per_step"] = runs
+    return runs[len(runs) // 2]
+
+
+def _e2e_trial(members, nsteps, stream, ins, outs, copied, stepped, read):
+    import torch
+    M, lanes = len(members), len(ins)
     start = torch.cuda.Event()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -389,7 +414,8 @@ def run_gpu(args):
     barrier()
     e2e_steps = max(2 * E2E_MEMBERS, min(args.steps, 200))   # the value leg's K steps
     h2d = sum(h.numel() * h.element_size() for h in members[0][2].values())
-    e2e_ms = e2e_members_ms(members, e2e_steps, stream)
+    e2e_info = {}
+    e2e_ms = e2e_members_ms(members, e2e_steps, stream, trials=3, info=e2e_info)
     barrier()
     e2e_value = N_TRACERS * g.N * world / (e2e_ms / 1e3)
     del others, members
@@ -436,7 +462,9 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "ms_per_step": e2e_ms, "steps": e2e_steps,
                     "pipeline": f"{E2E_MEMBERS} ensemble members take the steps in turn: each step copies its member's "
-                                "state in from pinned host memory and back; a member's copies overlap the other members' steps"},
+                                "state in from pinned host memory and back; a member's copies overlap the other members' steps",
+                    "trials_ms_per_step": e2e_info.get("trials_ms_per_step"), "statistic": "median of 3 trials",
+                    "host_link_gbs": e2e_info.get("host_link_gbs")},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
