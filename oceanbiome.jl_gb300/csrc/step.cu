@@ -185,14 +185,29 @@ struct PadCopyArgs {
     float* dst[MAX_NT];           // the padded arrays' first cell (x = -TMA_HX, y = -HALO)
     int nt;
 };
-// FP64 state (the mixed path) is rounded to FP32 on the way, as the cp.async staging rounds it
+// Whether padded cell (px, py) lies in the box of a tile that needs the periodic wrap (tile (ti, tj)
+// copies padded x in [32 ti, 32 ti + 40) and y in [8 tj, 8 tj + 14)).
+__device__ inline bool in_wrapping_box(int px, int py, int Nx, int Ny, bool periodic_x, bool periodic_y) {
+    const int ntx = (Nx + STEP_BX - 1) / STEP_BX, nty = (Ny + STEP_BY - 1) / STEP_BY;
+    const int ti1 = min(px / STEP_BX, ntx - 1), tj1 = min(py / STEP_BY, nty - 1);
+    const int ti0 = px >= TMA_TILE_W ? (px - TMA_TILE_W) / STEP_BX + 1 : 0;
+    const int tj0 = py >= TILE_H ? (py - TILE_H) / STEP_BY + 1 : 0;
+    for (int tj = tj0; tj <= tj1; tj++)
+        for (int ti = ti0; ti <= ti1; ti++)
+            if (tile_wraps_xy(ti * STEP_BX, tj * STEP_BY, Nx, Ny, periodic_x, periodic_y)) return true;
+    return false;
+}
+// FP64 state (the mixed path) is rounded to FP32 on the way, as the cp.async staging rounds it.
+// bands: only the cells of the boxes of the tiles that need the wrap (the call's first stage copies
+// the other tiles from the caller's arrays).
 template <typename TS>
 __global__ void pad_copy_kernel(PadCopyArgs<TS> p, int Nx, int Ny, int Nz, int64_t sj, int64_t sk, int64_t psj, int64_t psk,
-                                int periodic_x, int periodic_y) {
+                                int periodic_x, int periodic_y, int bands) {
     const int PW = Nx + 2 * TMA_HX, PH = Ny + 2 * HALO;
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= (int64_t)PW * PH * Nz) return;
     const int px = (int)(c % PW), py = (int)((c / PW) % PH), k = (int)(c / ((int64_t)PW * PH));
+    if (bands && !in_wrapping_box(px, py, Nx, Ny, periodic_x, periodic_y)) return;
     int x = px - TMA_HX, y = py - HALO;
     if (x < 0 || x >= Nx) {
         if (!periodic_x) return;
@@ -372,6 +387,10 @@ struct obgc_ctx {
     cudaStream_t graph_stream = nullptr;
     // timing
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    // the TMA-staged stages' side stream: the chlorophyll-sum pre-pass runs there beside the
+    // sinking-flux pre-pass (both read the stage's input, each writes its own buffer)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::vector<cudaEvent_t> prof_events;
     bool profile = false;
     double last_total_ms = 0, last_substep_ms = 0;
@@ -413,6 +432,9 @@ static int ctx_free(obgc_ctx* c) {
     if (c->mg_flux) cudaFree(c->mg_flux);
     if (c->ev_begin) cudaEventDestroy(c->ev_begin);
     if (c->ev_end) cudaEventDestroy(c->ev_end);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) cudaStreamDestroy(c->side);
     for (auto e : c->prof_events) cudaEventDestroy(e);
     delete c;
     return OBGC_OK;
@@ -578,6 +600,11 @@ extern "C" int obgc_create(const obgc_model_desc* desc, obgc_ctx** out) {
     if (rc == OBGC_OK && (cudaEventCreate(&c->ev_begin) != cudaSuccess || cudaEventCreate(&c->ev_end) != cudaSuccess))
         rc = fail(OBGC_ERR_CUDA, "cudaEventCreate");
     if (rc == OBGC_OK && tma_capable) rc = setup_tma(c);
+    if (rc == OBGC_OK && tma_capable &&
+        (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess))
+        rc = fail(OBGC_ERR_CUDA, "cudaStreamCreate / cudaEventCreate (pre-pass side stream)");
     // persistent grid size
     if (rc == OBGC_OK) {
         const FusedEntry* fe = c->V >= 0 ? find_fused(c->prec, c->V, c->NT) : nullptr;
@@ -1239,6 +1266,27 @@ static int enqueue_stage(obgc_ctx* c, StepPlan<TS, TC>& p, int stg, void* const*
     return OBGC_OK;
 }
 
+// The two pre-passes of a TMA-staged stage: the chlorophyll sums on the context's side stream (forked
+// from and joined back into st by events, so it works eagerly and under stream capture) beside the
+// sinking fluxes on st.
+template <typename TS, typename TC>
+static int launch_pre_passes(obgc_ctx* c, SubstepArgs<TS, TC>& a, cudaStream_t st) {
+    if (!c->side) {
+        int rc = launch_par_prefix(c, a, st);
+        return rc == OBGC_OK ? launch_sink_flux(c, a, st) : rc;
+    }
+    OBGC_CUDA(cudaEventRecord(c->ev_fork, st));
+    OBGC_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+    int rc = launch_par_prefix(c, a, c->side);
+    const cudaError_t e = cudaEventRecord(c->ev_join, c->side);   // joined even when the launch failed
+    if (rc == OBGC_OK) rc = launch_sink_flux(c, a, st);
+    const cudaError_t w = cudaStreamWaitEvent(st, c->ev_join, 0);
+    if (rc != OBGC_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord(pre-pass join)");
+    if (w != cudaSuccess) return cuda_fail(w, "cudaStreamWaitEvent(pre-pass join)");
+    return OBGC_OK;
+}
+
 // Whether the steps can stage tiles with the tensor-memory accelerator: FP32 arithmetic (FP32 or
 // mixed), the lean kernel (no closure, surface flux, forcing, fused modifier, sediment or replicate
 // outputs), no passive tracers, no model w, no implicit vertical solve, and at least 8 cells in a
@@ -1285,6 +1333,9 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
     for (int tj = 0; tj < a.nty && none_wrap; tj++)
         for (int ti = 0; ti < a.ntx && none_wrap; ti++) none_wrap = !tile_wraps(a, ti * STEP_BX, tj * STEP_BY);
     const bool copy_first = !none_wrap;
+    // FP32 with tensor maps of the caller's arrays: only the wrapping tiles' boxes are copied, and the
+    // first stage copies the other tiles from the caller's arrays
+    const bool bands = copy_first && !mixed && c->umaps_ok;
     c->copied_first = copy_first;
     if (copy_first) {
         PadCopyArgs<TS> pc;
@@ -1296,7 +1347,7 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
         }
         const int64_t n = (int64_t)(g.Nx + 2 * TMA_HX) * (g.Ny + 2 * HALO) * g.Nz;
         pad_copy_kernel<TS><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pc, g.Nx, g.Ny, g.Nz, g.stride_j, g.stride_k, c->pad_sj,
-                                                                     c->pad_sk, a.periodic_x, a.periodic_y);
+                                                                     c->pad_sk, a.periodic_x, a.periodic_y, bands ? 1 : 0);
         OBGC_LAUNCHED("pad_copy_kernel");
     }
     for (int s = 0; s < nsteps; s++) {
@@ -1307,7 +1358,7 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
             a.gamma = TC(rk3_gamma(stg));
             a.zeta = TC(rk3_zeta(stg));
             a.c_stage = rk3_c(stg);
-            const bool from_user = q == 0 && !copy_first;   // this stage reads the caller's arrays
+            const bool from_user = q == 0 && (!copy_first || bands);   // this stage reads the caller's arrays
             const int pin = q == 0 ? 1 : (q - 1) % 2;       // else the padded set it reads
             if constexpr (mixed) {
                 for (int t = 0; t < c->NT; t++) {
@@ -1332,10 +1383,10 @@ static int enqueue_steps_tma(obgc_ctx* c, StepPlan<TS, TC>& p, double dt, int ns
             a.out_halo = q != last;
             a.tma_layout = 2;
             a.tmap = from_user ? c->d_tmaps + 2 * MAX_NT : c->d_tmaps + (size_t)pin * MAX_NT;
+            a.tmap_wrap = q == 0 && bands ? c->d_tmaps + (size_t)1 * MAX_NT : nullptr;   // padded set 1
             a.tma_x0 = from_user ? -TMA_HX : 0;
             a.tma_y0 = from_user ? -HALO : 0;
-            int rc = launch_par_prefix(c, a, st);
-            if (rc == OBGC_OK) rc = launch_sink_flux(c, a, st);
+            int rc = launch_pre_passes(c, a, st);
             if (rc != OBGC_OK) return rc;
             if (profile) OBGC_CUDA(cudaEventRecord(c->prof_events[ev++], st));
             rc = p.fe->launch(&a, p.blocks, st);

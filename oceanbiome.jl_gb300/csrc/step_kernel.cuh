@@ -74,6 +74,9 @@ struct SubstepArgs {
     // on a periodic edge (that would need the wrap) are staged by cp.async
     const CUtensorMap* tmap;
     int tma_x0, tma_y0;
+    // a call's first stage when tmap holds the caller's arrays' maps: the tiles that need the
+    // periodic wrap are copied from padded set 1 through these maps instead (at (i0, j0)); NULL: none
+    const CUtensorMap* tmap_wrap;
     TC dx, dy, dz, Lz, inv_dx, inv_dy, inv_dz;
     int TZ, nseg, ntx, nty, n_items;
     const TS* in[MAX_NT];
@@ -231,10 +234,12 @@ constexpr int TMA_HX = 4;                                   // x halo of the pad
 
 // Whether the tile at (i0, j0) needs the periodic wrap: its staged halo leaves the grid in a
 // periodic direction.
+__host__ __device__ inline bool tile_wraps_xy(int i0, int j0, int Nx, int Ny, bool periodic_x, bool periodic_y) {
+    return (periodic_x && (i0 < TMA_HX || i0 + TMA_TILE_W - TMA_HX > Nx)) || (periodic_y && (j0 < HALO || j0 + STEP_BY + HALO > Ny));
+}
 template <typename TS, typename TC>
 __host__ __device__ inline bool tile_wraps(const SubstepArgs<TS, TC>& a, int i0, int j0) {
-    return (a.periodic_x && (i0 < TMA_HX || i0 + TMA_TILE_W - TMA_HX > a.Nx)) ||
-           (a.periodic_y && (j0 < HALO || j0 + STEP_BY + HALO > a.Ny));
+    return tile_wraps_xy(i0, j0, a.Nx, a.Ny, a.periodic_x, a.periodic_y);
 }
 template <bool SPLIT>
 __host__ __device__ constexpr int tile_w() { return SPLIT ? TMA_TILE_W : STEP_BX + 2 * HALO; }
@@ -432,11 +437,13 @@ __global__ void __launch_bounds__(STEP_BX * STEP_BY, sizeof(TC) != 4 ? 1 : NT <=
     // thread 0 arms the barrier and copies every tracer's tile of level kk of the work item at
     // (i0, j0): the box whose first cell is x = i0 - 4, y = j0 - 3 of the grid
     auto tma_issue = [&](int i0_, int j0_, int kk) {
+        const bool wrap = a.tmap_wrap != nullptr && tile_wraps(a, i0_, j0_);
+        const CUtensorMap* maps = wrap ? a.tmap_wrap : a.tmap;
+        const int x0 = i0_ + (wrap ? 0 : a.tma_x0), y0 = j0_ + (wrap ? 0 : a.tma_y0);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arm(&stage_bar, TILE_BYTES * NT);
 #pragma unroll 1
-        for (int t = 0; t < NT; t++)
-            tma_tile(tiles + t * TILE_SZ, a.tmap + t, i0_ + a.tma_x0, j0_ + a.tma_y0, kk, &stage_bar);
+        for (int t = 0; t < NT; t++) tma_tile(tiles + t * TILE_SZ, maps + t, x0, y0, kk, &stage_bar);
     };
 
     // forcings switched on at this stage's time
