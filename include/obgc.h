@@ -725,8 +725,9 @@ int obgc_tracer_budget(obgc_ctx* ctx, int32_t group, double* total, void* stream
  * sum_n scale[n]*fields[n] is written to *total (host) and the call returns after the stream has
  * finished it.  n_fields above OBGC_BUDGET_STATIC_MAX_FIELDS is rejected (OBGC_ERR_INVALID_ARGUMENT).
  *
- * The first call on each device looks up the array's device address on that device; make that
- * first call before any stream capture.  The address is kept for the life of the process: after
+ * The call synchronizes `stream` (the sum comes back to the host), so no call of it can be
+ * captured into a CUDA graph.  The first call on each device looks up the array's device address
+ * on that device.  The address is kept for the life of the process: after
  * a cudaDeviceReset (or any teardown of the device's primary context) the library's module is
  * loaded again elsewhere, so do not call this entry point on that device again.  All calls share
  * the one array: calls that overlap on the GPU (different streams or host threads without
