@@ -433,7 +433,7 @@ def run_gpu(args):
     # cells), scaled by the cells of this grid
     traffic = 177.8 * g.N if prec == "f32" else None
 
-    # the other precisions of the same workload (spec: mixed vs FP64), and the error
+    # the other precisions of the same workload (the metric's mixed vs FP64), and the error
     # statement of the timed precision after 1000 steps against the FP64 oracle
     arms, err = None, None
     if rank == 0 and not args.no_cpu_baseline:
