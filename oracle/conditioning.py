@@ -12,7 +12,7 @@ value and stage), for r one FP64 unit roundoff (2^-53) and one FP32 unit roundof
 implementation that rounds differently from the oracle differs from it by about the first; any
 that rounds to FP32 anywhere in the update by about the second.
 
-Only tests/ and bench.py's accuracy legs use this module, as the checker.
+Only tests/ and bench.py's accuracy legs use this module, as the oracle.
 """
 import os
 import sys

@@ -5,7 +5,7 @@
  * functors, TwoBand/MultiBand light, CarbonChemistry + root solvers, BoxModel RK3) plus a
  * restatement of the third-party Oceananigans pieces the path runs inside (WENO5 tracer
  * advection, RK3 substeps, vertically implicit diffusion).  Only tests/, __graft_entry__.smoke()
- * and bench.py's CPU-baseline leg may load it, and only as the checker.  It shares nothing with
+ * and bench.py's CPU-baseline leg may load it, and only as the oracle the GPU results are compared with.  It shares nothing with
  * the CUDA product but the parameter structs of include/obgc.h (the interface).
  *
  * Parity pins: the reference's own known-answer tests (test/test_light.jl, test/test_solvers.jl,

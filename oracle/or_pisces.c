@@ -2,7 +2,7 @@
  *
  * Follows src/Models/AdvectedPopulations/PISCES/ function by function: every tracer's tendency is
  * built the way the reference's functor for that tracer builds it, recomputing the shared terms it
- * recomputes (the GPU kernel fuses them; this file is the checker).  Paths below are relative to
+ * recomputes (the GPU kernel fuses them; this file is the oracle).  Paths below are relative to
  * that directory unless they start with src/.  Quirks kept verbatim:
  *   - the growth rate calls day_length(latitude, time) (growth_rate.jl:29) where the CBM day length
  *     takes (time, latitude) (src/Utils/Utils.jl:18); the energy-assimilation ratio calls it in the

@@ -2,7 +2,7 @@
 
 The oracle is a CPU FP64 restatement of OceanBioME.jl's tracer-tendency path (see
 obgc_oracle.h).  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as
-the checker.  It reuses only the parameter-struct mirrors of include/obgc.h.
+the oracle the GPU results are compared with.  It reuses only the parameter-struct mirrors of include/obgc.h.
 """
 import ctypes as C
 import os

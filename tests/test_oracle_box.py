@@ -1,5 +1,5 @@
 """Oracle (CPU) of BoxModel(; forcing, prescribed_tracers) (src/BoxModel/boxmodel.jl:65-106,
-timesteppers.jl:37-63): the forms the GPU box kernel is checked against."""
+timesteppers.jl:37-63): the forms the GPU BoxModel kernel is checked against."""
 import math
 
 import numpy as np
